@@ -1,0 +1,83 @@
+"""Regenerate the committed golden fixtures in tests/golden/.
+
+Run on a machine that has the reference tree (default /root/reference, or
+GGEM_REFERENCE_ROOT).  Two fixtures come out:
+
+* ggem_profile_3P.json -- the reference's PointParticle_Stokes_GGEM golden
+  velocity profiles (tests/integration_tests/resources/PointParticle_Stokes_GGEM/
+  output/output_velocity_profile_{x,y,z}_3P.txt), reduced to the columns that
+  pin the particle-side kernels: the coordinate, the three GGEM local-velocity
+  columns (pair kernel in field-target mode, ggem_stokes.C:360-424) and the
+  three unbounded xi-smoothed columns (ggem_stokes.C:201-251,
+  analytical_solution_stokes.C:66-102).  Columns are taken by position
+  (0, 7-9, 10-12); the files predate the csv writer at
+  pm_system_stokes.C:669-674.
+* ref_chebyshev_coeffs.json -- Chebyshev coefficients produced by the
+  reference's own src/chebyshev.C (compiled into oracle/_ref by
+  oracle/Makefile) for a grid of orders, intervals and quadrature methods,
+  stored as hex floats so the comparison is bit-exact.
+
+Usage:  python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import json
+import os
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parent.parent
+REF_ROOT = Path(os.environ.get("GGEM_REFERENCE_ROOT", "/root/reference"))
+PROFILE_DIR = (REF_ROOT / "tests" / "integration_tests" / "resources"
+               / "PointParticle_Stokes_GGEM")
+
+# Chebyshev cases: (N, eig_min, eig_max) spanning the reference defaults
+# (max_n_cheb 10..50, copss.C:794-797) and the BD_HI eigen interval golden
+# (out.eigenvalue 0.64154 1.32335).
+CHEB_CASES = [(10, 0.64154, 1.32335), (30, 0.2, 1.4), (50, 0.05, 2.0),
+              (16, 1.0, 4096.0), (5, 0.9, 1.1), (40, 0.3, 1.05)]
+
+
+def profiles() -> dict:
+    out = {"source": "tests/integration_tests/resources/PointParticle_Stokes_GGEM",
+           "alpha": 0.35, "box": [-15.0, 15.0], "n_mesh": [15, 15, 15],
+           "periodic": [False, False, False],
+           "beads": [[-5.0, 0.0, 0.0], [0.0, 0.0, 0.0], [5.0, 0.0, 0.0]],
+           "force": [0.3333, 0.0, 0.0], "print_decimals": 9,
+           "reference_tolerance": 1e-5, "axes": {}}
+    for name in "xyz":
+        g = np.loadtxt(PROFILE_DIR / "output" / f"output_velocity_profile_{name}_3P.txt")
+        out["axes"][name] = {"coord": g[:, 0].tolist(), "local": g[:, 7:10].tolist(),
+                             "exact": g[:, 10:13].tolist()}
+    return out
+
+
+def cheb_coeffs() -> dict:
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as O  # noqa: E402  (test infrastructure)
+
+    O.build_oracle(with_ref=True)
+    cases = []
+    for N, lmin, lmax in CHEB_CASES:
+        d = lmax - lmin
+        da, db = 2.0 / d, -(lmax + lmin) / d
+        for method in (0, 1, 2):
+            c = O.ref_cheb_coeffs(N, da, db, method)
+            if c is None:
+                raise SystemExit("oracle/_ref/libref_chebyshev.so was not built")
+            cases.append({"N": N, "da": da.hex(), "db": db.hex(), "method": method,
+                          "coef": [float(x).hex() for x in c]})
+    return {"source": "src/chebyshev.C via oracle/_ref", "cases": cases}
+
+
+def main() -> None:
+    (HERE / "ggem_profile_3P.json").write_text(json.dumps(profiles()))
+    (HERE / "ref_chebyshev_coeffs.json").write_text(json.dumps(cheb_coeffs(), indent=1))
+    print("wrote", HERE / "ggem_profile_3P.json", HERE / "ref_chebyshev_coeffs.json")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,246 @@
+"""The FP64 oracle against the reference's golden vectors and known answers.
+
+Pins: the PointParticle_Stokes_GGEM golden profiles (pair kernel in field
+mode and the unbounded xi-smoothed Green's function), the reference's own
+chebyshev.C (bit-exact), closed-form Chebyshev / spectral known answers and
+dense-matrix eigenvalues for the Lanczos bounds.
+"""
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import oracle as O
+
+GOLD = Path(__file__).resolve().parent / "golden"
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _build():
+    O.build_oracle(with_ref=True)
+
+
+def test_constants_match_reference_formulas():
+    c = O.constants(alpha=0.5)
+    # ggem_stokes.C:44, :59, :81, :112 with mu = 1/(6 pi), br0 = 1
+    assert c.one_eight_pi_mu == pytest.approx(0.75, rel=1e-15)
+    assert c.ksi == pytest.approx(np.sqrt(np.pi) / 3, rel=1e-15)
+    assert c.coeff_1 == pytest.approx(0.75 * 4 * 0.5 / np.sqrt(np.pi), rel=1e-15)
+    assert c.coeff_2 == pytest.approx(0.75 * 4 * (c.ksi - 0.5) / np.sqrt(np.pi), rel=1e-15)
+    # bead self mobility 1 - coeff_1 equals G_local(0) = coeff_2 when br0 = 1
+    assert 1 - c.coeff_1 == pytest.approx(c.coeff_2, rel=1e-14)
+    lag = O.constants(alpha=0.5, point_type=O.LAGRANGIAN_POINT, ibm_beta=0.75, hmin=2.0)
+    assert lag.ksi == pytest.approx(1 / 1.5, rel=1e-15)
+
+
+@pytest.mark.parametrize("axis", ["x", "y", "z"])
+def test_golden_velocity_profile(axis):
+    """Local GGEM velocity at the reference profile points, 3 beads, alpha 0.35.
+
+    The golden files were produced with the point-centred neighbour search of
+    radius search_radius_p = 4/alpha (copss.C:1074); the cut-off field
+    evaluation at that radius reproduces them to the printed 9 decimals.
+    """
+    g = json.loads((GOLD / "ggem_profile_3P.json").read_text())
+    c = O.constants(alpha=g["alpha"])
+    box = O.make_box([g["box"][0]] * 3, [g["box"][1]] * 3, [0, 0, 0])
+    xyz = np.array(g["beads"])
+    f = np.array([g["force"]] * 3)
+    ax = "xyz".index(axis)
+    A = g["axes"][axis]
+    pts = np.zeros((len(A["coord"]), 3))
+    pts[:, ax] = A["coord"]
+    ul = O.local_field_cutoff(c, box, xyz, f, pts, 4.0 / g["alpha"])
+    ue = O.exact_unbounded(c, xyz, f, pts)
+    tol = 0.5 * 10.0 ** (-g["print_decimals"]) + 1e-12
+    assert np.abs(ul - np.array(A["local"])).max() <= tol
+    assert np.abs(ue - np.array(A["exact"])).max() <= tol
+
+
+def test_chebyshev_coefficients_bit_exact_vs_reference_source():
+    d = json.loads((GOLD / "ref_chebyshev_coeffs.json").read_text())
+    for cs in d["cases"]:
+        c = O.cheb_coeffs(cs["N"], float.fromhex(cs["da"]), float.fromhex(cs["db"]),
+                          cs["method"])
+        ref = np.array([float.fromhex(x) for x in cs["coef"]])
+        assert np.array_equal(c, ref), (cs["N"], cs["method"])
+
+
+def test_chebyshev_coefficients_live_reference_build():
+    if O.ref_lib() is None:
+        pytest.skip("reference source tree not present on this machine")
+    rng = np.random.default_rng(3)
+    for _ in range(20):
+        N = int(rng.integers(2, 60))
+        lmin = float(rng.uniform(0.01, 1.0))
+        lmax = lmin * float(rng.uniform(1.1, 50.0))
+        d = lmax - lmin
+        for m in (0, 1, 2):
+            a = O.cheb_coeffs(N, 2 / d, -(lmax + lmin) / d, m)
+            b = O.ref_cheb_coeffs(N, 2 / d, -(lmax + lmin) / d, m)
+            assert np.array_equal(a, b)
+
+
+def test_chebyshev_diagonal_operator_known_answer():
+    """brownian_system.C:1181-1211 test operator M = diag(1..n): the Chebyshev
+    series must reproduce M^{-1/2} xi within the stated error estimate."""
+    n = 12
+    op = O.Operator("diag", dim=n)
+    xi = np.random.default_rng(0).standard_normal(n)
+    # err1 = sqrt(|y.M^2.y - xi.M.xi| / xi.M.xi) scales like the square root
+    # of the relative error of y, so tol 1e-4 asks for ~1e-8 accuracy
+    y, rep = O.cheb_inv_sqrt(op, xi, 50, 1.0 / 1.05, n * 1.05, 1e-4)
+    assert rep.converged == 1
+    exact = xi / np.sqrt(np.arange(1, n + 1))
+    assert np.abs(y - exact).max() / np.abs(exact).max() < 1e-6
+    assert rep.n_matvecs == 2 + 2 * (rep.n_terms - 1)
+    # an unreachable tolerance stops on the err2 <= 1e-9 rule unconverged
+    y2, rep2 = O.cheb_inv_sqrt(op, xi, 50, 1.0 / 1.05, n * 1.05, 1e-7)
+    assert rep2.converged == 0 and rep2.err2 <= 1e-9 and rep2.n_terms < 50
+
+
+def _suspension(n, phi, seed):
+    rng = np.random.default_rng(seed)
+    L = (n * 4.0 / 3.0 * np.pi / phi) ** (1 / 3)
+    pts = []
+    while len(pts) < n:
+        p = rng.uniform(0, L, 3)
+        ok = True
+        for q in pts:
+            d = p - q
+            d -= L * np.round(d / L)
+            if d @ d < 4.0:
+                ok = False
+                break
+        if ok:
+            pts.append(p)
+    return np.array(pts), L
+
+
+def test_cutoff_lists_match_brute_force():
+    xyz, L = _suspension(300, 0.1, 1)
+    box = O.make_box([0] * 3, [L] * 3, [1, 1, 1])
+    nb = O.neighbors_cutoff(box, xyz, 7.0)
+    for i, lst in enumerate(nb.lists()):
+        d = xyz - xyz[i]
+        d -= L * np.round(d / L)
+        r2 = (d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1]) + d[:, 2] * d[:, 2]
+        want = np.nonzero(r2 < 49.0)[0]
+        want = want[want != i]
+        assert np.array_equal(np.sort(lst), want)
+
+
+def test_reference_lists_self_removed_and_symmetric_within_cell():
+    xyz, L = _suspension(200, 0.05, 2)
+    box = O.make_box([0] * 3, [L] * 3, [1, 1, 1])
+    mesh = O.make_mesh(12, 12, 12, 0.5 * L / 12 + 8.0)
+    nb = O.neighbors_reference(box, mesh, xyz)
+    for i, lst in enumerate(nb.lists()):
+        assert i not in set(lst.tolist())
+        assert len(set(lst.tolist())) == len(lst)
+
+
+def test_local_mobility_spd_and_lanczos_bounds():
+    xyz, L = _suspension(120, 0.1, 4)
+    box = O.make_box([0] * 3, [L] * 3, [1, 1, 1])
+    c = O.constants(alpha=0.5)
+    nb = O.neighbors_cutoff(box, xyz, 7.0)
+    n = len(xyz)
+    M = np.zeros((3 * n, 3 * n))
+    for k in range(3 * n):
+        e = np.zeros(3 * n)
+        e[k] = 1
+        M[:, k] = O.local_matvec(c, box, xyz, nb, e, O.SELF_BEAD)
+    assert np.abs(M - M.T).max() < 1e-14
+    ev = np.linalg.eigvalsh(M)
+    assert ev[0] > 0
+    op = O.Operator(matvec=(c, box, xyz, nb, O.SELF_BEAD, 1))
+    lo, hi, a, b = O.lanczos(op, np.random.default_rng(1).standard_normal(3 * n), 3 * n)
+    assert lo == pytest.approx(ev[0], rel=1e-8)
+    assert hi == pytest.approx(ev[-1], rel=1e-8)
+    lo30, hi30, _, _ = O.lanczos(op, np.random.default_rng(1).standard_normal(3 * n), 30)
+    assert ev[0] <= lo30 + 1e-12 and hi30 <= ev[-1] + 1e-12
+    # brownian_system.C:846-920 defaults: tol 1e-3 on the iterate change
+    it, lam = O.power_iteration(op, 3 * n, tol=1e-3, maxits=5000)
+    assert it >= 0 and lam <= ev[-1] * (1 + 1e-12) and lam == pytest.approx(ev[-1], rel=1e-3)
+
+
+def test_chebyshev_on_local_mobility_matches_dense_inverse_sqrt():
+    xyz, L = _suspension(80, 0.1, 5)
+    box = O.make_box([0] * 3, [L] * 3, [1, 1, 1])
+    c = O.constants(alpha=0.5)
+    nb = O.neighbors_cutoff(box, xyz, 7.0)
+    n = len(xyz)
+    M = np.zeros((3 * n, 3 * n))
+    for k in range(3 * n):
+        e = np.zeros(3 * n)
+        e[k] = 1
+        M[:, k] = O.local_matvec(c, box, xyz, nb, e, O.SELF_BEAD)
+    w, V = np.linalg.eigh(M)
+    xi = np.random.default_rng(9).standard_normal(3 * n)
+    op = O.Operator(matvec=(c, box, xyz, nb, O.SELF_BEAD, 1))
+    y, rep = O.cheb_inv_sqrt(op, xi, 50, w[0] / 1.05, w[-1] * 1.05, 1e-4)
+    exact = V @ ((V.T @ xi) / np.sqrt(w))
+    assert rep.converged
+    # err1 is a first-order, sign-averaged estimate of the error of y, so the
+    # true error is checked at a looser level than err1**2
+    assert np.linalg.norm(y - exact) / np.linalg.norm(exact) < 1e-4
+    # err1 definition, brownian_system.C:1117-1125
+    My = M @ y
+    err1 = np.sqrt(abs(My @ My - xi @ (M @ xi)) / (xi @ (M @ xi)))
+    assert err1 == pytest.approx(rep.err1, rel=1e-6, abs=1e-12)
+
+
+def test_spread_and_element_rhs_consistent():
+    rng = np.random.default_rng(7)
+    L = 20.0
+    box = O.make_box([0] * 3, [L] * 3, [1, 1, 1])
+    c = O.constants(alpha=0.5)
+    xyz = rng.uniform(0, L, (40, 3))
+    f = rng.standard_normal((40, 3))
+    mesh = O.make_mesh(5, 5, 5, 0.5 * 4 + 8.0)
+    enb, _ = O.elem_lists(box, mesh, xyz)
+    ne, nq, nu = 125, 8, 20
+    q = rng.uniform(0, L, (ne * nq, 3))
+    qe = np.repeat(np.arange(ne), nq).astype(np.int32)
+    IF = rng.standard_normal((ne, nu * nq))
+    rho = O.spread_qp(c, box, enb, xyz, f, q, qe)
+    Fe = O.element_rhs(c, box, enb, xyz, f, ne, nq, nu, q, IF)
+    want = np.zeros((ne, 3 * nu))
+    for e in range(ne):
+        for qp in range(nq):
+            for j in range(3):
+                want[e, j * nu:(j + 1) * nu] += IF[e].reshape(nu, nq)[:, qp] * rho[e * nq + qp, j]
+    assert np.abs(Fe - want).max() < 1e-12
+    # direct evaluation of smoothed_force_exp for one point
+    e0 = 0
+    lst = enb.lists()[e0]
+    r = 0.0
+    for j in lst:
+        d = xyz[j] - q[0]
+        d -= L * np.round(d / L)
+        r += O.smoothed_force_exp(c, d) * f[j, 0]
+    assert rho[0, 0] == pytest.approx(r, rel=1e-13)
+
+
+def test_std_normal_stream_is_reproducible_and_normal():
+    a = O.std_normal_vector(123456789, 30000)
+    b = O.std_normal_vector(123456789, 30000)
+    assert np.array_equal(a, b)
+    assert abs(a.mean()) < 0.03 and abs(a.std() - 1) < 0.03
+    skipped = O.std_normal_vector(123456789, 3000, skip_vectors=2)
+    assert not np.array_equal(skipped, a[:3000])
+
+
+def test_philox_known_answer():
+    # Philox4x32-10 known-answer vector (Random123 kat_vectors: counter 0,
+    # key 0 -> 6627e8d5 e169c58d bc57ac4c 9b00dbd8)
+    out = O.philox_normals(0, 0, 2)
+    u53a = (0x6627e8d5 << 21) ^ (0xe169c58d >> 11)
+    u53b = (0xbc57ac4c << 21) ^ (0x9b00dbd8 >> 11)
+    u1 = (u53a + 0.5) * 2.0 ** -53
+    u2 = (u53b + 0.5) * 2.0 ** -53
+    r = np.sqrt(-2 * np.log(u1))
+    assert out[0] == pytest.approx(r * np.cos(2 * np.pi * u2), rel=1e-14)
+    assert out[1] == pytest.approx(r * np.sin(2 * np.pi * u2), rel=1e-14)
