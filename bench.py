@@ -1,0 +1,480 @@
+#!/usr/bin/env python
+"""Benchmark of the GGEM particle-side hot path on GB300.
+
+Workload (the metric's configuration): N = 200,000 beads of radius a = 1 in a
+periodic cube at volume fraction phi = 0.1 (L = 203.1), GGEM alpha = 0.5/a,
+local cut-off rc = 7a, seeded random non-overlapping placement and Philox
+N(0,1) noise (synthetic inputs; the reference ships none of this size).
+
+One "step" is one Brownian step of the local mobility, the particle-side
+part of Copss::fixman_integrate (copss.C:1560-1686):
+  cell list + pair list build -> noise xi -> Chebyshev y ~ M^{-1/2} xi
+  (FP32 pair sums, FP64 recurrence, err1 <= 1e-3, <= 50 terms) -> dw = M y.
+The eigen interval is computed by Lanczos once and reused until the series
+fails, the reference's policy (copss.C:1598-1671).
+
+value      steps/s with positions and noise resident on the device
+e2e        steps/s through the host-pointer C ABI (positions and xi copied
+           in from pinned host memory, dw copied out, every step)
+also       mobility matvecs/s, the plain FP64 GPU path (FP64 pair sweep,
+           Lanczos every step, error check every term), FP32-vs-FP64
+           velocity error, the pair kernel's roofline and the CPU baseline.
+
+--impl reference times the reference algorithm on the host cores (the FP64
+oracle restatement; the reference itself needs libMesh/PETSc/SLEPc) with all
+host threads, on the same workload and metric.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "copss-hydrodynamics-private_gb300"))
+
+METRIC = ("Brownian steps/s & mobility matvecs/s at N=200k vs plain FP64 GPU, "
+          "rel err ≤1e-6")
+N_BEADS = 200_000
+PHI = 0.1
+ALPHA = 0.5
+RC = 7.0
+CHEB_MAX = 50
+CHEB_TOL = 1e-3
+SEED = 20261203
+
+
+def workload_config(extra=None):
+    cfg = {"workload": "Brownian step of the GGEM local mobility: N=200000 beads a=1, "
+                       "phi=0.1 periodic cube, alpha=0.5, rc=7, Chebyshev tol 1e-3 <=50 terms",
+           "n_beads": N_BEADS, "phi": PHI, "alpha": ALPHA, "rc": RC, "nrhs": 1,
+           "cheb_max_terms": CHEB_MAX, "cheb_tol": CHEB_TOL,
+           "l2": "flushed between timed steps (512 MB write); inputs are ~40 MB"}
+    if extra:
+        cfg.update(extra)
+    return cfg
+
+
+# --------------------------------------------------------------------------
+# clocks sampled during the timed region
+# --------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# --------------------------------------------------------------------------
+# GB300 arm
+# --------------------------------------------------------------------------
+def run_gb300(args, rank, world):
+    import torch
+    import ggem_gb300 as G
+    from ggem_gb300 import build as B
+
+    B.build()
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    L_lib = G.lib()
+    import ctypes as C
+
+    xyz, L = G.make_suspension(SEED + rank, N_BEADS, PHI)
+    box = (L, L, L)
+
+    def make_ctx(prec, div=1):
+        return G.Context(alpha=ALPHA, box_hi=box, rc=RC, precision=prec, cell_div=div, device=dev)
+
+    # pick the cell size of the FP32 pair list (a two-candidate autotune)
+    d_xyz = torch.from_numpy(xyz.reshape(-1)).cuda()
+    best = None
+    for div in (1, 2):
+        ctx = make_ctx(G.FP32, div)
+        ctx.set_particles_dev(d_xyz.data_ptr(), N_BEADS)
+        ctx.build_cells()
+        f = torch.randn(3 * N_BEADS, dtype=torch.float64, device="cuda")
+        u = torch.empty_like(f)
+        for _ in range(3):
+            ctx.local_matvec_dev(f.data_ptr(), u.data_ptr(), 1, G.SELF_BEAD)
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(20):
+            ctx.set_particles_dev(d_xyz.data_ptr(), N_BEADS)
+            ctx.build_cells()
+            for _ in range(10):
+                ctx.local_matvec_dev(f.data_ptr(), u.data_ptr(), 1, G.SELF_BEAD)
+        ctx.synchronize()
+        dt = time.perf_counter() - t0
+        if best is None or dt < best[0]:
+            best = (dt, div)
+        ctx.close()
+    cell_div = best[1]
+    ctx = make_ctx(G.FP32, cell_div)
+    stream = torch.cuda.Stream(device=dev)
+    ctx.set_stream(stream.cuda_stream)
+
+    d_xi = torch.empty(3 * N_BEADS, dtype=torch.float64, device="cuda")
+    d_dw = torch.empty_like(d_xi)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    state = {"bounds": None, "lanczos_calls": 0, "reports": []}
+
+    def bounds(c):
+        lo, hi = c.lanczos_bounds(k=24, seed=7)
+        state["lanczos_calls"] += 1
+        return lo / 1.05, hi * 1.05  # eig_factor widening, copss.C:1607
+
+    def device_step(step_id):
+        ctx.set_particles_dev(d_xyz.data_ptr(), N_BEADS)
+        ctx.build_cells()
+        ctx.philox_normals_dev(SEED, step_id, 3 * N_BEADS, d_xi.data_ptr())
+        if state["bounds"] is None:
+            state["bounds"] = bounds(ctx)
+        for attempt in range(2):
+            lo, hi = state["bounds"]
+            rc, rep = ctx.brownian_displacement_dev(d_xi.data_ptr(), d_dw.data_ptr(), 1,
+                                                    CHEB_MAX, lo, hi, CHEB_TOL,
+                                                    check_every=args.check_every)
+            if rc == 0:
+                state["reports"].append(rep[0])
+                return
+            state["bounds"] = bounds(ctx)  # recompute and retry once
+        raise RuntimeError(f"Chebyshev failed twice: {rep}")
+
+    def timed(fn, steps, warmup, flush_l2=True):
+        for s in range(warmup):
+            fn(s)
+        torch.cuda.synchronize()
+        ts = []
+        for s in range(steps):
+            if flush_l2:
+                flush.zero_()
+            torch.cuda.synchronize()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            with torch.cuda.stream(stream):
+                fn(warmup + s)
+            b.record(stream)
+            b.synchronize()
+            ts.append(a.elapsed_time(b))
+        return ts
+
+    # ---- device-resident Brownian steps (value) --------------------------
+    if world > 1:
+        torch.distributed.barrier()
+    ctx.set_kernel_timing(False)
+    for s in range(args.warmup):
+        device_step(s)
+    torch.cuda.synchronize()
+    ctx.set_kernel_timing(True)
+    lc0 = ctx.launch_count()
+    t_wall0 = time.perf_counter()
+    with ClockSampler(dev) as clk:
+        ts = timed(device_step, args.steps, 0)
+    t_wall = time.perf_counter() - t_wall0
+    lc1 = ctx.launch_count()
+    kt = {name: ctx.kernel_timing(kind) for kind, name in
+          ((G.KERNEL_PAIR_FP32, "pair_fp32"), (G.KERNEL_CHEB_TERM, "cheb_term"),
+           (G.KERNEL_LIST_BUILD, "list_build"))}
+    ctx.set_kernel_timing(False)
+    ms_step = float(np.mean(ts))
+    if world > 1:
+        t = torch.tensor([ms_step], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_step = float(t.item())
+    steps_per_s = 1e3 / ms_step * world  # replicas: every rank runs its own suspension
+    n_pairs = ctx.pair_count()
+    reps = state["reports"][-args.steps:]
+
+    # ---- e2e through the host-pointer ABI --------------------------------
+    h_xyz = torch.from_numpy(xyz.reshape(-1).copy()).pin_memory()
+    h_dw = torch.empty(3 * N_BEADS, dtype=torch.float64).pin_memory()
+    xi_host = [torch.from_numpy(G.make_normals(SEED + 1000 + s, 3 * N_BEADS)).pin_memory()
+               for s in range(args.steps + args.warmup)]
+    ctx_e = make_ctx(G.FP32, cell_div)
+    ctx_e.set_particles(xyz)
+    ctx_e.build_cells()
+    e_bounds = state["bounds"]
+    RepArr = G.ChebReport * 1
+
+    def e2e_step(step_id):
+        nonlocal e_bounds
+        h_xi = xi_host[step_id % len(xi_host)]
+        rc = L_lib.ggem_set_particles(ctx_e.h, N_BEADS, C.c_void_p(h_xyz.data_ptr()))
+        rc |= L_lib.ggem_build_cells(ctx_e.h)
+        for attempt in range(2):
+            rep = RepArr()
+            rc2 = L_lib.ggem_brownian_displacement(ctx_e.h, 1, CHEB_MAX, e_bounds[0], e_bounds[1],
+                                                   CHEB_TOL, args.check_every,
+                                                   C.c_void_p(h_xi.data_ptr()),
+                                                   C.c_void_p(h_dw.data_ptr()), rep)
+            if rc2 == 0:
+                break
+            lo, hi = ctx_e.lanczos_bounds(k=24, seed=7)
+            e_bounds = (lo / 1.05, hi * 1.05)
+        if rc or rc2:
+            raise RuntimeError(f"e2e step failed rc={rc} rc2={rc2}")
+        _ = float(h_dw.numpy()[0])  # host read of the step's result
+
+    for s in range(args.warmup):
+        e2e_step(s)
+    e_ts = []
+    for s in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e2e_step(args.warmup + s)
+        e_ts.append((time.perf_counter() - t0) * 1e3)
+    e2e_ms = float(np.mean(e_ts))
+    ctx_e.close()
+
+    # ---- mobility matvec throughput (FP32, device resident) ------------
+    f = torch.randn(3 * N_BEADS, dtype=torch.float64, device="cuda")
+    u = torch.empty_like(f)
+    for _ in range(5):
+        ctx.local_matvec_dev(f.data_ptr(), u.data_ptr(), 1, G.SELF_BEAD)
+    mv_ts = []
+    for _ in range(max(10, args.steps)):
+        flush.zero_()
+        torch.cuda.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        ctx.local_matvec_dev(f.data_ptr(), u.data_ptr(), 1, G.SELF_BEAD)
+        b.record(stream)
+        b.synchronize()
+        mv_ts.append(a.elapsed_time(b))
+    matvecs_per_s = 1e3 / float(np.mean(mv_ts)) * world
+
+    # ---- accuracy: FP32 vs FP64 velocities at N=200k --------------------
+    ctx64 = make_ctx(G.FP64)
+    ctx64.set_particles_dev(d_xyz.data_ptr(), N_BEADS)
+    ctx64.build_cells()
+    fe = torch.from_numpy(G.make_normals(SEED + 5, 3 * N_BEADS)).cuda()
+    u32 = torch.empty_like(fe)
+    u64 = torch.empty_like(fe)
+    ctx.local_matvec_dev(fe.data_ptr(), u32.data_ptr(), 1, G.SELF_BEAD)
+    ctx.synchronize()
+    ctx64.local_matvec_dev(fe.data_ptr(), u64.data_ptr(), 1, G.SELF_BEAD)
+    ctx64.synchronize()
+    rel_err = float(torch.linalg.norm(u32 - u64) / torch.linalg.norm(u64))
+    comp_err = float((u32 - u64).abs().max() / u64.abs().max())
+
+    # ---- plain FP64 GPU path (the comparison baseline) ------------------
+    fp64 = None
+    if not args.skip_fp64:
+        st64 = {"reports": []}
+
+        def fp64_step(step_id):
+            ctx64.set_particles_dev(d_xyz.data_ptr(), N_BEADS)
+            ctx64.build_cells()
+            ctx64.philox_normals_dev(SEED, step_id, 3 * N_BEADS, d_xi.data_ptr())
+            lo, hi = ctx64.lanczos_bounds(k=24, seed=7)  # every step
+            rc, rep = ctx64.brownian_displacement_dev(d_xi.data_ptr(), d_dw.data_ptr(), 1,
+                                                      CHEB_MAX, lo / 1.05, hi * 1.05, CHEB_TOL,
+                                                      check_every=1)
+            st64["reports"].append(rep[0])
+
+        ctx64.set_stream(stream.cuda_stream)
+        ts64 = timed(fp64_step, args.fp64_steps, 1)
+        ctx64.set_stream(0)
+        fp64 = {"steps_per_s": 1e3 / float(np.mean(ts64)) * world,
+                "ms_per_step": float(np.mean(ts64)), "steps": args.fp64_steps,
+                "cheb_terms": [r["n_terms"] for r in st64["reports"][-args.fp64_steps:]],
+                "path": "FP64 cell-stencil pair sweep, Lanczos(24) every step, err1 check "
+                        "every term, one RHS, no graphs"}
+    ctx64.close()
+
+    # ---- roofline of the dominant kernel --------------------------------
+    peak = ctx.probe_fp32_peak()
+    pair_ms, pair_n = kt["pair_fp32"]
+    avg_pair_ms = pair_ms / max(pair_n, 1)
+    flops_per_launch = n_pairs * (28 + 19 * 1)
+    achieved = flops_per_launch / (avg_pair_ms * 1e-3) / 1e12
+    ctx.close()
+
+    result = {
+        "metric": METRIC, "value": steps_per_s, "unit": "Brownian steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 pair sums, f64 Chebyshev recurrence", "data": "synthetic (seeded)",
+        "config": workload_config({"parallelism": f"replicas x{world}", "cell_div": cell_div,
+                                   "check_every": args.check_every}),
+        "e2e": {"value": 1e3 / e2e_ms * world, "unit": "Brownian steps/s",
+                "ms_per_step": e2e_ms, "h2d_bytes_per_step": 2 * 24 * N_BEADS,
+                "d2h_bytes_per_step": 24 * N_BEADS},
+        "matvecs_per_s": matvecs_per_s, "matvec_ms": float(np.mean(mv_ts)),
+        "plain_fp64_gpu": fp64,
+        "speedup_vs_plain_fp64": (steps_per_s / fp64["steps_per_s"]) if fp64 else None,
+        "velocity_rel_err_fp32_vs_fp64": rel_err, "velocity_max_component_err": comp_err,
+        "cheb": {"terms": [r["n_terms"] for r in reps], "err1_max": max(r["err1"] for r in reps),
+                 "converged": all(r["converged"] for r in reps),
+                 "lanczos_calls": state["lanczos_calls"]},
+        "roofline": {"bound": "fp32", "kernel": "k_matvec_f32<1> (pair-list sum)",
+                     "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak if peak else None,
+                     "peak_source": "measured live: FP32 FMA-chain probe on this GPU "
+                                    "(MEASURED_PEAKS.json has no FP32 figure)",
+                     "flops_per_launch": flops_per_launch, "pairs": n_pairs,
+                     "avg_launch_ms": avg_pair_ms, "launches_timed": pair_n,
+                     "traffic": None},
+        "kernel_ms_in_timed_region": {k: v[0] for k, v in kt.items()},
+        "gpu_launches": int(lc1 - lc0),
+        "clocks": clk.summary(), "wall_s_timed": t_wall,
+    }
+    if rank == 0 and not args.no_cpu_baseline and world == 1:
+        result["cpu_baseline"] = cpu_baseline(xyz, L, state["bounds"], args)
+    return result
+
+
+# --------------------------------------------------------------------------
+# CPU baseline / reference arm: the FP64 oracle on the host cores
+# --------------------------------------------------------------------------
+def _oracle_step(O, c, box, xyz, xi, lo, hi, nthreads):
+    nb = O.neighbors_cutoff(box, xyz, RC)
+    op = O.Operator(matvec=(c, box, xyz, nb, O.SELF_BEAD, nthreads))
+    y, rep = O.cheb_inv_sqrt(op, xi, CHEB_MAX, lo, hi, CHEB_TOL)
+    dw = O.local_matvec(c, box, xyz, nb, y, O.SELF_BEAD, nthreads)
+    return rep, dw
+
+
+def cpu_baseline(xyz, L, bounds, args, steps=None):
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as O  # the checker, timed as the CPU baseline
+
+    O.build_oracle(with_ref=False)
+    nthreads = os.cpu_count() or 1
+    c = O.constants(alpha=ALPHA)
+    box = O.make_box([0] * 3, [L] * 3, [1, 1, 1])
+    if bounds is None:
+        nb = O.neighbors_cutoff(box, xyz, RC)
+        op = O.Operator(matvec=(c, box, xyz, nb, O.SELF_BEAD, nthreads))
+        lo, hi, _, _ = O.lanczos(op, np.random.default_rng(7).standard_normal(3 * len(xyz)), 24)
+        bounds = (lo / 1.05, hi * 1.05)
+    steps = steps or args.cpu_steps
+    rng = np.random.default_rng(11)
+    ts, terms = [], []
+    for s in range(steps):
+        xi = rng.standard_normal(3 * len(xyz))
+        t0 = time.perf_counter()
+        rep, _ = _oracle_step(O, c, box, xyz, xi, bounds[0], bounds[1], nthreads)
+        ts.append(time.perf_counter() - t0)
+        terms.append(rep.n_terms)
+    v = 1.0 / float(np.mean(ts))
+    return {"value": v, "unit": "Brownian steps/s", "cores": nthreads, "kind": "port",
+            "sample": f"{steps} full Brownian steps at N={len(xyz)} (cut-off list build + "
+                      f"reference-faithful Chebyshev, error check every term, + M y), FP64 "
+                      f"oracle with {nthreads} threads; terms {terms}",
+            "seconds": float(np.sum(ts))}
+
+
+def run_reference(args, rank, world):
+    import ggem_gb300 as G  # workload generator only (host code)
+    from ggem_gb300 import build as B
+
+    B.build()
+    xyz, L = G.make_suspension(SEED, N_BEADS, PHI)
+    budget_steps = max(1, min(args.steps, args.reference_max_steps))
+    cb = cpu_baseline(xyz, L, None, args, steps=budget_steps)
+    return {"metric": METRIC, "value": cb["value"], "unit": "Brownian steps/s", "n_gpus": world,
+            "steps": budget_steps, "warmup": 0, "ms_per_step": 1e3 / cb["value"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded)", "impl": "reference",
+            "config": workload_config({"parallelism": "host threads"}),
+            "cpu_baseline": cb,
+            "e2e": {"value": cb["value"], "unit": "Brownian steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--check-every", type=int, default=4)
+    ap.add_argument("--fp64-steps", type=int, default=2)
+    ap.add_argument("--skip-fp64", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--reference-max-steps", type=int, default=6)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        print(json.dumps(run_reference(args, rank, world)))
+        return
+    if world > 1:
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        torch.distributed.init_process_group("nccl")
+    res = run_gb300(args, rank, world)
+    if rank == 0:
+        print(json.dumps(res))
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,412 @@
+// ggem_cells.cu -- Kernel A: the sorted cell list and the cached FP32 pair
+// list.
+//
+// Replaces PointMesh::reinit (point_mesh.C:245-289): the element-point
+// containing list (:573-648) becomes a counting sort of particles by cell,
+// and the per-particle neighbour lists (:652-848) with their stored
+// displacement vectors (:220-241) become either an on-the-fly cell stencil
+// sweep (FP64 path) or a compact sliced-ELL list of (source slot, stencil
+// code) entries (FP32 path), built once per configuration.
+//
+// Bound: HBM.  Algorithmic bytes per particle of the cell build: 24 (read
+// xyz) + 4 (cell id) + 4 (order) + 4 (rank) + 32 (pos64) + 16 (pos32) plus
+// the scatter re-reads; the list build streams 4 B per listed pair twice.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "ggem_internal.cuh"
+
+namespace ggem {
+namespace {
+
+__device__ __forceinline__ int wrap_index(int k, int n) {
+  k %= n;
+  return k < 0 ? k + n : k;
+}
+
+// cell coordinate along one axis, as the oracle and the reference's element
+// search would compute it: floor((x - lo) / h), periodic axes wrapped first
+__global__ void k_assign(int64_t n, const double *__restrict__ xyz, Grid g,
+                         int32_t *__restrict__ cell_of, int32_t *__restrict__ count,
+                         double4_32a *__restrict__ wrapped, int *__restrict__ err) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double p[3];
+  int c[3];
+  bool bad = false;
+  for (int d = 0; d < 3; ++d) {
+    double x = xyz[3 * i + d];
+    double t = x - g.lo[d];
+    if (g.periodic[d]) {
+      t = fmod(t, g.L[d]);
+      if (t < 0) t += g.L[d];
+      if (t >= g.L[d]) t = 0.0;
+      // keep the caller's value when it already lies in the box
+      if (!(x >= g.lo[d] && x < g.lo[d] + g.L[d])) x = g.lo[d] + t;
+    } else if (!(t >= 0.0 && t <= g.L[d])) {
+      bad = true;
+    }
+    p[d] = x;
+    int k = (int)floor(t / g.h[d]);
+    c[d] = k < 0 ? 0 : (k >= g.nc[d] ? g.nc[d] - 1 : k);
+  }
+  if (bad) atomicOr(err, kErrOutOfDomain);
+  const int32_t id = c[0] + g.nc[0] * (c[1] + g.nc[1] * c[2]);
+  cell_of[i] = id;
+  atomicAdd(&count[id], 1);
+  wrapped[i] = make_double4_32a(p[0], p[1], p[2], 0.0);
+}
+
+// ---- exclusive scan (warp shuffles, 1024-element blocks) ----------------
+template <typename T>
+__global__ void k_scan_block(const T *__restrict__ in, T *__restrict__ out,
+                             int64_t *__restrict__ block_sums, int64_t n) {
+  __shared__ T warp_tot[32];
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  T v = (i < n) ? in[i] : T(0);
+  T x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    T y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warp_tot[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    const int nw = blockDim.x >> 5;
+    T w = (lane < nw) ? warp_tot[lane] : T(0);
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      T y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    if (lane < nw) warp_tot[lane] = w;  // inclusive warp prefix
+  }
+  __syncthreads();
+  const T base = warp ? warp_tot[warp - 1] : T(0);
+  if (i < n) out[i] = base + x - v;
+  if (threadIdx.x == blockDim.x - 1 && block_sums) block_sums[blockIdx.x] = (int64_t)(base + x);
+}
+
+template <typename T>
+__global__ void k_scan_add(T *__restrict__ out, const int64_t *__restrict__ block_off, int64_t n,
+                           const T *__restrict__ in, T *__restrict__ total_slot) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) {
+    out[i] += (T)block_off[blockIdx.x];
+    if (i == n - 1 && total_slot) *total_slot = out[i] + in[i];
+  }
+}
+
+template <typename T>
+__global__ void k_scan_total(T *__restrict__ out, const T *__restrict__ in, int64_t n) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) out[n] = (n > 0) ? out[n - 1] + in[n - 1] : T(0);
+}
+
+template <typename T>
+int scan_impl(ggem_ctx *c, const T *in, T *out, int64_t n, int level) {
+  const int B = 1024;
+  const int64_t nb = (n + B - 1) / B;
+  if (n <= 0) {
+    k_scan_total<T><<<1, 1, 0, c->stream>>>(out, in, 0);
+    return check_launch(c, "scan");
+  }
+  if ((int)c->scan_scratch.size() <= 2 * level + 1) {
+    c->scan_scratch.resize(2 * level + 2, nullptr);
+  }
+  for (int k = 0; k < 2; ++k)
+    if (!c->scan_scratch[2 * level + k]) c->scan_scratch[2 * level + k] = new DevBuf<int64_t>();
+  DevBuf<int64_t> &sums = *c->scan_scratch[2 * level];
+  DevBuf<int64_t> &offs = *c->scan_scratch[2 * level + 1];
+  cudaError_t e = sums.ensure(nb + 1);
+  if (e == cudaSuccess) e = offs.ensure(nb + 1);
+  if (e != cudaSuccess) return cuda_fail(c, e, "scan scratch");
+  k_scan_block<T><<<(unsigned)nb, B, 0, c->stream>>>(in, out, sums.p, n);
+  int rc = check_launch(c, "scan block");
+  if (rc) return rc;
+  if (nb > 1) {
+    rc = scan_impl<int64_t>(c, sums.p, offs.p, nb, level + 1);
+    if (rc) return rc;
+    k_scan_add<T><<<(unsigned)nb, B, 0, c->stream>>>(out, offs.p, n, in, out + n);
+    return check_launch(c, "scan add");
+  }
+  k_scan_total<T><<<1, 1, 0, c->stream>>>(out, in, n);
+  return check_launch(c, "scan total");
+}
+
+__global__ void k_scatter(int64_t n, const int32_t *__restrict__ cell_of,
+                          const int32_t *__restrict__ start, int32_t *__restrict__ fill,
+                          int32_t *__restrict__ order) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int32_t cid = cell_of[i];
+  const int32_t slot = start[cid] + atomicAdd(&fill[cid], 1);
+  order[slot] = (int32_t)i;
+}
+
+// ascending particle id inside each cell (deterministic slot order, and the
+// order of build_elem_point_containing_list, point_mesh.C:585-631)
+__global__ void k_sort_cells(int64_t ncell, const int32_t *__restrict__ start,
+                             int32_t *__restrict__ order) {
+  const int64_t cidx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (cidx >= ncell) return;
+  const int32_t b = start[cidx], e = start[cidx + 1];
+  for (int32_t k = b + 1; k < e; ++k) {
+    const int32_t v = order[k];
+    int32_t m = k - 1;
+    while (m >= b && order[m] > v) {
+      order[m + 1] = order[m];
+      --m;
+    }
+    order[m + 1] = v;
+  }
+}
+
+__global__ void k_gather_sorted(int64_t n, Grid g, const int32_t *__restrict__ order,
+                                const int32_t *__restrict__ cell_of,
+                                const double4_32a *__restrict__ wrapped,
+                                int32_t *__restrict__ rank, double4_32a *__restrict__ pos64,
+                                float4 *__restrict__ pos32) {
+  const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const int32_t i = order[s];
+  rank[i] = (int32_t)s;
+  const double4_32a p = wrapped[i];
+  pos64[s] = p;
+  const int32_t cid = cell_of[i];
+  const int cx = cid % g.nc[0], cy = (cid / g.nc[0]) % g.nc[1], cz = cid / (g.nc[0] * g.nc[1]);
+  // position relative to the cell centre: |rel| <= h/2 keeps FP32 exact to
+  // ~1e-7 of h whatever the box size
+  const double rx = p.x - (g.lo[0] + (cx + 0.5) * g.h[0]);
+  const double ry = p.y - (g.lo[1] + (cy + 0.5) * g.h[1]);
+  const double rz = p.z - (g.lo[2] + (cz + 0.5) * g.h[2]);
+  pos32[s] = make_float4((float)rx, (float)ry, (float)rz, __int_as_float(cid));
+}
+
+// neighbour cell of cell coordinate (cx,cy,cz) shifted by o; -1 if outside a
+// non-periodic axis
+__device__ __forceinline__ int32_t shifted_cell(const Grid &g, int cx, int cy, int cz, int4 o) {
+  int c[3] = {cx + o.x, cy + o.y, cz + o.z};
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    if (c[d] < 0 || c[d] >= g.nc[d]) {
+      if (!g.periodic[d]) return -1;
+      c[d] = wrap_index(c[d], g.nc[d]);
+    }
+  }
+  return c[0] + g.nc[0] * (c[1] + g.nc[1] * c[2]);
+}
+
+// exact FP64 cut-off decision, the oracle's predicate: minimum-image vector
+// (pm_periodic_boundary.C:350-374) and (dx*dx + dy*dy) + dz*dz < rc^2
+// without contraction
+__device__ __forceinline__ bool exact_within(const Grid &g, double4_32a a, double4_32a b, double rc2) {
+  double d[3] = {b.x - a.x, b.y - a.y, b.z - a.z};
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    if (g.periodic[k]) {
+      const double xs = g.L[k];
+      if (d[k] <= -xs / 2.0) d[k] += xs;
+      if (d[k] > xs / 2.0) d[k] -= xs;
+    }
+  }
+  const double r2 = __dadd_rn(__dadd_rn(__dmul_rn(d[0], d[0]), __dmul_rn(d[1], d[1])),
+                              __dmul_rn(d[2], d[2]));
+  return r2 < rc2;
+}
+
+// Pass 1 (count) and pass 2 (fill) of the pair list: one thread per target
+// slot; FP32 cell-relative distance classifies a candidate unless it falls
+// in the rounding band around rc^2, where the exact FP64 test decides.
+template <bool FILL>
+__global__ void k_pair_list(int64_t n, Grid g, const int4 *__restrict__ stencil, int nst,
+                            const float4 *__restrict__ shift, const int32_t *__restrict__ start,
+                            const float4 *__restrict__ pos32, const double4_32a *__restrict__ pos64,
+                            float rc2_lo, float rc2_hi, double rc2,
+                            int32_t *__restrict__ count, const int64_t *__restrict__ slice_off,
+                            const int32_t *__restrict__ slice_width,
+                            uint32_t *__restrict__ list, int *__restrict__ err) {
+  const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const float4 pi = pos32[s];
+  const int32_t cid = __float_as_int(pi.w);
+  const int cx = cid % g.nc[0], cy = (cid / g.nc[0]) % g.nc[1], cz = cid / (g.nc[0] * g.nc[1]);
+  int32_t cnt = 0;
+  int64_t base = 0;
+  int32_t width = 0;
+  const int lane = (int)(s & (kSlice - 1));
+  if (FILL) {
+    base = slice_off[s / kSlice];
+    width = slice_width[s / kSlice];
+  }
+  double4_32a pi64 = make_double4_32a(0, 0, 0, 0);
+  bool have64 = false;
+  for (int k = 0; k < nst; ++k) {
+    const int32_t nc = shifted_cell(g, cx, cy, cz, stencil[k]);
+    if (nc < 0) continue;
+    const float4 sh = shift[k];
+    const int32_t b = start[nc], e = start[nc + 1];
+    for (int32_t t = b; t < e; ++t) {
+      if (t == s) continue;
+      const float4 pj = pos32[t];
+      const float dx = (pj.x - pi.x) + sh.x;
+      const float dy = (pj.y - pi.y) + sh.y;
+      const float dz = (pj.z - pi.z) + sh.z;
+      const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+      bool in;
+      if (r2 < rc2_lo) in = true;
+      else if (r2 > rc2_hi) in = false;
+      else {
+        if (!have64) {
+          pi64 = pos64[s];
+          have64 = true;
+        }
+        in = exact_within(g, pi64, pos64[t], rc2);
+      }
+      if (!in) continue;
+      if (FILL) {
+        if (cnt < width) list[base + (int64_t)cnt * kSlice + lane] = ((uint32_t)t << kCodeBits) | (uint32_t)k;
+        else atomicOr(err, kErrListOverflow);
+      }
+      ++cnt;
+    }
+  }
+  if (!FILL) count[s] = cnt;
+  else {
+    for (int32_t m = cnt; m < width; ++m) list[base + (int64_t)m * kSlice + lane] = kPad;
+  }
+}
+
+__global__ void k_slice_width(int64_t n, int64_t nslice, const int32_t *__restrict__ count,
+                              int32_t *__restrict__ width, int64_t *__restrict__ width_x32) {
+  const int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (w >= nslice) return;
+  const int64_t s = w * kSlice + lane;
+  int v = (s < n) ? count[s] : 0;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+  if (lane == 0) {
+    width[w] = v;
+    width_x32[w] = (int64_t)v * kSlice;
+  }
+}
+
+}  // namespace
+
+int device_exclusive_scan_i32(ggem_ctx *c, const int32_t *in, int32_t *out, int64_t n) {
+  return scan_impl<int32_t>(c, in, out, n, 0);
+}
+int device_exclusive_scan_i64(ggem_ctx *c, const int64_t *in, int64_t *out, int64_t n) {
+  return scan_impl<int64_t>(c, in, out, n, 0);
+}
+
+int build_cells(ggem_ctx *c) {
+  const int64_t n = c->n;
+  const Grid &g = c->grid;
+  cudaError_t e = cudaSuccess;
+  if ((e = c->cell_of.ensure(n)) || (e = c->cell_count.ensure(g.ncell)) ||
+      (e = c->cell_fill.ensure(g.ncell)) || (e = c->cell_start.ensure(g.ncell + 1)) ||
+      (e = c->order.ensure(n)) || (e = c->rank.ensure(n)) || (e = c->wrapped.ensure(n)) ||
+      (e = c->pos64.ensure(n)) || (e = c->pos32.ensure(n)))
+    return cuda_fail(c, e, "cell buffers");
+  cudaStream_t st = c->stream;
+  if ((e = cudaMemsetAsync(c->cell_count.p, 0, sizeof(int32_t) * g.ncell, st)) ||
+      (e = cudaMemsetAsync(c->cell_fill.p, 0, sizeof(int32_t) * g.ncell, st)) ||
+      (e = cudaMemsetAsync(c->err.p, 0, sizeof(int), st)))
+    return cuda_fail(c, e, "cell memset");
+  const int T = 256;
+  const unsigned bn = (unsigned)((n + T - 1) / T);
+  if (n > 0) {
+    k_assign<<<bn, T, 0, st>>>(n, c->xyz_in.p, g, c->cell_of.p, c->cell_count.p, c->wrapped.p,
+                               c->err.p);
+    if (int rc = check_launch(c, "assign")) return rc;
+  }
+  if (int rc = device_exclusive_scan_i32(c, c->cell_count.p, c->cell_start.p, g.ncell)) return rc;
+  if (n > 0) {
+    k_scatter<<<bn, T, 0, st>>>(n, c->cell_of.p, c->cell_start.p, c->cell_fill.p, c->order.p);
+    if (int rc = check_launch(c, "scatter")) return rc;
+    k_sort_cells<<<(unsigned)((g.ncell + T - 1) / T), T, 0, st>>>(g.ncell, c->cell_start.p,
+                                                                   c->order.p);
+    if (int rc = check_launch(c, "sort cells")) return rc;
+    k_gather_sorted<<<bn, T, 0, st>>>(n, g, c->order.p, c->cell_of.p, c->wrapped.p, c->rank.p,
+                                      c->pos64.p, c->pos32.p);
+    if (int rc = check_launch(c, "gather sorted")) return rc;
+  }
+  int flags = 0;
+  if (int rc = read_error_flags(c, &flags)) return rc;
+  if (flags & kErrOutOfDomain)
+    return fail(c, GGEM_ERR_OUT_OF_DOMAIN,
+                "a particle lies outside the box on a non-periodic axis "
+                "(point_mesh.C:602-613: no element contains it)");
+  c->cells_built = true;
+  c->list_built = false;
+  return GGEM_OK;
+}
+
+int build_pair_list(ggem_ctx *c) {
+  const int64_t n = c->n;
+  const int64_t nslice = (n + kSlice - 1) / kSlice;
+  cudaError_t e = cudaSuccess;
+  if ((e = c->nb_count.ensure(n)) || (e = c->slice_width.ensure(nslice)) ||
+      (e = c->slice_off.ensure(2 * nslice + 1)))
+    return cuda_fail(c, e, "pair list buffers");
+  cudaStream_t st = c->stream;
+  if (n == 0) {
+    if ((e = cudaMemsetAsync(c->slice_off.p, 0, sizeof(int64_t), st)))
+      return cuda_fail(c, e, "memset");
+    c->n_pairs = 0;
+    c->list_built = true;
+    return GGEM_OK;
+  }
+  const int T = 256;
+  const unsigned bn = (unsigned)((n + T - 1) / T);
+  const int nst = (int)c->stencil.size();
+  if ((e = cudaMemsetAsync(c->err.p, 0, sizeof(int), st))) return cuda_fail(c, e, "memset");
+  kt_start(c, kKListBuild);
+  k_pair_list<false><<<bn, T, 0, st>>>(n, c->grid, c->d_stencil.p, nst, c->d_shift.p,
+                                        c->cell_start.p, c->pos32.p, c->pos64.p, c->rc2_lo,
+                                        c->rc2_hi, c->rc2, c->nb_count.p, nullptr, nullptr,
+                                        nullptr, c->err.p);
+  if (int rc = check_launch(c, "pair count")) return rc;
+  int64_t *width_x32 = c->slice_off.p + nslice + 1;
+  k_slice_width<<<(unsigned)((nslice * 32 + T - 1) / T), T, 0, st>>>(
+      n, nslice, c->nb_count.p, c->slice_width.p, width_x32);
+  if (int rc = check_launch(c, "slice width")) return rc;
+  if (int rc = device_exclusive_scan_i64(c, width_x32, c->slice_off.p, nslice)) return rc;
+  int64_t total = 0;
+  if ((e = cudaMemcpyAsync(&total, c->slice_off.p + nslice, sizeof(int64_t),
+                           cudaMemcpyDeviceToHost, st)) ||
+      (e = cudaStreamSynchronize(st)))
+    return cuda_fail(c, e, "list size");
+  if ((e = c->nb_list.ensure((size_t)std::max<int64_t>(total, 1))))
+    return cuda_fail(c, e, "pair list");
+  k_pair_list<true><<<bn, T, 0, st>>>(n, c->grid, c->d_stencil.p, nst, c->d_shift.p,
+                                       c->cell_start.p, c->pos32.p, c->pos64.p, c->rc2_lo,
+                                       c->rc2_hi, c->rc2, c->nb_count.p, c->slice_off.p,
+                                       c->slice_width.p, c->nb_list.p, c->err.p);
+  kt_stop(c, kKListBuild);
+  if (int rc = check_launch(c, "pair fill")) return rc;
+  int flags = 0;
+  if (int rc = read_error_flags(c, &flags)) return rc;
+  if (flags & kErrListOverflow)
+    return fail(c, GGEM_ERR_CELL_OVERFLOW, "pair list fill exceeded its counted width");
+  // total ordered pairs
+  std::vector<int32_t> cnt(n > 0 ? n : 1);
+  if (n > 0) {
+    if ((e = cudaMemcpyAsync(cnt.data(), c->nb_count.p, sizeof(int32_t) * n,
+                             cudaMemcpyDeviceToHost, st)) ||
+        (e = cudaStreamSynchronize(st)))
+      return cuda_fail(c, e, "pair count");
+  }
+  int64_t np = 0;
+  for (int64_t i = 0; i < n; ++i) np += cnt[i];
+  c->n_pairs = np;
+  c->list_built = true;
+  return GGEM_OK;
+}
+
+}  // namespace ggem

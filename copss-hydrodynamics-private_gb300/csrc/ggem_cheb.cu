@@ -1,0 +1,569 @@
+// ggem_cheb.cu -- Kernel C: the FP64 Chebyshev M^{-1/2} xi recurrence, the
+// Lanczos spectral bounds, power iteration and the device noise generator.
+//
+// Vectors live on the device in slot order ([r][3n] doubles); the pair sums
+// come from ggem_pair.cu.  The recurrence is fused into one pass per term
+// (x_{k+1}, y += c_k x_{k+1} and both norms), bound by HBM/L2:
+// 40 B x 3n per right-hand side per term of algorithmic traffic.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "ggem_internal.cuh"
+
+namespace ggem {
+namespace {
+
+constexpr int kMaxRhs = 64;
+constexpr int kVecThreads = 256;
+
+struct RhsCoef {
+  double c[kMaxRhs];
+};
+
+int vec_blocks(int64_t D) {
+  int64_t g = (D + 4 * kVecThreads - 1) / (4 * kVecThreads);
+  return (int)std::max<int64_t>(1, std::min<int64_t>(g, 592));
+}
+
+__device__ __forceinline__ double block_sum(double v, double *sh) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if (lane == 0) sh[warp] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (warp == 0) {
+    t = (lane < (int)(blockDim.x >> 5)) ? sh[lane] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+  }
+  __syncthreads();
+  return t;  // valid in thread 0
+}
+
+// partial[r][blockIdx.x] = sum_k a[r][k] * b[r][k]
+__global__ void __launch_bounds__(kVecThreads) k_dot_partials(int64_t D, const double *__restrict__ a,
+                                                              const double *__restrict__ b,
+                                                              double *__restrict__ partial) {
+  __shared__ double sh[32];
+  const int r = blockIdx.y;
+  const double *pa = a + (int64_t)r * D, *pb = b + (int64_t)r * D;
+  double acc = 0.0;
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < D;
+       k += (int64_t)gridDim.x * blockDim.x)
+    acc += pa[k] * pb[k];
+  const double t = block_sum(acc, sh);
+  if (threadIdx.x == 0) partial[(int64_t)r * gridDim.x + blockIdx.x] = t;
+}
+
+// out[q] = sum_b partial[q][b], fixed order (deterministic)
+__global__ void __launch_bounds__(kVecThreads) k_finalize(int G, const double *__restrict__ partial,
+                                                          double *__restrict__ out) {
+  __shared__ double sh[32];
+  const int q = blockIdx.x;
+  double acc = 0.0;
+  for (int b = threadIdx.x; b < G; b += blockDim.x) acc += partial[(int64_t)q * G + b];
+  const double t = block_sum(acc, sh);
+  if (threadIdx.x == 0) out[q] = t;
+}
+
+// x1 = db * x0 + da * x1   (VecAXPBY(x1, db, da, x0), brownian_system.C:1041)
+__global__ void k_cheb_first(int64_t D, int nrhs, double da, double db,
+                             const double *__restrict__ x0, double *__restrict__ x1) {
+  const int64_t tot = D * nrhs;
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < tot;
+       k += (int64_t)gridDim.x * blockDim.x)
+    x1[k] = db * x0[k] + da * x1[k];
+}
+
+// dw = c0 x0 (norm -> q0), dw += c1 x1, ||x1|| -> q1  (brownian_system.C:1050-1056)
+__global__ void __launch_bounds__(kVecThreads) k_cheb_init(int64_t D, double c0, double c1,
+                                                           const double *__restrict__ x0,
+                                                           const double *__restrict__ x1,
+                                                           double *__restrict__ dw,
+                                                           double *__restrict__ partial) {
+  __shared__ double sh[32];
+  const int r = blockIdx.y, nrhs = gridDim.y;
+  const int64_t off = (int64_t)r * D;
+  double a4 = 0.0, a3 = 0.0;
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < D;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    const double t = c0 * x0[off + k];
+    a4 += t * t;
+    const double v = x1[off + k];
+    dw[off + k] = t + c1 * v;
+    a3 += v * v;
+  }
+  const double s4 = block_sum(a4, sh);
+  const double s3 = block_sum(a3, sh);
+  if (threadIdx.x == 0) {
+    partial[(int64_t)(0 * nrhs + r) * gridDim.x + blockIdx.x] = s4;
+    partial[(int64_t)(1 * nrhs + r) * gridDim.x + blockIdx.x] = s3;
+  }
+}
+
+// one term (brownian_system.C:1091-1108):
+//   ||dw|| -> q0 ; xm = (2db x1 + 2da xm) - x0 ; dw += c[r] xm ; ||xm|| -> q1
+__global__ void __launch_bounds__(kVecThreads) k_cheb_term(int64_t D, double two_da,
+                                                           double two_db, RhsCoef cf,
+                                                           const double *__restrict__ x0,
+                                                           const double *__restrict__ x1,
+                                                           double *__restrict__ xm,
+                                                           double *__restrict__ dw,
+                                                           double *__restrict__ partial) {
+  __shared__ double sh[32];
+  const int r = blockIdx.y, nrhs = gridDim.y;
+  const int64_t off = (int64_t)r * D;
+  const double c = cf.c[r];
+  double a4 = 0.0, a3 = 0.0;
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < D;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    const double y = dw[off + k];
+    a4 += y * y;
+    double v = two_db * x1[off + k] + two_da * xm[off + k];
+    v -= x0[off + k];
+    xm[off + k] = v;
+    dw[off + k] = y + c * v;
+    a3 += v * v;
+  }
+  const double s4 = block_sum(a4, sh);
+  const double s3 = block_sum(a3, sh);
+  if (threadIdx.x == 0) {
+    partial[(int64_t)(0 * nrhs + r) * gridDim.x + blockIdx.x] = s4;
+    partial[(int64_t)(1 * nrhs + r) * gridDim.x + blockIdx.x] = s3;
+  }
+}
+
+__global__ void k_copy(int64_t tot, const double *__restrict__ a, double *__restrict__ b) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < tot;
+       k += (int64_t)gridDim.x * blockDim.x)
+    b[k] = a[k];
+}
+
+__global__ void k_scale(int64_t tot, double s, const double *__restrict__ a, double *__restrict__ b) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < tot;
+       k += (int64_t)gridDim.x * blockDim.x)
+    b[k] = a[k] * s;
+}
+
+__global__ void k_fill(int64_t tot, double v, double *__restrict__ b) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < tot;
+       k += (int64_t)gridDim.x * blockDim.x)
+    b[k] = v;
+}
+
+// b = a + s * b
+__global__ void k_axpy_into(int64_t tot, double s, const double *__restrict__ a,
+                            double *__restrict__ b) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < tot;
+       k += (int64_t)gridDim.x * blockDim.x)
+    b[k] = b[k] + s * a[k];
+}
+
+// Lanczos: partial[i][b] = Q_i . w for i < m
+__global__ void __launch_bounds__(kVecThreads) k_multi_dot(int64_t D, const double *__restrict__ Q,
+                                                           const double *__restrict__ w,
+                                                           double *__restrict__ partial) {
+  __shared__ double sh[32];
+  const int i = blockIdx.y;
+  const double *q = Q + (int64_t)i * D;
+  double acc = 0.0;
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < D;
+       k += (int64_t)gridDim.x * blockDim.x)
+    acc += q[k] * w[k];
+  const double t = block_sum(acc, sh);
+  if (threadIdx.x == 0) partial[(int64_t)i * gridDim.x + blockIdx.x] = t;
+}
+
+// w -= sum_i h_i Q_i
+__global__ void k_sub_proj(int64_t D, int m, const double *__restrict__ Q,
+                           const double *__restrict__ h, double *__restrict__ w) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < D;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    double v = w[k];
+    for (int i = 0; i < m; ++i) v -= h[i] * Q[(int64_t)i * D + k];
+    w[k] = v;
+  }
+}
+
+// Philox4x32-10 (Salmon et al., SC'11) + Box-Muller
+__device__ __forceinline__ void philox10(uint32_t c[4], uint32_t k0, uint32_t k1) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    const uint32_t hi0 = __umulhi(0xD2511F53u, c[0]), lo0 = 0xD2511F53u * c[0];
+    const uint32_t hi1 = __umulhi(0xCD9E8D57u, c[2]), lo1 = 0xCD9E8D57u * c[2];
+    const uint32_t n0 = hi1 ^ c[1] ^ k0;
+    const uint32_t n2 = hi0 ^ c[3] ^ k1;
+    c[0] = n0;
+    c[1] = lo1;
+    c[2] = n2;
+    c[3] = lo0;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+}
+
+__global__ void k_philox_normals(int64_t n, uint64_t seed, uint64_t stream,
+                                 double *__restrict__ out) {
+  const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (2 * p >= n) return;
+  uint32_t c[4] = {(uint32_t)p, (uint32_t)((uint64_t)p >> 32), (uint32_t)stream,
+                   (uint32_t)(stream >> 32)};
+  philox10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+  const uint64_t a = ((uint64_t)c[0] << 21) ^ (c[1] >> 11);
+  const uint64_t b = ((uint64_t)c[2] << 21) ^ (c[3] >> 11);
+  const double u1 = ((double)a + 0.5) * 0x1.0p-53;
+  const double u2 = ((double)b + 0.5) * 0x1.0p-53;
+  const double r = sqrt(-2.0 * log(u1));
+  const double two_pi = 6.283185307179586476925286766559;
+  double sn, cs;
+  sincos(two_pi * u2, &sn, &cs);
+  out[2 * p] = r * cs;
+  if (2 * p + 1 < n) out[2 * p + 1] = r * sn;
+}
+
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    cudaGetDevice(&prev);
+    if (prev != dev) cudaSetDevice(dev);
+  }
+  ~DeviceGuard() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+};
+
+int grid1(int64_t tot) {
+  return (int)std::max<int64_t>(1, std::min<int64_t>((tot + 255) / 256, 4096));
+}
+
+// results[q] of the partial arrays, copied to the pinned host mirror
+int finalize_to_host(ggem_ctx *c, int nq, int G, double *host) {
+  double *out = c->w_red.p + (size_t)nq * G;
+  k_finalize<<<nq, kVecThreads, 0, c->stream>>>(G, c->w_red.p, out);
+  if (int rc = check_launch(c, "finalize")) return rc;
+  cudaError_t e = cudaMemcpyAsync(host, out, sizeof(double) * nq, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e) return cuda_fail(c, e, "reduction readback");
+  return GGEM_OK;
+}
+
+int sumsq_to_host(ggem_ctx *c, int nrhs, int64_t D, const double *v, double *host) {
+  const int G = vec_blocks(D);
+  k_dot_partials<<<dim3(G, nrhs), kVecThreads, 0, c->stream>>>(D, v, v, c->w_red.p);
+  if (int rc = check_launch(c, "sumsq")) return rc;
+  return finalize_to_host(c, nrhs, G, host);
+}
+
+int dot_to_host(ggem_ctx *c, int nrhs, int64_t D, const double *a, const double *b, double *host) {
+  const int G = vec_blocks(D);
+  k_dot_partials<<<dim3(G, nrhs), kVecThreads, 0, c->stream>>>(D, a, b, c->w_red.p);
+  if (int rc = check_launch(c, "dot")) return rc;
+  return finalize_to_host(c, nrhs, G, host);
+}
+
+int brownian_self_mode(const ggem_ctx *c) {
+  // the mobility of _MatMult_Stokes: compute_point_velocity adds -coeff_1 f + f
+  // for beads (pm_system_stokes.C:450-453); Lagrangian points carry G(0) f in
+  // local_solution_bead (ggem_stokes.C:485-499)
+  return c->prm.point_type == GGEM_LAGRANGIAN_POINT ? GGEM_SELF_LAGRANGIAN : GGEM_SELF_BEAD;
+}
+
+int ensure_cheb_buffers(ggem_ctx *c, size_t len) {
+  cudaError_t e;
+  if ((e = c->w_in.ensure(len)) || (e = c->w_out.ensure(len)) || (e = c->w_c.ensure(len)) ||
+      (e = c->w_d.ensure(len)) || (e = c->w_e.ensure(len)) || (e = c->w_y.ensure(len)) ||
+      (e = c->w_red.ensure(4 * kMaxRhs * 600)))
+    return cuda_fail(c, e, "chebyshev workspace");
+  return GGEM_OK;
+}
+
+// Chebyshev on slot-ordered xi (c->w_in); leaves y in c->w_y
+int cheb_slots(ggem_ctx *c, int nrhs, int N, double eig_min, double eig_max, double tol,
+               int check_every, ggem_cheb_report *rep) {
+  const int64_t D = 3 * c->n;
+  const int64_t tot = D * nrhs;
+  const int sm = brownian_self_mode(c);
+  const int G = vec_blocks(D);
+  cudaStream_t st = c->stream;
+  double *x0 = c->w_c.p, *x1 = c->w_d.p, *xm = c->w_e.p, *dw = c->w_y.p, *dm = c->w_out.p;
+  // brownian_system.C:1001-1003 and the coefficients of :1021-1024
+  const double d_eig = eig_max - eig_min;
+  const double da = 2.0 / d_eig;
+  const double db = -(eig_max + eig_min) / d_eig;
+  std::vector<double> X(N + 1);
+  cheb_coeffs_host(N, da, db, GGEM_CHEB_GAUSS, X.data());
+  std::vector<double> aux2(nrhs), aux1(nrhs), aux3(nrhs), aux4(nrhs);
+  std::vector<int> active(nrhs, 1);
+  for (int r = 0; r < nrhs; ++r) rep[r] = ggem_cheb_report{0, 1, 0, 0.0, 0.0};
+  double *h = c->h_red;
+  // x0 = xi; x1 = M x0; aux2 = x1.x0; x1 = db x0 + da x1
+  k_copy<<<grid1(tot), 256, 0, st>>>(tot, c->w_in.p, x0);
+  if (int rc = check_launch(c, "copy")) return rc;
+  if (int rc = matvec_slots(c, nrhs, x0, x1, sm)) return rc;
+  if (int rc = dot_to_host(c, nrhs, D, x1, x0, h)) return rc;
+  for (int r = 0; r < nrhs; ++r) aux2[r] = h[r];
+  k_cheb_first<<<grid1(tot), 256, 0, st>>>(D, nrhs, da, db, x0, x1);
+  if (int rc = check_launch(c, "cheb first")) return rc;
+  k_cheb_init<<<dim3(G, nrhs), kVecThreads, 0, st>>>(D, X[0], X[1], x0, x1, dw, c->w_red.p);
+  if (int rc = check_launch(c, "cheb init")) return rc;
+  if (int rc = finalize_to_host(c, 2 * nrhs, G, h)) return rc;
+  for (int r = 0; r < nrhs; ++r) {
+    aux4[r] = std::sqrt(h[r]);
+    aux3[r] = std::sqrt(h[nrhs + r]) * std::fabs(X[1]);
+  }
+  if (int rc = matvec_slots(c, nrhs, dw, dm, sm)) return rc;
+  if (int rc = sumsq_to_host(c, nrhs, D, dm, h)) return rc;
+  for (int r = 0; r < nrhs; ++r) {
+    aux1[r] = h[r];
+    rep[r].n_matvecs = 2;
+    if (aux2[r] != 0.0) rep[r].err1 = std::sqrt(std::fabs(aux1[r] - aux2[r]) / aux2[r]);
+    if (aux4[r] != 0.0) rep[r].err2 = aux3[r] / aux4[r];
+  }
+  const double two_da = 2. * da, two_db = 2. * db;
+  int n_active = nrhs;
+  for (int i = 1; i < N && n_active > 0; ++i) {
+    if (int rc = matvec_slots(c, nrhs, x1, xm, sm)) return rc;
+    RhsCoef cf;
+    for (int r = 0; r < nrhs; ++r) cf.c[r] = active[r] ? X[i + 1] : 0.0;
+    kt_start(c, kKChebTerm);
+    k_cheb_term<<<dim3(G, nrhs), kVecThreads, 0, st>>>(D, two_da, two_db, cf, x0, x1, xm, dw,
+                                                        c->w_red.p);
+    kt_stop(c, kKChebTerm);
+    if (int rc = check_launch(c, "cheb term")) return rc;
+    if (int rc = finalize_to_host(c, 2 * nrhs, G, h)) return rc;
+    for (int r = 0; r < nrhs; ++r) {
+      if (!active[r]) continue;
+      aux4[r] = std::sqrt(h[r]);
+      aux3[r] = std::sqrt(h[nrhs + r]) * std::fabs(X[i + 1]);
+      rep[r].n_matvecs += 1;
+      rep[r].n_terms = i + 1;
+      if (aux4[r] != 0.0) rep[r].err2 = aux3[r] / aux4[r];
+    }
+    const bool check = (check_every <= 1) || (i % check_every == 0) || (i == N - 1);
+    if (check) {
+      if (int rc = matvec_slots(c, nrhs, dw, dm, sm)) return rc;
+      if (int rc = sumsq_to_host(c, nrhs, D, dm, h)) return rc;
+    }
+    for (int r = 0; r < nrhs; ++r) {
+      if (!active[r]) continue;
+      if (check) {
+        rep[r].n_matvecs += 1;
+        aux1[r] = h[r];
+        if (aux2[r] != 0.0) rep[r].err1 = std::sqrt(std::fabs(aux1[r] - aux2[r]) / aux2[r]);
+        if (rep[r].err1 <= tol) {  // brownian_system.C:1138-1147
+          rep[r].converged = 1;
+          active[r] = 0;
+          --n_active;
+          continue;
+        }
+      }
+      if (rep[r].err2 <= 1E-9) {  // :1150
+        active[r] = 0;
+        --n_active;
+      }
+    }
+    // x0 <- x1, x1 <- xm (:1152-1153) by rotating the buffers
+    double *t = x0;
+    x0 = x1;
+    x1 = xm;
+    xm = t;
+  }
+  return GGEM_OK;
+}
+
+}  // namespace
+}  // namespace ggem
+
+using namespace ggem;
+
+static int cheb_common(ggem_ctx *ctx, int nrhs, int N, double eig_min, double eig_max,
+                       double tol, int check_every, ggem_cheb_report *rep) {
+  if (!ctx || nrhs < 1 || nrhs > kMaxRhs || N < 1 || !rep || !(tol >= 0))
+    return ggem::fail(ctx, GGEM_ERR_BAD_ARG, "chebyshev: bad arguments (nrhs in [1, 64], N >= 1)");
+  if (!(eig_min >= 0) || !(eig_max >= 0) || !(eig_min < eig_max))
+    return ggem::fail(ctx, GGEM_ERR_INVALID_RANGE, "invalid eigenvalue range (copss.C:1609-1615)");
+  if (!ctx->cells_built || (ctx->prm.precision == GGEM_FP32 && !ctx->list_built))
+    return ggem::fail(ctx, GGEM_ERR_BAD_ARG, "call ggem_build_cells first");
+  return GGEM_OK;
+}
+
+extern "C" int ggem_cheb_inv_sqrt_dev(ggem_ctx *ctx, int nrhs, int N, double eig_min,
+                                      double eig_max, double tol_cheb, int check_every,
+                                      double *d_xi, ggem_cheb_report *rep) {
+  if (int rc = cheb_common(ctx, nrhs, N, eig_min, eig_max, tol_cheb, check_every, rep)) return rc;
+  DeviceGuard dg(ctx->device);
+  const size_t len = (size_t)ctx->n * 3 * nrhs;
+  if (int rc = ensure_cheb_buffers(ctx, len)) return rc;
+  if (int rc = permute_to_slots(ctx, nrhs, d_xi, ctx->w_in.p)) return rc;
+  if (int rc = cheb_slots(ctx, nrhs, N, eig_min, eig_max, tol_cheb, check_every, rep)) return rc;
+  return permute_from_slots(ctx, nrhs, ctx->w_y.p, d_xi);
+}
+
+extern "C" int ggem_cheb_inv_sqrt(ggem_ctx *ctx, int nrhs, int N, double eig_min, double eig_max,
+                                  double tol_cheb, int check_every, double *xi,
+                                  ggem_cheb_report *rep) {
+  if (int rc = cheb_common(ctx, nrhs, N, eig_min, eig_max, tol_cheb, check_every, rep)) return rc;
+  if (!xi && ctx->n) return GGEM_ERR_BAD_ARG;
+  DeviceGuard dg(ctx->device);
+  const size_t len = (size_t)ctx->n * 3 * nrhs;
+  cudaError_t e = ctx->w_a.ensure(len);
+  if (e) return cuda_fail(ctx, e, "cheb io");
+  if (len && (e = cudaMemcpyAsync(ctx->w_a.p, xi, 8 * len, cudaMemcpyHostToDevice, ctx->stream)))
+    return cuda_fail(ctx, e, "cheb h2d");
+  if (int rc = ggem_cheb_inv_sqrt_dev(ctx, nrhs, N, eig_min, eig_max, tol_cheb, check_every,
+                                      ctx->w_a.p, rep))
+    return rc;
+  if (len && (e = cudaMemcpyAsync(xi, ctx->w_a.p, 8 * len, cudaMemcpyDeviceToHost, ctx->stream)))
+    return cuda_fail(ctx, e, "cheb d2h");
+  if ((e = cudaStreamSynchronize(ctx->stream))) return cuda_fail(ctx, e, "cheb sync");
+  return GGEM_OK;
+}
+
+extern "C" int ggem_brownian_displacement(ggem_ctx *ctx, int nrhs, int N, double eig_min,
+                                          double eig_max, double tol_cheb, int check_every,
+                                          const double *xi, double *dw, ggem_cheb_report *rep) {
+  if (int rc = cheb_common(ctx, nrhs, N, eig_min, eig_max, tol_cheb, check_every, rep)) return rc;
+  if (ctx->n && (!xi || !dw)) return GGEM_ERR_BAD_ARG;
+  DeviceGuard dg(ctx->device);
+  const size_t len = (size_t)ctx->n * 3 * nrhs;
+  cudaError_t e;
+  if ((e = ctx->w_a.ensure(len)) || (e = ctx->w_b.ensure(len))) return cuda_fail(ctx, e, "bd io");
+  if (len && (e = cudaMemcpyAsync(ctx->w_a.p, xi, 8 * len, cudaMemcpyHostToDevice, ctx->stream)))
+    return cuda_fail(ctx, e, "bd h2d");
+  int rc = ggem_brownian_displacement_dev(ctx, nrhs, N, eig_min, eig_max, tol_cheb, check_every,
+                                          ctx->w_a.p, ctx->w_b.p, rep);
+  if (rc) return rc;
+  if (len && (e = cudaMemcpyAsync(dw, ctx->w_b.p, 8 * len, cudaMemcpyDeviceToHost, ctx->stream)))
+    return cuda_fail(ctx, e, "bd d2h");
+  if ((e = cudaStreamSynchronize(ctx->stream))) return cuda_fail(ctx, e, "bd sync");
+  return GGEM_OK;
+}
+
+extern "C" int ggem_brownian_displacement_dev(ggem_ctx *ctx, int nrhs, int N, double eig_min,
+                                              double eig_max, double tol_cheb, int check_every,
+                                              const double *d_xi, double *d_dw,
+                                              ggem_cheb_report *rep) {
+  if (int rc = cheb_common(ctx, nrhs, N, eig_min, eig_max, tol_cheb, check_every, rep)) return rc;
+  if (ctx->n && (!d_xi || !d_dw)) return GGEM_ERR_BAD_ARG;
+  DeviceGuard dg(ctx->device);
+  const size_t len = (size_t)ctx->n * 3 * nrhs;
+  if (int rc = ensure_cheb_buffers(ctx, len)) return rc;
+  if (int rc = permute_to_slots(ctx, nrhs, d_xi, ctx->w_in.p)) return rc;
+  if (int rc = cheb_slots(ctx, nrhs, N, eig_min, eig_max, tol_cheb, check_every, rep)) return rc;
+  bool all = true;
+  for (int r = 0; r < nrhs; ++r) all = all && rep[r].converged;
+  if (!all)
+    return ggem::fail(ctx, GGEM_ERR_CHEB_NOT_CONVERGED,
+                      "Chebyshev polynomial fails to converge (brownian_system.C:1162-1163)");
+  // hi_ewald: dw = M y (copss.C:1686)
+  if (int rc = matvec_slots(ctx, nrhs, ctx->w_y.p, ctx->w_out.p, brownian_self_mode(ctx)))
+    return rc;
+  return permute_from_slots(ctx, nrhs, ctx->w_out.p, d_dw);
+}
+
+extern "C" int ggem_lanczos_bounds(ggem_ctx *ctx, int k, uint64_t seed, double *eig_min,
+                                   double *eig_max) {
+  if (!ctx || !eig_min || !eig_max) return GGEM_ERR_BAD_ARG;
+  if (k < 2 || k > 512) return ggem::fail(ctx, GGEM_ERR_BAD_ARG, "Lanczos steps must be in [2, 512]");
+  if (!ctx->cells_built || (ctx->prm.precision == GGEM_FP32 && !ctx->list_built))
+    return ggem::fail(ctx, GGEM_ERR_BAD_ARG, "call ggem_build_cells first");
+  DeviceGuard dg(ctx->device);
+  const int64_t D = 3 * ctx->n;
+  if (D == 0) return ggem::fail(ctx, GGEM_ERR_BAD_ARG, "no particles");
+  k = (int)std::min<int64_t>(k, D);
+  cudaError_t e;
+  if ((e = ctx->lz_Q.ensure((size_t)D * (k + 1))) || (e = ctx->w_out.ensure(D)) ||
+      (e = ctx->w_red.ensure(std::max(4 * kMaxRhs * 600, (k + 2) * 600 + 1024))))
+    return cuda_fail(ctx, e, "lanczos workspace");
+  cudaStream_t st = ctx->stream;
+  const int sm = brownian_self_mode(ctx);
+  const int G = vec_blocks(D);
+  double *Q = ctx->lz_Q.p, *w = ctx->w_out.p, *h = ctx->h_red;
+  // start vector: N(0,1) from the counter-based generator
+  k_philox_normals<<<(unsigned)((D / 2 + 256) / 256), 256, 0, st>>>(D, seed, 0x4C414E43ull, Q);
+  if (int rc = check_launch(ctx, "lanczos start")) return rc;
+  if (int rc = sumsq_to_host(ctx, 1, D, Q, h)) return rc;
+  k_scale<<<grid1(D), 256, 0, st>>>(D, 1.0 / std::sqrt(h[0]), Q, Q);
+  std::vector<double> a(k), b(k);
+  int m = k;
+  double *hdev = ctx->w_red.p + (size_t)(k + 2) * 600;
+  for (int j = 0; j < k; ++j) {
+    double *q = Q + (size_t)j * D;
+    if (int rc = matvec_slots(ctx, 1, q, w, sm)) return rc;
+    if (int rc = dot_to_host(ctx, 1, D, q, w, h)) return rc;
+    a[j] = h[0];
+    for (int pass = 0; pass < 2; ++pass) {
+      k_multi_dot<<<dim3(G, j + 1), kVecThreads, 0, st>>>(D, Q, w, ctx->w_red.p);
+      if (int rc = check_launch(ctx, "lanczos dots")) return rc;
+      k_finalize<<<j + 1, kVecThreads, 0, st>>>(G, ctx->w_red.p, hdev);
+      if (int rc = check_launch(ctx, "lanczos finalize")) return rc;
+      k_sub_proj<<<grid1(D), 256, 0, st>>>(D, j + 1, Q, hdev, w);
+      if (int rc = check_launch(ctx, "lanczos project")) return rc;
+    }
+    if (int rc = sumsq_to_host(ctx, 1, D, w, h)) return rc;
+    const double beta = std::sqrt(h[0]);
+    b[j] = beta;
+    if (j == k - 1) break;
+    if (beta < 1e-14 * std::fabs(a[j]) + 1e-300) {
+      m = j + 1;
+      break;
+    }
+    k_scale<<<grid1(D), 256, 0, st>>>(D, 1.0 / beta, w, Q + (size_t)(j + 1) * D);
+    if (int rc = check_launch(ctx, "lanczos next")) return rc;
+  }
+  tridiag_extremes(m, a.data(), b.data(), eig_min, eig_max);
+  if (!(*eig_min > 0.0) || !(*eig_max > 0.0))
+    return ggem::fail(ctx, GGEM_ERR_NOT_SPD,
+                      "eigenvalue <= 0 (brownian_system.C:835-840): mobility not positive definite");
+  return GGEM_OK;
+}
+
+extern "C" int ggem_power_iteration(ggem_ctx *ctx, double tol, int maxits, double *eig) {
+  if (!ctx || !(tol > 0) || maxits < 1 || !eig) return GGEM_ERR_BAD_ARG;
+  if (!ctx->cells_built || (ctx->prm.precision == GGEM_FP32 && !ctx->list_built))
+    return ggem::fail(ctx, GGEM_ERR_BAD_ARG, "call ggem_build_cells first");
+  DeviceGuard dg(ctx->device);
+  const int64_t D = 3 * ctx->n;
+  if (D == 0) return ggem::fail(ctx, GGEM_ERR_BAD_ARG, "no particles");
+  if (int rc = ensure_cheb_buffers(ctx, D)) return rc;
+  cudaStream_t st = ctx->stream;
+  const int sm = brownian_self_mode(ctx);
+  double *v0 = ctx->w_c.p, *v1 = ctx->w_d.p, *w0 = ctx->w_e.p, *h = ctx->h_red;
+  *eig = NAN;
+  // brownian_system.C:868-871
+  k_fill<<<grid1(D), 256, 0, st>>>(D, 1.0, v0);
+  if (int rc = sumsq_to_host(ctx, 1, D, v0, h)) return rc;
+  k_scale<<<grid1(D), 256, 0, st>>>(D, 1.0 / std::sqrt(h[0]), v0, v0);
+  for (int it = 0; it < maxits; ++it) {
+    if (int rc = matvec_slots(ctx, 1, v0, w0, sm)) return rc;
+    if (int rc = sumsq_to_host(ctx, 1, D, w0, h)) return rc;
+    k_scale<<<grid1(D), 256, 0, st>>>(D, 1.0 / std::sqrt(h[0]), w0, w0);
+    k_copy<<<grid1(D), 256, 0, st>>>(D, w0, v1);
+    k_axpy_into<<<grid1(D), 256, 0, st>>>(D, -1.0, v0, w0);
+    if (int rc = check_launch(ctx, "power step")) return rc;
+    if (int rc = sumsq_to_host(ctx, 1, D, w0, h)) return rc;
+    const double norm = std::sqrt(h[0]);
+    k_copy<<<grid1(D), 256, 0, st>>>(D, v1, v0);
+    if (norm < tol) {
+      if (int rc = matvec_slots(ctx, 1, v0, w0, sm)) return rc;
+      if (int rc = dot_to_host(ctx, 1, D, v0, w0, h)) return rc;
+      *eig = h[0];
+      return it;
+    }
+  }
+  return ggem::fail(ctx, GGEM_ERR_CHEB_NOT_CONVERGED, "power iteration did not reach tol");
+}
+
+extern "C" int ggem_philox_normals_dev(ggem_ctx *ctx, uint64_t seed, uint64_t stream, int64_t n,
+                                       double *d_out) {
+  if (!ctx || n < 0 || (n > 0 && !d_out)) return GGEM_ERR_BAD_ARG;
+  if (n == 0) return GGEM_OK;
+  DeviceGuard dg(ctx->device);
+  const int64_t pairs = (n + 1) / 2;
+  k_philox_normals<<<(unsigned)((pairs + 255) / 256), 256, 0, ctx->stream>>>(n, seed, stream, d_out);
+  return check_launch(ctx, "philox");
+}

@@ -1,0 +1,160 @@
+// ggem_diag.cu -- measurement hooks (include/ggem_diag.h): launch counts,
+// per-kernel CUDA-event timing and the FP32 FMA throughput probe.
+#include <cuda_runtime.h>
+
+#include "ggem_diag.h"
+#include "ggem_internal.cuh"
+
+namespace ggem {
+
+static cudaEvent_t take_event(ggem_ctx *c) {
+  if (!c->ev_pool.empty()) {
+    cudaEvent_t e = c->ev_pool.back();
+    c->ev_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  if (cudaEventCreate(&e) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return e;
+}
+
+void kt_start(ggem_ctx *c, int kind) {
+  if (!c->timing) return;
+  cudaEvent_t e = take_event(c);
+  if (!e) return;
+  cudaEventRecord(e, c->stream);
+  c->ktimer[kind].ev.push_back(e);
+}
+
+void kt_stop(ggem_ctx *c, int kind) {
+  if (!c->timing) return;
+  auto &t = c->ktimer[kind];
+  if (t.ev.size() % 2 == 0) return;  // unmatched start
+  cudaEvent_t e = take_event(c);
+  if (!e) {
+    c->ev_pool.push_back(t.ev.back());
+    t.ev.pop_back();
+    return;
+  }
+  cudaEventRecord(e, c->stream);
+  t.ev.push_back(e);
+}
+
+static int drain(ggem_ctx *c) {
+  cudaError_t err = cudaStreamSynchronize(c->stream);
+  if (err) return cuda_fail(c, err, "timing sync");
+  for (auto &t : c->ktimer) {
+    for (size_t k = 0; k + 1 < t.ev.size(); k += 2) {
+      float ms = 0.f;
+      if (cudaEventElapsedTime(&ms, t.ev[k], t.ev[k + 1]) == cudaSuccess) {
+        t.total_ms += ms;
+        t.count += 1;
+      } else {
+        cudaGetLastError();
+      }
+      c->ev_pool.push_back(t.ev[k]);
+      c->ev_pool.push_back(t.ev[k + 1]);
+    }
+    t.ev.clear();
+  }
+  return GGEM_OK;
+}
+
+namespace {
+// eight independent FMA chains per thread; the store keeps the chains alive
+__global__ void __launch_bounds__(256) k_fma_probe(int iters, float seed, float *sink) {
+  float a0 = seed + threadIdx.x, a1 = a0 + 1.f, a2 = a0 + 2.f, a3 = a0 + 3.f;
+  float a4 = a0 + 4.f, a5 = a0 + 5.f, a6 = a0 + 6.f, a7 = a0 + 7.f;
+  const float m = 0.999999f, b = 1e-7f;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+      a0 = fmaf(a0, m, b);
+      a1 = fmaf(a1, m, b);
+      a2 = fmaf(a2, m, b);
+      a3 = fmaf(a3, m, b);
+      a4 = fmaf(a4, m, b);
+      a5 = fmaf(a5, m, b);
+      a6 = fmaf(a6, m, b);
+      a7 = fmaf(a7, m, b);
+    }
+  }
+  const float s = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+  if (s == 12345.678f) sink[threadIdx.x] = s;  // never true for these inputs
+}
+}  // namespace
+
+}  // namespace ggem
+
+using namespace ggem;
+
+extern "C" int ggem_get_launch_count(const ggem_ctx *ctx, int64_t *count) {
+  if (!ctx || !count) return GGEM_ERR_BAD_ARG;
+  *count = ctx->launches;
+  return GGEM_OK;
+}
+
+extern "C" int ggem_get_pair_count(const ggem_ctx *ctx, int64_t *count) {
+  if (!ctx || !count) return GGEM_ERR_BAD_ARG;
+  if (!ctx->list_built) return GGEM_ERR_BAD_ARG;
+  *count = ctx->n_pairs;
+  return GGEM_OK;
+}
+
+extern "C" int ggem_set_kernel_timing(ggem_ctx *ctx, int enable) {
+  if (!ctx) return GGEM_ERR_BAD_ARG;
+  if (int rc = drain(ctx)) return rc;
+  for (auto &t : ctx->ktimer) {
+    t.total_ms = 0.0;
+    t.count = 0;
+  }
+  ctx->timing = enable != 0;
+  return GGEM_OK;
+}
+
+extern "C" int ggem_get_kernel_timing(ggem_ctx *ctx, int kernel, double *total_ms,
+                                      int64_t *launches) {
+  if (!ctx || kernel < 0 || kernel > 3 || !total_ms || !launches) return GGEM_ERR_BAD_ARG;
+  if (int rc = drain(ctx)) return rc;
+  *total_ms = ctx->ktimer[kernel].total_ms;
+  *launches = ctx->ktimer[kernel].count;
+  return GGEM_OK;
+}
+
+extern "C" int ggem_probe_fp32_peak(ggem_ctx *ctx, double *tflops) {
+  if (!ctx || !tflops) return GGEM_ERR_BAD_ARG;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+  if (sms <= 0) sms = 1;
+  DevBuf<float> sink;
+  cudaError_t e = sink.ensure(256);
+  if (e) return cuda_fail(ctx, e, "probe buffer");
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  const int blocks = sms * 8, threads = 256, iters = 2048;
+  double best = 0.0;
+  for (int rep = 0; rep < 4; ++rep) {
+    cudaEventRecord(a, ctx->stream);
+    k_fma_probe<<<blocks, threads, 0, ctx->stream>>>(iters, 1.0f + rep, sink.p);
+    cudaEventRecord(b, ctx->stream);
+    if (int rc = check_launch(ctx, "fma probe")) {
+      cudaEventDestroy(a);
+      cudaEventDestroy(b);
+      return rc;
+    }
+    cudaEventSynchronize(b);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    const double flops = 2.0 * 8 * 16 * (double)iters * blocks * threads;
+    if (rep > 0 && ms > 0) best = std::max(best, flops / (ms * 1e-3) / 1e12);
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  *tflops = best;
+  return GGEM_OK;
+}

@@ -1,0 +1,184 @@
+// ggem_internal.cuh -- shared declarations of the GB300 GGEM library.
+//
+// Data layout in HBM (all per context):
+//   xyz_in     double[3n]   caller positions, original particle order
+//   cell_of    int32[n]     cell (element) id of each particle
+//   cell_start int32[ncell+1] sorted cell list (exclusive scan of counts)
+//   order      int32[n]     slot -> original id, ascending within a cell
+//   rank       int32[n]     original id -> slot
+//   pos64      double4_32a[n]   wrapped positions in slot order (FP64 paths)
+//   pos32      float4[n]    position relative to its cell centre (x,y,z) and
+//                           the cell id bits (w), slot order (FP32 path)
+//   pair list  uint32       sliced-ELL (32 slots per slice), entry =
+//                           (source slot << 7) | stencil code, built once
+//                           per configuration with an FP32 filter and an
+//                           exact FP64 decision in the rounding band
+//   tab        float4[2*kTableN] cubic pieces of A(s), B(s), s = r^2, with
+//                           G(x) = A I + B x x^T (FP32 path)
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "ggem_gb300.h"
+
+namespace ggem {
+
+constexpr int kTableN = 512;       // cubic pieces of the FP32 tensor table
+constexpr int kCodeBits = 7;       // stencil code bits of a pair entry
+constexpr int kMaxCode = 1 << kCodeBits;
+constexpr uint32_t kPad = 0xFFFFFFFFu;
+constexpr int kSlice = 32;         // slots per sliced-ELL slice
+constexpr int kMaxRhsChunk = 8;    // right-hand sides per pair-kernel pass
+
+// device error bits
+enum : int {
+  kErrOutOfDomain = 1,
+  kErrListOverflow = 2,
+  kErrTimeout = 4,
+  kErrBadIndex = 8,
+};
+
+// derived GGEM constants (ggem_stokes.C:39-114) in FP64
+struct DevConsts {
+  double one_eight_pi_mu, alpha, alpha2, alpha3_pi_23, two_alpha_sqrt_pi, coeff_1;
+  double ksi, two_ksi_sqrt_pi, coeff_2, r_eps;
+};
+
+// uniform cell grid over the box (cells == elements in reference mode)
+struct Grid {
+  double lo[3], L[3], h[3];
+  float h32[3];
+  int nc[3];
+  int periodic[3];
+  int64_t ncell;
+};
+
+template <typename T>
+struct DevBuf {
+  T *p = nullptr;
+  size_t count = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf &) = delete;
+  DevBuf &operator=(const DevBuf &) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    count = 0;
+  }
+  // grows (never shrinks); contents are not preserved
+  cudaError_t ensure(size_t n) {
+    if (n <= count && p) return cudaSuccess;
+    release();
+    size_t want = n ? n : 1;
+    cudaError_t e = cudaMalloc(&p, want * sizeof(T));
+    if (e == cudaSuccess) count = want;
+    else p = nullptr;
+    return e;
+  }
+};
+
+}  // namespace ggem
+
+struct ggem_ctx {
+  ggem_params prm{};
+  ggem_constants cst{};
+  ggem::DevConsts dc{};
+  ggem::Grid grid{};
+  int device = 0;
+  cudaStream_t stream = nullptr;      // active stream
+  cudaStream_t own_stream = nullptr;  // created by the library
+  std::string last_error;
+
+  // stencils: offsets (dx,dy,dz,0); code k = index into the list
+  std::vector<int4> stencil;          // neighbour cells (excludes (0,0,0) in reference mode)
+  ggem::DevBuf<int4> d_stencil;
+  ggem::DevBuf<float4> d_shift;       // FP32 offset * h for each stencil code
+  float rc2_lo = 0.f, rc2_hi = 0.f;   // FP32 rounding band of the cutoff test
+  double rc2 = 0.0;
+  double search_radius_e = 0.0;
+
+  // particles
+  int64_t n = 0;
+  bool cells_built = false;
+  ggem::DevBuf<double> xyz_in;
+  ggem::DevBuf<int32_t> cell_of, cell_count, cell_start, cell_fill, order, rank;
+  ggem::DevBuf<double4_32a> wrapped, pos64;
+  ggem::DevBuf<float4> pos32;
+  ggem::DevBuf<int> err;
+
+  // FP32 pair list
+  bool list_built = false;
+  int64_t n_pairs = 0;
+  ggem::DevBuf<int32_t> nb_count, slice_width;
+  ggem::DevBuf<int64_t> slice_off;
+  ggem::DevBuf<uint32_t> nb_list;
+  ggem::DevBuf<float4> tab;
+  float tab_inv_ds = 0.f;
+  double tab_max_err = 0.0;
+
+  // scan scratch (one per recursion level)
+  std::vector<ggem::DevBuf<int64_t> *> scan_scratch;
+
+  // vector workspaces (FP64 slot order) and FP32 staging
+  ggem::DevBuf<double> w_in, w_out, w_a, w_b, w_c, w_d, w_e, w_y;
+  ggem::DevBuf<float4> w_f32;
+  ggem::DevBuf<double> w_red;   // reduction partials
+  ggem::DevBuf<double> lz_Q;    // Lanczos basis
+  double *h_red = nullptr;      // pinned host mirror of reductions
+  double *h_stage = nullptr;    // pinned host staging
+  size_t h_stage_bytes = 0;
+
+  // measurement hooks (ggem_diag.h)
+  int64_t launches = 0;
+  bool timing = false;
+  struct KTimer {
+    std::vector<cudaEvent_t> ev;  // start/stop pairs
+    double total_ms = 0.0;
+    int64_t count = 0;
+  } ktimer[4];
+  std::vector<cudaEvent_t> ev_pool;
+
+  ~ggem_ctx();
+};
+
+namespace ggem {
+
+// kernel kinds of the timing hooks
+enum : int { kKPairF32 = 0, kKPairF64 = 1, kKChebTerm = 2, kKListBuild = 3 };
+
+void kt_start(ggem_ctx *c, int kind);
+void kt_stop(ggem_ctx *c, int kind);
+
+int fail(ggem_ctx *c, int code, const std::string &msg);
+int cuda_fail(ggem_ctx *c, cudaError_t e, const char *what);
+int check_launch(ggem_ctx *c, const char *what);
+int read_error_flags(ggem_ctx *c, int *flags);
+int ensure_host_stage(ggem_ctx *c, size_t bytes);
+
+// host-side helpers (ggem_host.cpp)
+void compute_constants(const ggem_params &p, ggem_constants *c);
+int fit_tensor_table(const ggem_constants &c, double s_max, int nt, std::vector<float4> &tab,
+                     double *max_err);
+void tridiag_extremes(int k, const double *a, const double *b, double *lmin, double *lmax);
+void cheb_coeffs_host(int N, double da, double db, int method, double *coef);
+
+// cell build and pair list (ggem_cells.cu)
+int build_cells(ggem_ctx *c);
+int build_pair_list(ggem_ctx *c);
+int device_exclusive_scan_i32(ggem_ctx *c, const int32_t *in, int32_t *out, int64_t n);
+int device_exclusive_scan_i64(ggem_ctx *c, const int64_t *in, int64_t *out, int64_t n);
+
+// pair sums (ggem_pair.cu); vectors in slot order, [r][slot][3] doubles
+int matvec_slots(ggem_ctx *c, int nrhs, const double *d_f_slot, double *d_u_slot,
+                 int self_mode);
+int matvec_f32_staged(ggem_ctx *c, int nrhs, double *d_u_slot, int self_mode);
+double self_coefficient(const ggem_ctx *c, int self_mode);
+int permute_to_slots(ggem_ctx *c, int nrhs, const double *d_orig, double *d_slot);
+int permute_from_slots(ggem_ctx *c, int nrhs, const double *d_slot, double *d_orig);
+
+}  // namespace ggem

@@ -1,0 +1,337 @@
+// ggem_pair.cu -- Kernel B: the local regularized-Stokeslet pair sums.
+//
+// u_i = sum_j G(r_ij) f_j + self term, with G the local regularized Green's
+// tensor of GGEMStokes::green_tensor_local_regularized (ggem_stokes.C:304-357)
+// summed as GGEMStokes::local_solution_bead (ggem_stokes.C:427-503) and the
+// self term of PMSystemStokes::compute_point_velocity (pm_system_stokes.C:446-455).
+//
+// Two arithmetic paths:
+//  * FP64 ("plain"): one thread per target slot sweeps the neighbour cells of
+//    the stencil, minimum image and cut-off in FP64, erf/exp per pair.
+//  * FP32: one thread per target slot walks its cached sliced-ELL list; the
+//    displacement is formed from cell-relative coordinates plus the stencil
+//    shift (exact cell offsets), G = A(s) I + B(s) x x^T from a piecewise
+//    cubic table in s = r^2, and the three components accumulate with Kahan
+//    compensation; the compensated sum is returned in FP64.
+// Algorithmic work per in-cutoff ordered pair: 28 + 19*nrhs flops (FMA = 2,
+// rsqrt/exp/erf = 1 each), bound by the FP32 pipe.
+#include <cuda_runtime.h>
+
+#include "ggem_internal.cuh"
+
+namespace ggem {
+namespace {
+
+__device__ __forceinline__ int wrap_i(int k, int n) {
+  k %= n;
+  return k < 0 ? k + n : k;
+}
+
+__device__ __forceinline__ void min_image(const Grid &g, double d[3]) {
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    if (g.periodic[k]) {
+      const double xs = g.L[k];
+      if (d[k] <= -xs / 2.0) d[k] += xs;
+      if (d[k] > xs / 2.0) d[k] -= xs;
+    }
+  }
+}
+
+// green_tensor_local_regularized applied to f: G f = k[(c1+c2) f + (c1-c2)(x.f/r^2) x]
+__device__ __forceinline__ void green_apply64(const DevConsts &K, const double x[3], double r,
+                                              const double f[3], double out[3]) {
+  if (r < K.r_eps) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a) out[a] = K.coeff_2 * f[a];
+    return;
+  }
+  const double r2 = r * r;
+  const double kr = K.ksi * r, kr2 = kr * kr;
+  const double ar = K.alpha * r, ar2 = ar * ar;
+  const double c1 = (erf(kr) - erf(ar)) / r;
+  const double c2 = K.two_ksi_sqrt_pi * exp(-kr2) - K.two_alpha_sqrt_pi * exp(-ar2);
+  const double xf = (x[0] * f[0] + x[1] * f[1] + x[2] * f[2]) / r2;
+  const double p = (c1 + c2) * K.one_eight_pi_mu, m = (c1 - c2) * xf * K.one_eight_pi_mu;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) out[a] = p * f[a] + m * x[a];
+}
+
+__device__ __forceinline__ void self_term(const DevConsts &K, int self_mode, const double f[3],
+                                          double u[3]) {
+  if (self_mode == GGEM_SELF_BEAD) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a) u[a] = (u[a] - K.coeff_1 * f[a]) + f[a];
+  } else if (self_mode == GGEM_SELF_LAGRANGIAN) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a) u[a] = u[a] + K.coeff_2 * f[a];
+  }
+}
+
+// FP64 plain sweep.  own_first: reference mode (own cell, then the element
+// stencil that excludes (0,0,0), no cut-off); otherwise the cut-off stencil.
+template <int NR>
+__global__ void __launch_bounds__(128) k_matvec_f64(int64_t n, Grid g, DevConsts K,
+                                                    const int4 *__restrict__ stencil, int nst,
+                                                    int own_first, int use_cutoff, double rc2,
+                                                    const int32_t *__restrict__ start,
+                                                    const double4_32a *__restrict__ pos64,
+                                                    const float4 *__restrict__ pos32,
+                                                    const double *__restrict__ f,
+                                                    double *__restrict__ u, int self_mode,
+                                                    int nrhs_total, int r0) {
+  const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const double4_32a pi = pos64[s];
+  const int32_t cid = __float_as_int(pos32[s].w);
+  const int cx = cid % g.nc[0], cy = (cid / g.nc[0]) % g.nc[1], cz = cid / (g.nc[0] * g.nc[1]);
+  double acc[NR][3];
+#pragma unroll
+  for (int r = 0; r < NR; ++r) acc[r][0] = acc[r][1] = acc[r][2] = 0.0;
+  const int64_t vstride = 3 * n;
+  for (int k = own_first ? -1 : 0; k < nst; ++k) {
+    int4 o = (k < 0) ? make_int4(0, 0, 0, 0) : stencil[k];
+    int c[3] = {cx + o.x, cy + o.y, cz + o.z};
+    bool ok = true;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      if (c[d] < 0 || c[d] >= g.nc[d]) {
+        if (!g.periodic[d]) ok = false;
+        else c[d] = wrap_i(c[d], g.nc[d]);
+      }
+    }
+    if (!ok) continue;
+    const int32_t nc = c[0] + g.nc[0] * (c[1] + g.nc[1] * c[2]);
+    const int32_t b = start[nc], e = start[nc + 1];
+    for (int32_t t = b; t < e; ++t) {
+      if (t == s) continue;
+      const double4_32a pj = pos64[t];
+      double x[3] = {pj.x - pi.x, pj.y - pi.y, pj.z - pi.z};
+      min_image(g, x);
+      if (use_cutoff) {
+        const double r2c = __dadd_rn(__dadd_rn(__dmul_rn(x[0], x[0]), __dmul_rn(x[1], x[1])),
+                                     __dmul_rn(x[2], x[2]));
+        if (!(r2c < rc2)) continue;
+      }
+      const double r = sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]);
+#pragma unroll
+      for (int q = 0; q < NR; ++q) {
+        const double *fj = f + (int64_t)(r0 + q) * vstride + 3 * (int64_t)t;
+        const double fv[3] = {fj[0], fj[1], fj[2]};
+        double g3[3];
+        green_apply64(K, x, r, fv, g3);
+        acc[q][0] += g3[0];
+        acc[q][1] += g3[1];
+        acc[q][2] += g3[2];
+      }
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < NR; ++q) {
+    const double *fi = f + (int64_t)(r0 + q) * vstride + 3 * s;
+    const double fv[3] = {fi[0], fi[1], fi[2]};
+    self_term(K, self_mode, fv, acc[q]);
+    double *ui = u + (int64_t)(r0 + q) * vstride + 3 * s;
+    ui[0] = acc[q][0];
+    ui[1] = acc[q][1];
+    ui[2] = acc[q][2];
+  }
+  (void)nrhs_total;
+}
+
+__device__ __forceinline__ void kahan_add(float &sum, float &comp, float v) {
+  const float y = v - comp;
+  const float t = sum + y;
+  comp = (t - sum) - y;
+  sum = t;
+}
+
+// FP32 list walk; f32 is [r][n] float4 (x,y,z,0), u is [r][n][3] doubles
+template <int NR>
+__global__ void __launch_bounds__(256) k_matvec_f32(
+    int64_t n, const float4 *__restrict__ pos32, const int32_t *__restrict__ count,
+    const int64_t *__restrict__ slice_off, const uint32_t *__restrict__ list,
+    const float4 *__restrict__ shift_g, int nshift, const float4 *__restrict__ tab,
+    float inv_ds, float self_c, const float4 *__restrict__ f32, double *__restrict__ u,
+    int r0) {
+  __shared__ float4 shift[kMaxCode];
+  for (int k = threadIdx.x; k < nshift; k += blockDim.x) shift[k] = shift_g[k];
+  __syncthreads();
+  const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const int lane = (int)(s & (kSlice - 1));
+  const int64_t base = slice_off[s / kSlice] + lane;
+  const int32_t cnt = count[s];
+  const float4 pi = pos32[s];
+  float sx[NR], sy[NR], sz[NR], cx[NR], cy[NR], cz[NR];
+#pragma unroll
+  for (int q = 0; q < NR; ++q) {
+    const float4 fi = f32[(int64_t)(r0 + q) * n + s];
+    sx[q] = self_c * fi.x;
+    sy[q] = self_c * fi.y;
+    sz[q] = self_c * fi.z;
+    cx[q] = cy[q] = cz[q] = 0.f;
+  }
+  const float top = (float)(kTableN - 1);
+  for (int32_t m = 0; m < cnt; ++m) {
+    const uint32_t e = __ldg(list + base + (int64_t)m * kSlice);
+    const uint32_t j = e >> kCodeBits;
+    const float4 sh = shift[e & (kMaxCode - 1)];
+    const float4 pj = __ldg(pos32 + j);
+    const float dx = (pj.x - pi.x) + sh.x;
+    const float dy = (pj.y - pi.y) + sh.y;
+    const float dz = (pj.z - pi.z) + sh.z;
+    const float s2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+    const float uu = s2 * inv_ds;
+    const float fi = fminf(floorf(uu), top);  // last piece extrapolates past s_max
+    const float t = uu - fi;
+    const int idx = (int)fi;
+    const float4 ta = __ldg(tab + 2 * idx);
+    const float4 tb = __ldg(tab + 2 * idx + 1);
+    const float A = fmaf(fmaf(fmaf(ta.w, t, ta.z), t, ta.y), t, ta.x);
+    const float B = fmaf(fmaf(fmaf(tb.w, t, tb.z), t, tb.y), t, tb.x);
+#pragma unroll
+    for (int q = 0; q < NR; ++q) {
+      const float4 fj = __ldg(f32 + (int64_t)(r0 + q) * n + j);
+      const float bxf = B * fmaf(dz, fj.z, fmaf(dy, fj.y, dx * fj.x));
+      kahan_add(sx[q], cx[q], fmaf(A, fj.x, bxf * dx));
+      kahan_add(sy[q], cy[q], fmaf(A, fj.y, bxf * dy));
+      kahan_add(sz[q], cz[q], fmaf(A, fj.z, bxf * dz));
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < NR; ++q) {
+    double *ui = u + ((int64_t)(r0 + q) * n + s) * 3;
+    ui[0] = (double)sx[q] - (double)cx[q];
+    ui[1] = (double)sy[q] - (double)cy[q];
+    ui[2] = (double)sz[q] - (double)cz[q];
+  }
+}
+
+__global__ void k_slots_to_f32(int64_t n, int nrhs, const double *__restrict__ f,
+                               float4 *__restrict__ f32) {
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k >= n * nrhs) return;
+  const double *p = f + 3 * k;
+  f32[k] = make_float4((float)p[0], (float)p[1], (float)p[2], 0.f);
+}
+
+// orig [r][n][3] -> slots [r][n][3]
+__global__ void k_to_slots(int64_t n, int nrhs, const int32_t *__restrict__ order,
+                           const double *__restrict__ orig, double *__restrict__ slot) {
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k >= n * nrhs) return;
+  const int64_t r = k / n, s = k - r * n;
+  const int64_t i = order[s];
+  const double *src = orig + (r * n + i) * 3;
+  double *dst = slot + (r * n + s) * 3;
+  dst[0] = src[0];
+  dst[1] = src[1];
+  dst[2] = src[2];
+}
+
+__global__ void k_from_slots(int64_t n, int nrhs, const int32_t *__restrict__ rank,
+                             const double *__restrict__ slot, double *__restrict__ orig) {
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k >= n * nrhs) return;
+  const int64_t r = k / n, i = k - r * n;
+  const int64_t s = rank[i];
+  const double *src = slot + (r * n + s) * 3;
+  double *dst = orig + (r * n + i) * 3;
+  dst[0] = src[0];
+  dst[1] = src[1];
+  dst[2] = src[2];
+}
+
+template <int NR>
+int launch_f64(ggem_ctx *c, const double *f, double *u, int self_mode, int r0) {
+  const int T = 128;
+  const unsigned bn = (unsigned)((c->n + T - 1) / T);
+  const bool ref = c->prm.nb_mode == GGEM_NB_REFERENCE;
+  kt_start(c, kKPairF64);
+  k_matvec_f64<NR><<<bn, T, 0, c->stream>>>(c->n, c->grid, c->dc, c->d_stencil.p,
+                                             (int)c->stencil.size(), ref ? 1 : 0, ref ? 0 : 1,
+                                             c->rc2, c->cell_start.p, c->pos64.p, c->pos32.p, f,
+                                             u, self_mode, 0, r0);
+  kt_stop(c, kKPairF64);
+  return check_launch(c, "matvec f64");
+}
+
+template <int NR>
+int launch_f32(ggem_ctx *c, const float4 *f32, double *u, float self_c, int r0) {
+  const int T = 256;
+  const unsigned bn = (unsigned)((c->n + T - 1) / T);
+  kt_start(c, kKPairF32);
+  k_matvec_f32<NR><<<bn, T, 0, c->stream>>>(c->n, c->pos32.p, c->nb_count.p, c->slice_off.p,
+                                             c->nb_list.p, c->d_shift.p,
+                                             (int)c->stencil.size(), c->tab.p, c->tab_inv_ds,
+                                             self_c, f32, u, r0);
+  kt_stop(c, kKPairF32);
+  return check_launch(c, "matvec f32");
+}
+
+}  // namespace
+
+int permute_to_slots(ggem_ctx *c, int nrhs, const double *d_orig, double *d_slot) {
+  const int64_t tot = c->n * nrhs;
+  if (tot == 0) return GGEM_OK;
+  k_to_slots<<<(unsigned)((tot + 255) / 256), 256, 0, c->stream>>>(c->n, nrhs, c->order.p,
+                                                                   d_orig, d_slot);
+  return check_launch(c, "to slots");
+}
+
+int permute_from_slots(ggem_ctx *c, int nrhs, const double *d_slot, double *d_orig) {
+  const int64_t tot = c->n * nrhs;
+  if (tot == 0) return GGEM_OK;
+  k_from_slots<<<(unsigned)((tot + 255) / 256), 256, 0, c->stream>>>(c->n, nrhs, c->rank.p,
+                                                                     d_slot, d_orig);
+  return check_launch(c, "from slots");
+}
+
+double self_coefficient(const ggem_ctx *c, int self_mode) {
+  if (self_mode == GGEM_SELF_BEAD) return 1.0 - c->cst.coeff_1;
+  if (self_mode == GGEM_SELF_LAGRANGIAN) return c->cst.coeff_2;
+  return 0.0;
+}
+
+// u = M f on slot-ordered FP64 vectors [r][n][3]
+int matvec_slots(ggem_ctx *c, int nrhs, const double *f, double *u, int self_mode) {
+  if (c->n == 0) return GGEM_OK;
+  if (c->prm.precision == GGEM_FP64) {
+    int r0 = 0;
+    while (r0 < nrhs) {
+      const int left = nrhs - r0;
+      int rc;
+      if (left >= 4) rc = launch_f64<4>(c, f, u, self_mode, r0), r0 += 4;
+      else if (left >= 2) rc = launch_f64<2>(c, f, u, self_mode, r0), r0 += 2;
+      else rc = launch_f64<1>(c, f, u, self_mode, r0), r0 += 1;
+      if (rc) return rc;
+    }
+    return GGEM_OK;
+  }
+  cudaError_t e = c->w_f32.ensure((size_t)c->n * nrhs);
+  if (e) return cuda_fail(c, e, "f32 staging");
+  const int64_t tot = c->n * nrhs;
+  k_slots_to_f32<<<(unsigned)((tot + 255) / 256), 256, 0, c->stream>>>(c->n, nrhs, f,
+                                                                       c->w_f32.p);
+  if (int rc = check_launch(c, "to f32")) return rc;
+  return matvec_f32_staged(c, nrhs, u, self_mode);
+}
+
+// FP32 pair sum from the already staged c->w_f32 ([r][n] float4)
+int matvec_f32_staged(ggem_ctx *c, int nrhs, double *u, int self_mode) {
+  const float self_c = (float)self_coefficient(c, self_mode);
+  int r0 = 0;
+  while (r0 < nrhs) {
+    const int left = nrhs - r0;
+    int rc;
+    if (left >= 8) rc = launch_f32<8>(c, c->w_f32.p, u, self_c, r0), r0 += 8;
+    else if (left >= 4) rc = launch_f32<4>(c, c->w_f32.p, u, self_c, r0), r0 += 4;
+    else if (left >= 2) rc = launch_f32<2>(c, c->w_f32.p, u, self_c, r0), r0 += 2;
+    else rc = launch_f32<1>(c, c->w_f32.p, u, self_c, r0), r0 += 1;
+    if (rc) return rc;
+  }
+  return GGEM_OK;
+}
+
+}  // namespace ggem

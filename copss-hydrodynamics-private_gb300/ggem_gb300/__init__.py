@@ -1,0 +1,374 @@
+"""Python binding of the GB300 GGEM library (ctypes over the C ABI).
+
+The compute path is ``_lib/libggem_gb300.so`` (hand-written CUDA for
+sm_103a); this module only marshals arguments.  There is no CPU fallback:
+if the library is missing, :func:`lib` raises.
+
+Layout conventions follow the reference's PETSc vectors
+(brownian_system.C:72-75): forces and velocities are ``[nrhs, n, 3]``
+float64, positions ``[n, 3]`` float64.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "_lib" / "libggem_gb300.so"
+
+GGEM_OK = 0
+POLYMER_BEAD, POINT_PARTICLE, LAGRANGIAN_POINT = 0, 1, 2
+SELF_NONE, SELF_BEAD, SELF_LAGRANGIAN = 0, 1, 2
+NB_REFERENCE, NB_CUTOFF = 0, 1
+FP64, FP32 = 0, 1
+CHEB_GAUSS, CHEB_GAUSS_RADAU, CHEB_GAUSS_LOBATTO = 0, 1, 2
+ERR_BAD_ARG, ERR_CUDA, ERR_CELL_OVERFLOW, ERR_TIMEOUT = -1, -2, -3, -4
+ERR_NOT_SPD, ERR_CHEB_NOT_CONVERGED, ERR_SURROGATE_REJECTED = -5, -6, -7
+ERR_OUT_OF_DOMAIN, ERR_NO_DEVICE, ERR_OOM, ERR_INVALID_RANGE = -8, -9, -10, -11
+KERNEL_PAIR_FP32, KERNEL_PAIR_FP64, KERNEL_CHEB_TERM, KERNEL_LIST_BUILD = 0, 1, 2, 3
+
+
+class Params(C.Structure):
+    _fields_ = [("mu", C.c_double), ("alpha", C.c_double), ("br0", C.c_double),
+                ("point_type", C.c_int), ("ibm_beta", C.c_double), ("hmin", C.c_double),
+                ("box_lo", C.c_double * 3), ("box_hi", C.c_double * 3),
+                ("periodic", C.c_int * 3), ("nb_mode", C.c_int), ("rc", C.c_double),
+                ("n_mesh", C.c_int * 3), ("search_radius_e", C.c_double),
+                ("precision", C.c_int), ("cell_div", C.c_int), ("device", C.c_int)]
+
+
+class Constants(C.Structure):
+    _fields_ = [(n, C.c_double) for n in (
+        "mu", "alpha", "ksi", "br0", "one_eight_pi_mu", "alpha2", "alpha3",
+        "alpha3_pi_23", "two_alpha_sqrt_pi", "coeff_1", "ksi2", "ksi3",
+        "ksi3_pi_23", "two_ksi_sqrt_pi", "coeff_2", "r_eps")]
+
+
+class ChebReport(C.Structure):
+    _fields_ = [("converged", C.c_int), ("n_terms", C.c_int), ("n_matvecs", C.c_int),
+                ("err1", C.c_double), ("err2", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class GGEMError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"ggem error {code}: {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def lib():
+    """Load the CUDA library; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise RuntimeError(f"{LIB_PATH} is missing: run ggem_gb300.build.build() first "
+                           "(the GGEM path has no CPU fallback)")
+    L = C.CDLL(str(LIB_PATH))
+    vp, i64, d, i = C.c_void_p, C.c_int64, C.c_double, C.c_int
+    P = C.POINTER
+    sig = {
+        "ggem_default_params": (None, [P(Params)]),
+        "ggem_create": (i, [P(Params), P(vp)]),
+        "ggem_destroy": (None, [vp]),
+        "ggem_strerror": (C.c_char_p, [i]),
+        "ggem_last_error": (C.c_char_p, [vp]),
+        "ggem_get_constants": (i, [vp, P(Constants)]),
+        "ggem_set_stream": (i, [vp, vp]),
+        "ggem_synchronize": (i, [vp]),
+        "ggem_set_particles": (i, [vp, i64, vp]),
+        "ggem_set_particles_dev": (i, [vp, i64, vp]),
+        "ggem_build_cells": (i, [vp]),
+        "ggem_neighbor_pair_count": (i, [vp, P(i64)]),
+        "ggem_get_neighbors": (i, [vp, vp, vp, i64]),
+        "ggem_get_cell_of_particles": (i, [vp, vp]),
+        "ggem_local_matvec": (i, [vp, i, vp, vp, i]),
+        "ggem_local_matvec_dev": (i, [vp, i, vp, vp, i]),
+        "ggem_green_tensor_local": (i, [vp, i64, vp, vp]),
+        "ggem_local_field": (i, [vp, i64, vp, vp, vp]),
+        "ggem_spread_qp": (i, [vp, i64, vp, vp, vp, d, vp]),
+        "ggem_element_rhs": (i, [vp, i64, i, i, vp, vp, vp, d, vp]),
+        "ggem_cheb_coeffs": (i, [i, d, d, i, vp]),
+        "ggem_cheb_inv_sqrt": (i, [vp, i, i, d, d, d, i, vp, P(ChebReport)]),
+        "ggem_cheb_inv_sqrt_dev": (i, [vp, i, i, d, d, d, i, vp, P(ChebReport)]),
+        "ggem_brownian_displacement": (i, [vp, i, i, d, d, d, i, vp, vp, P(ChebReport)]),
+        "ggem_brownian_displacement_dev": (i, [vp, i, i, d, d, d, i, vp, vp, P(ChebReport)]),
+        "ggem_get_launch_count": (i, [vp, P(i64)]),
+        "ggem_get_pair_count": (i, [vp, P(i64)]),
+        "ggem_probe_fp32_peak": (i, [vp, P(d)]),
+        "ggem_set_kernel_timing": (i, [vp, i]),
+        "ggem_get_kernel_timing": (i, [vp, i, P(d), P(i64)]),
+        "ggem_lanczos_bounds": (i, [vp, i, C.c_uint64, P(d), P(d)]),
+        "ggem_power_iteration": (i, [vp, d, i, P(d)]),
+        "ggem_std_random_vector": (i, [C.c_uint64, i64, i64, d, d, vp]),
+        "ggem_philox_normals_dev": (i, [vp, C.c_uint64, C.c_uint64, i64, vp]),
+        "ggem_make_suspension": (i, [C.c_uint64, i64, d, d, vp, P(d)]),
+        "ggem_make_chains": (i, [C.c_uint64, i64, i, d, d, d, vp, P(d)]),
+        "ggem_make_normals": (i, [C.c_uint64, i64, vp]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def _p(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def _f64(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def cheb_coeffs(N, da, db, method=CHEB_GAUSS) -> np.ndarray:
+    c = np.zeros(N + 1)
+    rc = lib().ggem_cheb_coeffs(int(N), float(da), float(db), int(method), _p(c))
+    if rc:
+        raise GGEMError(rc, lib().ggem_strerror(rc).decode())
+    return c
+
+
+def std_random_vector(seed, n, mean=0.0, std=1.0, skip_vectors=0) -> np.ndarray:
+    out = np.zeros(n)
+    rc = lib().ggem_std_random_vector(int(seed), int(skip_vectors), int(n), float(mean),
+                                      float(std), _p(out))
+    if rc:
+        raise GGEMError(rc, "bad arguments")
+    return out
+
+
+def make_suspension(seed, n, phi, radius=1.0):
+    xyz = np.zeros((n, 3))
+    L = C.c_double()
+    rc = lib().ggem_make_suspension(int(seed), int(n), float(phi), float(radius), _p(xyz),
+                                    C.byref(L))
+    if rc:
+        raise GGEMError(rc, "suspension generation failed")
+    return xyz, L.value
+
+
+def make_chains(seed, n_chains, beads, bond=2.0, phi=0.05, radius=1.0):
+    xyz = np.zeros((n_chains * beads, 3))
+    L = C.c_double()
+    rc = lib().ggem_make_chains(int(seed), int(n_chains), int(beads), float(bond), float(phi),
+                                float(radius), _p(xyz), C.byref(L))
+    if rc:
+        raise GGEMError(rc, "chain generation failed")
+    return xyz, L.value
+
+
+def make_normals(seed, n) -> np.ndarray:
+    out = np.zeros(n)
+    rc = lib().ggem_make_normals(int(seed), int(n), _p(out))
+    if rc:
+        raise GGEMError(rc, "bad arguments")
+    return out
+
+
+def default_params() -> Params:
+    p = Params()
+    lib().ggem_default_params(C.byref(p))
+    return p
+
+
+class Context:
+    """One GGEM context: constants, box, cell lists and device workspaces."""
+
+    def __init__(self, *, alpha=0.5, mu=None, br0=1.0, point_type=POLYMER_BEAD,
+                 ibm_beta=0.75, hmin=1.0, box_lo=(0.0, 0.0, 0.0), box_hi=(1.0, 1.0, 1.0),
+                 periodic=(1, 1, 1), nb_mode=NB_CUTOFF, rc=7.0, n_mesh=(1, 1, 1),
+                 search_radius_e=0.0, precision=FP32, cell_div=0, device=0):
+        p = default_params()
+        if mu is not None:
+            p.mu = float(mu)
+        p.alpha, p.br0, p.point_type = float(alpha), float(br0), int(point_type)
+        p.ibm_beta, p.hmin = float(ibm_beta), float(hmin)
+        for k in range(3):
+            p.box_lo[k], p.box_hi[k] = float(box_lo[k]), float(box_hi[k])
+            p.periodic[k] = int(bool(periodic[k]))
+            p.n_mesh[k] = int(n_mesh[k])
+        p.nb_mode, p.rc, p.search_radius_e = int(nb_mode), float(rc), float(search_radius_e)
+        p.precision, p.cell_div, p.device = int(precision), int(cell_div), int(device)
+        self.params = p
+        h = C.c_void_p()
+        rc_ = lib().ggem_create(C.byref(p), C.byref(h))
+        if rc_:
+            raise GGEMError(rc_, lib().ggem_strerror(rc_).decode())
+        self.h = h
+        self.n = 0
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().ggem_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, rc):
+        if rc < 0:
+            raise GGEMError(rc, lib().ggem_last_error(self.h).decode())
+        return rc
+
+    def constants(self) -> Constants:
+        c = Constants()
+        self._check(lib().ggem_get_constants(self.h, C.byref(c)))
+        return c
+
+    def set_stream(self, stream_ptr):
+        self._check(lib().ggem_set_stream(self.h, C.c_void_p(stream_ptr or None)))
+
+    def synchronize(self):
+        self._check(lib().ggem_synchronize(self.h))
+
+    def set_particles(self, xyz):
+        xyz = _f64(xyz).reshape(-1, 3)
+        self._check(lib().ggem_set_particles(self.h, len(xyz), _p(xyz)))
+        self.n = len(xyz)
+
+    def set_particles_dev(self, d_ptr, n):
+        self._check(lib().ggem_set_particles_dev(self.h, int(n), C.c_void_p(d_ptr)))
+        self.n = int(n)
+
+    def build_cells(self):
+        self._check(lib().ggem_build_cells(self.h))
+
+    def pair_count(self) -> int:
+        v = C.c_int64()
+        self._check(lib().ggem_neighbor_pair_count(self.h, C.byref(v)))
+        return v.value
+
+    def neighbors(self):
+        off = np.zeros(self.n + 1, np.int64)
+        self._check(lib().ggem_get_neighbors(self.h, _p(off), None, 0))
+        ids = np.zeros(max(int(off[-1]), 1), np.int32)
+        self._check(lib().ggem_get_neighbors(self.h, _p(off), _p(ids), len(ids)))
+        return off, ids[:off[-1]]
+
+    def cell_of_particles(self):
+        out = np.zeros(self.n, np.int32)
+        self._check(lib().ggem_get_cell_of_particles(self.h, _p(out)))
+        return out
+
+    def local_matvec(self, f, self_mode=SELF_BEAD):
+        f = _f64(f)
+        nrhs = f.size // (3 * self.n) if self.n else 1
+        u = np.zeros_like(f)
+        self._check(lib().ggem_local_matvec(self.h, nrhs, _p(f), _p(u), int(self_mode)))
+        return u
+
+    def local_matvec_dev(self, d_f, d_u, nrhs=1, self_mode=SELF_BEAD):
+        self._check(lib().ggem_local_matvec_dev(self.h, int(nrhs), C.c_void_p(d_f),
+                                                C.c_void_p(d_u), int(self_mode)))
+
+    def green_tensor_local(self, x):
+        x = _f64(x).reshape(-1, 3)
+        G = np.zeros((len(x), 3, 3))
+        self._check(lib().ggem_green_tensor_local(self.h, len(x), _p(x), _p(G)))
+        return G
+
+    def local_field(self, targets, f):
+        t = _f64(targets).reshape(-1, 3)
+        f = _f64(f)
+        u = np.zeros_like(t)
+        self._check(lib().ggem_local_field(self.h, len(t), _p(t), _p(f), _p(u)))
+        return u
+
+    def spread_qp(self, qxyz, f, qp_elem=None, spread_rc=0.0):
+        q = _f64(qxyz).reshape(-1, 3)
+        f = _f64(f)
+        rho = np.zeros_like(q)
+        qe = None if qp_elem is None else np.ascontiguousarray(qp_elem, np.int32)
+        self._check(lib().ggem_spread_qp(self.h, len(q), _p(q), _p(qe) if qe is not None else None,
+                                         _p(f), float(spread_rc), _p(rho)))
+        return rho
+
+    def element_rhs(self, n_elem, nq, n_u, qxyz, int_force, f, spread_rc=0.0):
+        q, IF, f = _f64(qxyz), _f64(int_force), _f64(f)
+        Fe = np.zeros((n_elem, 3 * n_u))
+        self._check(lib().ggem_element_rhs(self.h, int(n_elem), int(nq), int(n_u), _p(q), _p(IF),
+                                           _p(f), float(spread_rc), _p(Fe)))
+        return Fe
+
+    def cheb_inv_sqrt(self, xi, N, eig_min, eig_max, tol, check_every=1):
+        xi = _f64(xi).copy()
+        nrhs = xi.size // (3 * self.n)
+        reps = (ChebReport * nrhs)()
+        self._check(lib().ggem_cheb_inv_sqrt(self.h, nrhs, int(N), float(eig_min), float(eig_max),
+                                             float(tol), int(check_every), _p(xi), reps))
+        return xi, [r.as_dict() for r in reps]
+
+    def cheb_inv_sqrt_dev(self, d_xi, nrhs, N, eig_min, eig_max, tol, check_every=1):
+        reps = (ChebReport * nrhs)()
+        self._check(lib().ggem_cheb_inv_sqrt_dev(self.h, int(nrhs), int(N), float(eig_min),
+                                                 float(eig_max), float(tol), int(check_every),
+                                                 C.c_void_p(d_xi), reps))
+        return [r.as_dict() for r in reps]
+
+    def brownian_displacement_dev(self, d_xi, d_dw, nrhs, N, eig_min, eig_max, tol,
+                                  check_every=1):
+        reps = (ChebReport * nrhs)()
+        rc = lib().ggem_brownian_displacement_dev(self.h, int(nrhs), int(N), float(eig_min),
+                                                  float(eig_max), float(tol), int(check_every),
+                                                  C.c_void_p(d_xi), C.c_void_p(d_dw), reps)
+        return rc, [r.as_dict() for r in reps]
+
+    def brownian_displacement(self, xi, N, eig_min, eig_max, tol, check_every=1):
+        xi = _f64(xi)
+        nrhs = xi.size // (3 * self.n)
+        dw = np.zeros_like(xi)
+        reps = (ChebReport * nrhs)()
+        rc = lib().ggem_brownian_displacement(self.h, nrhs, int(N), float(eig_min),
+                                              float(eig_max), float(tol), int(check_every),
+                                              _p(xi), _p(dw), reps)
+        return rc, dw, [r.as_dict() for r in reps]
+
+    def launch_count(self) -> int:
+        v = C.c_int64()
+        self._check(lib().ggem_get_launch_count(self.h, C.byref(v)))
+        return v.value
+
+    def set_kernel_timing(self, enable: bool):
+        self._check(lib().ggem_set_kernel_timing(self.h, int(bool(enable))))
+
+    def kernel_timing(self, kernel: int):
+        t, n = C.c_double(), C.c_int64()
+        self._check(lib().ggem_get_kernel_timing(self.h, int(kernel), C.byref(t), C.byref(n)))
+        return t.value, n.value
+
+    def probe_fp32_peak(self) -> float:
+        v = C.c_double()
+        self._check(lib().ggem_probe_fp32_peak(self.h, C.byref(v)))
+        return v.value
+
+    def lanczos_bounds(self, k=30, seed=1):
+        lo, hi = C.c_double(), C.c_double()
+        self._check(lib().ggem_lanczos_bounds(self.h, int(k), int(seed), C.byref(lo), C.byref(hi)))
+        return lo.value, hi.value
+
+    def power_iteration(self, tol=1e-3, maxits=50):
+        e = C.c_double()
+        it = self._check(lib().ggem_power_iteration(self.h, float(tol), int(maxits), C.byref(e)))
+        return it, e.value
+
+    def philox_normals_dev(self, seed, stream, n, d_out):
+        self._check(lib().ggem_philox_normals_dev(self.h, int(seed), int(stream), int(n),
+                                                  C.c_void_p(d_out)))

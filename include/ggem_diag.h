@@ -1,0 +1,41 @@
+/*
+ * ggem_diag.h -- measurement hooks of the GGEM library.
+ *
+ * Not part of the reference's interface (the reference has no GPU): these
+ * report what the library launched and the FP32 issue rate of the device, so
+ * that benchmarks can state kernel counts and roofline fractions.
+ */
+#ifndef GGEM_DIAG_H
+#define GGEM_DIAG_H
+
+#include <stdint.h>
+
+#include "ggem_gb300.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* number of CUDA kernels this context has launched so far */
+int ggem_get_launch_count(const ggem_ctx *ctx, int64_t *count);
+/* ordered in-cutoff pairs of the current FP32 pair list (the work unit of
+ * the pair kernel) */
+int ggem_get_pair_count(const ggem_ctx *ctx, int64_t *count);
+/* dense FP32 FMA throughput of this device in TFLOP/s (FMA = 2 flops),
+ * measured with CUDA events over a register-resident FMA chain kernel on the
+ * context's stream */
+int ggem_probe_fp32_peak(ggem_ctx *ctx, double *tflops);
+/* kernel timing: when enabled, CUDA events on the context's stream bracket
+ * every launch of the kernels below; totals are read back (with a stream
+ * synchronisation) by ggem_get_kernel_timing.  Enabling resets the totals. */
+#define GGEM_KERNEL_PAIR_FP32 0  /* FP32 pair-list sum                        */
+#define GGEM_KERNEL_PAIR_FP64 1  /* FP64 cell-stencil sum                     */
+#define GGEM_KERNEL_CHEB_TERM 2  /* fused Chebyshev term                       */
+#define GGEM_KERNEL_LIST_BUILD 3 /* pair-list count + fill                     */
+int ggem_set_kernel_timing(ggem_ctx *ctx, int enable);
+int ggem_get_kernel_timing(ggem_ctx *ctx, int kernel, double *total_ms, int64_t *launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

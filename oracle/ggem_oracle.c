@@ -534,7 +534,7 @@ void orc_local_field_cutoff(const orc_consts *c, const orc_box *b, int64_t n,
     for (int64_t j = 0; j < n; ++j) {
       double x[3], G[9];
       orc_point_vector(b, pt, xyz + 3 * j, x);
-      if (rc > 0 && !(sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]) < rc)) continue;
+      if (rc > 0 && !((x[0] * x[0] + x[1] * x[1]) + x[2] * x[2] < rc * rc)) continue;
       orc_green_local(c, x, G);
       for (int a = 0; a < 3; ++a)
         for (int bb = 0; bb < 3; ++bb) acc[a] += G[3 * a + bb] * f[3 * j + bb];
@@ -572,7 +572,7 @@ static void rho_at(const orc_consts *c, const orc_box *b,
     for (int64_t j = 0; j < n; ++j) {
       double x[3];
       orc_point_vector(b, q, xyz + 3 * j, x);
-      if (!(sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]) < rc)) continue;
+      if (!((x[0] * x[0] + x[1] * x[1]) + x[2] * x[2] < rc * rc)) continue;
       const double g = orc_smoothed_force_exp(c, x);
       for (int d = 0; d < 3; ++d) rho[d] += g * f[3 * j + d];
     }

@@ -1,0 +1,367 @@
+"""Parity of the CUDA library (through the C ABI) with the FP64 oracle.
+
+Tolerances (spec contract):
+  * neighbour and cell lists: bit-exact as sorted index sets;
+  * FP64 results: 1e-12 relative (norm-wise);
+  * FP32 pair sum: 1e-6 relative velocity error (norm-wise), the per-component
+    error is reported against the largest component;
+  * Chebyshev: reference-faithful mode reproduces the oracle's terms and
+    stopping decisions on the same xi.
+"""
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import ggem_gb300 as G
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+GOLD = Path(__file__).resolve().parent / "golden"
+
+FP64_TOL = 1e-12
+FP32_TOL = 1e-6
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    from ggem_gb300 import build as B
+    B.build()
+    O.build_oracle(with_ref=False)
+
+
+def rel(a, b):
+    return np.linalg.norm(np.asarray(a) - np.asarray(b)) / np.linalg.norm(np.asarray(b))
+
+
+def suspension(n, phi, seed):
+    xyz, L = G.make_suspension(seed, n, phi)
+    return xyz, L
+
+
+def test_golden_velocity_profile_local_field():
+    """The reference's PointParticle_Stokes_GGEM golden profiles through
+    ggem_local_field (cut-off at search_radius_p = 4/alpha, copss.C:1074)."""
+    g = json.loads((GOLD / "ggem_profile_3P.json").read_text())
+    lo, hi = g["box"]
+    with G.Context(alpha=g["alpha"], box_lo=(lo,) * 3, box_hi=(hi,) * 3, periodic=(0, 0, 0),
+                   rc=4.0 / g["alpha"], precision=G.FP64) as ctx:
+        ctx.set_particles(np.array(g["beads"]))
+        ctx.build_cells()
+        f = np.array([g["force"]] * 3)
+        tol = 0.5 * 10.0 ** (-g["print_decimals"]) + 1e-12
+        for ax, name in enumerate("xyz"):
+            A = g["axes"][name]
+            pts = np.zeros((len(A["coord"]), 3))
+            pts[:, ax] = A["coord"]
+            u = ctx.local_field(pts, f)
+            assert np.abs(u - np.array(A["local"])).max() <= tol
+
+
+def test_constants_and_green_tensor_match_oracle():
+    with G.Context(alpha=0.5, box_hi=(30.0,) * 3, precision=G.FP64) as ctx:
+        k = ctx.constants()
+        c = O.constants(alpha=0.5)
+        for name in ("ksi", "coeff_1", "coeff_2", "one_eight_pi_mu", "alpha3_pi_23"):
+            assert getattr(k, name) == getattr(c, name)
+        rng = np.random.default_rng(0)
+        x = rng.normal(size=(200, 3)) * 3
+        x[0] = 0.0
+        x[1] = [1e-7, 0, 0]
+        Gd = ctx.green_tensor_local(x)
+        Go = np.array([O.green_local(c, v) for v in x])
+        assert np.abs(Gd - Go).max() <= 1e-14 * np.abs(Go).max()
+
+
+@pytest.mark.parametrize("prec", [G.FP64, G.FP32])
+@pytest.mark.parametrize("cell_div", [1, 2])
+def test_cutoff_neighbor_lists_bit_exact(prec, cell_div):
+    if prec == G.FP64 and cell_div == 2:
+        pytest.skip("FP64 sweeps rc-sized cells")
+    xyz, L = suspension(3000, 0.1, 11)
+    with G.Context(box_hi=(L,) * 3, rc=7.0, precision=prec, cell_div=cell_div) as ctx:
+        ctx.set_particles(xyz)
+        ctx.build_cells()
+        off, ids = ctx.neighbors()
+        want = O.neighbors_cutoff(O.make_box([0] * 3, [L] * 3, [1, 1, 1]), xyz, 7.0)
+        assert np.array_equal(off, want.offsets)
+        assert np.array_equal(ids, want.ids)
+        assert ctx.pair_count() == want.offsets[-1]
+
+
+def test_cutoff_lists_with_boundary_pairs_bit_exact():
+    """Pairs placed at |r| = rc within rounding: the FP32 filter must defer
+    to the exact FP64 predicate."""
+    rng = np.random.default_rng(5)
+    L = 40.0
+    base = rng.uniform(0, L, (400, 3))
+    d = rng.normal(size=(400, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    eps = rng.choice([-1, 0, 1], size=(400, 1)) * 1e-14
+    other = np.mod(base + d * (7.0 + eps), L)
+    xyz = np.concatenate([base, other])
+    box = O.make_box([0] * 3, [L] * 3, [1, 1, 1])
+    want = O.neighbors_cutoff(box, xyz, 7.0)
+    for prec in (G.FP64, G.FP32):
+        with G.Context(box_hi=(L,) * 3, rc=7.0, precision=prec) as ctx:
+            ctx.set_particles(xyz)
+            ctx.build_cells()
+            off, ids = ctx.neighbors()
+            assert np.array_equal(off, want.offsets) and np.array_equal(ids, want.ids)
+
+
+def test_reference_mode_lists_bit_exact():
+    xyz, L = suspension(600, 0.05, 3)
+    nm = 16
+    h = L / nm
+    sre = 0.5 * h + 4.0 / 0.5 + 1e-3
+    box = O.make_box([0] * 3, [L] * 3, [1, 1, 1])
+    mesh = O.make_mesh(nm, nm, nm, sre)
+    want = O.neighbors_reference(box, mesh, xyz)
+    with G.Context(box_hi=(L,) * 3, nb_mode=G.NB_REFERENCE, n_mesh=(nm,) * 3,
+                   search_radius_e=sre, precision=G.FP64) as ctx:
+        ctx.set_particles(xyz)
+        ctx.build_cells()
+        off, ids = ctx.neighbors()
+        wl = [np.sort(x) for x in want.lists()]
+        assert np.array_equal(off, np.concatenate([[0], np.cumsum([len(x) for x in wl])]))
+        assert np.array_equal(ids, np.concatenate(wl))
+        _, eop = O.elem_lists(box, mesh, xyz)
+        assert np.array_equal(ctx.cell_of_particles(), eop)
+
+
+@pytest.mark.parametrize("self_mode", [G.SELF_NONE, G.SELF_BEAD, G.SELF_LAGRANGIAN])
+@pytest.mark.parametrize("nrhs", [1, 3])
+def test_fp64_matvec_cutoff(self_mode, nrhs):
+    xyz, L = suspension(2000, 0.1, 21)
+    box = O.make_box([0] * 3, [L] * 3, [1, 1, 1])
+    c = O.constants(alpha=0.5)
+    nb = O.neighbors_cutoff(box, xyz, 7.0)
+    f = np.random.default_rng(2).standard_normal((nrhs, len(xyz), 3))
+    want = O.local_matvec(c, box, xyz, nb, f, self_mode)
+    with G.Context(box_hi=(L,) * 3, rc=7.0, precision=G.FP64) as ctx:
+        ctx.set_particles(xyz)
+        ctx.build_cells()
+        got = ctx.local_matvec(f, self_mode)
+    assert rel(got, want) <= FP64_TOL
+
+
+def test_fp64_matvec_reference_mode_non_periodic_axis():
+    rng = np.random.default_rng(4)
+    L = np.array([36.0, 36.0, 20.0])
+    xyz = rng.uniform(0, 1, (700, 3)) * L
+    nm = (12, 12, 7)
+    sre = 0.5 * 3.0 + 4.0 / 0.5 + 1e-3
+    box = O.make_box([0] * 3, L, [1, 1, 0])
+    mesh = O.make_mesh(*nm, sre)
+    c = O.constants(alpha=0.5)
+    nb = O.neighbors_reference(box, mesh, xyz)
+    f = rng.standard_normal((len(xyz), 3))
+    want = O.local_matvec(c, box, xyz, nb, f, O.SELF_BEAD)
+    with G.Context(box_hi=tuple(L), periodic=(1, 1, 0), nb_mode=G.NB_REFERENCE, n_mesh=nm,
+                   search_radius_e=sre, precision=G.FP64) as ctx:
+        ctx.set_particles(xyz)
+        ctx.build_cells()
+        got = ctx.local_matvec(f, G.SELF_BEAD)
+    assert rel(got, want) <= FP64_TOL
+
+
+@pytest.mark.parametrize("nrhs", [1, 5, 8])
+@pytest.mark.parametrize("cell_div", [1, 2])
+def test_fp32_matvec_error(nrhs, cell_div):
+    xyz, L = suspension(5000, 0.1, 31)
+    box = O.make_box([0] * 3, [L] * 3, [1, 1, 1])
+    c = O.constants(alpha=0.5)
+    nb = O.neighbors_cutoff(box, xyz, 7.0)
+    f = np.random.default_rng(3).standard_normal((nrhs, len(xyz), 3))
+    want = O.local_matvec(c, box, xyz, nb, f, O.SELF_BEAD, nthreads=8)
+    with G.Context(box_hi=(L,) * 3, rc=7.0, precision=G.FP32, cell_div=cell_div) as ctx:
+        ctx.set_particles(xyz)
+        ctx.build_cells()
+        got = ctx.local_matvec(f, G.SELF_BEAD)
+    err = rel(got, want)
+    comp = np.abs(got - want).max() / np.abs(want).max()
+    print(f"FP32 nrhs={nrhs} div={cell_div}: norm-wise {err:.2e}, max component {comp:.2e}")
+    assert err <= FP32_TOL
+    assert comp <= 10 * FP32_TOL
+
+
+def test_fp32_matvec_chains_short_bonds():
+    xyz, L = G.make_chains(4, 150, 20, 2.0, 0.05)
+    box = O.make_box([0] * 3, [L] * 3, [1, 1, 1])
+    c = O.constants(alpha=0.5)
+    nb = O.neighbors_cutoff(box, xyz, 7.0)
+    f = np.random.default_rng(6).standard_normal((len(xyz), 3))
+    want = O.local_matvec(c, box, xyz, nb, f, O.SELF_BEAD)
+    with G.Context(box_hi=(L,) * 3, rc=7.0, precision=G.FP32) as ctx:
+        ctx.set_particles(xyz)
+        ctx.build_cells()
+        assert rel(ctx.local_matvec(f, G.SELF_BEAD), want) <= FP32_TOL
+
+
+def test_spread_and_element_rhs_reference_mode():
+    rng = np.random.default_rng(8)
+    L = 24.0
+    nm = 6
+    xyz = rng.uniform(0, L, (150, 3))
+    f = rng.standard_normal((150, 3))
+    sre = 0.5 * (L / nm) + 4.0 / 0.5 + 1e-3
+    box = O.make_box([0] * 3, [L] * 3, [1, 1, 1])
+    mesh = O.make_mesh(nm, nm, nm, sre)
+    c = O.constants(alpha=0.5)
+    enb, _ = O.elem_lists(box, mesh, xyz)
+    ne, nq, nu = nm ** 3, 8, 20
+    # 2x2x2 Gauss points inside each element
+    g1 = 0.5 - 0.5 / np.sqrt(3.0)
+    h = L / nm
+    q = []
+    for e in range(ne):
+        ix, iy, iz = e % nm, (e // nm) % nm, e // (nm * nm)
+        for a in (g1, 1 - g1):
+            for b in (g1, 1 - g1):
+                for cc in (g1, 1 - g1):
+                    q.append([(ix + cc) * h, (iy + b) * h, (iz + a) * h])
+    q = np.array(q)
+    qe = np.repeat(np.arange(ne), nq).astype(np.int32)
+    IF = rng.standard_normal((ne, nu * nq))
+    rho_o = O.spread_qp(c, box, enb, xyz, f, q, qe)
+    Fe_o = O.element_rhs(c, box, enb, xyz, f, ne, nq, nu, q, IF)
+    with G.Context(box_hi=(L,) * 3, nb_mode=G.NB_REFERENCE, n_mesh=(nm,) * 3,
+                   search_radius_e=sre, precision=G.FP64) as ctx:
+        ctx.set_particles(xyz)
+        ctx.build_cells()
+        rho = ctx.spread_qp(q, f, qe)
+        Fe = ctx.element_rhs(ne, nq, nu, q, IF, f)
+    assert rel(rho, rho_o) <= FP64_TOL
+    assert rel(Fe, Fe_o) <= FP64_TOL
+
+
+def test_spread_cutoff_mode():
+    xyz, L = suspension(800, 0.1, 13)
+    f = np.random.default_rng(1).standard_normal((len(xyz), 3))
+    q = np.random.default_rng(2).uniform(0, L, (3000, 3))
+    box = O.make_box([0] * 3, [L] * 3, [1, 1, 1])
+    c = O.constants(alpha=0.5)
+    want = O.spread_qp(c, box, None, xyz, f, q, None, rc=8.0)
+    with G.Context(box_hi=(L,) * 3, rc=7.0, precision=G.FP64) as ctx:
+        ctx.set_particles(xyz)
+        ctx.build_cells()
+        got = ctx.spread_qp(q, f, None, spread_rc=8.0)
+    assert rel(got, want) <= FP64_TOL
+
+
+def _dense(c, box, xyz, nb):
+    n = len(xyz)
+    E = np.eye(3 * n).reshape(3 * n, n, 3)
+    return O.local_matvec(c, box, xyz, nb, E, O.SELF_BEAD, nthreads=8).reshape(3 * n, 3 * n).T
+
+
+def test_chebyshev_faithful_matches_oracle_fp64():
+    xyz, L = suspension(400, 0.1, 41)
+    box = O.make_box([0] * 3, [L] * 3, [1, 1, 1])
+    c = O.constants(alpha=0.5)
+    nb = O.neighbors_cutoff(box, xyz, 7.0)
+    M = _dense(c, box, xyz, nb)
+    w = np.linalg.eigvalsh(M)
+    lmin, lmax = w[0] / 1.05, w[-1] * 1.05
+    xi = O.std_normal_vector(123456789, 3 * len(xyz))
+    op = O.Operator(matvec=(c, box, xyz, nb, O.SELF_BEAD, 1))
+    for tol in (1e-2, 1e-3):
+        y_o, rep_o = O.cheb_inv_sqrt(op, xi, 30, lmin, lmax, tol)
+        with G.Context(box_hi=(L,) * 3, rc=7.0, precision=G.FP64) as ctx:
+            ctx.set_particles(xyz)
+            ctx.build_cells()
+            y, rep = ctx.cheb_inv_sqrt(xi, 30, lmin, lmax, tol)
+        r = rep[0]
+        assert r["converged"] == rep_o.converged and r["n_terms"] == rep_o.n_terms
+        assert r["n_matvecs"] == rep_o.n_matvecs
+        assert r["err1"] == pytest.approx(rep_o.err1, rel=1e-8)
+        assert r["err2"] == pytest.approx(rep_o.err2, rel=1e-8)
+        assert rel(y, y_o) <= 1e-11
+
+
+def test_chebyshev_fp32_batched_rhs_accuracy():
+    xyz, L = suspension(1500, 0.1, 43)
+    box = O.make_box([0] * 3, [L] * 3, [1, 1, 1])
+    c = O.constants(alpha=0.5)
+    nb = O.neighbors_cutoff(box, xyz, 7.0)
+    op = O.Operator(matvec=(c, box, xyz, nb, O.SELF_BEAD, 8))
+    xi = np.random.default_rng(7).standard_normal((4, 3 * len(xyz)))
+    with G.Context(box_hi=(L,) * 3, rc=7.0, precision=G.FP32) as ctx:
+        ctx.set_particles(xyz)
+        ctx.build_cells()
+        lo, hi = ctx.lanczos_bounds(k=40, seed=5)
+        y, reps = ctx.cheb_inv_sqrt(xi, 50, lo / 1.05, hi * 1.05, 1e-3, check_every=1)
+    for r in range(4):
+        y_o, rep_o = O.cheb_inv_sqrt(op, xi[r], 50, lo / 1.05, hi * 1.05, 1e-3)
+        assert reps[r]["converged"] == 1
+        assert rel(y.reshape(4, -1)[r], y_o) <= 1e-5
+
+
+def test_lanczos_bounds_vs_dense_eigenvalues():
+    xyz, L = suspension(160, 0.05, 51)
+    box = O.make_box([0] * 3, [L] * 3, [1, 1, 1])
+    c = O.constants(alpha=0.5)
+    nb = O.neighbors_cutoff(box, xyz, 7.0)
+    w = np.linalg.eigvalsh(_dense(c, box, xyz, nb))
+    for prec, tol in ((G.FP64, 1e-9), (G.FP32, 1e-5)):
+        with G.Context(box_hi=(L,) * 3, rc=7.0, precision=prec) as ctx:
+            ctx.set_particles(xyz)
+            ctx.build_cells()
+            lo, hi = ctx.lanczos_bounds(k=3 * len(xyz), seed=1)
+            assert lo == pytest.approx(w[0], rel=tol) and hi == pytest.approx(w[-1], rel=tol)
+            lo30, hi30 = ctx.lanczos_bounds(k=30, seed=1)
+            assert w[0] * (1 - tol) <= lo30 and hi30 <= w[-1] * (1 + tol)
+            it, lam = ctx.power_iteration(tol=1e-3, maxits=5000)
+            assert lam == pytest.approx(w[-1], rel=2e-3)
+
+
+def test_philox_noise_matches_oracle():
+    import torch
+    n = 10001
+    d = torch.empty(n, dtype=torch.float64, device="cuda")
+    with G.Context(box_hi=(30.0,) * 3) as ctx:
+        ctx.philox_normals_dev(99, 7, n, d.data_ptr())
+        ctx.synchronize()
+    got = d.cpu().numpy()
+    want = O.philox_normals(99, 7, n)
+    assert np.abs(got - want).max() <= 1e-13
+    assert abs(got.mean()) < 0.05 and abs(got.std() - 1) < 0.05
+
+
+def test_errors_are_reported_not_raised_on_device():
+    with G.Context(box_hi=(20.0,) * 3, periodic=(0, 0, 0), precision=G.FP64) as ctx:
+        ctx.set_particles(np.array([[1.0, 1.0, 1.0], [25.0, 1.0, 1.0]]))
+        with pytest.raises(G.GGEMError) as e:
+            ctx.build_cells()
+        assert e.value.code == G.ERR_OUT_OF_DOMAIN
+    with pytest.raises(G.GGEMError) as e:
+        G.Context(box_hi=(15.0,) * 3, rc=7.0)  # periodic edge < 3 rc
+    assert e.value.code == G.ERR_BAD_ARG
+    xyz, L = suspension(200, 0.05, 2)
+    with G.Context(box_hi=(L,) * 3, rc=7.0, precision=G.FP64) as ctx:
+        ctx.set_particles(xyz)
+        ctx.build_cells()
+        with pytest.raises(G.GGEMError) as e:
+            ctx.cheb_inv_sqrt(np.ones(3 * len(xyz)), 10, 2.0, 1.0, 0.1)
+        assert e.value.code == G.ERR_INVALID_RANGE
+
+
+def test_device_pointer_matvec_with_torch_stream():
+    import torch
+    xyz, L = suspension(1000, 0.1, 61)
+    f = np.random.default_rng(0).standard_normal((2, len(xyz), 3))
+    with G.Context(box_hi=(L,) * 3, rc=7.0, precision=G.FP32) as ctx:
+        ctx.set_particles(xyz)
+        ctx.build_cells()
+        want = ctx.local_matvec(f, G.SELF_BEAD)
+        s = torch.cuda.Stream()
+        df = torch.from_numpy(f).cuda()
+        du = torch.empty_like(df)
+        ctx.set_stream(s.cuda_stream)
+        torch.cuda.current_stream().synchronize()
+        ctx.local_matvec_dev(df.data_ptr(), du.data_ptr(), 2, G.SELF_BEAD)
+        s.synchronize()
+        ctx.set_stream(0)
+        assert np.array_equal(du.cpu().numpy(), want)
