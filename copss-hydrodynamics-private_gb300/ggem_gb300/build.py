@@ -61,8 +61,10 @@ def up_to_date() -> bool:
     if not LIB.exists():
         return False
     t = LIB.stat().st_mtime
-    deps = list(sources()) + list(CSRC.glob("*.cuh")) + list(INCLUDE.glob("*.h")) + [Path(__file__)]
-    return all(d.stat().st_mtime <= t for d in deps)
+    deps = (list(sources()) + list(CSRC.glob("*.cuh")) + list(INCLUDE.glob("*.h")) +
+            list((ROOT / "cpp").glob("*")) + [Path(__file__)])
+    tools = [OUT_DIR / s.stem for s in (ROOT / "cpp").glob("*.cpp")]
+    return all(x.exists() for x in tools) and all(d.stat().st_mtime <= t for d in deps)
 
 
 def build(force: bool = False, verbose_ptxas: bool = False) -> Path:
@@ -80,7 +82,27 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> Path:
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    build_tools()
     return LIB
+
+
+CPP = ROOT / "cpp"
+
+
+def build_tools() -> list:
+    """C++ host programs over the C ABI (cpp/*.cpp), linked to the library
+    with an $ORIGIN rpath so they run from ggem_gb300/_lib/."""
+    outs = []
+    for src in sorted(CPP.glob("*.cpp")):
+        exe = OUT_DIR / src.stem
+        cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", f"-I{INCLUDE}", f"-I{CPP}",
+               str(src), "-o", str(exe), f"-L{OUT_DIR}", "-lggem_gb300",
+               "-Wl,-rpath,$ORIGIN"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"g++ failed on {src.name}:\n{r.stdout}\n{r.stderr}")
+        outs.append(exe)
+    return outs
 
 
 if __name__ == "__main__":
