@@ -448,7 +448,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--check-every", type=int, default=4)
+    ap.add_argument("--check-every", type=int, default=0)
     ap.add_argument("--fp64-steps", type=int, default=2)
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")

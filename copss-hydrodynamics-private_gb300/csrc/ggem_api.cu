@@ -134,11 +134,14 @@ int upload_stencil(ggem_ctx *c) {
                    cudaMemcpyHostToDevice);
     if (e) return cuda_fail(c, e, "stencil upload");
   }
-  std::vector<float4> sh(std::max<size_t>(1, c->stencil.size()));
-  for (size_t k = 0; k < c->stencil.size(); ++k) {
-    const int4 o = c->stencil[k];
-    sh[k] = make_float4((float)(o.x * c->grid.h[0]), (float)(o.y * c->grid.h[1]),
-                        (float)(o.z * c->grid.h[2]), 0.f);
+  // FP32 cell shift per entry code (cut-off mode only: codes < kMaxCode)
+  std::vector<float4> sh(kMaxCode, make_float4(0.f, 0.f, 0.f, 0.f));
+  if (c->prm.nb_mode == GGEM_NB_CUTOFF) {
+    for (size_t k = 0; k < c->stencil.size(); ++k) {
+      const int4 o = c->stencil[k];
+      sh[o.w] = make_float4((float)(o.x * c->grid.h[0]), (float)(o.y * c->grid.h[1]),
+                            (float)(o.z * c->grid.h[2]), 0.f);
+    }
   }
   e = c->d_shift.ensure(sh.size());
   if (e == cudaSuccess)
@@ -213,8 +216,11 @@ int validate_and_setup(ggem_ctx *c) {
           const double gy = std::max(0, std::abs(dy) - 1) * g.h[1];
           const double gz = std::max(0, std::abs(dz) - 1) * g.h[2];
           if (gx * gx + gy * gy + gz * gz >= p.rc * p.rc) continue;
-          // a non-periodic axis with fewer cells than the offset never wraps
-          c->stencil.push_back(make_int4(dx, dy, dz, 0));
+          // w: the offset's index in the full (2 div + 1)^3 cube, the code a
+          // pair entry carries (decoded arithmetically by the pair kernel)
+          const int side = 2 * div + 1;
+          const int code = ((dz + div) * side + (dy + div)) * side + (dx + div);
+          c->stencil.push_back(make_int4(dx, dy, dz, code));
         }
     c->rc2 = p.rc * p.rc;
     c->rc2_lo = (float)(c->rc2 * (1.0 - 1e-4));

@@ -268,7 +268,10 @@ __global__ void k_pair_list(int64_t n, Grid g, const int4 *__restrict__ stencil,
       }
       if (!in) continue;
       if (FILL) {
-        if (cnt < width) list[base + (int64_t)cnt * kSlice + lane] = ((uint32_t)t << kCodeBits) | (uint32_t)k;
+        // entry code: the stencil offset in (2d+1)^3 index space (int4.w)
+        if (cnt < width)
+          list[base + (int64_t)cnt * kSlice + lane] =
+              ((uint32_t)t << kCodeBits) | (uint32_t)stencil[k].w;
         else atomicOr(err, kErrListOverflow);
       }
       ++cnt;

@@ -281,96 +281,129 @@ int ensure_cheb_buffers(ggem_ctx *c, size_t len) {
   return GGEM_OK;
 }
 
-// Chebyshev on slot-ordered xi (c->w_in); leaves y in c->w_y
+// Chebyshev on slot-ordered xi (c->w_in); leaves y in c->w_y.
+//
+// check_every = 1: the reference's loop (brownian_system.C:1089-1155): the
+//   error-check matvec dw_mid = M dw and both estimators every term.
+// check_every = k > 1: err1/err2 are evaluated at every k-th term (and the
+//   last); the norms of a term come from the fused term kernel.
+// check_every = 0: the first check is at the degree the previous call
+//   converged at (8 on the first call), then every term; the prediction is
+//   lowered by one whenever the first check already passes.
+// Only check points synchronise with the host.  On return *dm_is_my tells
+// whether c->w_out holds M y for every right-hand side (the last check ran
+// on the final y), which the Brownian displacement reuses.
 int cheb_slots(ggem_ctx *c, int nrhs, int N, double eig_min, double eig_max, double tol,
-               int check_every, ggem_cheb_report *rep) {
+               int check_every, ggem_cheb_report *rep, bool *dm_is_my) {
   const int64_t D = 3 * c->n;
   const int64_t tot = D * nrhs;
   const int sm = brownian_self_mode(c);
   const int G = vec_blocks(D);
   cudaStream_t st = c->stream;
   double *x0 = c->w_c.p, *x1 = c->w_d.p, *xm = c->w_e.p, *dw = c->w_y.p, *dm = c->w_out.p;
+  // reduction regions: term norms [2 nrhs][G], |dm|^2 [nrhs][G], xi.M.xi
+  // [nrhs][G], then the 4 nrhs finalized values
+  double *p_term = c->w_red.p;
+  double *p_dm = p_term + (size_t)2 * nrhs * G;
+  double *p_aux2 = p_dm + (size_t)nrhs * G;
   // brownian_system.C:1001-1003 and the coefficients of :1021-1024
   const double d_eig = eig_max - eig_min;
   const double da = 2.0 / d_eig;
   const double db = -(eig_max + eig_min) / d_eig;
   std::vector<double> X(N + 1);
   cheb_coeffs_host(N, da, db, GGEM_CHEB_GAUSS, X.data());
-  std::vector<double> aux2(nrhs), aux1(nrhs), aux3(nrhs), aux4(nrhs);
   std::vector<int> active(nrhs, 1);
   for (int r = 0; r < nrhs; ++r) rep[r] = ggem_cheb_report{0, 1, 0, 0.0, 0.0};
   double *h = c->h_red;
-  // x0 = xi; x1 = M x0; aux2 = x1.x0; x1 = db x0 + da x1
+  const bool faithful = check_every == 1;
+  const int k_first = (check_every == 0) ? std::max(2, c->cheb_pred_terms > 0 ? c->cheb_pred_terms : 8)
+                                         : 0;
+  *dm_is_my = false;
+  // x0 = xi; x1 = M x0; aux2 = x1.x0; x1 = db x0 + da x1   (:1036-1041)
   k_copy<<<grid1(tot), 256, 0, st>>>(tot, c->w_in.p, x0);
   if (int rc = check_launch(c, "copy")) return rc;
   if (int rc = matvec_slots(c, nrhs, x0, x1, sm)) return rc;
-  if (int rc = dot_to_host(c, nrhs, D, x1, x0, h)) return rc;
-  for (int r = 0; r < nrhs; ++r) aux2[r] = h[r];
+  k_dot_partials<<<dim3(G, nrhs), kVecThreads, 0, st>>>(D, x1, x0, p_aux2);
+  if (int rc = check_launch(c, "aux2")) return rc;
   k_cheb_first<<<grid1(tot), 256, 0, st>>>(D, nrhs, da, db, x0, x1);
   if (int rc = check_launch(c, "cheb first")) return rc;
-  k_cheb_init<<<dim3(G, nrhs), kVecThreads, 0, st>>>(D, X[0], X[1], x0, x1, dw, c->w_red.p);
+  // dw = c0 x0, dw += c1 x1 with both norms   (:1050-1056)
+  k_cheb_init<<<dim3(G, nrhs), kVecThreads, 0, st>>>(D, X[0], X[1], x0, x1, dw, p_term);
   if (int rc = check_launch(c, "cheb init")) return rc;
-  if (int rc = finalize_to_host(c, 2 * nrhs, G, h)) return rc;
-  for (int r = 0; r < nrhs; ++r) {
-    aux4[r] = std::sqrt(h[r]);
-    aux3[r] = std::sqrt(h[nrhs + r]) * std::fabs(X[1]);
-  }
-  if (int rc = matvec_slots(c, nrhs, dw, dm, sm)) return rc;
-  if (int rc = sumsq_to_host(c, nrhs, D, dm, h)) return rc;
-  for (int r = 0; r < nrhs; ++r) {
-    aux1[r] = h[r];
-    rep[r].n_matvecs = 2;
-    if (aux2[r] != 0.0) rep[r].err1 = std::sqrt(std::fabs(aux1[r] - aux2[r]) / aux2[r]);
-    if (aux4[r] != 0.0) rep[r].err2 = aux3[r] / aux4[r];
+  for (int r = 0; r < nrhs; ++r) rep[r].n_matvecs = 1;
+
+  // evaluate err1 / err2 of the current dw for the active right-hand sides
+  auto check_now = [&](double coef_abs, bool apply_rules) -> int {
+    if (int rc = matvec_slots(c, nrhs, dw, dm, sm)) return rc;
+    k_dot_partials<<<dim3(G, nrhs), kVecThreads, 0, st>>>(D, dm, dm, p_dm);
+    if (int rc = check_launch(c, "dm norm")) return rc;
+    if (int rc = finalize_to_host(c, 4 * nrhs, G, h)) return rc;
+    for (int r = 0; r < nrhs; ++r) {
+      if (!active[r]) continue;
+      const double aux4 = std::sqrt(h[r]);
+      const double aux3 = std::sqrt(h[nrhs + r]) * coef_abs;
+      const double aux1 = h[2 * nrhs + r], aux2 = h[3 * nrhs + r];
+      rep[r].n_matvecs += 1;
+      if (aux2 != 0.0) rep[r].err1 = std::sqrt(std::fabs(aux1 - aux2) / aux2);
+      if (aux4 != 0.0) rep[r].err2 = aux3 / aux4;
+      if (!apply_rules) continue;
+      if (rep[r].err1 <= tol) {  // :1138-1147
+        rep[r].converged = 1;
+        active[r] = 0;
+        continue;
+      }
+      if (rep[r].err2 <= 1E-9) active[r] = 0;  // :1150
+    }
+    return GGEM_OK;
+  };
+
+  if (faithful) {  // the estimators before the loop (:1064-1072)
+    if (int rc = check_now(std::fabs(X[1]), false)) return rc;
+    *dm_is_my = true;
   }
   const double two_da = 2. * da, two_db = 2. * db;
-  int n_active = nrhs;
-  for (int i = 1; i < N && n_active > 0; ++i) {
+  int first_check = -1;
+  for (int i = 1; i < N; ++i) {
+    int n_active = 0;
+    for (int r = 0; r < nrhs; ++r) n_active += active[r];
+    if (n_active == 0) break;
     if (int rc = matvec_slots(c, nrhs, x1, xm, sm)) return rc;
     RhsCoef cf;
     for (int r = 0; r < nrhs; ++r) cf.c[r] = active[r] ? X[i + 1] : 0.0;
     kt_start(c, kKChebTerm);
     k_cheb_term<<<dim3(G, nrhs), kVecThreads, 0, st>>>(D, two_da, two_db, cf, x0, x1, xm, dw,
-                                                        c->w_red.p);
+                                                        p_term);
     kt_stop(c, kKChebTerm);
     if (int rc = check_launch(c, "cheb term")) return rc;
-    if (int rc = finalize_to_host(c, 2 * nrhs, G, h)) return rc;
-    for (int r = 0; r < nrhs; ++r) {
-      if (!active[r]) continue;
-      aux4[r] = std::sqrt(h[r]);
-      aux3[r] = std::sqrt(h[nrhs + r]) * std::fabs(X[i + 1]);
-      rep[r].n_matvecs += 1;
-      rep[r].n_terms = i + 1;
-      if (aux4[r] != 0.0) rep[r].err2 = aux3[r] / aux4[r];
-    }
-    const bool check = (check_every <= 1) || (i % check_every == 0) || (i == N - 1);
-    if (check) {
-      if (int rc = matvec_slots(c, nrhs, dw, dm, sm)) return rc;
-      if (int rc = sumsq_to_host(c, nrhs, D, dm, h)) return rc;
-    }
-    for (int r = 0; r < nrhs; ++r) {
-      if (!active[r]) continue;
-      if (check) {
+    for (int r = 0; r < nrhs; ++r)
+      if (active[r]) {
         rep[r].n_matvecs += 1;
-        aux1[r] = h[r];
-        if (aux2[r] != 0.0) rep[r].err1 = std::sqrt(std::fabs(aux1[r] - aux2[r]) / aux2[r]);
-        if (rep[r].err1 <= tol) {  // brownian_system.C:1138-1147
-          rep[r].converged = 1;
-          active[r] = 0;
-          --n_active;
-          continue;
-        }
+        rep[r].n_terms = i + 1;
       }
-      if (rep[r].err2 <= 1E-9) {  // :1150
-        active[r] = 0;
-        --n_active;
-      }
+    bool check;
+    if (faithful) check = true;
+    else if (check_every > 1) check = (i % check_every == 0) || (i == N - 1);
+    else check = (i + 1 >= k_first) || (i == N - 1);
+    *dm_is_my = false;
+    if (check) {
+      if (int rc = check_now(std::fabs(X[i + 1]), true)) return rc;
+      *dm_is_my = true;
+      if (first_check < 0) first_check = i + 1;
     }
     // x0 <- x1, x1 <- xm (:1152-1153) by rotating the buffers
     double *t = x0;
     x0 = x1;
     x1 = xm;
     xm = t;
+  }
+  if (check_every == 0) {
+    int worst = 0;
+    bool all = true;
+    for (int r = 0; r < nrhs; ++r) {
+      all = all && rep[r].converged;
+      worst = std::max(worst, rep[r].n_terms);
+    }
+    if (all) c->cheb_pred_terms = (worst == first_check) ? std::max(2, worst - 1) : worst;
   }
   return GGEM_OK;
 }
@@ -399,7 +432,9 @@ extern "C" int ggem_cheb_inv_sqrt_dev(ggem_ctx *ctx, int nrhs, int N, double eig
   const size_t len = (size_t)ctx->n * 3 * nrhs;
   if (int rc = ensure_cheb_buffers(ctx, len)) return rc;
   if (int rc = permute_to_slots(ctx, nrhs, d_xi, ctx->w_in.p)) return rc;
-  if (int rc = cheb_slots(ctx, nrhs, N, eig_min, eig_max, tol_cheb, check_every, rep)) return rc;
+  bool dm_is_my = false;
+  if (int rc = cheb_slots(ctx, nrhs, N, eig_min, eig_max, tol_cheb, check_every, rep, &dm_is_my))
+    return rc;
   return permute_from_slots(ctx, nrhs, ctx->w_y.p, d_xi);
 }
 
@@ -453,15 +488,20 @@ extern "C" int ggem_brownian_displacement_dev(ggem_ctx *ctx, int nrhs, int N, do
   const size_t len = (size_t)ctx->n * 3 * nrhs;
   if (int rc = ensure_cheb_buffers(ctx, len)) return rc;
   if (int rc = permute_to_slots(ctx, nrhs, d_xi, ctx->w_in.p)) return rc;
-  if (int rc = cheb_slots(ctx, nrhs, N, eig_min, eig_max, tol_cheb, check_every, rep)) return rc;
+  bool dm_is_my = false;
+  if (int rc = cheb_slots(ctx, nrhs, N, eig_min, eig_max, tol_cheb, check_every, rep, &dm_is_my))
+    return rc;
   bool all = true;
   for (int r = 0; r < nrhs; ++r) all = all && rep[r].converged;
   if (!all)
     return ggem::fail(ctx, GGEM_ERR_CHEB_NOT_CONVERGED,
                       "Chebyshev polynomial fails to converge (brownian_system.C:1162-1163)");
-  // hi_ewald: dw = M y (copss.C:1686)
-  if (int rc = matvec_slots(ctx, nrhs, ctx->w_y.p, ctx->w_out.p, brownian_self_mode(ctx)))
-    return rc;
+  // hi_ewald: dw = M y (copss.C:1686); the last error check already
+  // computed M y when it ran on the final y
+  if (!dm_is_my) {
+    if (int rc = matvec_slots(ctx, nrhs, ctx->w_y.p, ctx->w_out.p, brownian_self_mode(ctx)))
+      return rc;
+  }
   return permute_from_slots(ctx, nrhs, ctx->w_out.p, d_dw);
 }
 

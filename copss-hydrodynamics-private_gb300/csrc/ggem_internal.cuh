@@ -120,6 +120,11 @@ struct ggem_ctx {
   ggem::DevBuf<float4> tab;
   float tab_inv_ds = 0.f;
   double tab_max_err = 0.0;
+  // single-RHS pair kernel: 32-byte source records, work counter, grid
+  ggem::DevBuf<float4> w_src;          // 2 float4 per slot
+  ggem::DevBuf<unsigned int> work;     // slice counter of the persistent grid
+  int pair_grid = 0;                   // CTAs of the persistent pair kernel
+  int cheb_pred_terms = 0;             // degree the last adaptive Chebyshev needed
 
   // scan scratch (one per recursion level)
   std::vector<ggem::DevBuf<int64_t> *> scan_scratch;

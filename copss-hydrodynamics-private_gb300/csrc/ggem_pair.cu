@@ -17,6 +17,8 @@
 // rsqrt/exp/erf = 1 each), bound by the FP32 pipe.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "ggem_internal.cuh"
 
 namespace ggem {
@@ -146,6 +148,98 @@ __device__ __forceinline__ void kahan_add(float &sum, float &comp, float v) {
   sum = t;
 }
 
+// One 32-byte record per source (position relative to its cell centre and
+// the force of the single right-hand side) and per table piece (cubic
+// coefficients of A and of B): each pair then issues one 32-byte gather for
+// the source and one for the tensor instead of four 16-byte gathers.
+struct __align__(32) Rec32 {
+  float4 a, b;
+};
+
+__global__ void k_build_src(int64_t n, const float4 *__restrict__ pos32,
+                            const double *__restrict__ f, Rec32 *__restrict__ src) {
+  const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  Rec32 r;
+  r.a = pos32[s];
+  r.b = make_float4((float)f[3 * s], (float)f[3 * s + 1], (float)f[3 * s + 2], 0.f);
+  src[s] = r;
+}
+
+// add a short plain-FP32 block sum into a Kahan-compensated accumulator
+__device__ __forceinline__ void fold(float &sum, float &comp, float &blk) {
+  kahan_add(sum, comp, blk);
+  blk = 0.f;
+}
+
+// Single right-hand side pair sum.  Persistent warps take 32-target slices
+// from a work counter (dynamic balance of the uneven list lengths and no
+// tail wave); per pair: one coalesced list word, one 32-byte source gather,
+// one 32-byte table gather, the cell shift decoded from the entry code.
+// Sums run as plain FP32 over blocks of 8 pairs folded into a Kahan
+// accumulator per component.
+template <int CD>
+__global__ void __launch_bounds__(256) k_pair_f32_r1(
+    int64_t n, int64_t nslice, const Rec32 *__restrict__ src, const int32_t *__restrict__ count,
+    const int64_t *__restrict__ slice_off, const uint32_t *__restrict__ list,
+    const Rec32 *__restrict__ tab, float inv_ds, float hx, float hy, float hz, float self_c,
+    double *__restrict__ u, unsigned int *__restrict__ work) {
+  constexpr int SIDE = 2 * CD + 1;
+  const int lane = threadIdx.x & 31;
+  const float top = (float)(kTableN - 1);
+  for (;;) {
+    unsigned int sl = 0;
+    if (lane == 0) sl = atomicAdd(work, 1u);
+    sl = __shfl_sync(0xffffffffu, sl, 0);
+    if (sl >= nslice) break;
+    const int64_t s = (int64_t)sl * kSlice + lane;
+    const bool act = s < n;
+    const int32_t cnt = act ? count[s] : 0;
+    const uint32_t *lp = list + slice_off[sl] + lane;
+    Rec32 ri;
+    ri.a = make_float4(0.f, 0.f, 0.f, 0.f);
+    ri.b = ri.a;
+    if (act) ri = src[s];
+    float sx = self_c * ri.b.x, sy = self_c * ri.b.y, sz = self_c * ri.b.z;
+    float cx = 0.f, cy = 0.f, cz = 0.f, bx = 0.f, by = 0.f, bz = 0.f;
+    for (int32_t m = 0; m < cnt; ++m) {
+      const uint32_t e = __ldg(lp + (int64_t)m * kSlice);
+      const uint32_t j = e >> kCodeBits;
+      const int code = (int)(e & (kMaxCode - 1));
+      const int ox = code % SIDE - CD, oy = (code / SIDE) % SIDE - CD, oz = code / (SIDE * SIDE) - CD;
+      const Rec32 rj = src[j];
+      const float dx = (rj.a.x - ri.a.x) + (float)ox * hx;
+      const float dy = (rj.a.y - ri.a.y) + (float)oy * hy;
+      const float dz = (rj.a.z - ri.a.z) + (float)oz * hz;
+      const float s2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+      const float uu = s2 * inv_ds;
+      const float fi = fminf(floorf(uu), top);
+      const float t = uu - fi;
+      const Rec32 tr = tab[(int)fi];
+      const float A = fmaf(fmaf(fmaf(tr.a.w, t, tr.a.z), t, tr.a.y), t, tr.a.x);
+      const float B = fmaf(fmaf(fmaf(tr.b.w, t, tr.b.z), t, tr.b.y), t, tr.b.x);
+      const float bxf = B * fmaf(dz, rj.b.z, fmaf(dy, rj.b.y, dx * rj.b.x));
+      bx += fmaf(A, rj.b.x, bxf * dx);
+      by += fmaf(A, rj.b.y, bxf * dy);
+      bz += fmaf(A, rj.b.z, bxf * dz);
+      if ((m & 7) == 7) {
+        fold(sx, cx, bx);
+        fold(sy, cy, by);
+        fold(sz, cz, bz);
+      }
+    }
+    fold(sx, cx, bx);
+    fold(sy, cy, by);
+    fold(sz, cz, bz);
+    if (act) {
+      double *ui = u + 3 * s;
+      ui[0] = (double)sx - (double)cx;
+      ui[1] = (double)sy - (double)cy;
+      ui[2] = (double)sz - (double)cz;
+    }
+  }
+}
+
 // FP32 list walk; f32 is [r][n] float4 (x,y,z,0), u is [r][n][3] doubles
 template <int NR>
 __global__ void __launch_bounds__(256) k_matvec_f32(
@@ -263,11 +357,48 @@ int launch_f32(ggem_ctx *c, const float4 *f32, double *u, float self_c, int r0) 
   const unsigned bn = (unsigned)((c->n + T - 1) / T);
   kt_start(c, kKPairF32);
   k_matvec_f32<NR><<<bn, T, 0, c->stream>>>(c->n, c->pos32.p, c->nb_count.p, c->slice_off.p,
-                                             c->nb_list.p, c->d_shift.p,
-                                             (int)c->stencil.size(), c->tab.p, c->tab_inv_ds,
-                                             self_c, f32, u, r0);
+                                             c->nb_list.p, c->d_shift.p, kMaxCode, c->tab.p,
+                                             c->tab_inv_ds, self_c, f32, u, r0);
   kt_stop(c, kKPairF32);
   return check_launch(c, "matvec f32");
+}
+
+// single right-hand side: records from FP64 slot-order f, then the
+// persistent pair kernel over a grid that fills every SM once
+int launch_f32_r1(ggem_ctx *c, const double *f, double *u, float self_c) {
+  const int64_t n = c->n;
+  cudaError_t e;
+  if ((e = c->w_src.ensure(2 * (size_t)n)) || (e = c->work.ensure(1)))
+    return cuda_fail(c, e, "pair records");
+  Rec32 *src = reinterpret_cast<Rec32 *>(c->w_src.p);
+  k_build_src<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(n, c->pos32.p, f, src);
+  if (int rc = check_launch(c, "pair records")) return rc;
+  const int cd = c->prm.cell_div;
+  if (c->pair_grid == 0) {
+    int sms = 1, per_sm = 1;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+    if (cd == 2)
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pair_f32_r1<2>, 256, 0);
+    else
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pair_f32_r1<1>, 256, 0);
+    c->pair_grid = std::max(1, sms * std::max(1, per_sm));
+  }
+  if ((e = cudaMemsetAsync(c->work.p, 0, sizeof(unsigned int), c->stream)))
+    return cuda_fail(c, e, "work counter");
+  const int64_t nslice = (n + kSlice - 1) / kSlice;
+  const Grid &g = c->grid;
+  const Rec32 *tab = reinterpret_cast<const Rec32 *>(c->tab.p);
+  kt_start(c, kKPairF32);
+  if (cd == 2)
+    k_pair_f32_r1<2><<<c->pair_grid, 256, 0, c->stream>>>(
+        n, nslice, src, c->nb_count.p, c->slice_off.p, c->nb_list.p, tab, c->tab_inv_ds,
+        g.h32[0], g.h32[1], g.h32[2], self_c, u, c->work.p);
+  else
+    k_pair_f32_r1<1><<<c->pair_grid, 256, 0, c->stream>>>(
+        n, nslice, src, c->nb_count.p, c->slice_off.p, c->nb_list.p, tab, c->tab_inv_ds,
+        g.h32[0], g.h32[1], g.h32[2], self_c, u, c->work.p);
+  kt_stop(c, kKPairF32);
+  return check_launch(c, "pair f32 r1");
 }
 
 }  // namespace
@@ -309,6 +440,7 @@ int matvec_slots(ggem_ctx *c, int nrhs, const double *f, double *u, int self_mod
     }
     return GGEM_OK;
   }
+  if (nrhs == 1) return launch_f32_r1(c, f, u, (float)self_coefficient(c, self_mode));
   cudaError_t e = c->w_f32.ensure((size_t)c->n * nrhs);
   if (e) return cuda_fail(c, e, "f32 staging");
   const int64_t tot = c->n * nrhs;

@@ -365,3 +365,27 @@ def test_device_pointer_matvec_with_torch_stream():
         s.synchronize()
         ctx.set_stream(0)
         assert np.array_equal(du.cpu().numpy(), want)
+
+
+@pytest.mark.parametrize("check_every", [0, 3])
+def test_chebyshev_sparse_checks_and_displacement(check_every):
+    """Sparse error checks return a y whose reported err1 is its own and a
+    Brownian displacement dw = M y equal to an explicit matvec of y."""
+    xyz, L = suspension(3000, 0.1, 47)
+    xi = np.random.default_rng(12).standard_normal(3 * len(xyz))
+    with G.Context(box_hi=(L,) * 3, rc=7.0, precision=G.FP32) as ctx:
+        ctx.set_particles(xyz)
+        ctx.build_cells()
+        lo, hi = ctx.lanczos_bounds(k=24, seed=5)
+        y_ref, rep_ref = ctx.cheb_inv_sqrt(xi, 50, lo / 1.05, hi * 1.05, 1e-3, check_every=1)
+        for _ in range(3):  # the adaptive mode learns the degree across calls
+            rc, dw, rep = ctx.brownian_displacement(xi, 50, lo / 1.05, hi * 1.05, 1e-3,
+                                                    check_every=check_every)
+            assert rc == 0 and rep[0]["converged"] and rep[0]["err1"] <= 1e-3
+            assert rep[0]["n_terms"] >= rep_ref[0]["n_terms"]
+        y, rep2 = ctx.cheb_inv_sqrt(xi, 50, lo / 1.05, hi * 1.05, 1e-3, check_every=check_every)
+        assert rep2[0]["n_terms"] == rep[0]["n_terms"] or check_every == 0
+        My = ctx.local_matvec(y, G.SELF_BEAD)
+        if rep2[0]["n_terms"] == rep[0]["n_terms"]:
+            assert rel(dw, My) <= 1e-12
+        assert rel(y, y_ref) <= 5e-3
