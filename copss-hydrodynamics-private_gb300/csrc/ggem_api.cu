@@ -235,6 +235,10 @@ int validate_and_setup(ggem_ctx *c) {
       if (e == cudaSuccess)
         e = cudaMemcpy(c->tab.p, tab.data(), sizeof(float4) * tab.size(), cudaMemcpyHostToDevice);
       if (e) return cuda_fail(c, e, "table upload");
+      // the analytic exp x polynomial form replaces the table lookup when its
+      // FP32 evaluation error stays within 1e-6 of the tensor scale
+      c->use_poly = fit_tensor_poly(c->cst, s_max, c->poly_a, c->poly_b, &c->poly_x0,
+                                    &c->poly_x1, c->poly_e, &c->poly_max_err) == 0;
     }
   } else {
     return fail(c, GGEM_ERR_BAD_ARG, "nb_mode must be GGEM_NB_REFERENCE or GGEM_NB_CUTOFF");
@@ -460,17 +464,13 @@ extern "C" int ggem_get_neighbors(ggem_ctx *ctx, int64_t *offsets, int32_t *ids,
     return cuda_fail(ctx, e, "neighbour readback");
   std::vector<std::vector<int32_t>> lists(n);
   if (ctx->prm.precision == GGEM_FP32) {
-    const int64_t nslice = (n + kSlice - 1) / kSlice;
-    std::vector<int64_t> soff(nslice + 1);
-    std::vector<int32_t> cnt(n);
+    std::vector<int64_t> off(n + 1, 0);
     int64_t total = 0;
     if (n > 0) {
-      if ((e = cudaMemcpyAsync(soff.data(), ctx->slice_off.p, 8 * (nslice + 1),
-                               cudaMemcpyDeviceToHost, st)) ||
-          (e = cudaMemcpyAsync(cnt.data(), ctx->nb_count.p, 4 * n, cudaMemcpyDeviceToHost, st)) ||
+      if ((e = cudaMemcpyAsync(off.data(), ctx->nb_off.p, 8 * (n + 1), cudaMemcpyDeviceToHost, st)) ||
           (e = cudaStreamSynchronize(st)))
         return cuda_fail(ctx, e, "list readback");
-      total = soff[nslice];
+      total = off[n];
     }
     std::vector<uint32_t> lst(std::max<int64_t>(total, 1));
     if (total > 0) {
@@ -479,9 +479,8 @@ extern "C" int ggem_get_neighbors(ggem_ctx *ctx, int64_t *offsets, int32_t *ids,
         return cuda_fail(ctx, e, "list readback");
     }
     for (int64_t s = 0; s < n; ++s) {
-      const int64_t base = soff[s / kSlice] + (s % kSlice);
       auto &L = lists[order[s]];
-      for (int m = 0; m < cnt[s]; ++m) L.push_back(order[lst[base + (int64_t)m * kSlice] >> kCodeBits]);
+      for (int64_t m = off[s]; m < off[s + 1]; ++m) L.push_back(order[lst[m] >> kCodeBits]);
     }
   } else {
     const bool ref = ctx->prm.nb_mode == GGEM_NB_REFERENCE;

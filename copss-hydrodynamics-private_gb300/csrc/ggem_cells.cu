@@ -5,7 +5,7 @@
 // containing list (:573-648) becomes a counting sort of particles by cell,
 // and the per-particle neighbour lists (:652-848) with their stored
 // displacement vectors (:220-241) become either an on-the-fly cell stencil
-// sweep (FP64 path) or a compact sliced-ELL list of (source slot, stencil
+// sweep (FP64 path) or a compact CSR list of (source slot, stencil
 // code) entries (FP32 path), built once per configuration.
 //
 // Bound: HBM.  Algorithmic bytes per particle of the cell build: 24 (read
@@ -220,34 +220,33 @@ __device__ __forceinline__ bool exact_within(const Grid &g, double4_32a a, doubl
 
 // Pass 1 (count) and pass 2 (fill) of the pair list: one thread per target
 // slot; FP32 cell-relative distance classifies a candidate unless it falls
-// in the rounding band around rc^2, where the exact FP64 test decides.
+// in the rounding band around rc^2, where the exact FP64 test decides.  The
+// list is CSR in slot order: entries of target s at off[s] .. off[s+1].
 template <bool FILL>
 __global__ void k_pair_list(int64_t n, Grid g, const int4 *__restrict__ stencil, int nst,
                             const float4 *__restrict__ shift, const int32_t *__restrict__ start,
                             const float4 *__restrict__ pos32, const double4_32a *__restrict__ pos64,
-                            float rc2_lo, float rc2_hi, double rc2,
-                            int32_t *__restrict__ count, const int64_t *__restrict__ slice_off,
-                            const int32_t *__restrict__ slice_width,
-                            uint32_t *__restrict__ list, int *__restrict__ err) {
+                            float rc2_lo, float rc2_hi, double rc2, int32_t *__restrict__ count,
+                            const int64_t *__restrict__ off, uint32_t *__restrict__ list,
+                            int *__restrict__ err) {
   const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (s >= n) return;
   const float4 pi = pos32[s];
   const int32_t cid = __float_as_int(pi.w);
   const int cx = cid % g.nc[0], cy = (cid / g.nc[0]) % g.nc[1], cz = cid / (g.nc[0] * g.nc[1]);
   int32_t cnt = 0;
-  int64_t base = 0;
-  int32_t width = 0;
-  const int lane = (int)(s & (kSlice - 1));
+  int64_t base = 0, cap = 0;
   if (FILL) {
-    base = slice_off[s / kSlice];
-    width = slice_width[s / kSlice];
+    base = off[s];
+    cap = off[s + 1] - base;
   }
   double4_32a pi64 = make_double4_32a(0, 0, 0, 0);
   bool have64 = false;
   for (int k = 0; k < nst; ++k) {
-    const int32_t nc = shifted_cell(g, cx, cy, cz, stencil[k]);
+    const int4 o = stencil[k];
+    const int32_t nc = shifted_cell(g, cx, cy, cz, o);
     if (nc < 0) continue;
-    const float4 sh = shift[k];
+    const float4 sh = shift[o.w];  // shifts are indexed by the offset code
     const int32_t b = start[nc], e = start[nc + 1];
     for (int32_t t = b; t < e; ++t) {
       if (t == s) continue;
@@ -269,33 +268,18 @@ __global__ void k_pair_list(int64_t n, Grid g, const int4 *__restrict__ stencil,
       if (!in) continue;
       if (FILL) {
         // entry code: the stencil offset in (2d+1)^3 index space (int4.w)
-        if (cnt < width)
-          list[base + (int64_t)cnt * kSlice + lane] =
-              ((uint32_t)t << kCodeBits) | (uint32_t)stencil[k].w;
+        if (cnt < cap) list[base + cnt] = ((uint32_t)t << kCodeBits) | (uint32_t)o.w;
         else atomicOr(err, kErrListOverflow);
       }
       ++cnt;
     }
   }
   if (!FILL) count[s] = cnt;
-  else {
-    for (int32_t m = cnt; m < width; ++m) list[base + (int64_t)m * kSlice + lane] = kPad;
-  }
 }
 
-__global__ void k_slice_width(int64_t n, int64_t nslice, const int32_t *__restrict__ count,
-                              int32_t *__restrict__ width, int64_t *__restrict__ width_x32) {
-  const int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (w >= nslice) return;
-  const int64_t s = w * kSlice + lane;
-  int v = (s < n) ? count[s] : 0;
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
-  if (lane == 0) {
-    width[w] = v;
-    width_x32[w] = (int64_t)v * kSlice;
-  }
+__global__ void k_widen(int64_t n, const int32_t *__restrict__ in, int64_t *__restrict__ out) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) out[i] = in[i];
 }
 
 }  // namespace
@@ -352,15 +336,12 @@ int build_cells(ggem_ctx *c) {
 
 int build_pair_list(ggem_ctx *c) {
   const int64_t n = c->n;
-  const int64_t nslice = (n + kSlice - 1) / kSlice;
   cudaError_t e = cudaSuccess;
-  if ((e = c->nb_count.ensure(n)) || (e = c->slice_width.ensure(nslice)) ||
-      (e = c->slice_off.ensure(2 * nslice + 1)))
+  if ((e = c->nb_count.ensure(n)) || (e = c->nb_cnt64.ensure(n)) || (e = c->nb_off.ensure(n + 1)))
     return cuda_fail(c, e, "pair list buffers");
   cudaStream_t st = c->stream;
   if (n == 0) {
-    if ((e = cudaMemsetAsync(c->slice_off.p, 0, sizeof(int64_t), st)))
-      return cuda_fail(c, e, "memset");
+    if ((e = cudaMemsetAsync(c->nb_off.p, 0, sizeof(int64_t), st))) return cuda_fail(c, e, "memset");
     c->n_pairs = 0;
     c->list_built = true;
     return GGEM_OK;
@@ -373,41 +354,27 @@ int build_pair_list(ggem_ctx *c) {
   k_pair_list<false><<<bn, T, 0, st>>>(n, c->grid, c->d_stencil.p, nst, c->d_shift.p,
                                         c->cell_start.p, c->pos32.p, c->pos64.p, c->rc2_lo,
                                         c->rc2_hi, c->rc2, c->nb_count.p, nullptr, nullptr,
-                                        nullptr, c->err.p);
+                                        c->err.p);
   if (int rc = check_launch(c, "pair count")) return rc;
-  int64_t *width_x32 = c->slice_off.p + nslice + 1;
-  k_slice_width<<<(unsigned)((nslice * 32 + T - 1) / T), T, 0, st>>>(
-      n, nslice, c->nb_count.p, c->slice_width.p, width_x32);
-  if (int rc = check_launch(c, "slice width")) return rc;
-  if (int rc = device_exclusive_scan_i64(c, width_x32, c->slice_off.p, nslice)) return rc;
+  k_widen<<<bn, T, 0, st>>>(n, c->nb_count.p, c->nb_cnt64.p);
+  if (int rc = check_launch(c, "pair widen")) return rc;
+  if (int rc = device_exclusive_scan_i64(c, c->nb_cnt64.p, c->nb_off.p, n)) return rc;
   int64_t total = 0;
-  if ((e = cudaMemcpyAsync(&total, c->slice_off.p + nslice, sizeof(int64_t),
-                           cudaMemcpyDeviceToHost, st)) ||
+  if ((e = cudaMemcpyAsync(&total, c->nb_off.p + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st)) ||
       (e = cudaStreamSynchronize(st)))
     return cuda_fail(c, e, "list size");
-  if ((e = c->nb_list.ensure((size_t)std::max<int64_t>(total, 1))))
-    return cuda_fail(c, e, "pair list");
+  if ((e = c->nb_list.ensure((size_t)std::max<int64_t>(total, 1)))) return cuda_fail(c, e, "pair list");
   k_pair_list<true><<<bn, T, 0, st>>>(n, c->grid, c->d_stencil.p, nst, c->d_shift.p,
                                        c->cell_start.p, c->pos32.p, c->pos64.p, c->rc2_lo,
-                                       c->rc2_hi, c->rc2, c->nb_count.p, c->slice_off.p,
-                                       c->slice_width.p, c->nb_list.p, c->err.p);
+                                       c->rc2_hi, c->rc2, nullptr, c->nb_off.p, c->nb_list.p,
+                                       c->err.p);
   kt_stop(c, kKListBuild);
   if (int rc = check_launch(c, "pair fill")) return rc;
   int flags = 0;
   if (int rc = read_error_flags(c, &flags)) return rc;
   if (flags & kErrListOverflow)
-    return fail(c, GGEM_ERR_CELL_OVERFLOW, "pair list fill exceeded its counted width");
-  // total ordered pairs
-  std::vector<int32_t> cnt(n > 0 ? n : 1);
-  if (n > 0) {
-    if ((e = cudaMemcpyAsync(cnt.data(), c->nb_count.p, sizeof(int32_t) * n,
-                             cudaMemcpyDeviceToHost, st)) ||
-        (e = cudaStreamSynchronize(st)))
-      return cuda_fail(c, e, "pair count");
-  }
-  int64_t np = 0;
-  for (int64_t i = 0; i < n; ++i) np += cnt[i];
-  c->n_pairs = np;
+    return fail(c, GGEM_ERR_CELL_OVERFLOW, "pair list fill exceeded its counted length");
+  c->n_pairs = total;
   c->list_built = true;
   return GGEM_OK;
 }

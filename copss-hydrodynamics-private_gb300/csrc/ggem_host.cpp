@@ -142,6 +142,89 @@ int fit_tensor_table(const ggem_constants &c, double s_max, int nt, std::vector<
   return (worst < 1e-5) ? 0 : -1;
 }
 
+// Analytic form of the FP32 tensor: A(s) = e^{-alpha^2 s} a(s) and
+// B(s) = e^{-alpha^2 s} b(s).  a and b are entire in s (the 1/r singularities
+// of the two erf terms cancel), so one Chebyshev interpolant of degree
+// kPolyDeg on [0, s_max] reaches ~1e-9; it is stored as monomials in
+// x = 2 s / s_max - 1 for FP32 Horner evaluation.  The returned max_err is
+// measured with FP32 arithmetic (fused multiply-adds, as on the device) on a
+// dense grid, relative to |A| + |B| s; the caller falls back to the table when
+// it is too large.
+int fit_tensor_poly(const ggem_constants &c, double s_max, float *a, float *b, float *x0,
+                    float *x1, float *e_coef, double *max_err) {
+  const int deg = kPolyDeg;
+  const double al2 = c.alpha2;
+  std::vector<double> fa(deg + 1), fb(deg + 1);
+  for (int j = 0; j <= deg; ++j) {
+    const double xj = std::cos(kPi * (j + 0.5) / (deg + 1));
+    const double s = (xj + 1.0) * 0.5 * s_max;
+    double A, B, sc;
+    tensor_ab(c, s, &A, &B, &sc);
+    fa[j] = A * std::exp(al2 * s);
+    fb[j] = B * std::exp(al2 * s);
+  }
+  std::vector<double> ca(deg + 1), cb(deg + 1);
+  for (int k = 0; k <= deg; ++k) {
+    double sa = 0.0, sb = 0.0;
+    for (int j = 0; j <= deg; ++j) {
+      const double t = std::cos(k * kPi * (j + 0.5) / (deg + 1));
+      sa += fa[j] * t;
+      sb += fb[j] * t;
+    }
+    ca[k] = sa * 2.0 / (deg + 1);
+    cb[k] = sb * 2.0 / (deg + 1);
+  }
+  ca[0] *= 0.5;
+  cb[0] *= 0.5;
+  // Chebyshev -> monomial coefficients (T_k expanded by the recurrence)
+  std::vector<std::vector<double>> T(deg + 1, std::vector<double>(deg + 1, 0.0));
+  T[0][0] = 1.0;
+  if (deg >= 1) T[1][1] = 1.0;
+  for (int k = 2; k <= deg; ++k)
+    for (int q = 0; q <= k; ++q) T[k][q] = (q > 0 ? 2.0 * T[k - 1][q - 1] : 0.0) - T[k - 2][q];
+  for (int q = 0; q < 16; ++q) {
+    a[q] = 0.f;
+    b[q] = 0.f;
+  }
+  for (int q = 0; q <= deg; ++q) {
+    double ma = 0.0, mb = 0.0;
+    for (int k = 0; k <= deg; ++k) {
+      ma += ca[k] * T[k][q];
+      mb += cb[k] * T[k][q];
+    }
+    a[q] = (float)ma;
+    b[q] = (float)mb;
+  }
+  *x1 = (float)(2.0 / s_max);
+  *x0 = -1.0f;
+  // exponent coefficient split into two floats (hi + lo)
+  const double ecoef = -al2 / std::log(2.0);
+  e_coef[0] = (float)ecoef;
+  e_coef[1] = (float)(ecoef - (double)e_coef[0]);
+  double worst = 0.0;
+  const int samples = 20000;
+  for (int i = 0; i <= samples; ++i) {
+    const double s = s_max * i / samples;
+    const float s32 = (float)s;
+    const float x = std::fmaf(s32, *x1, *x0);
+    float pa = a[deg], pb = b[deg];
+    for (int q = deg - 1; q >= 0; --q) {
+      pa = std::fmaf(pa, x, a[q]);
+      pb = std::fmaf(pb, x, b[q]);
+    }
+    const float pe = s32 * e_coef[0];
+    const float re = std::fmaf(s32, e_coef[1], std::fmaf(s32, e_coef[0], -pe));
+    const float E0 = std::exp2f(pe);
+    const float E = std::fmaf(E0, re * 0.6931471805599453f, E0);
+    double A, B, sc;
+    tensor_ab(c, (double)s32, &A, &B, &sc);
+    const double e = (std::fabs((double)(pa * E) - A) + std::fabs((double)(pb * E) - B) * s) / sc;
+    worst = std::max(worst, e);
+  }
+  if (max_err) *max_err = worst;
+  return (worst <= 1e-6) ? 0 : -1;
+}
+
 // smallest / largest eigenvalue of a symmetric tridiagonal matrix (diagonal
 // a, off-diagonal b) by Sturm-sequence bisection
 static int sturm_below(int k, const double *a, const double *b, double x) {

@@ -9,7 +9,7 @@
 //   pos64      double4_32a[n]   wrapped positions in slot order (FP64 paths)
 //   pos32      float4[n]    position relative to its cell centre (x,y,z) and
 //                           the cell id bits (w), slot order (FP32 path)
-//   pair list  uint32       sliced-ELL (32 slots per slice), entry =
+//   pair list  uint32       CSR in slot order, entry =
 //                           (source slot << 7) | stencil code, built once
 //                           per configuration with an FP32 filter and an
 //                           exact FP64 decision in the rounding band
@@ -30,9 +30,9 @@ namespace ggem {
 constexpr int kTableN = 512;       // cubic pieces of the FP32 tensor table
 constexpr int kCodeBits = 7;       // stencil code bits of a pair entry
 constexpr int kMaxCode = 1 << kCodeBits;
-constexpr uint32_t kPad = 0xFFFFFFFFu;
-constexpr int kSlice = 32;         // slots per sliced-ELL slice
 constexpr int kMaxRhsChunk = 8;    // right-hand sides per pair-kernel pass
+constexpr int kPolyDeg = 13;       // degree of the analytic tensor polynomials
+constexpr int kGroup = 4;          // lanes per target in the pair kernel
 
 // device error bits
 enum : int {
@@ -114,15 +114,21 @@ struct ggem_ctx {
   // FP32 pair list
   bool list_built = false;
   int64_t n_pairs = 0;
-  ggem::DevBuf<int32_t> nb_count, slice_width;
-  ggem::DevBuf<int64_t> slice_off;
+  ggem::DevBuf<int32_t> nb_count;     // entries per target
+  ggem::DevBuf<int64_t> nb_cnt64, nb_off;  // widened counts, CSR offsets (n+1)
   ggem::DevBuf<uint32_t> nb_list;
   ggem::DevBuf<float4> tab;
   float tab_inv_ds = 0.f;
   double tab_max_err = 0.0;
+  // analytic tensor: A = e^{-alpha^2 s} a(x), B = e^{-alpha^2 s} b(x),
+  // x = s * poly_x1 + poly_x0, a and b monomials of degree kPolyDeg
+  bool use_poly = false;
+  float poly_a[16] = {0}, poly_b[16] = {0};
+  float poly_x0 = 0.f, poly_x1 = 0.f, poly_e[2] = {0.f, 0.f};  // exponent hi + lo
+  double poly_max_err = 0.0;
   // single-RHS pair kernel: 32-byte source records, work counter, grid
   ggem::DevBuf<float4> w_src;          // 2 float4 per slot
-  ggem::DevBuf<unsigned int> work;     // slice counter of the persistent grid
+  ggem::DevBuf<unsigned int> work;     // spare device counter
   int pair_grid = 0;                   // CTAs of the persistent pair kernel
   int cheb_pred_terms = 0;             // degree the last adaptive Chebyshev needed
 
@@ -169,6 +175,8 @@ int ensure_host_stage(ggem_ctx *c, size_t bytes);
 void compute_constants(const ggem_params &p, ggem_constants *c);
 int fit_tensor_table(const ggem_constants &c, double s_max, int nt, std::vector<float4> &tab,
                      double *max_err);
+int fit_tensor_poly(const ggem_constants &c, double s_max, float *a, float *b, float *x0,
+                    float *x1, float *e_coef, double *max_err);
 void tridiag_extremes(int k, const double *a, const double *b, double *lmin, double *lmax);
 void cheb_coeffs_host(int N, double da, double db, int method, double *coef);
 

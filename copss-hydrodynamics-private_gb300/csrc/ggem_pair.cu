@@ -8,11 +8,13 @@
 // Two arithmetic paths:
 //  * FP64 ("plain"): one thread per target slot sweeps the neighbour cells of
 //    the stencil, minimum image and cut-off in FP64, erf/exp per pair.
-//  * FP32: one thread per target slot walks its cached sliced-ELL list; the
-//    displacement is formed from cell-relative coordinates plus the stencil
-//    shift (exact cell offsets), G = A(s) I + B(s) x x^T from a piecewise
-//    cubic table in s = r^2, and the three components accumulate with Kahan
-//    compensation; the compensated sum is returned in FP64.
+//  * FP32: groups of kGroup lanes share one target and walk its cached CSR
+//    pair list (consecutive entries, so the gathered sources of a group sit
+//    in the same cells).  The displacement is formed from cell-relative
+//    coordinates plus the stencil shift (exact cell offsets);
+//    G = A(s) I + B(s) x x^T with A, B = e^{-alpha^2 s} times a polynomial
+//    in s (or a cubic table when that fit is not accurate enough); each lane
+//    keeps Kahan-compensated FP32 sums and the group reduces in FP64.
 // Algorithmic work per in-cutoff ordered pair: 28 + 19*nrhs flops (FMA = 2,
 // rsqrt/exp/erf = 1 each), bound by the FP32 pipe.
 #include <cuda_runtime.h>
@@ -148,13 +150,63 @@ __device__ __forceinline__ void kahan_add(float &sum, float &comp, float v) {
   sum = t;
 }
 
-// One 32-byte record per source (position relative to its cell centre and
-// the force of the single right-hand side) and per table piece (cubic
-// coefficients of A and of B): each pair then issues one 32-byte gather for
-// the source and one for the tensor instead of four 16-byte gathers.
+// one 32-byte record per source (cell-relative position, force of the single
+// right-hand side): a single 32-byte gather per pair
 struct __align__(32) Rec32 {
   float4 a, b;
 };
+
+// the analytic tensor, passed by value (constant bank)
+struct PolyAB {
+  float a[kPolyDeg + 1], b[kPolyDeg + 1];
+  float x0, x1, e_hi, e_lo;  // x = s x1 + x0; e^{-alpha^2 s} = 2^{s (e_hi + e_lo)}
+};
+
+template <bool POLY>
+__device__ __forceinline__ void tensor_ab32(float s2, const PolyAB &P,
+                                            const Rec32 *__restrict__ tab, float inv_ds,
+                                            float &A, float &B) {
+  if (POLY) {
+    const float x = fmaf(s2, P.x1, P.x0);
+    float a = P.a[kPolyDeg], b = P.b[kPolyDeg];
+#pragma unroll
+    for (int q = kPolyDeg - 1; q >= 0; --q) {
+      a = fmaf(a, x, P.a[q]);
+      b = fmaf(b, x, P.b[q]);
+    }
+    // e^{-alpha^2 s} = 2^{p + r}: p = s e_hi rounded, r its exact residual plus
+    // s e_lo, so the exponent keeps ~1e-7 relative accuracy at s ~ rc^2
+    const float p = s2 * P.e_hi;
+    const float r = fmaf(s2, P.e_lo, fmaf(s2, P.e_hi, -p));
+    const float E0 = exp2f(p);
+    const float E = fmaf(E0, r * 0.6931471805599453f, E0);
+    A = a * E;
+    B = b * E;
+  } else {
+    const float uu = s2 * inv_ds;
+    const float fi = fminf(floorf(uu), (float)(kTableN - 1));  // last piece extrapolates
+    const float t = uu - fi;
+    const Rec32 tr = tab[(int)fi];
+    A = fmaf(fmaf(fmaf(tr.a.w, t, tr.a.z), t, tr.a.y), t, tr.a.x);
+    B = fmaf(fmaf(fmaf(tr.b.w, t, tr.b.z), t, tr.b.y), t, tr.b.x);
+  }
+}
+
+template <int CD>
+__device__ __forceinline__ void decode_shift(uint32_t e, float hx, float hy, float hz, float &sx,
+                                             float &sy, float &sz) {
+  constexpr int SIDE = 2 * CD + 1;
+  const int code = (int)(e & (kMaxCode - 1));
+  sx = (float)(code % SIDE - CD) * hx;
+  sy = (float)((code / SIDE) % SIDE - CD) * hy;
+  sz = (float)(code / (SIDE * SIDE) - CD) * hz;
+}
+
+__device__ __forceinline__ double group_sum(double v) {
+#pragma unroll
+  for (int o = kGroup / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
 
 __global__ void k_build_src(int64_t n, const float4 *__restrict__ pos32,
                             const double *__restrict__ f, Rec32 *__restrict__ src) {
@@ -166,124 +218,86 @@ __global__ void k_build_src(int64_t n, const float4 *__restrict__ pos32,
   src[s] = r;
 }
 
-// add a short plain-FP32 block sum into a Kahan-compensated accumulator
-__device__ __forceinline__ void fold(float &sum, float &comp, float &blk) {
-  kahan_add(sum, comp, blk);
-  blk = 0.f;
-}
-
-// Single right-hand side pair sum.  Persistent warps take 32-target slices
-// from a work counter (dynamic balance of the uneven list lengths and no
-// tail wave); per pair: one coalesced list word, one 32-byte source gather,
-// one 32-byte table gather, the cell shift decoded from the entry code.
-// Sums run as plain FP32 over blocks of 8 pairs folded into a Kahan
-// accumulator per component.
-template <int CD>
-__global__ void __launch_bounds__(256) k_pair_f32_r1(
-    int64_t n, int64_t nslice, const Rec32 *__restrict__ src, const int32_t *__restrict__ count,
-    const int64_t *__restrict__ slice_off, const uint32_t *__restrict__ list,
-    const Rec32 *__restrict__ tab, float inv_ds, float hx, float hy, float hz, float self_c,
-    double *__restrict__ u, unsigned int *__restrict__ work) {
-  constexpr int SIDE = 2 * CD + 1;
-  const int lane = threadIdx.x & 31;
-  const float top = (float)(kTableN - 1);
-  for (;;) {
-    unsigned int sl = 0;
-    if (lane == 0) sl = atomicAdd(work, 1u);
-    sl = __shfl_sync(0xffffffffu, sl, 0);
-    if (sl >= nslice) break;
-    const int64_t s = (int64_t)sl * kSlice + lane;
-    const bool act = s < n;
-    const int32_t cnt = act ? count[s] : 0;
-    const uint32_t *lp = list + slice_off[sl] + lane;
-    Rec32 ri;
-    ri.a = make_float4(0.f, 0.f, 0.f, 0.f);
-    ri.b = ri.a;
-    if (act) ri = src[s];
-    float sx = self_c * ri.b.x, sy = self_c * ri.b.y, sz = self_c * ri.b.z;
-    float cx = 0.f, cy = 0.f, cz = 0.f, bx = 0.f, by = 0.f, bz = 0.f;
-    for (int32_t m = 0; m < cnt; ++m) {
-      const uint32_t e = __ldg(lp + (int64_t)m * kSlice);
-      const uint32_t j = e >> kCodeBits;
-      const int code = (int)(e & (kMaxCode - 1));
-      const int ox = code % SIDE - CD, oy = (code / SIDE) % SIDE - CD, oz = code / (SIDE * SIDE) - CD;
-      const Rec32 rj = src[j];
-      const float dx = (rj.a.x - ri.a.x) + (float)ox * hx;
-      const float dy = (rj.a.y - ri.a.y) + (float)oy * hy;
-      const float dz = (rj.a.z - ri.a.z) + (float)oz * hz;
-      const float s2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-      const float uu = s2 * inv_ds;
-      const float fi = fminf(floorf(uu), top);
-      const float t = uu - fi;
-      const Rec32 tr = tab[(int)fi];
-      const float A = fmaf(fmaf(fmaf(tr.a.w, t, tr.a.z), t, tr.a.y), t, tr.a.x);
-      const float B = fmaf(fmaf(fmaf(tr.b.w, t, tr.b.z), t, tr.b.y), t, tr.b.x);
-      const float bxf = B * fmaf(dz, rj.b.z, fmaf(dy, rj.b.y, dx * rj.b.x));
-      bx += fmaf(A, rj.b.x, bxf * dx);
-      by += fmaf(A, rj.b.y, bxf * dy);
-      bz += fmaf(A, rj.b.z, bxf * dz);
-      if ((m & 7) == 7) {
-        fold(sx, cx, bx);
-        fold(sy, cy, by);
-        fold(sz, cz, bz);
-      }
+// single right-hand side
+template <int CD, bool POLY>
+__global__ void __launch_bounds__(256) k_pair_r1(
+    int64_t n, const Rec32 *__restrict__ src, const int64_t *__restrict__ off,
+    const uint32_t *__restrict__ list, PolyAB P, const Rec32 *__restrict__ tab, float inv_ds,
+    float hx, float hy, float hz, double self_c, double *__restrict__ u) {
+  const int64_t gid = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / kGroup;
+  const int sub = (int)(threadIdx.x % kGroup);
+  const bool act = gid < n;
+  const int64_t s = act ? gid : n - 1;
+  const int64_t b = off[s], e = act ? off[s + 1] : b;
+  const Rec32 ri = src[s];
+  float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
+  float bx = 0.f, by = 0.f, bz = 0.f;
+  int blk = 0;
+  for (int64_t m = b + sub; m < e; m += kGroup) {
+    const uint32_t en = __ldg(list + m);
+    const Rec32 rj = src[en >> kCodeBits];
+    float ox, oy, oz;
+    decode_shift<CD>(en, hx, hy, hz, ox, oy, oz);
+    const float dx = (rj.a.x - ri.a.x) + ox;
+    const float dy = (rj.a.y - ri.a.y) + oy;
+    const float dz = (rj.a.z - ri.a.z) + oz;
+    const float s2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+    float A, B;
+    tensor_ab32<POLY>(s2, P, tab, inv_ds, A, B);
+    const float bxf = B * fmaf(dz, rj.b.z, fmaf(dy, rj.b.y, dx * rj.b.x));
+    bx += fmaf(A, rj.b.x, bxf * dx);
+    by += fmaf(A, rj.b.y, bxf * dy);
+    bz += fmaf(A, rj.b.z, bxf * dz);
+    if (++blk == 8) {
+      kahan_add(sx, cx, bx);
+      kahan_add(sy, cy, by);
+      kahan_add(sz, cz, bz);
+      bx = by = bz = 0.f;
+      blk = 0;
     }
-    fold(sx, cx, bx);
-    fold(sy, cy, by);
-    fold(sz, cz, bz);
-    if (act) {
-      double *ui = u + 3 * s;
-      ui[0] = (double)sx - (double)cx;
-      ui[1] = (double)sy - (double)cy;
-      ui[2] = (double)sz - (double)cz;
-    }
+  }
+  kahan_add(sx, cx, bx);
+  kahan_add(sy, cy, by);
+  kahan_add(sz, cz, bz);
+  const double ux = group_sum((double)sx - (double)cx);
+  const double uy = group_sum((double)sy - (double)cy);
+  const double uz = group_sum((double)sz - (double)cz);
+  if (act && sub == 0) {
+    double *ui = u + 3 * s;
+    ui[0] = ux + self_c * (double)ri.b.x;
+    ui[1] = uy + self_c * (double)ri.b.y;
+    ui[2] = uz + self_c * (double)ri.b.z;
   }
 }
 
-// FP32 list walk; f32 is [r][n] float4 (x,y,z,0), u is [r][n][3] doubles
-template <int NR>
-__global__ void __launch_bounds__(256) k_matvec_f32(
-    int64_t n, const float4 *__restrict__ pos32, const int32_t *__restrict__ count,
-    const int64_t *__restrict__ slice_off, const uint32_t *__restrict__ list,
-    const float4 *__restrict__ shift_g, int nshift, const float4 *__restrict__ tab,
-    float inv_ds, float self_c, const float4 *__restrict__ f32, double *__restrict__ u,
-    int r0) {
-  __shared__ float4 shift[kMaxCode];
-  for (int k = threadIdx.x; k < nshift; k += blockDim.x) shift[k] = shift_g[k];
-  __syncthreads();
-  const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (s >= n) return;
-  const int lane = (int)(s & (kSlice - 1));
-  const int64_t base = slice_off[s / kSlice] + lane;
-  const int32_t cnt = count[s];
+// NR right-hand sides r0 .. r0+NR-1: f32 is [r][n] float4, u [r][n][3]
+template <int CD, bool POLY, int NR>
+__global__ void __launch_bounds__(256) k_pair_nr(
+    int64_t n, const float4 *__restrict__ pos32, const float4 *__restrict__ f32,
+    const int64_t *__restrict__ off, const uint32_t *__restrict__ list, PolyAB P,
+    const Rec32 *__restrict__ tab, float inv_ds, float hx, float hy, float hz, double self_c,
+    double *__restrict__ u, int r0) {
+  const int64_t gid = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / kGroup;
+  const int sub = (int)(threadIdx.x % kGroup);
+  const bool act = gid < n;
+  const int64_t s = act ? gid : n - 1;
+  const int64_t b = off[s], e = act ? off[s + 1] : b;
   const float4 pi = pos32[s];
   float sx[NR], sy[NR], sz[NR], cx[NR], cy[NR], cz[NR];
 #pragma unroll
-  for (int q = 0; q < NR; ++q) {
-    const float4 fi = f32[(int64_t)(r0 + q) * n + s];
-    sx[q] = self_c * fi.x;
-    sy[q] = self_c * fi.y;
-    sz[q] = self_c * fi.z;
-    cx[q] = cy[q] = cz[q] = 0.f;
-  }
-  const float top = (float)(kTableN - 1);
-  for (int32_t m = 0; m < cnt; ++m) {
-    const uint32_t e = __ldg(list + base + (int64_t)m * kSlice);
-    const uint32_t j = e >> kCodeBits;
-    const float4 sh = shift[e & (kMaxCode - 1)];
+  for (int q = 0; q < NR; ++q) sx[q] = sy[q] = sz[q] = cx[q] = cy[q] = cz[q] = 0.f;
+  for (int64_t m = b + sub; m < e; m += kGroup) {
+    const uint32_t en = __ldg(list + m);
+    const uint32_t j = en >> kCodeBits;
     const float4 pj = __ldg(pos32 + j);
-    const float dx = (pj.x - pi.x) + sh.x;
-    const float dy = (pj.y - pi.y) + sh.y;
-    const float dz = (pj.z - pi.z) + sh.z;
+    float ox, oy, oz;
+    decode_shift<CD>(en, hx, hy, hz, ox, oy, oz);
+    const float dx = (pj.x - pi.x) + ox;
+    const float dy = (pj.y - pi.y) + oy;
+    const float dz = (pj.z - pi.z) + oz;
     const float s2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-    const float uu = s2 * inv_ds;
-    const float fi = fminf(floorf(uu), top);  // last piece extrapolates past s_max
-    const float t = uu - fi;
-    const int idx = (int)fi;
-    const float4 ta = __ldg(tab + 2 * idx);
-    const float4 tb = __ldg(tab + 2 * idx + 1);
-    const float A = fmaf(fmaf(fmaf(ta.w, t, ta.z), t, ta.y), t, ta.x);
-    const float B = fmaf(fmaf(fmaf(tb.w, t, tb.z), t, tb.y), t, tb.x);
+    float A, B;
+    tensor_ab32<POLY>(s2, P, tab, inv_ds, A, B);
 #pragma unroll
     for (int q = 0; q < NR; ++q) {
       const float4 fj = __ldg(f32 + (int64_t)(r0 + q) * n + j);
@@ -295,10 +309,16 @@ __global__ void __launch_bounds__(256) k_matvec_f32(
   }
 #pragma unroll
   for (int q = 0; q < NR; ++q) {
-    double *ui = u + ((int64_t)(r0 + q) * n + s) * 3;
-    ui[0] = (double)sx[q] - (double)cx[q];
-    ui[1] = (double)sy[q] - (double)cy[q];
-    ui[2] = (double)sz[q] - (double)cz[q];
+    const double ux = group_sum((double)sx[q] - (double)cx[q]);
+    const double uy = group_sum((double)sy[q] - (double)cy[q]);
+    const double uz = group_sum((double)sz[q] - (double)cz[q]);
+    if (act && sub == 0) {
+      const float4 fi = f32[(int64_t)(r0 + q) * n + s];
+      double *ui = u + ((int64_t)(r0 + q) * n + s) * 3;
+      ui[0] = ux + self_c * (double)fi.x;
+      ui[1] = uy + self_c * (double)fi.y;
+      ui[2] = uz + self_c * (double)fi.z;
+    }
   }
 }
 
@@ -351,54 +371,68 @@ int launch_f64(ggem_ctx *c, const double *f, double *u, int self_mode, int r0) {
   return check_launch(c, "matvec f64");
 }
 
-template <int NR>
-int launch_f32(ggem_ctx *c, const float4 *f32, double *u, float self_c, int r0) {
-  const int T = 256;
-  const unsigned bn = (unsigned)((c->n + T - 1) / T);
-  kt_start(c, kKPairF32);
-  k_matvec_f32<NR><<<bn, T, 0, c->stream>>>(c->n, c->pos32.p, c->nb_count.p, c->slice_off.p,
-                                             c->nb_list.p, c->d_shift.p, kMaxCode, c->tab.p,
-                                             c->tab_inv_ds, self_c, f32, u, r0);
-  kt_stop(c, kKPairF32);
-  return check_launch(c, "matvec f32");
+PolyAB poly_of(const ggem_ctx *c) {
+  PolyAB P;
+  for (int q = 0; q <= kPolyDeg; ++q) {
+    P.a[q] = c->poly_a[q];
+    P.b[q] = c->poly_b[q];
+  }
+  P.x0 = c->poly_x0;
+  P.x1 = c->poly_x1;
+  P.e_hi = c->poly_e[0];
+  P.e_lo = c->poly_e[1];
+  return P;
 }
 
-// single right-hand side: records from FP64 slot-order f, then the
-// persistent pair kernel over a grid that fills every SM once
-int launch_f32_r1(ggem_ctx *c, const double *f, double *u, float self_c) {
+template <int CD, bool POLY>
+void launch_r1(ggem_ctx *c, const Rec32 *src, double *u, double self_c) {
+  const int64_t threads = c->n * kGroup;
+  const Grid &g = c->grid;
+  k_pair_r1<CD, POLY><<<(unsigned)((threads + 255) / 256), 256, 0, c->stream>>>(
+      c->n, src, c->nb_off.p, c->nb_list.p, poly_of(c),
+      reinterpret_cast<const Rec32 *>(c->tab.p), c->tab_inv_ds, g.h32[0], g.h32[1], g.h32[2],
+      self_c, u);
+}
+
+// single right-hand side: records from FP64 slot-order f, then the pair sum
+int launch_f32_r1(ggem_ctx *c, const double *f, double *u, double self_c) {
   const int64_t n = c->n;
   cudaError_t e;
-  if ((e = c->w_src.ensure(2 * (size_t)n)) || (e = c->work.ensure(1)))
-    return cuda_fail(c, e, "pair records");
+  if ((e = c->w_src.ensure(2 * (size_t)n))) return cuda_fail(c, e, "pair records");
   Rec32 *src = reinterpret_cast<Rec32 *>(c->w_src.p);
   k_build_src<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(n, c->pos32.p, f, src);
   if (int rc = check_launch(c, "pair records")) return rc;
-  const int cd = c->prm.cell_div;
-  if (c->pair_grid == 0) {
-    int sms = 1, per_sm = 1;
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
-    if (cd == 2)
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pair_f32_r1<2>, 256, 0);
-    else
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pair_f32_r1<1>, 256, 0);
-    c->pair_grid = std::max(1, sms * std::max(1, per_sm));
-  }
-  if ((e = cudaMemsetAsync(c->work.p, 0, sizeof(unsigned int), c->stream)))
-    return cuda_fail(c, e, "work counter");
-  const int64_t nslice = (n + kSlice - 1) / kSlice;
-  const Grid &g = c->grid;
-  const Rec32 *tab = reinterpret_cast<const Rec32 *>(c->tab.p);
   kt_start(c, kKPairF32);
-  if (cd == 2)
-    k_pair_f32_r1<2><<<c->pair_grid, 256, 0, c->stream>>>(
-        n, nslice, src, c->nb_count.p, c->slice_off.p, c->nb_list.p, tab, c->tab_inv_ds,
-        g.h32[0], g.h32[1], g.h32[2], self_c, u, c->work.p);
-  else
-    k_pair_f32_r1<1><<<c->pair_grid, 256, 0, c->stream>>>(
-        n, nslice, src, c->nb_count.p, c->slice_off.p, c->nb_list.p, tab, c->tab_inv_ds,
-        g.h32[0], g.h32[1], g.h32[2], self_c, u, c->work.p);
+  const bool cd2 = c->prm.cell_div == 2;
+  if (c->use_poly) cd2 ? launch_r1<2, true>(c, src, u, self_c) : launch_r1<1, true>(c, src, u, self_c);
+  else cd2 ? launch_r1<2, false>(c, src, u, self_c) : launch_r1<1, false>(c, src, u, self_c);
   kt_stop(c, kKPairF32);
   return check_launch(c, "pair f32 r1");
+}
+
+template <int CD, bool POLY, int NR>
+void launch_nr_t(ggem_ctx *c, double *u, double self_c, int r0) {
+  const int64_t threads = c->n * kGroup;
+  const Grid &g = c->grid;
+  k_pair_nr<CD, POLY, NR><<<(unsigned)((threads + 255) / 256), 256, 0, c->stream>>>(
+      c->n, c->pos32.p, c->w_f32.p, c->nb_off.p, c->nb_list.p, poly_of(c),
+      reinterpret_cast<const Rec32 *>(c->tab.p), c->tab_inv_ds, g.h32[0], g.h32[1], g.h32[2],
+      self_c, u, r0);
+}
+
+template <int NR>
+int launch_nr(ggem_ctx *c, double *u, double self_c, int r0) {
+  const bool cd2 = c->prm.cell_div == 2;
+  kt_start(c, kKPairF32);
+  if (c->use_poly) {
+    if (cd2) launch_nr_t<2, true, NR>(c, u, self_c, r0);
+    else launch_nr_t<1, true, NR>(c, u, self_c, r0);
+  } else {
+    if (cd2) launch_nr_t<2, false, NR>(c, u, self_c, r0);
+    else launch_nr_t<1, false, NR>(c, u, self_c, r0);
+  }
+  kt_stop(c, kKPairF32);
+  return check_launch(c, "pair f32");
 }
 
 }  // namespace
@@ -440,7 +474,7 @@ int matvec_slots(ggem_ctx *c, int nrhs, const double *f, double *u, int self_mod
     }
     return GGEM_OK;
   }
-  if (nrhs == 1) return launch_f32_r1(c, f, u, (float)self_coefficient(c, self_mode));
+  if (nrhs == 1) return launch_f32_r1(c, f, u, self_coefficient(c, self_mode));
   cudaError_t e = c->w_f32.ensure((size_t)c->n * nrhs);
   if (e) return cuda_fail(c, e, "f32 staging");
   const int64_t tot = c->n * nrhs;
@@ -452,15 +486,15 @@ int matvec_slots(ggem_ctx *c, int nrhs, const double *f, double *u, int self_mod
 
 // FP32 pair sum from the already staged c->w_f32 ([r][n] float4)
 int matvec_f32_staged(ggem_ctx *c, int nrhs, double *u, int self_mode) {
-  const float self_c = (float)self_coefficient(c, self_mode);
+  const double self_c = self_coefficient(c, self_mode);
   int r0 = 0;
   while (r0 < nrhs) {
     const int left = nrhs - r0;
     int rc;
-    if (left >= 8) rc = launch_f32<8>(c, c->w_f32.p, u, self_c, r0), r0 += 8;
-    else if (left >= 4) rc = launch_f32<4>(c, c->w_f32.p, u, self_c, r0), r0 += 4;
-    else if (left >= 2) rc = launch_f32<2>(c, c->w_f32.p, u, self_c, r0), r0 += 2;
-    else rc = launch_f32<1>(c, c->w_f32.p, u, self_c, r0), r0 += 1;
+    if (left >= 8) rc = launch_nr<8>(c, u, self_c, r0), r0 += 8;
+    else if (left >= 4) rc = launch_nr<4>(c, u, self_c, r0), r0 += 4;
+    else if (left >= 2) rc = launch_nr<2>(c, u, self_c, r0), r0 += 2;
+    else rc = launch_nr<1>(c, u, self_c, r0), r0 += 1;
     if (rc) return rc;
   }
   return GGEM_OK;
