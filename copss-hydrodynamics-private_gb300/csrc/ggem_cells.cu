@@ -218,63 +218,121 @@ __device__ __forceinline__ bool exact_within(const Grid &g, double4_32a a, doubl
   return r2 < rc2;
 }
 
-// Pass 1 (count) and pass 2 (fill) of the pair list: one thread per target
-// slot; FP32 cell-relative distance classifies a candidate unless it falls
-// in the rounding band around rc^2, where the exact FP64 test decides.  The
-// list is CSR in slot order: entries of target s at off[s] .. off[s+1].
+// Warp-per-cell pair list (count and fill passes).  The candidates of a
+// target cell are the concatenation of its stencil cells (stencil order,
+// slot order inside a cell); lanes take 32 consecutive candidates with
+// coalesced loads, the cell's targets are broadcast one at a time by
+// shuffle, and a ballot prefix places each accepted candidate.  Entries
+// therefore come out in exactly the per-target order of a sequential sweep.
+constexpr int kListWarps = 8;     // warps per CTA
+constexpr int kMaxStencil = 128;  // stencil cells per target cell
+
 template <bool FILL>
-__global__ void k_pair_list(int64_t n, Grid g, const int4 *__restrict__ stencil, int nst,
-                            const float4 *__restrict__ shift, const int32_t *__restrict__ start,
-                            const float4 *__restrict__ pos32, const double4_32a *__restrict__ pos64,
-                            float rc2_lo, float rc2_hi, double rc2, int32_t *__restrict__ count,
-                            const int64_t *__restrict__ off, uint32_t *__restrict__ list,
-                            int *__restrict__ err) {
-  const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (s >= n) return;
-  const float4 pi = pos32[s];
-  const int32_t cid = __float_as_int(pi.w);
-  const int cx = cid % g.nc[0], cy = (cid / g.nc[0]) % g.nc[1], cz = cid / (g.nc[0] * g.nc[1]);
-  int32_t cnt = 0;
-  int64_t base = 0, cap = 0;
-  if (FILL) {
-    base = off[s];
-    cap = off[s + 1] - base;
+__global__ void __launch_bounds__(32 * kListWarps) k_pair_list_warp(
+    Grid g, const int4 *__restrict__ stencil, int nst, const float4 *__restrict__ shift,
+    const int32_t *__restrict__ start, const float4 *__restrict__ pos32,
+    const double4_32a *__restrict__ pos64, float rc2_lo, float rc2_hi, double rc2,
+    int32_t *__restrict__ count, const int64_t *__restrict__ off, uint32_t *__restrict__ list,
+    int *__restrict__ err) {
+  __shared__ int32_t s_base[kListWarps][kMaxStencil];
+  __shared__ int32_t s_pre[kListWarps][kMaxStencil + 1];
+  __shared__ int32_t s_code[kListWarps][kMaxStencil];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t C = blockIdx.x * (int64_t)kListWarps + w;
+  if (C >= g.ncell) return;  // whole warp
+  const int32_t tb = start[C], te = start[C + 1];
+  if (te <= tb) return;
+  const int cx = (int)(C % g.nc[0]), cy = (int)((C / g.nc[0]) % g.nc[1]),
+            cz = (int)(C / ((int64_t)g.nc[0] * g.nc[1]));
+  // stencil cell ranges and their running prefix (warp scan over chunks)
+  int32_t carry = 0;
+  for (int k0 = 0; k0 < nst; k0 += 32) {
+    const int k = k0 + lane;
+    int32_t cnt = 0, base = 0, code = 0;
+    if (k < nst) {
+      const int4 o = stencil[k];
+      const int32_t nc = shifted_cell(g, cx, cy, cz, o);
+      code = o.w;
+      if (nc >= 0) {
+        base = start[nc];
+        cnt = start[nc + 1] - base;
+      }
+    }
+    int32_t incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    if (k < nst) {
+      s_base[w][k] = base;
+      s_code[w][k] = code;
+      s_pre[w][k] = carry + incl - cnt;
+    }
+    carry += __shfl_sync(0xffffffffu, incl, 31);
   }
-  double4_32a pi64 = make_double4_32a(0, 0, 0, 0);
-  bool have64 = false;
-  for (int k = 0; k < nst; ++k) {
-    const int4 o = stencil[k];
-    const int32_t nc = shifted_cell(g, cx, cy, cz, o);
-    if (nc < 0) continue;
-    const float4 sh = shift[o.w];  // shifts are indexed by the offset code
-    const int32_t b = start[nc], e = start[nc + 1];
-    for (int32_t t = b; t < e; ++t) {
-      if (t == s) continue;
-      const float4 pj = pos32[t];
-      const float dx = (pj.x - pi.x) + sh.x;
-      const float dy = (pj.y - pi.y) + sh.y;
-      const float dz = (pj.z - pi.z) + sh.z;
-      const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-      bool in;
-      if (r2 < rc2_lo) in = true;
-      else if (r2 > rc2_hi) in = false;
-      else {
-        if (!have64) {
-          pi64 = pos64[s];
-          have64 = true;
+  if (lane == 0) s_pre[w][nst] = carry;
+  __syncwarp();
+  const int32_t V = carry;
+  const unsigned lt_mask = (1u << lane) - 1u;
+  for (int32_t t0 = tb; t0 < te; t0 += 32) {
+    const int ntc = min(32, te - t0);
+    const int32_t own = t0 + lane;
+    const bool own_ok = lane < ntc;
+    const float4 po = own_ok ? pos32[own] : make_float4(0.f, 0.f, 0.f, 0.f);
+    int64_t own_base = 0, own_cap = 0;
+    if (FILL && own_ok) {
+      own_base = off[own];
+      own_cap = off[own + 1] - own_base;
+    }
+    int32_t own_cnt = 0;
+    for (int32_t v0 = 0; v0 < V; v0 += 32) {
+      const int32_t v = v0 + lane;
+      const bool valid = v < V;
+      // stencil cell of candidate v: the last k with s_pre[k] <= v
+      int lo = 0, hi = nst - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (s_pre[w][mid] <= v) lo = mid;
+        else hi = mid - 1;
+      }
+      const int32_t t = valid ? s_base[w][lo] + (v - s_pre[w][lo]) : 0;
+      const int code = s_code[w][lo];
+      const float4 sh = shift[code];
+      const float4 pj = valid ? pos32[t] : make_float4(0.f, 0.f, 0.f, 0.f);
+      for (int i = 0; i < ntc; ++i) {
+        const float pix = __shfl_sync(0xffffffffu, po.x, i);
+        const float piy = __shfl_sync(0xffffffffu, po.y, i);
+        const float piz = __shfl_sync(0xffffffffu, po.z, i);
+        const int32_t ti = t0 + i;
+        const float dx = (pj.x - pix) + sh.x;
+        const float dy = (pj.y - piy) + sh.y;
+        const float dz = (pj.z - piz) + sh.z;
+        const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+        bool in = valid && t != ti;
+        if (in) {
+          if (r2 < rc2_lo) in = true;
+          else if (r2 > rc2_hi) in = false;
+          else in = exact_within(g, pos64[ti], pos64[t], rc2);
         }
-        in = exact_within(g, pi64, pos64[t], rc2);
+        const unsigned bal = __ballot_sync(0xffffffffu, in);
+        if (FILL) {
+          const int64_t at = __shfl_sync(0xffffffffu, own_base + own_cnt, i);
+          const int64_t cap_end = __shfl_sync(0xffffffffu, own_base + own_cap, i);
+          if (in) {
+            const int64_t pos = at + __popc(bal & lt_mask);
+            if (pos < cap_end) list[pos] = ((uint32_t)t << kCodeBits) | (uint32_t)code;
+            else atomicOr(err, kErrListOverflow);
+          }
+        }
+        if (lane == i) own_cnt += __popc(bal);
       }
-      if (!in) continue;
-      if (FILL) {
-        // entry code: the stencil offset in (2d+1)^3 index space (int4.w)
-        if (cnt < cap) list[base + cnt] = ((uint32_t)t << kCodeBits) | (uint32_t)o.w;
-        else atomicOr(err, kErrListOverflow);
-      }
-      ++cnt;
+    }
+    if (own_ok) {
+      if (!FILL) count[own] = own_cnt;
+      else if (own_cnt != own_cap) atomicOr(err, kErrListOverflow);
     }
   }
-  if (!FILL) count[s] = cnt;
 }
 
 __global__ void k_widen(int64_t n, const int32_t *__restrict__ in, int64_t *__restrict__ out) {
@@ -349,12 +407,13 @@ int build_pair_list(ggem_ctx *c) {
   const int T = 256;
   const unsigned bn = (unsigned)((n + T - 1) / T);
   const int nst = (int)c->stencil.size();
+  if (nst > kMaxStencil) return fail(c, GGEM_ERR_BAD_ARG, "stencil too large for the list builder");
   if ((e = cudaMemsetAsync(c->err.p, 0, sizeof(int), st))) return cuda_fail(c, e, "memset");
   kt_start(c, kKListBuild);
-  k_pair_list<false><<<bn, T, 0, st>>>(n, c->grid, c->d_stencil.p, nst, c->d_shift.p,
-                                        c->cell_start.p, c->pos32.p, c->pos64.p, c->rc2_lo,
-                                        c->rc2_hi, c->rc2, c->nb_count.p, nullptr, nullptr,
-                                        c->err.p);
+  const unsigned cb = (unsigned)((c->grid.ncell + kListWarps - 1) / kListWarps);
+  k_pair_list_warp<false><<<cb, 32 * kListWarps, 0, st>>>(
+      c->grid, c->d_stencil.p, nst, c->d_shift.p, c->cell_start.p, c->pos32.p, c->pos64.p,
+      c->rc2_lo, c->rc2_hi, c->rc2, c->nb_count.p, nullptr, nullptr, c->err.p);
   if (int rc = check_launch(c, "pair count")) return rc;
   k_widen<<<bn, T, 0, st>>>(n, c->nb_count.p, c->nb_cnt64.p);
   if (int rc = check_launch(c, "pair widen")) return rc;
@@ -364,10 +423,9 @@ int build_pair_list(ggem_ctx *c) {
       (e = cudaStreamSynchronize(st)))
     return cuda_fail(c, e, "list size");
   if ((e = c->nb_list.ensure((size_t)std::max<int64_t>(total, 1)))) return cuda_fail(c, e, "pair list");
-  k_pair_list<true><<<bn, T, 0, st>>>(n, c->grid, c->d_stencil.p, nst, c->d_shift.p,
-                                       c->cell_start.p, c->pos32.p, c->pos64.p, c->rc2_lo,
-                                       c->rc2_hi, c->rc2, nullptr, c->nb_off.p, c->nb_list.p,
-                                       c->err.p);
+  k_pair_list_warp<true><<<cb, 32 * kListWarps, 0, st>>>(
+      c->grid, c->d_stencil.p, nst, c->d_shift.p, c->cell_start.p, c->pos32.p, c->pos64.p,
+      c->rc2_lo, c->rc2_hi, c->rc2, nullptr, c->nb_off.p, c->nb_list.p, c->err.p);
   kt_stop(c, kKListBuild);
   if (int rc = check_launch(c, "pair fill")) return rc;
   int flags = 0;
