@@ -71,26 +71,32 @@ class ClockSampler:
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, index=0):
+    def __init__(self, index=0, period_ms=20):
         self.index = index
+        self.period_ms = period_ms
         self.proc = None
-        self.lines = []
+        self.lines = []      # (host arrival time, csv line)
+        self.windows = []    # timed regions (host perf_counter start, end)
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", str(self.period_ms)],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            time.sleep(0.3)  # let the first samples arrive before the load starts
         except (OSError, FileNotFoundError):
             self.proc = None
         return self
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.perf_counter(), line.strip()))
+
+    def mark(self, t0, t1):
+        self.windows.append((t0, t1))
 
     def __exit__(self, *a):
         if self.proc:
@@ -100,10 +106,10 @@ class ClockSampler:
             except subprocess.TimeoutExpired:
                 self.proc.kill()
 
-    def summary(self):
+    def _parse(self, lines):
         sm, mx, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        for _, ln in lines:
             parts = [p.strip() for p in ln.split(",")]
             if len(parts) < 9:
                 continue
@@ -115,10 +121,25 @@ class ClockSampler:
             for nm, v in zip(names, parts[5:9]):
                 if v.lower() == "active":
                     reasons.add(nm)
+        return sm, mx, reasons
+
+    def summary(self):
+        """Clocks of the samples taken inside the marked timed regions; when
+        those regions are too short for three samples, all samples taken
+        while the measured phases ran (the GPU is loaded throughout)."""
+        inside = [x for x in self.lines
+                  if any(t0 <= x[0] <= t1 + 0.05 for t0, t1 in self.windows)]
+        sm, mx, reasons = self._parse(inside)
+        scope = "timed regions"
+        if len(sm) < 3:
+            sm, mx, reasons = self._parse(self.lines)
+            scope = "all measured phases (timed regions shorter than 3 samples)"
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm),
+                "samples_in_timed_regions": len(inside), "period_ms": self.period_ms,
+                "scope": scope}
 
 
 # --------------------------------------------------------------------------
@@ -222,12 +243,13 @@ def run_gb300(args, rank, world):
     for s in range(args.warmup):
         device_step(s)
     torch.cuda.synchronize()
+    clk = ClockSampler(dev).__enter__()
     ctx.set_kernel_timing(True)
     lc0 = ctx.launch_count()
     t_wall0 = time.perf_counter()
-    with ClockSampler(dev) as clk:
-        ts = timed(device_step, args.steps, 0)
+    ts = timed(device_step, args.steps, 0)
     t_wall = time.perf_counter() - t_wall0
+    clk.mark(t_wall0, t_wall0 + t_wall)
     lc1 = ctx.launch_count()
     kt = {name: ctx.kernel_timing(kind) for kind, name in
           ((G.KERNEL_PAIR_FP32, "pair_fp32"), (G.KERNEL_CHEB_TERM, "cheb_term"),
@@ -280,7 +302,9 @@ def run_gb300(args, rank, world):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         e2e_step(args.warmup + s)
-        e_ts.append((time.perf_counter() - t0) * 1e3)
+        t1 = time.perf_counter()
+        e_ts.append((t1 - t0) * 1e3)
+        clk.mark(t0, t1)
     e2e_ms = float(np.mean(e_ts))
     ctx_e.close()
 
@@ -300,6 +324,7 @@ def run_gb300(args, rank, world):
         b.record(stream)
         b.synchronize()
         mv_ts.append(a.elapsed_time(b))
+    clk.__exit__(None, None, None)
     matvecs_per_s = 1e3 / float(np.mean(mv_ts)) * world
 
     # ---- accuracy: FP32 vs FP64 velocities at N=200k --------------------
@@ -366,7 +391,7 @@ def run_gb300(args, rank, world):
         "cheb": {"terms": [r["n_terms"] for r in reps], "err1_max": max(r["err1"] for r in reps),
                  "converged": all(r["converged"] for r in reps),
                  "lanczos_calls": state["lanczos_calls"]},
-        "roofline": {"bound": "fp32", "kernel": "k_matvec_f32<1> (pair-list sum)",
+        "roofline": {"bound": "fp32", "kernel": "k_pair_r1 (CSR pair-list sum, one RHS)",
                      "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak if peak else None,
                      "peak_source": "measured live: FP32 FMA-chain probe on this GPU "

@@ -396,9 +396,11 @@ extern "C" int ggem_set_particles_dev(ggem_ctx *ctx, int64_t n, const double *d_
 extern "C" int ggem_build_cells(ggem_ctx *ctx) {
   if (!ctx) return GGEM_ERR_BAD_ARG;
   DeviceGuard dg(ctx->device);
-  if (int rc = build_cells(ctx)) return rc;
-  if (ctx->prm.precision == GGEM_FP32 && ctx->prm.nb_mode == GGEM_NB_CUTOFF)
-    return build_pair_list(ctx);
+  // the FP32 path builds its pair list right after the cells; both error
+  // checks then share the list's single host readback
+  const bool with_list = ctx->prm.precision == GGEM_FP32 && ctx->prm.nb_mode == GGEM_NB_CUTOFF;
+  if (int rc = build_cells(ctx, with_list)) return rc;
+  if (with_list) return build_pair_list(ctx);
   return GGEM_OK;
 }
 

@@ -233,7 +233,7 @@ __global__ void __launch_bounds__(32 * kListWarps) k_pair_list_warp(
     const int32_t *__restrict__ start, const float4 *__restrict__ pos32,
     const double4_32a *__restrict__ pos64, float rc2_lo, float rc2_hi, double rc2,
     int32_t *__restrict__ count, const int64_t *__restrict__ off, uint32_t *__restrict__ list,
-    int *__restrict__ err) {
+    int64_t list_cap, int *__restrict__ err) {
   __shared__ int32_t s_base[kListWarps][kMaxStencil];
   __shared__ int32_t s_pre[kListWarps][kMaxStencil + 1];
   __shared__ int32_t s_code[kListWarps][kMaxStencil];
@@ -321,8 +321,9 @@ __global__ void __launch_bounds__(32 * kListWarps) k_pair_list_warp(
           const int64_t cap_end = __shfl_sync(0xffffffffu, own_base + own_cap, i);
           if (in) {
             const int64_t pos = at + __popc(bal & lt_mask);
-            if (pos < cap_end) list[pos] = ((uint32_t)t << kCodeBits) | (uint32_t)code;
-            else atomicOr(err, kErrListOverflow);
+            if (pos >= cap_end) atomicOr(err, kErrListOverflow);
+            else if (pos >= list_cap) atomicOr(err, kErrListCapacity);
+            else list[pos] = ((uint32_t)t << kCodeBits) | (uint32_t)code;
           }
         }
         if (lane == i) own_cnt += __popc(bal);
@@ -349,7 +350,7 @@ int device_exclusive_scan_i64(ggem_ctx *c, const int64_t *in, int64_t *out, int6
   return scan_impl<int64_t>(c, in, out, n, 0);
 }
 
-int build_cells(ggem_ctx *c) {
+int build_cells(ggem_ctx *c, bool defer_flags) {
   const int64_t n = c->n;
   const Grid &g = c->grid;
   cudaError_t e = cudaSuccess;
@@ -381,14 +382,24 @@ int build_cells(ggem_ctx *c) {
                                       c->pos64.p, c->pos32.p);
     if (int rc = check_launch(c, "gather sorted")) return rc;
   }
-  int flags = 0;
-  if (int rc = read_error_flags(c, &flags)) return rc;
-  if (flags & kErrOutOfDomain)
+  c->cells_built = false;
+  c->list_built = false;
+  if (!defer_flags) {
+    int flags = 0;
+    if (int rc = read_error_flags(c, &flags)) return rc;
+    if (int rc = cell_flag_error(c, flags)) return rc;
+  }
+  c->cells_built = true;
+  return GGEM_OK;
+}
+
+int cell_flag_error(ggem_ctx *c, int flags) {
+  if (flags & kErrOutOfDomain) {
+    c->cells_built = false;
     return fail(c, GGEM_ERR_OUT_OF_DOMAIN,
                 "a particle lies outside the box on a non-periodic axis "
                 "(point_mesh.C:602-613: no element contains it)");
-  c->cells_built = true;
-  c->list_built = false;
+  }
   return GGEM_OK;
 }
 
@@ -401,6 +412,7 @@ int build_pair_list(ggem_ctx *c) {
   if (n == 0) {
     if ((e = cudaMemsetAsync(c->nb_off.p, 0, sizeof(int64_t), st))) return cuda_fail(c, e, "memset");
     c->n_pairs = 0;
+    c->cells_built = true;
     c->list_built = true;
     return GGEM_OK;
   }
@@ -408,29 +420,53 @@ int build_pair_list(ggem_ctx *c) {
   const unsigned bn = (unsigned)((n + T - 1) / T);
   const int nst = (int)c->stencil.size();
   if (nst > kMaxStencil) return fail(c, GGEM_ERR_BAD_ARG, "stencil too large for the list builder");
-  if ((e = cudaMemsetAsync(c->err.p, 0, sizeof(int), st))) return cuda_fail(c, e, "memset");
+  // The error word still holds the cell build's flags; they are read back
+  // together with the list length after a speculative fill into the list
+  // as allocated (its size from earlier builds), so a rebuild of a similar
+  // configuration costs one host synchronisation.  A fill that ran past the
+  // allocation is repeated once the list has grown.
   kt_start(c, kKListBuild);
   const unsigned cb = (unsigned)((c->grid.ncell + kListWarps - 1) / kListWarps);
   k_pair_list_warp<false><<<cb, 32 * kListWarps, 0, st>>>(
       c->grid, c->d_stencil.p, nst, c->d_shift.p, c->cell_start.p, c->pos32.p, c->pos64.p,
-      c->rc2_lo, c->rc2_hi, c->rc2, c->nb_count.p, nullptr, nullptr, c->err.p);
+      c->rc2_lo, c->rc2_hi, c->rc2, c->nb_count.p, nullptr, nullptr, 0, c->err.p);
   if (int rc = check_launch(c, "pair count")) return rc;
   k_widen<<<bn, T, 0, st>>>(n, c->nb_count.p, c->nb_cnt64.p);
   if (int rc = check_launch(c, "pair widen")) return rc;
   if (int rc = device_exclusive_scan_i64(c, c->nb_cnt64.p, c->nb_off.p, n)) return rc;
-  int64_t total = 0;
-  if ((e = cudaMemcpyAsync(&total, c->nb_off.p + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st)) ||
+  const bool speculate = c->nb_list.p != nullptr;
+  if (speculate) {
+    k_pair_list_warp<true><<<cb, 32 * kListWarps, 0, st>>>(
+        c->grid, c->d_stencil.p, nst, c->d_shift.p, c->cell_start.p, c->pos32.p, c->pos64.p,
+        c->rc2_lo, c->rc2_hi, c->rc2, nullptr, c->nb_off.p, c->nb_list.p,
+        (int64_t)c->nb_list.count, c->err.p);
+    if (int rc = check_launch(c, "pair fill")) return rc;
+  }
+  kt_stop(c, kKListBuild);  // a regrown refill below is left out of the timing
+  // one readback: list length and error word
+  int64_t *h = reinterpret_cast<int64_t *>(c->h_red);
+  h[1] = 0;
+  if ((e = cudaMemcpyAsync(&h[0], c->nb_off.p + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st)) ||
+      (e = cudaMemcpyAsync(&h[1], c->err.p, sizeof(int), cudaMemcpyDeviceToHost, st)) ||
       (e = cudaStreamSynchronize(st)))
     return cuda_fail(c, e, "list size");
-  if ((e = c->nb_list.ensure((size_t)std::max<int64_t>(total, 1)))) return cuda_fail(c, e, "pair list");
-  k_pair_list_warp<true><<<cb, 32 * kListWarps, 0, st>>>(
-      c->grid, c->d_stencil.p, nst, c->d_shift.p, c->cell_start.p, c->pos32.p, c->pos64.p,
-      c->rc2_lo, c->rc2_hi, c->rc2, nullptr, c->nb_off.p, c->nb_list.p, c->err.p);
-  kt_stop(c, kKListBuild);
-  if (int rc = check_launch(c, "pair fill")) return rc;
-  int flags = 0;
-  if (int rc = read_error_flags(c, &flags)) return rc;
-  if (flags & kErrListOverflow)
+  const int64_t total = h[0];
+  int flags = (int)h[1];
+  if (int rc = cell_flag_error(c, flags)) return rc;
+  c->cells_built = true;
+  if (!speculate || (flags & kErrListCapacity) || total > (int64_t)c->nb_list.count) {
+    // grow with headroom so that a slowly varying configuration refills in place
+    const size_t want = (size_t)std::max<int64_t>(total + total / 16, 1);
+    if ((e = c->nb_list.ensure(want))) return cuda_fail(c, e, "pair list");
+    if ((e = cudaMemsetAsync(c->err.p, 0, sizeof(int), st))) return cuda_fail(c, e, "memset");
+    k_pair_list_warp<true><<<cb, 32 * kListWarps, 0, st>>>(
+        c->grid, c->d_stencil.p, nst, c->d_shift.p, c->cell_start.p, c->pos32.p, c->pos64.p,
+        c->rc2_lo, c->rc2_hi, c->rc2, nullptr, c->nb_off.p, c->nb_list.p,
+        (int64_t)c->nb_list.count, c->err.p);
+    if (int rc = check_launch(c, "pair fill")) return rc;
+    if (int rc = read_error_flags(c, &flags)) return rc;
+  }
+  if (flags & (kErrListOverflow | kErrListCapacity))
     return fail(c, GGEM_ERR_CELL_OVERFLOW, "pair list fill exceeded its counted length");
   c->n_pairs = total;
   c->list_built = true;

@@ -23,6 +23,11 @@ static cudaEvent_t take_event(ggem_ctx *c) {
 
 void kt_start(ggem_ctx *c, int kind) {
   if (!c->timing) return;
+  auto &t = c->ktimer[kind];
+  if (t.ev.size() % 2 == 1) {  // a start left open by an error return: restart it
+    cudaEventRecord(t.ev.back(), c->stream);
+    return;
+  }
   cudaEvent_t e = take_event(c);
   if (!e) return;
   cudaEventRecord(e, c->stream);

@@ -40,6 +40,7 @@ enum : int {
   kErrListOverflow = 2,
   kErrTimeout = 4,
   kErrBadIndex = 8,
+  kErrListCapacity = 16,  // speculative list fill ran past the allocated list
 };
 
 // derived GGEM constants (ggem_stokes.C:39-114) in FP64
@@ -181,7 +182,9 @@ void tridiag_extremes(int k, const double *a, const double *b, double *lmin, dou
 void cheb_coeffs_host(int N, double da, double db, int method, double *coef);
 
 // cell build and pair list (ggem_cells.cu)
-int build_cells(ggem_ctx *c);
+// defer_flags: leave the device error word unread (build_pair_list reads it)
+int build_cells(ggem_ctx *c, bool defer_flags = false);
+int cell_flag_error(ggem_ctx *c, int flags);
 int build_pair_list(ggem_ctx *c);
 int device_exclusive_scan_i32(ggem_ctx *c, const int32_t *in, int32_t *out, int64_t n);
 int device_exclusive_scan_i64(ggem_ctx *c, const int64_t *in, int64_t *out, int64_t n);
