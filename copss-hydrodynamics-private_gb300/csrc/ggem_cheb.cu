@@ -363,27 +363,40 @@ int cheb_slots(ggem_ctx *c, int nrhs, int N, double eig_min, double eig_max, dou
   }
   const double two_da = 2. * da, two_db = 2. * db;
   int first_check = -1;
+  // Terms that no error check follows need neither norm: on the FP32
+  // single-RHS path they run as one fused pair-sum + recurrence kernel that
+  // also writes the FP32 records of the next x1 (records_fresh).
+  const bool can_fuse = nrhs == 1 && c->prm.precision == GGEM_FP32 &&
+                        c->prm.nb_mode == GGEM_NB_CUTOFF;
+  bool records_fresh = false;
   for (int i = 1; i < N; ++i) {
     int n_active = 0;
     for (int r = 0; r < nrhs; ++r) n_active += active[r];
     if (n_active == 0) break;
-    if (int rc = matvec_slots(c, nrhs, x1, xm, sm)) return rc;
-    RhsCoef cf;
-    for (int r = 0; r < nrhs; ++r) cf.c[r] = active[r] ? X[i + 1] : 0.0;
-    kt_start(c, kKChebTerm);
-    k_cheb_term<<<dim3(G, nrhs), kVecThreads, 0, st>>>(D, two_da, two_db, cf, x0, x1, xm, dw,
-                                                        p_term);
-    kt_stop(c, kKChebTerm);
-    if (int rc = check_launch(c, "cheb term")) return rc;
+    bool check;
+    if (faithful) check = true;
+    else if (check_every > 1) check = (i % check_every == 0) || (i == N - 1);
+    else check = (i + 1 >= k_first) || (i == N - 1);
+    if (can_fuse && !check) {
+      if (int rc = pair_cheb_term(c, records_fresh, x0, x1, xm, dw, two_da, two_db, X[i + 1], sm))
+        return rc;
+      records_fresh = true;
+    } else {
+      if (int rc = matvec_slots(c, nrhs, x1, xm, sm)) return rc;
+      RhsCoef cf;
+      for (int r = 0; r < nrhs; ++r) cf.c[r] = active[r] ? X[i + 1] : 0.0;
+      kt_start(c, kKChebTerm);
+      k_cheb_term<<<dim3(G, nrhs), kVecThreads, 0, st>>>(D, two_da, two_db, cf, x0, x1, xm, dw,
+                                                          p_term);
+      kt_stop(c, kKChebTerm);
+      if (int rc = check_launch(c, "cheb term")) return rc;
+      records_fresh = false;
+    }
     for (int r = 0; r < nrhs; ++r)
       if (active[r]) {
         rep[r].n_matvecs += 1;
         rep[r].n_terms = i + 1;
       }
-    bool check;
-    if (faithful) check = true;
-    else if (check_every > 1) check = (i % check_every == 0) || (i == N - 1);
-    else check = (i + 1 >= k_first) || (i == N - 1);
     *dm_is_my = false;
     if (check) {
       if (int rc = check_now(std::fabs(X[i + 1]), true)) return rc;

@@ -122,7 +122,7 @@ extern "C" int ggem_set_kernel_timing(ggem_ctx *ctx, int enable) {
 
 extern "C" int ggem_get_kernel_timing(ggem_ctx *ctx, int kernel, double *total_ms,
                                       int64_t *launches) {
-  if (!ctx || kernel < 0 || kernel > 3 || !total_ms || !launches) return GGEM_ERR_BAD_ARG;
+  if (!ctx || kernel < 0 || kernel > 4 || !total_ms || !launches) return GGEM_ERR_BAD_ARG;
   if (int rc = drain(ctx)) return rc;
   *total_ms = ctx->ktimer[kernel].total_ms;
   *launches = ctx->ktimer[kernel].count;

@@ -127,10 +127,12 @@ struct ggem_ctx {
   float poly_a[16] = {0}, poly_b[16] = {0};
   float poly_x0 = 0.f, poly_x1 = 0.f, poly_e[2] = {0.f, 0.f};  // exponent hi + lo
   double poly_max_err = 0.0;
-  // single-RHS pair kernel: 32-byte source records, work counter, grid
-  ggem::DevBuf<float4> w_src;          // 2 float4 per slot
-  ggem::DevBuf<unsigned int> work;     // spare device counter
-  int pair_grid = 0;                   // CTAs of the persistent pair kernel
+  // single-RHS pair kernel: 32-byte source records (2 float4 per slot):
+  // w_src for plain matvecs, w_rec[2] for the fused Chebyshev chain (the
+  // records of x_k in w_rec[rec_cur], those of x_{k+1} written to the other)
+  ggem::DevBuf<float4> w_src;
+  ggem::DevBuf<float4> w_rec[2];
+  int rec_cur = 0;
   int cheb_pred_terms = 0;             // degree the last adaptive Chebyshev needed
 
   // scan scratch (one per recursion level)
@@ -152,7 +154,7 @@ struct ggem_ctx {
     std::vector<cudaEvent_t> ev;  // start/stop pairs
     double total_ms = 0.0;
     int64_t count = 0;
-  } ktimer[4];
+  } ktimer[5];
   std::vector<cudaEvent_t> ev_pool;
 
   ~ggem_ctx();
@@ -161,7 +163,7 @@ struct ggem_ctx {
 namespace ggem {
 
 // kernel kinds of the timing hooks
-enum : int { kKPairF32 = 0, kKPairF64 = 1, kKChebTerm = 2, kKListBuild = 3 };
+enum : int { kKPairF32 = 0, kKPairF64 = 1, kKChebTerm = 2, kKListBuild = 3, kKPairCheb = 4 };
 
 void kt_start(ggem_ctx *c, int kind);
 void kt_stop(ggem_ctx *c, int kind);
@@ -192,8 +194,12 @@ int device_exclusive_scan_i64(ggem_ctx *c, const int64_t *in, int64_t *out, int6
 // pair sums (ggem_pair.cu); vectors in slot order, [r][slot][3] doubles
 int matvec_slots(ggem_ctx *c, int nrhs, const double *d_f_slot, double *d_u_slot,
                  int self_mode);
-int matvec_f32_staged(ggem_ctx *c, int nrhs, double *d_u_slot, int self_mode);
+int matvec_f32_staged(ggem_ctx *c, int nrhs, const double *d_f_slot, double *d_u_slot,
+                      int self_mode);
 double self_coefficient(const ggem_ctx *c, int self_mode);
+int pair_cheb_term(ggem_ctx *c, bool records_fresh, const double *x0, const double *x1,
+                   double *xm, double *dw, double two_da, double two_db, double coef,
+                   int self_mode);
 int permute_to_slots(ggem_ctx *c, int nrhs, const double *d_orig, double *d_slot);
 int permute_from_slots(ggem_ctx *c, int nrhs, const double *d_slot, double *d_orig);
 

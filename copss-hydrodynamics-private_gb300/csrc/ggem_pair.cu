@@ -202,10 +202,55 @@ __device__ __forceinline__ void decode_shift(uint32_t e, float hx, float hy, flo
   sz = (float)(code / (SIDE * SIDE) - CD) * hz;
 }
 
-__device__ __forceinline__ double group_sum(double v) {
+// GB300 issues FP64 at a small fraction of the FP32 rate, so the group
+// reduction stays in FP32: each lane's Kahan pair (s, -c) is a float-float
+// value, summed across the group with error-free transformations (Knuth's
+// TwoSum), and only the final hi + lo per output component is formed in FP64.
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+
+// (hi, lo) += (h2, l2), renormalised so that |lo| <= ulp(hi) / 2
+__device__ __forceinline__ void ff_add(float &hi, float &lo, float h2, float l2) {
+  float s, e;
+  two_sum(hi, h2, s, e);
+  e += lo + l2;
+  hi = s + e;
+  lo = e - (hi - s);
+}
+
+__device__ __forceinline__ void group_ff(float &hi, float &lo) {
 #pragma unroll
-  for (int o = kGroup / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
+  for (int o = kGroup / 2; o > 0; o >>= 1) {
+    const float h2 = __shfl_xor_sync(0xffffffffu, hi, o);
+    const float l2 = __shfl_xor_sync(0xffffffffu, lo, o);
+    ff_add(hi, lo, h2, l2);
+  }
+}
+
+// float -> double from the bit fields with integer operations (exact for
+// normal floats; subnormals, below 1.2e-38, become signed zero)
+__device__ __forceinline__ double f2d_bits(float x) {
+  const uint32_t b = __float_as_uint(x);
+  const uint32_t sign = b & 0x80000000u, ex = (b >> 23) & 0xffu, m = b & 0x7fffffu;
+  if (ex == 0u) return __hiloint2double((int)sign, 0);
+  const uint32_t e64 = ex == 0xffu ? 0x7ffu : ex + (1023u - 127u);
+  return __hiloint2double((int)(sign | (e64 << 20) | (m >> 3)), (int)(m << 29));
+}
+
+// lanes sub = 0, 1, 2 of a group write component sub of the target:
+// u = (hi + lo) + self_c f with the FP64 force of the target
+__device__ __forceinline__ void group_store(bool act, int sub, int64_t s, float hx, float lx,
+                                            float hy, float ly, float hz, float lz,
+                                            double self_c, const double *__restrict__ f,
+                                            double *__restrict__ u) {
+  if (!act || sub >= 3) return;
+  const float h = sub == 0 ? hx : (sub == 1 ? hy : hz);
+  const float l = sub == 0 ? lx : (sub == 1 ? ly : lz);
+  const double v = f2d_bits(h) + f2d_bits(l);
+  u[3 * s + sub] = fma(self_c, f[3 * s + sub], v);
 }
 
 __global__ void k_build_src(int64_t n, const float4 *__restrict__ pos32,
@@ -218,18 +263,22 @@ __global__ void k_build_src(int64_t n, const float4 *__restrict__ pos32,
   src[s] = r;
 }
 
-// single right-hand side
+// float-float sum of one target's pair terms, complete on every lane of the group
+struct PairSum {
+  float hx, lx, hy, ly, hz, lz;
+};
+
+// the pair loop of one target slot s over its CSR entries (one right-hand
+// side, 32-byte source records); lanes sub = 0..kGroup-1 take every
+// kGroup-th entry, so a group reads consecutive list words
 template <int CD, bool POLY>
-__global__ void __launch_bounds__(256) k_pair_r1(
-    int64_t n, const Rec32 *__restrict__ src, const int64_t *__restrict__ off,
-    const uint32_t *__restrict__ list, PolyAB P, const Rec32 *__restrict__ tab, float inv_ds,
-    float hx, float hy, float hz, double self_c, double *__restrict__ u) {
-  const int64_t gid = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / kGroup;
-  const int sub = (int)(threadIdx.x % kGroup);
-  const bool act = gid < n;
-  const int64_t s = act ? gid : n - 1;
+__device__ __forceinline__ PairSum pair_sum_r1(int64_t s, bool act, int sub, const Rec32 &ri,
+                                               const Rec32 *__restrict__ src,
+                                               const int64_t *__restrict__ off,
+                                               const uint32_t *__restrict__ list,
+                                               const PolyAB &P, const Rec32 *__restrict__ tab,
+                                               float inv_ds, float hx, float hy, float hz) {
   const int64_t b = off[s], e = act ? off[s + 1] : b;
-  const Rec32 ri = src[s];
   float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
   float bx = 0.f, by = 0.f, bz = 0.f;
   int blk = 0;
@@ -259,14 +308,66 @@ __global__ void __launch_bounds__(256) k_pair_r1(
   kahan_add(sx, cx, bx);
   kahan_add(sy, cy, by);
   kahan_add(sz, cz, bz);
-  const double ux = group_sum((double)sx - (double)cx);
-  const double uy = group_sum((double)sy - (double)cy);
-  const double uz = group_sum((double)sz - (double)cz);
-  if (act && sub == 0) {
-    double *ui = u + 3 * s;
-    ui[0] = ux + self_c * (double)ri.b.x;
-    ui[1] = uy + self_c * (double)ri.b.y;
-    ui[2] = uz + self_c * (double)ri.b.z;
+  // Kahan keeps sum = s - c: the float-float value is (s, -c)
+  PairSum r{sx, -cx, sy, -cy, sz, -cz};
+  group_ff(r.hx, r.lx);
+  group_ff(r.hy, r.ly);
+  group_ff(r.hz, r.lz);
+  return r;
+}
+
+// u = M f, single right-hand side
+template <int CD, bool POLY>
+__global__ void __launch_bounds__(256) k_pair_r1(
+    int64_t n, const Rec32 *__restrict__ src, const int64_t *__restrict__ off,
+    const uint32_t *__restrict__ list, PolyAB P, const Rec32 *__restrict__ tab, float inv_ds,
+    float hx, float hy, float hz, double self_c, const double *__restrict__ f,
+    double *__restrict__ u) {
+  const int64_t gid = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / kGroup;
+  const int sub = (int)(threadIdx.x % kGroup);
+  const bool act = gid < n;
+  const int64_t s = act ? gid : n - 1;
+  const Rec32 ri = src[s];
+  const PairSum r =
+      pair_sum_r1<CD, POLY>(s, act, sub, ri, src, off, list, P, tab, inv_ds, hx, hy, hz);
+  group_store(act, sub, s, r.hx, r.lx, r.hy, r.ly, r.hz, r.lz, self_c, f, u);
+}
+
+// One Chebyshev term with the pair sum (brownian_system.C:1091-1108 for one
+// right-hand side, without the norms of the error estimators):
+//   m = M x1 (pair sum + self term),  xm = (2db x1 + 2da m) - x0,
+//   dw += coef xm,  and the 32-byte records of xm for the next term.
+// src holds the records of x1; next must be a different buffer.
+template <int CD, bool POLY>
+__global__ void __launch_bounds__(256) k_pair_cheb(
+    int64_t n, const Rec32 *__restrict__ src, const int64_t *__restrict__ off,
+    const uint32_t *__restrict__ list, PolyAB P, const Rec32 *__restrict__ tab, float inv_ds,
+    float hx, float hy, float hz, double self_c, double two_da, double two_db, double coef,
+    const double *__restrict__ x0, const double *__restrict__ x1, double *__restrict__ xm,
+    double *__restrict__ dw, Rec32 *__restrict__ next) {
+  const int64_t gid = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / kGroup;
+  const int sub = (int)(threadIdx.x % kGroup);
+  const bool act = gid < n;
+  const int64_t s = act ? gid : n - 1;
+  const Rec32 ri = src[s];
+  const PairSum r =
+      pair_sum_r1<CD, POLY>(s, act, sub, ri, src, off, list, P, tab, inv_ds, hx, hy, hz);
+  if (!act) return;
+  float *nf = reinterpret_cast<float *>(next + s);
+  if (sub < 3) {
+    const float h = sub == 0 ? r.hx : (sub == 1 ? r.hy : r.hz);
+    const float l = sub == 0 ? r.lx : (sub == 1 ? r.ly : r.lz);
+    const int64_t k = 3 * s + sub;
+    const double xk = x1[k];
+    const double m = fma(self_c, xk, f2d_bits(h) + f2d_bits(l));
+    double v = two_db * xk + two_da * m;
+    v -= x0[k];
+    xm[k] = v;
+    dw[k] = dw[k] + coef * v;
+    nf[4 + sub] = __double2float_rn(v);
+  } else {
+    reinterpret_cast<float4 *>(nf)[0] = ri.a;  // the target's position record
+    nf[7] = 0.f;
   }
 }
 
@@ -276,7 +377,7 @@ __global__ void __launch_bounds__(256) k_pair_nr(
     int64_t n, const float4 *__restrict__ pos32, const float4 *__restrict__ f32,
     const int64_t *__restrict__ off, const uint32_t *__restrict__ list, PolyAB P,
     const Rec32 *__restrict__ tab, float inv_ds, float hx, float hy, float hz, double self_c,
-    double *__restrict__ u, int r0) {
+    const double *__restrict__ f, double *__restrict__ u, int r0) {
   const int64_t gid = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / kGroup;
   const int sub = (int)(threadIdx.x % kGroup);
   const bool act = gid < n;
@@ -309,16 +410,15 @@ __global__ void __launch_bounds__(256) k_pair_nr(
   }
 #pragma unroll
   for (int q = 0; q < NR; ++q) {
-    const double ux = group_sum((double)sx[q] - (double)cx[q]);
-    const double uy = group_sum((double)sy[q] - (double)cy[q]);
-    const double uz = group_sum((double)sz[q] - (double)cz[q]);
-    if (act && sub == 0) {
-      const float4 fi = f32[(int64_t)(r0 + q) * n + s];
-      double *ui = u + ((int64_t)(r0 + q) * n + s) * 3;
-      ui[0] = ux + self_c * (double)fi.x;
-      ui[1] = uy + self_c * (double)fi.y;
-      ui[2] = uz + self_c * (double)fi.z;
-    }
+    cx[q] = -cx[q];
+    cy[q] = -cy[q];
+    cz[q] = -cz[q];
+    group_ff(sx[q], cx[q]);
+    group_ff(sy[q], cy[q]);
+    group_ff(sz[q], cz[q]);
+    const int64_t roff = (int64_t)(r0 + q) * n * 3;
+    group_store(act, sub, s, sx[q], cx[q], sy[q], cy[q], sz[q], cz[q], self_c, f + roff,
+                u + roff);
   }
 }
 
@@ -385,13 +485,13 @@ PolyAB poly_of(const ggem_ctx *c) {
 }
 
 template <int CD, bool POLY>
-void launch_r1(ggem_ctx *c, const Rec32 *src, double *u, double self_c) {
+void launch_r1(ggem_ctx *c, const Rec32 *src, const double *f, double *u, double self_c) {
   const int64_t threads = c->n * kGroup;
   const Grid &g = c->grid;
   k_pair_r1<CD, POLY><<<(unsigned)((threads + 255) / 256), 256, 0, c->stream>>>(
       c->n, src, c->nb_off.p, c->nb_list.p, poly_of(c),
       reinterpret_cast<const Rec32 *>(c->tab.p), c->tab_inv_ds, g.h32[0], g.h32[1], g.h32[2],
-      self_c, u);
+      self_c, f, u);
 }
 
 // single right-hand side: records from FP64 slot-order f, then the pair sum
@@ -404,32 +504,44 @@ int launch_f32_r1(ggem_ctx *c, const double *f, double *u, double self_c) {
   if (int rc = check_launch(c, "pair records")) return rc;
   kt_start(c, kKPairF32);
   const bool cd2 = c->prm.cell_div == 2;
-  if (c->use_poly) cd2 ? launch_r1<2, true>(c, src, u, self_c) : launch_r1<1, true>(c, src, u, self_c);
-  else cd2 ? launch_r1<2, false>(c, src, u, self_c) : launch_r1<1, false>(c, src, u, self_c);
+  if (c->use_poly) cd2 ? launch_r1<2, true>(c, src, f, u, self_c) : launch_r1<1, true>(c, src, f, u, self_c);
+  else cd2 ? launch_r1<2, false>(c, src, f, u, self_c) : launch_r1<1, false>(c, src, f, u, self_c);
   kt_stop(c, kKPairF32);
   return check_launch(c, "pair f32 r1");
 }
 
+template <int CD, bool POLY>
+void launch_cheb(ggem_ctx *c, const Rec32 *src, Rec32 *next, double self_c, double two_da,
+                 double two_db, double coef, const double *x0, const double *x1, double *xm,
+                 double *dw) {
+  const int64_t threads = c->n * kGroup;
+  const Grid &g = c->grid;
+  k_pair_cheb<CD, POLY><<<(unsigned)((threads + 255) / 256), 256, 0, c->stream>>>(
+      c->n, src, c->nb_off.p, c->nb_list.p, poly_of(c),
+      reinterpret_cast<const Rec32 *>(c->tab.p), c->tab_inv_ds, g.h32[0], g.h32[1], g.h32[2],
+      self_c, two_da, two_db, coef, x0, x1, xm, dw, next);
+}
+
 template <int CD, bool POLY, int NR>
-void launch_nr_t(ggem_ctx *c, double *u, double self_c, int r0) {
+void launch_nr_t(ggem_ctx *c, const double *f, double *u, double self_c, int r0) {
   const int64_t threads = c->n * kGroup;
   const Grid &g = c->grid;
   k_pair_nr<CD, POLY, NR><<<(unsigned)((threads + 255) / 256), 256, 0, c->stream>>>(
       c->n, c->pos32.p, c->w_f32.p, c->nb_off.p, c->nb_list.p, poly_of(c),
       reinterpret_cast<const Rec32 *>(c->tab.p), c->tab_inv_ds, g.h32[0], g.h32[1], g.h32[2],
-      self_c, u, r0);
+      self_c, f, u, r0);
 }
 
 template <int NR>
-int launch_nr(ggem_ctx *c, double *u, double self_c, int r0) {
+int launch_nr(ggem_ctx *c, const double *f, double *u, double self_c, int r0) {
   const bool cd2 = c->prm.cell_div == 2;
   kt_start(c, kKPairF32);
   if (c->use_poly) {
-    if (cd2) launch_nr_t<2, true, NR>(c, u, self_c, r0);
-    else launch_nr_t<1, true, NR>(c, u, self_c, r0);
+    if (cd2) launch_nr_t<2, true, NR>(c, f, u, self_c, r0);
+    else launch_nr_t<1, true, NR>(c, f, u, self_c, r0);
   } else {
-    if (cd2) launch_nr_t<2, false, NR>(c, u, self_c, r0);
-    else launch_nr_t<1, false, NR>(c, u, self_c, r0);
+    if (cd2) launch_nr_t<2, false, NR>(c, f, u, self_c, r0);
+    else launch_nr_t<1, false, NR>(c, f, u, self_c, r0);
   }
   kt_stop(c, kKPairF32);
   return check_launch(c, "pair f32");
@@ -451,6 +563,38 @@ int permute_from_slots(ggem_ctx *c, int nrhs, const double *d_slot, double *d_or
   k_from_slots<<<(unsigned)((tot + 255) / 256), 256, 0, c->stream>>>(c->n, nrhs, c->rank.p,
                                                                      d_slot, d_orig);
   return check_launch(c, "from slots");
+}
+
+// One fused Chebyshev term on the FP32 single-RHS path (k_pair_cheb).
+// records_fresh: c->w_rec[c->rec_cur] already holds the records of x1 (the
+// previous fused term wrote them); otherwise they are built here first.
+int pair_cheb_term(ggem_ctx *c, bool records_fresh, const double *x0, const double *x1,
+                   double *xm, double *dw, double two_da, double two_db, double coef,
+                   int self_mode) {
+  const int64_t n = c->n;
+  if (n == 0) return GGEM_OK;
+  cudaError_t e;
+  if ((e = c->w_rec[0].ensure(2 * (size_t)n)) || (e = c->w_rec[1].ensure(2 * (size_t)n)))
+    return cuda_fail(c, e, "chebyshev records");
+  Rec32 *cur = reinterpret_cast<Rec32 *>(c->w_rec[c->rec_cur].p);
+  Rec32 *nxt = reinterpret_cast<Rec32 *>(c->w_rec[c->rec_cur ^ 1].p);
+  if (!records_fresh) {
+    k_build_src<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(n, c->pos32.p, x1, cur);
+    if (int rc = check_launch(c, "chebyshev records")) return rc;
+  }
+  const double self_c = self_coefficient(c, self_mode);
+  kt_start(c, kKPairCheb);
+  const bool cd2 = c->prm.cell_div == 2;
+  if (c->use_poly) {
+    if (cd2) launch_cheb<2, true>(c, cur, nxt, self_c, two_da, two_db, coef, x0, x1, xm, dw);
+    else launch_cheb<1, true>(c, cur, nxt, self_c, two_da, two_db, coef, x0, x1, xm, dw);
+  } else {
+    if (cd2) launch_cheb<2, false>(c, cur, nxt, self_c, two_da, two_db, coef, x0, x1, xm, dw);
+    else launch_cheb<1, false>(c, cur, nxt, self_c, two_da, two_db, coef, x0, x1, xm, dw);
+  }
+  kt_stop(c, kKPairCheb);
+  c->rec_cur ^= 1;
+  return check_launch(c, "pair chebyshev term");
 }
 
 double self_coefficient(const ggem_ctx *c, int self_mode) {
@@ -481,20 +625,21 @@ int matvec_slots(ggem_ctx *c, int nrhs, const double *f, double *u, int self_mod
   k_slots_to_f32<<<(unsigned)((tot + 255) / 256), 256, 0, c->stream>>>(c->n, nrhs, f,
                                                                        c->w_f32.p);
   if (int rc = check_launch(c, "to f32")) return rc;
-  return matvec_f32_staged(c, nrhs, u, self_mode);
+  return matvec_f32_staged(c, nrhs, f, u, self_mode);
 }
 
-// FP32 pair sum from the already staged c->w_f32 ([r][n] float4)
-int matvec_f32_staged(ggem_ctx *c, int nrhs, double *u, int self_mode) {
+// FP32 pair sum from the already staged c->w_f32 ([r][n] float4); f is the
+// FP64 slot-order force of the self term
+int matvec_f32_staged(ggem_ctx *c, int nrhs, const double *f, double *u, int self_mode) {
   const double self_c = self_coefficient(c, self_mode);
   int r0 = 0;
   while (r0 < nrhs) {
     const int left = nrhs - r0;
     int rc;
-    if (left >= 8) rc = launch_nr<8>(c, u, self_c, r0), r0 += 8;
-    else if (left >= 4) rc = launch_nr<4>(c, u, self_c, r0), r0 += 4;
-    else if (left >= 2) rc = launch_nr<2>(c, u, self_c, r0), r0 += 2;
-    else rc = launch_nr<1>(c, u, self_c, r0), r0 += 1;
+    if (left >= 8) rc = launch_nr<8>(c, f, u, self_c, r0), r0 += 8;
+    else if (left >= 4) rc = launch_nr<4>(c, f, u, self_c, r0), r0 += 4;
+    else if (left >= 2) rc = launch_nr<2>(c, f, u, self_c, r0), r0 += 2;
+    else rc = launch_nr<1>(c, f, u, self_c, r0), r0 += 1;
     if (rc) return rc;
   }
   return GGEM_OK;

@@ -27,7 +27,8 @@ CHEB_GAUSS, CHEB_GAUSS_RADAU, CHEB_GAUSS_LOBATTO = 0, 1, 2
 ERR_BAD_ARG, ERR_CUDA, ERR_CELL_OVERFLOW, ERR_TIMEOUT = -1, -2, -3, -4
 ERR_NOT_SPD, ERR_CHEB_NOT_CONVERGED, ERR_SURROGATE_REJECTED = -5, -6, -7
 ERR_OUT_OF_DOMAIN, ERR_NO_DEVICE, ERR_OOM, ERR_INVALID_RANGE = -8, -9, -10, -11
-KERNEL_PAIR_FP32, KERNEL_PAIR_FP64, KERNEL_CHEB_TERM, KERNEL_LIST_BUILD = 0, 1, 2, 3
+KERNEL_PAIR_FP32, KERNEL_PAIR_FP64, KERNEL_CHEB_TERM, KERNEL_LIST_BUILD, KERNEL_PAIR_CHEB = (
+    0, 1, 2, 3, 4)
 
 
 class Params(C.Structure):

@@ -32,6 +32,7 @@ int ggem_probe_fp32_peak(ggem_ctx *ctx, double *tflops);
 #define GGEM_KERNEL_PAIR_FP64 1  /* FP64 cell-stencil sum                     */
 #define GGEM_KERNEL_CHEB_TERM 2  /* fused Chebyshev term                       */
 #define GGEM_KERNEL_LIST_BUILD 3 /* pair-list count + fill                     */
+#define GGEM_KERNEL_PAIR_CHEB 4  /* FP32 pair sum with the Chebyshev term fused */
 int ggem_set_kernel_timing(ggem_ctx *ctx, int enable);
 int ggem_get_kernel_timing(ggem_ctx *ctx, int kernel, double *total_ms, int64_t *launches);
 

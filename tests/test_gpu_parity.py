@@ -389,3 +389,33 @@ def test_chebyshev_sparse_checks_and_displacement(check_every):
         if rep2[0]["n_terms"] == rep[0]["n_terms"]:
             assert rel(dw, My) <= 1e-12
         assert rel(y, y_ref) <= 5e-3
+
+
+def test_fused_chebyshev_terms_match_unfused_path():
+    """Terms without an error check run as one fused pair-sum + recurrence
+    kernel on the FP32 single-RHS path; its y equals the unfused path's and
+    the FP64 oracle's within the FP32 pair-sum tolerance."""
+    xyz, L = suspension(2000, 0.1, 53)
+    box = O.make_box([0] * 3, [L] * 3, [1, 1, 1])
+    c = O.constants(alpha=0.5)
+    nb = O.neighbors_cutoff(box, xyz, 7.0)
+    op = O.Operator(matvec=(c, box, xyz, nb, O.SELF_BEAD, 8))
+    xi = np.random.default_rng(21).standard_normal(3 * len(xyz))
+    N = 12
+    with G.Context(box_hi=(L,) * 3, rc=7.0, precision=G.FP32) as ctx:
+        ctx.set_particles(xyz)
+        ctx.build_cells()
+        lo, hi = ctx.lanczos_bounds(k=30, seed=3)
+        lo, hi = lo / 1.05, hi * 1.05
+        y1, r1 = ctx.cheb_inv_sqrt(xi, N, lo, hi, 0.0, check_every=1)
+        ctx.set_kernel_timing(True)
+        y2, r2 = ctx.cheb_inv_sqrt(xi, N, lo, hi, 0.0, check_every=N - 1)
+        fused_ms, fused_n = ctx.kernel_timing(G.KERNEL_PAIR_CHEB)
+        ctx.set_kernel_timing(False)
+    assert r1[0]["n_terms"] == r2[0]["n_terms"] == N
+    assert fused_n == N - 2  # terms 1 .. N-2; the last term is checked
+    assert rel(y2, y1) <= 1e-12
+    y_o, rep_o = O.cheb_inv_sqrt(op, xi, N, lo, hi, 0.0)
+    assert rep_o.n_terms == N
+    assert rel(y2, y_o) <= 1e-5
+    assert r2[0]["err1"] == pytest.approx(rep_o.err1, rel=1e-3)
