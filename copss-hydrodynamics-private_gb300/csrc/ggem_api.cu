@@ -466,23 +466,18 @@ extern "C" int ggem_get_neighbors(ggem_ctx *ctx, int64_t *offsets, int32_t *ids,
     return cuda_fail(ctx, e, "neighbour readback");
   std::vector<std::vector<int32_t>> lists(n);
   if (ctx->prm.precision == GGEM_FP32) {
-    std::vector<int64_t> off(n + 1, 0);
-    int64_t total = 0;
+    const int64_t W = ctx->nb_w;
+    std::vector<int32_t> cnt(std::max<int64_t>(n, 1));
+    std::vector<uint32_t> lst(std::max<int64_t>(n * W, 1));
     if (n > 0) {
-      if ((e = cudaMemcpyAsync(off.data(), ctx->nb_off.p, 8 * (n + 1), cudaMemcpyDeviceToHost, st)) ||
-          (e = cudaStreamSynchronize(st)))
-        return cuda_fail(ctx, e, "list readback");
-      total = off[n];
-    }
-    std::vector<uint32_t> lst(std::max<int64_t>(total, 1));
-    if (total > 0) {
-      if ((e = cudaMemcpyAsync(lst.data(), ctx->nb_list.p, 4 * total, cudaMemcpyDeviceToHost, st)) ||
+      if ((e = cudaMemcpyAsync(cnt.data(), ctx->nb_cnt.p, 4 * n, cudaMemcpyDeviceToHost, st)) ||
+          (e = cudaMemcpyAsync(lst.data(), ctx->nb_list.p, 4 * n * W, cudaMemcpyDeviceToHost, st)) ||
           (e = cudaStreamSynchronize(st)))
         return cuda_fail(ctx, e, "list readback");
     }
     for (int64_t s = 0; s < n; ++s) {
       auto &L = lists[order[s]];
-      for (int64_t m = off[s]; m < off[s + 1]; ++m) L.push_back(order[lst[m] >> kCodeBits]);
+      for (int64_t m = s * W; m < s * W + cnt[s]; ++m) L.push_back(order[lst[m] >> kCodeBits]);
     }
   } else {
     const bool ref = ctx->prm.nb_mode == GGEM_NB_REFERENCE;

@@ -5,15 +5,16 @@
 // containing list (:573-648) becomes a counting sort of particles by cell,
 // and the per-particle neighbour lists (:652-848) with their stored
 // displacement vectors (:220-241) become either an on-the-fly cell stencil
-// sweep (FP64 path) or a compact CSR list of (source slot, stencil
-// code) entries (FP32 path), built once per configuration.
+// sweep (FP64 path) or fixed-width rows of (source slot, stencil code)
+// entries (FP32 path), built in one pass per configuration.
 //
 // Bound: HBM.  Algorithmic bytes per particle of the cell build: 24 (read
 // xyz) + 4 (cell id) + 4 (order) + 4 (rank) + 32 (pos64) + 16 (pos32) plus
-// the scatter re-reads; the list build streams 4 B per listed pair twice.
+// the scatter re-reads; the list build writes 4 B per listed pair once.
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <vector>
 
 #include "ggem_internal.cuh"
@@ -218,22 +219,24 @@ __device__ __forceinline__ bool exact_within(const Grid &g, double4_32a a, doubl
   return r2 < rc2;
 }
 
-// Warp-per-cell pair list (count and fill passes).  The candidates of a
-// target cell are the concatenation of its stencil cells (stencil order,
-// slot order inside a cell); lanes take 32 consecutive candidates with
-// coalesced loads, the cell's targets are broadcast one at a time by
+// Warp-per-cell pair list, one pass into fixed-width rows.  The candidates
+// of a target cell are the concatenation of its stencil cells (stencil
+// order, slot order inside a cell); lanes take 32 consecutive candidates
+// with coalesced loads, the cell's targets are broadcast one at a time by
 // shuffle, and a ballot prefix places each accepted candidate.  Entries
 // therefore come out in exactly the per-target order of a sequential sweep.
+// Row s holds entries [s*W, s*W + cnt[s]); a row longer than W is counted
+// but not stored: the kernel records the longest row and sets
+// kErrListCapacity, and the host rebuilds with a wider W.
 constexpr int kListWarps = 8;     // warps per CTA
 constexpr int kMaxStencil = 128;  // stencil cells per target cell
 
-template <bool FILL>
 __global__ void __launch_bounds__(32 * kListWarps) k_pair_list_warp(
     Grid g, const int4 *__restrict__ stencil, int nst, const float4 *__restrict__ shift,
     const int32_t *__restrict__ start, const float4 *__restrict__ pos32,
-    const double4_32a *__restrict__ pos64, float rc2_lo, float rc2_hi, double rc2,
-    int32_t *__restrict__ count, const int64_t *__restrict__ off, uint32_t *__restrict__ list,
-    int64_t list_cap, int *__restrict__ err) {
+    const double4_32a *__restrict__ pos64, float rc2_lo, float rc2_hi, double rc2, int W,
+    int32_t *__restrict__ count, uint32_t *__restrict__ list,
+    unsigned long long *__restrict__ stat, int *__restrict__ err) {
   __shared__ int32_t s_base[kListWarps][kMaxStencil];
   __shared__ int32_t s_pre[kListWarps][kMaxStencil + 1];
   __shared__ int32_t s_code[kListWarps][kMaxStencil];
@@ -275,16 +278,13 @@ __global__ void __launch_bounds__(32 * kListWarps) k_pair_list_warp(
   __syncwarp();
   const int32_t V = carry;
   const unsigned lt_mask = (1u << lane) - 1u;
+  unsigned long long cell_total = 0;
+  int32_t cell_max = 0;
   for (int32_t t0 = tb; t0 < te; t0 += 32) {
     const int ntc = min(32, te - t0);
     const int32_t own = t0 + lane;
     const bool own_ok = lane < ntc;
     const float4 po = own_ok ? pos32[own] : make_float4(0.f, 0.f, 0.f, 0.f);
-    int64_t own_base = 0, own_cap = 0;
-    if (FILL && own_ok) {
-      own_base = off[own];
-      own_cap = off[own + 1] - own_base;
-    }
     int32_t own_cnt = 0;
     for (int32_t v0 = 0; v0 < V; v0 += 32) {
       const int32_t v = v0 + lane;
@@ -316,29 +316,31 @@ __global__ void __launch_bounds__(32 * kListWarps) k_pair_list_warp(
           else in = exact_within(g, pos64[ti], pos64[t], rc2);
         }
         const unsigned bal = __ballot_sync(0xffffffffu, in);
-        if (FILL) {
-          const int64_t at = __shfl_sync(0xffffffffu, own_base + own_cnt, i);
-          const int64_t cap_end = __shfl_sync(0xffffffffu, own_base + own_cap, i);
-          if (in) {
-            const int64_t pos = at + __popc(bal & lt_mask);
-            if (pos >= cap_end) atomicOr(err, kErrListOverflow);
-            else if (pos >= list_cap) atomicOr(err, kErrListCapacity);
-            else list[pos] = ((uint32_t)t << kCodeBits) | (uint32_t)code;
-          }
+        const int32_t at = __shfl_sync(0xffffffffu, own_cnt, i);
+        if (in) {
+          const int32_t k = at + __popc(bal & lt_mask);
+          if (k < W) list[(int64_t)ti * W + k] = ((uint32_t)t << kCodeBits) | (uint32_t)code;
         }
         if (lane == i) own_cnt += __popc(bal);
       }
     }
     if (own_ok) {
-      if (!FILL) count[own] = own_cnt;
-      else if (own_cnt != own_cap) atomicOr(err, kErrListOverflow);
+      count[own] = own_cnt;
+      cell_total += (unsigned long long)own_cnt;
+      cell_max = max(cell_max, own_cnt);
     }
   }
-}
-
-__global__ void k_widen(int64_t n, const int32_t *__restrict__ in, int64_t *__restrict__ out) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i < n) out[i] = in[i];
+  // one atomic per warp (per cell) for the list statistics
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    cell_total += __shfl_xor_sync(0xffffffffu, cell_total, o);
+    cell_max = max(cell_max, __shfl_xor_sync(0xffffffffu, cell_max, o));
+  }
+  if (lane == 0) {
+    atomicAdd(&stat[0], cell_total);
+    atomicMax(&stat[1], (unsigned long long)cell_max);
+    if (cell_max > W) atomicOr(err, kErrListCapacity);
+  }
 }
 
 }  // namespace
@@ -406,71 +408,60 @@ int cell_flag_error(ggem_ctx *c, int flags) {
 int build_pair_list(ggem_ctx *c) {
   const int64_t n = c->n;
   cudaError_t e = cudaSuccess;
-  if ((e = c->nb_count.ensure(n)) || (e = c->nb_cnt64.ensure(n)) || (e = c->nb_off.ensure(n + 1)))
+  if ((e = c->nb_cnt.ensure(n)) || (e = c->nb_stat.ensure(2)))
     return cuda_fail(c, e, "pair list buffers");
   cudaStream_t st = c->stream;
+  if (c->nb_w <= 0) {
+    // first build: twice the mean row length of a uniform suspension plus slack
+    const Grid &g = c->grid;
+    const double vol = g.L[0] * g.L[1] * g.L[2];
+    const double mean = vol > 0 ? (double)n / vol * 4.18879020478639 * c->rc2 * std::sqrt(c->rc2)
+                                : 0.0;
+    c->nb_w = (int)std::min<double>(((int64_t)(2.0 * mean) + 16 + 7) / 8 * 8, 1 << 20);
+  }
   if (n == 0) {
-    if ((e = cudaMemsetAsync(c->nb_off.p, 0, sizeof(int64_t), st))) return cuda_fail(c, e, "memset");
     c->n_pairs = 0;
     c->cells_built = true;
     c->list_built = true;
     return GGEM_OK;
   }
-  const int T = 256;
-  const unsigned bn = (unsigned)((n + T - 1) / T);
   const int nst = (int)c->stencil.size();
   if (nst > kMaxStencil) return fail(c, GGEM_ERR_BAD_ARG, "stencil too large for the list builder");
-  // The error word still holds the cell build's flags; they are read back
-  // together with the list length after a speculative fill into the list
-  // as allocated (its size from earlier builds), so a rebuild of a similar
-  // configuration costs one host synchronisation.  A fill that ran past the
-  // allocation is repeated once the list has grown.
-  kt_start(c, kKListBuild);
+  // The error word still holds the cell build's flags; they come back with
+  // the list statistics in one host synchronisation.  A row longer than the
+  // current width makes the host widen the rows and fill once more.
   const unsigned cb = (unsigned)((c->grid.ncell + kListWarps - 1) / kListWarps);
-  k_pair_list_warp<false><<<cb, 32 * kListWarps, 0, st>>>(
-      c->grid, c->d_stencil.p, nst, c->d_shift.p, c->cell_start.p, c->pos32.p, c->pos64.p,
-      c->rc2_lo, c->rc2_hi, c->rc2, c->nb_count.p, nullptr, nullptr, 0, c->err.p);
-  if (int rc = check_launch(c, "pair count")) return rc;
-  k_widen<<<bn, T, 0, st>>>(n, c->nb_count.p, c->nb_cnt64.p);
-  if (int rc = check_launch(c, "pair widen")) return rc;
-  if (int rc = device_exclusive_scan_i64(c, c->nb_cnt64.p, c->nb_off.p, n)) return rc;
-  const bool speculate = c->nb_list.p != nullptr;
-  if (speculate) {
-    k_pair_list_warp<true><<<cb, 32 * kListWarps, 0, st>>>(
+  unsigned long long *h = reinterpret_cast<unsigned long long *>(c->h_red);
+  for (int attempt = 0; attempt < 2; ++attempt) {
+    const int W = c->nb_w;
+    if ((e = c->nb_list.ensure((size_t)n * W))) return cuda_fail(c, e, "pair list");
+    if ((e = cudaMemsetAsync(c->nb_stat.p, 0, 2 * sizeof(unsigned long long), st)))
+      return cuda_fail(c, e, "memset");
+    if (attempt == 0) kt_start(c, kKListBuild);
+    k_pair_list_warp<<<cb, 32 * kListWarps, 0, st>>>(
         c->grid, c->d_stencil.p, nst, c->d_shift.p, c->cell_start.p, c->pos32.p, c->pos64.p,
-        c->rc2_lo, c->rc2_hi, c->rc2, nullptr, c->nb_off.p, c->nb_list.p,
-        (int64_t)c->nb_list.count, c->err.p);
-    if (int rc = check_launch(c, "pair fill")) return rc;
-  }
-  kt_stop(c, kKListBuild);  // a regrown refill below is left out of the timing
-  // one readback: list length and error word
-  int64_t *h = reinterpret_cast<int64_t *>(c->h_red);
-  h[1] = 0;
-  if ((e = cudaMemcpyAsync(&h[0], c->nb_off.p + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st)) ||
-      (e = cudaMemcpyAsync(&h[1], c->err.p, sizeof(int), cudaMemcpyDeviceToHost, st)) ||
-      (e = cudaStreamSynchronize(st)))
-    return cuda_fail(c, e, "list size");
-  const int64_t total = h[0];
-  int flags = (int)h[1];
-  if (int rc = cell_flag_error(c, flags)) return rc;
-  c->cells_built = true;
-  if (!speculate || (flags & kErrListCapacity) || total > (int64_t)c->nb_list.count) {
-    // grow with headroom so that a slowly varying configuration refills in place
-    const size_t want = (size_t)std::max<int64_t>(total + total / 16, 1);
-    if ((e = c->nb_list.ensure(want))) return cuda_fail(c, e, "pair list");
+        c->rc2_lo, c->rc2_hi, c->rc2, W, c->nb_cnt.p, c->nb_list.p, c->nb_stat.p, c->err.p);
+    if (attempt == 0) kt_stop(c, kKListBuild);  // a widened refill is left out
+    if (int rc = check_launch(c, "pair list")) return rc;
+    h[2] = 0;
+    if ((e = cudaMemcpyAsync(h, c->nb_stat.p, 2 * sizeof(unsigned long long),
+                             cudaMemcpyDeviceToHost, st)) ||
+        (e = cudaMemcpyAsync(&h[2], c->err.p, sizeof(int), cudaMemcpyDeviceToHost, st)) ||
+        (e = cudaStreamSynchronize(st)))
+      return cuda_fail(c, e, "list statistics");
+    const int flags = (int)h[2];
+    if (int rc = cell_flag_error(c, flags)) return rc;
+    c->cells_built = true;
+    if (!(flags & kErrListCapacity)) {
+      c->n_pairs = (int64_t)h[0];
+      c->list_built = true;
+      return GGEM_OK;
+    }
+    const unsigned long long longest = h[1];
+    c->nb_w = (int)std::min<unsigned long long>((longest + longest / 8 + 8 + 7) / 8 * 8, 1u << 24);
     if ((e = cudaMemsetAsync(c->err.p, 0, sizeof(int), st))) return cuda_fail(c, e, "memset");
-    k_pair_list_warp<true><<<cb, 32 * kListWarps, 0, st>>>(
-        c->grid, c->d_stencil.p, nst, c->d_shift.p, c->cell_start.p, c->pos32.p, c->pos64.p,
-        c->rc2_lo, c->rc2_hi, c->rc2, nullptr, c->nb_off.p, c->nb_list.p,
-        (int64_t)c->nb_list.count, c->err.p);
-    if (int rc = check_launch(c, "pair fill")) return rc;
-    if (int rc = read_error_flags(c, &flags)) return rc;
   }
-  if (flags & (kErrListOverflow | kErrListCapacity))
-    return fail(c, GGEM_ERR_CELL_OVERFLOW, "pair list fill exceeded its counted length");
-  c->n_pairs = total;
-  c->list_built = true;
-  return GGEM_OK;
+  return fail(c, GGEM_ERR_CELL_OVERFLOW, "pair list rows exceeded their width twice");
 }
 
 }  // namespace ggem

@@ -9,10 +9,11 @@
 //   pos64      double4_32a[n]   wrapped positions in slot order (FP64 paths)
 //   pos32      float4[n]    position relative to its cell centre (x,y,z) and
 //                           the cell id bits (w), slot order (FP32 path)
-//   pair list  uint32       CSR in slot order, entry =
-//                           (source slot << 7) | stencil code, built once
-//                           per configuration with an FP32 filter and an
-//                           exact FP64 decision in the rounding band
+//   pair list  uint32[n][W] fixed-width rows in slot order (row s holds
+//                           nb_cnt[s] entries), entry =
+//                           (source slot << 7) | stencil code, built in one
+//                           pass per configuration with an FP32 filter and
+//                           an exact FP64 decision in the rounding band
 //   tab        float4[2*kTableN] cubic pieces of A(s), B(s), s = r^2, with
 //                           G(x) = A I + B x x^T (FP32 path)
 #pragma once
@@ -115,8 +116,9 @@ struct ggem_ctx {
   // FP32 pair list
   bool list_built = false;
   int64_t n_pairs = 0;
-  ggem::DevBuf<int32_t> nb_count;     // entries per target
-  ggem::DevBuf<int64_t> nb_cnt64, nb_off;  // widened counts, CSR offsets (n+1)
+  ggem::DevBuf<int32_t> nb_cnt;       // entries per target row
+  ggem::DevBuf<unsigned long long> nb_stat;  // [0] total entries, [1] longest row
+  int nb_w = 0;                       // row width (multiple of 8)
   ggem::DevBuf<uint32_t> nb_list;
   ggem::DevBuf<float4> tab;
   float tab_inv_ds = 0.f;

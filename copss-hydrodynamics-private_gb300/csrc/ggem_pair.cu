@@ -14,7 +14,8 @@
 //    coordinates plus the stencil shift (exact cell offsets);
 //    G = A(s) I + B(s) x x^T with A, B = e^{-alpha^2 s} times a polynomial
 //    in s (or a cubic table when that fit is not accurate enough); each lane
-//    keeps Kahan-compensated FP32 sums and the group reduces in FP64.
+//    keeps Kahan-compensated FP32 sums; the group reduces them as float-float
+//    values in FP32 and forms one FP64 add per output component.
 // Algorithmic work per in-cutoff ordered pair: 28 + 19*nrhs flops (FMA = 2,
 // rsqrt/exp/erf = 1 each), bound by the FP32 pipe.
 #include <cuda_runtime.h>
@@ -157,8 +158,10 @@ struct __align__(32) Rec32 {
 };
 
 // the analytic tensor, passed by value (constant bank)
+// (a_q, b_q) interleaved so that both polynomials advance in one packed
+// FP32x2 FMA per degree (Blackwell FFMA2)
 struct PolyAB {
-  float a[kPolyDeg + 1], b[kPolyDeg + 1];
+  float2 ab[kPolyDeg + 1];
   float x0, x1, e_hi, e_lo;  // x = s x1 + x0; e^{-alpha^2 s} = 2^{s (e_hi + e_lo)}
 };
 
@@ -168,20 +171,19 @@ __device__ __forceinline__ void tensor_ab32(float s2, const PolyAB &P,
                                             float &A, float &B) {
   if (POLY) {
     const float x = fmaf(s2, P.x1, P.x0);
-    float a = P.a[kPolyDeg], b = P.b[kPolyDeg];
+    const float2 xx = make_float2(x, x);
+    float2 ab = P.ab[kPolyDeg];
 #pragma unroll
-    for (int q = kPolyDeg - 1; q >= 0; --q) {
-      a = fmaf(a, x, P.a[q]);
-      b = fmaf(b, x, P.b[q]);
-    }
+    for (int q = kPolyDeg - 1; q >= 0; --q) ab = __ffma2_rn(ab, xx, P.ab[q]);
     // e^{-alpha^2 s} = 2^{p + r}: p = s e_hi rounded, r its exact residual plus
     // s e_lo, so the exponent keeps ~1e-7 relative accuracy at s ~ rc^2
     const float p = s2 * P.e_hi;
     const float r = fmaf(s2, P.e_lo, fmaf(s2, P.e_hi, -p));
     const float E0 = exp2f(p);
     const float E = fmaf(E0, r * 0.6931471805599453f, E0);
-    A = a * E;
-    B = b * E;
+    ab = __fmul2_rn(ab, make_float2(E, E));
+    A = ab.x;
+    B = ab.y;
   } else {
     const float uu = s2 * inv_ds;
     const float fi = fminf(floorf(uu), (float)(kTableN - 1));  // last piece extrapolates
@@ -274,13 +276,14 @@ struct PairSum {
 template <int CD, bool POLY>
 __device__ __forceinline__ PairSum pair_sum_r1(int64_t s, bool act, int sub, const Rec32 &ri,
                                                const Rec32 *__restrict__ src,
-                                               const int64_t *__restrict__ off,
+                                               const int32_t *__restrict__ cnt, int W,
                                                const uint32_t *__restrict__ list,
                                                const PolyAB &P, const Rec32 *__restrict__ tab,
                                                float inv_ds, float hx, float hy, float hz) {
-  const int64_t b = off[s], e = act ? off[s + 1] : b;
+  const int64_t b = s * (int64_t)W, e = act ? b + cnt[s] : b;
   float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
-  float bx = 0.f, by = 0.f, bz = 0.f;
+  float2 bxy = make_float2(0.f, 0.f);
+  float bz = 0.f;
   int blk = 0;
   for (int64_t m = b + sub; m < e; m += kGroup) {
     const uint32_t en = __ldg(list + m);
@@ -293,20 +296,24 @@ __device__ __forceinline__ PairSum pair_sum_r1(int64_t s, bool act, int sub, con
     const float s2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
     float A, B;
     tensor_ab32<POLY>(s2, P, tab, inv_ds, A, B);
-    const float bxf = B * fmaf(dz, rj.b.z, fmaf(dy, rj.b.y, dx * rj.b.x));
-    bx += fmaf(A, rj.b.x, bxf * dx);
-    by += fmaf(A, rj.b.y, bxf * dy);
+    // G f = A f + B (x.f) x, the x and y components packed (FFMA2)
+    const float2 dxy = make_float2(dx, dy), fxy = make_float2(rj.b.x, rj.b.y);
+    const float2 pxy = __fmul2_rn(dxy, fxy);
+    const float bxf = B * fmaf(dz, rj.b.z, pxy.x + pxy.y);
+    bxy = __fadd2_rn(bxy, __ffma2_rn(make_float2(A, A), fxy,
+                                     __fmul2_rn(make_float2(bxf, bxf), dxy)));
     bz += fmaf(A, rj.b.z, bxf * dz);
     if (++blk == 8) {
-      kahan_add(sx, cx, bx);
-      kahan_add(sy, cy, by);
+      kahan_add(sx, cx, bxy.x);
+      kahan_add(sy, cy, bxy.y);
       kahan_add(sz, cz, bz);
-      bx = by = bz = 0.f;
+      bxy = make_float2(0.f, 0.f);
+      bz = 0.f;
       blk = 0;
     }
   }
-  kahan_add(sx, cx, bx);
-  kahan_add(sy, cy, by);
+  kahan_add(sx, cx, bxy.x);
+  kahan_add(sy, cy, bxy.y);
   kahan_add(sz, cz, bz);
   // Kahan keeps sum = s - c: the float-float value is (s, -c)
   PairSum r{sx, -cx, sy, -cy, sz, -cz};
@@ -319,7 +326,7 @@ __device__ __forceinline__ PairSum pair_sum_r1(int64_t s, bool act, int sub, con
 // u = M f, single right-hand side
 template <int CD, bool POLY>
 __global__ void __launch_bounds__(256) k_pair_r1(
-    int64_t n, const Rec32 *__restrict__ src, const int64_t *__restrict__ off,
+    int64_t n, const Rec32 *__restrict__ src, const int32_t *__restrict__ cnt, int W,
     const uint32_t *__restrict__ list, PolyAB P, const Rec32 *__restrict__ tab, float inv_ds,
     float hx, float hy, float hz, double self_c, const double *__restrict__ f,
     double *__restrict__ u) {
@@ -329,7 +336,7 @@ __global__ void __launch_bounds__(256) k_pair_r1(
   const int64_t s = act ? gid : n - 1;
   const Rec32 ri = src[s];
   const PairSum r =
-      pair_sum_r1<CD, POLY>(s, act, sub, ri, src, off, list, P, tab, inv_ds, hx, hy, hz);
+      pair_sum_r1<CD, POLY>(s, act, sub, ri, src, cnt, W, list, P, tab, inv_ds, hx, hy, hz);
   group_store(act, sub, s, r.hx, r.lx, r.hy, r.ly, r.hz, r.lz, self_c, f, u);
 }
 
@@ -340,7 +347,7 @@ __global__ void __launch_bounds__(256) k_pair_r1(
 // src holds the records of x1; next must be a different buffer.
 template <int CD, bool POLY>
 __global__ void __launch_bounds__(256) k_pair_cheb(
-    int64_t n, const Rec32 *__restrict__ src, const int64_t *__restrict__ off,
+    int64_t n, const Rec32 *__restrict__ src, const int32_t *__restrict__ cnt, int W,
     const uint32_t *__restrict__ list, PolyAB P, const Rec32 *__restrict__ tab, float inv_ds,
     float hx, float hy, float hz, double self_c, double two_da, double two_db, double coef,
     const double *__restrict__ x0, const double *__restrict__ x1, double *__restrict__ xm,
@@ -351,7 +358,7 @@ __global__ void __launch_bounds__(256) k_pair_cheb(
   const int64_t s = act ? gid : n - 1;
   const Rec32 ri = src[s];
   const PairSum r =
-      pair_sum_r1<CD, POLY>(s, act, sub, ri, src, off, list, P, tab, inv_ds, hx, hy, hz);
+      pair_sum_r1<CD, POLY>(s, act, sub, ri, src, cnt, W, list, P, tab, inv_ds, hx, hy, hz);
   if (!act) return;
   float *nf = reinterpret_cast<float *>(next + s);
   if (sub < 3) {
@@ -375,14 +382,14 @@ __global__ void __launch_bounds__(256) k_pair_cheb(
 template <int CD, bool POLY, int NR>
 __global__ void __launch_bounds__(256) k_pair_nr(
     int64_t n, const float4 *__restrict__ pos32, const float4 *__restrict__ f32,
-    const int64_t *__restrict__ off, const uint32_t *__restrict__ list, PolyAB P,
+    const int32_t *__restrict__ cnt, int W, const uint32_t *__restrict__ list, PolyAB P,
     const Rec32 *__restrict__ tab, float inv_ds, float hx, float hy, float hz, double self_c,
     const double *__restrict__ f, double *__restrict__ u, int r0) {
   const int64_t gid = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / kGroup;
   const int sub = (int)(threadIdx.x % kGroup);
   const bool act = gid < n;
   const int64_t s = act ? gid : n - 1;
-  const int64_t b = off[s], e = act ? off[s + 1] : b;
+  const int64_t b = s * (int64_t)W, e = act ? b + cnt[s] : b;
   const float4 pi = pos32[s];
   float sx[NR], sy[NR], sz[NR], cx[NR], cy[NR], cz[NR];
 #pragma unroll
@@ -473,10 +480,7 @@ int launch_f64(ggem_ctx *c, const double *f, double *u, int self_mode, int r0) {
 
 PolyAB poly_of(const ggem_ctx *c) {
   PolyAB P;
-  for (int q = 0; q <= kPolyDeg; ++q) {
-    P.a[q] = c->poly_a[q];
-    P.b[q] = c->poly_b[q];
-  }
+  for (int q = 0; q <= kPolyDeg; ++q) P.ab[q] = make_float2(c->poly_a[q], c->poly_b[q]);
   P.x0 = c->poly_x0;
   P.x1 = c->poly_x1;
   P.e_hi = c->poly_e[0];
@@ -489,7 +493,7 @@ void launch_r1(ggem_ctx *c, const Rec32 *src, const double *f, double *u, double
   const int64_t threads = c->n * kGroup;
   const Grid &g = c->grid;
   k_pair_r1<CD, POLY><<<(unsigned)((threads + 255) / 256), 256, 0, c->stream>>>(
-      c->n, src, c->nb_off.p, c->nb_list.p, poly_of(c),
+      c->n, src, c->nb_cnt.p, c->nb_w, c->nb_list.p, poly_of(c),
       reinterpret_cast<const Rec32 *>(c->tab.p), c->tab_inv_ds, g.h32[0], g.h32[1], g.h32[2],
       self_c, f, u);
 }
@@ -517,7 +521,7 @@ void launch_cheb(ggem_ctx *c, const Rec32 *src, Rec32 *next, double self_c, doub
   const int64_t threads = c->n * kGroup;
   const Grid &g = c->grid;
   k_pair_cheb<CD, POLY><<<(unsigned)((threads + 255) / 256), 256, 0, c->stream>>>(
-      c->n, src, c->nb_off.p, c->nb_list.p, poly_of(c),
+      c->n, src, c->nb_cnt.p, c->nb_w, c->nb_list.p, poly_of(c),
       reinterpret_cast<const Rec32 *>(c->tab.p), c->tab_inv_ds, g.h32[0], g.h32[1], g.h32[2],
       self_c, two_da, two_db, coef, x0, x1, xm, dw, next);
 }
@@ -527,7 +531,7 @@ void launch_nr_t(ggem_ctx *c, const double *f, double *u, double self_c, int r0)
   const int64_t threads = c->n * kGroup;
   const Grid &g = c->grid;
   k_pair_nr<CD, POLY, NR><<<(unsigned)((threads + 255) / 256), 256, 0, c->stream>>>(
-      c->n, c->pos32.p, c->w_f32.p, c->nb_off.p, c->nb_list.p, poly_of(c),
+      c->n, c->pos32.p, c->w_f32.p, c->nb_cnt.p, c->nb_w, c->nb_list.p, poly_of(c),
       reinterpret_cast<const Rec32 *>(c->tab.p), c->tab_inv_ds, g.h32[0], g.h32[1], g.h32[2],
       self_c, f, u, r0);
 }

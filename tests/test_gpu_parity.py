@@ -418,4 +418,7 @@ def test_fused_chebyshev_terms_match_unfused_path():
     y_o, rep_o = O.cheb_inv_sqrt(op, xi, N, lo, hi, 0.0)
     assert rep_o.n_terms == N
     assert rel(y2, y_o) <= 1e-5
-    assert r2[0]["err1"] == pytest.approx(rep_o.err1, rel=1e-3)
+    # err1 = sqrt(|y.M.M.y - xi.M.xi| / xi.M.xi) cancels to ~1e-9 relative
+    # here, below the FP32 pair-sum error, so only the FP32 runs agree closely
+    assert r2[0]["err1"] == pytest.approx(r1[0]["err1"], rel=1e-6)
+    assert 0.5 * rep_o.err1 <= r2[0]["err1"] <= 2.0 * rep_o.err1
