@@ -366,6 +366,9 @@ def run_gb300(args, rank, world):
                         "every term, one RHS, no graphs"}
     ctx64.close()
 
+    # ---- polymer suspension, 64 batched noise right-hand sides ----------
+    poly = None if args.skip_polymer else polymer_leg(G, torch, dev, flush, peak_fn=None)
+
     # ---- roofline of the dominant kernel --------------------------------
     # the dominant kernel of the timed steps: the fused pair-sum + Chebyshev
     # term (k_pair_cheb) or the plain pair sum (k_pair_r1), whichever took
@@ -411,10 +414,91 @@ def run_gb300(args, rank, world):
         "kernel_ms_in_timed_region": {k: v[0] for k, v in kt.items()},
         "gpu_launches": int(lc1 - lc0),
         "clocks": clk.summary(), "wall_s_timed": t_wall,
+        "polymer_64rhs": poly,
     }
     if rank == 0 and not args.no_cpu_baseline and world == 1:
         result["cpu_baseline"] = cpu_baseline(xyz, L, state["bounds"], args)
     return result
+
+
+# --------------------------------------------------------------------------
+# polymer suspension with 64 batched right-hand sides
+# --------------------------------------------------------------------------
+POLY_CHAINS, POLY_BEADS, POLY_PHI, POLY_NRHS = 5000, 20, 0.05, 64
+
+
+def polymer_leg(G, torch, dev, flush, peak_fn=None, reps=5):
+    """5000 chains x 20 beads (N = 100k, bond 2a, self-avoiding growth) at
+    phi = 0.05: the batched 64-RHS mobility matvec and one Brownian step of
+    64 noise vectors (adaptive Chebyshev, tol 1e-3, <= 50 terms), device
+    resident, L2 flushed before each timed call."""
+    xyz, L = G.make_chains(SEED + 7, POLY_CHAINS, POLY_BEADS, 2.0, POLY_PHI)
+    n = len(xyz)
+    ctx = G.Context(alpha=ALPHA, box_hi=(L,) * 3, rc=RC, precision=G.FP32, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    d_xyz = torch.from_numpy(xyz.reshape(-1)).cuda()
+    torch.cuda.synchronize()
+    ctx.set_stream(stream.cuda_stream)
+    ctx.set_particles_dev(d_xyz.data_ptr(), n)
+    ctx.build_cells()
+    pairs = ctx.pair_count()
+    R = POLY_NRHS
+    f = torch.randn(R * 3 * n, dtype=torch.float64, device="cuda")
+    u = torch.empty_like(f)
+    torch.cuda.synchronize()
+    for _ in range(3):
+        ctx.local_matvec_dev(f.data_ptr(), u.data_ptr(), R, G.SELF_BEAD)
+    ctx.synchronize()
+    ctx.set_kernel_timing(True)
+    mv = []
+    for _ in range(reps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        ctx.local_matvec_dev(f.data_ptr(), u.data_ptr(), R, G.SELF_BEAD)
+        b.record(stream)
+        b.synchronize()
+        mv.append(a.elapsed_time(b))
+    k_ms, k_n = ctx.kernel_timing(G.KERNEL_PAIR_FP32)
+    ctx.set_kernel_timing(False)
+    lo, hi = ctx.lanczos_bounds(k=24, seed=7)
+    lo, hi = lo / 1.05, hi * 1.05
+    xi = torch.randn(R * 3 * n, dtype=torch.float64, device="cuda")
+    dw = torch.empty_like(xi)
+    torch.cuda.synchronize()
+    terms = []
+    for _ in range(2):  # the adaptive schedule learns the degree
+        rc, rp = ctx.brownian_displacement_dev(xi.data_ptr(), dw.data_ptr(), R, CHEB_MAX, lo, hi,
+                                               CHEB_TOL, check_every=0)
+    st = []
+    for _ in range(reps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        rc, rp = ctx.brownian_displacement_dev(xi.data_ptr(), dw.data_ptr(), R, CHEB_MAX, lo, hi,
+                                               CHEB_TOL, check_every=0)
+        ctx.synchronize()
+        st.append((time.perf_counter() - t0) * 1e3)
+        terms.append(max(r["n_terms"] for r in rp))
+    ok = rc == 0 and all(r["converged"] for r in rp)
+    peak = ctx.probe_fp32_peak()
+    ctx.close()
+    avg = k_ms / max(k_n, 1)
+    flops = pairs * (28 + 19 * R)
+    tf = flops / (avg * 1e-3) / 1e12
+    return {"workload": f"{POLY_CHAINS} chains x {POLY_BEADS} beads (N={n}), bond 2a, "
+                        f"phi={POLY_PHI}, L={L:.1f}, {R} noise right-hand sides",
+            "pairs": pairs, "matvec_ms": float(np.mean(mv)),
+            "matvecs_per_s": R * 1e3 / float(np.mean(mv)),
+            "brownian_step_ms_64rhs": float(np.mean(st)),
+            "brownian_steps_per_s_x_rhs": R * 1e3 / float(np.mean(st)),
+            "cheb_terms": terms, "converged": ok,
+            "kernel": "k_pair_b64 (lanes over 64 right-hand sides)",
+            "kernel_avg_launch_ms": avg, "kernel_tflops": tf, "fp32_peak_tflops": peak,
+            "kernel_frac_of_fp32_peak": tf / peak if peak else None,
+            "flops_per_launch": flops}
 
 
 # --------------------------------------------------------------------------
@@ -488,6 +572,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--reference-max-steps", type=int, default=6)
+    ap.add_argument("--skip-polymer", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
 

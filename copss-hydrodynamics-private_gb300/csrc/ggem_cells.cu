@@ -309,11 +309,13 @@ __global__ void __launch_bounds__(32 * kListWarps) k_pair_list_warp(
         const float dy = (pj.y - piy) + sh.y;
         const float dz = (pj.z - piz) + sh.z;
         const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-        bool in = valid && t != ti;
-        if (in) {
-          if (r2 < rc2_lo) in = true;
-          else if (r2 > rc2_hi) in = false;
-          else in = exact_within(g, pos64[ti], pos64[t], rc2);
+        // accepted below rc2_lo, rejected above rc2_hi; in between (FP32
+        // rounding of |r| = rc) the exact FP64 test decides, behind a
+        // warp-uniform branch so that the common case carries none of it
+        bool in = valid && t != ti && !(r2 > rc2_hi);
+        const bool band = in && !(r2 < rc2_lo);
+        if (__any_sync(0xffffffffu, band)) {
+          if (band) in = exact_within(g, pos64[ti], pos64[t], rc2);
         }
         const unsigned bal = __ballot_sync(0xffffffffu, in);
         const int32_t at = __shfl_sync(0xffffffffu, own_cnt, i);

@@ -143,6 +143,7 @@ struct ggem_ctx {
   // vector workspaces (FP64 slot order) and FP32 staging
   ggem::DevBuf<double> w_in, w_out, w_a, w_b, w_c, w_d, w_e, w_y;
   ggem::DevBuf<float4> w_f32;
+  ggem::DevBuf<float> w_fb;     // batched forces [slot][3][64] FP32
   ggem::DevBuf<double> w_red;   // reduction partials
   ggem::DevBuf<double> lz_Q;    // Lanczos basis
   double *h_red = nullptr;      // pinned host mirror of reductions

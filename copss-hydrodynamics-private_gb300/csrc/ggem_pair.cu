@@ -429,6 +429,123 @@ __global__ void __launch_bounds__(256) k_pair_nr(
   }
 }
 
+// ---- batched right-hand sides: 64 per pass, lanes over right-hand sides ----
+//
+// Forces of a pass are staged as FP32 [slot][3][64] (768 B per source, the
+// pair (2l, 2l+1) of right-hand sides at float2 index l), so the 32 lanes of
+// a warp read one source's forces with three coalesced 256-byte loads.  A
+// warp owns one target slot: its lanes first evaluate the tensors of 32
+// entries of the target's row at once (one entry per lane) into shared
+// memory, then walk those entries with every lane updating its two
+// right-hand sides in packed FP32x2 arithmetic.  Block-Kahan sums per lane;
+// the CTA transposes the float-float results through shared memory so that
+// the FP64 velocities [r][slot][3] (self term added in FP64) are written
+// coalesced.
+constexpr int kBatchR = 64;      // right-hand sides per pass
+constexpr int kBatchMinRhs = 16; // fewer go through k_pair_nr in chunks of 8
+constexpr int kBatchWarps = 8;   // target slots per CTA
+
+__global__ void __launch_bounds__(256) k_stage_b64(int64_t n, int nr, const double *__restrict__ f,
+                                                   float *__restrict__ fb) {
+  // block: 32 slots x 64 right-hand sides; smem [r][96 + 1]
+  __shared__ float t[kBatchR][97];
+  const int64_t s0 = blockIdx.x * 32LL;
+  const int ns = (int)(n - s0 < 32 ? n - s0 : 32);
+  for (int k = threadIdx.x; k < kBatchR * 96; k += blockDim.x) {
+    const int r = k / 96, q = k - r * 96;
+    t[r][q] = (r < nr && q < 3 * ns) ? (float)f[((int64_t)r * n + s0) * 3 + q] : 0.f;
+  }
+  __syncthreads();
+  float *out = fb + s0 * 3 * kBatchR;
+  for (int k = threadIdx.x; k < ns * 3 * kBatchR; k += blockDim.x) {
+    const int sc = k / kBatchR, r = k - sc * kBatchR;
+    out[k] = t[r][sc];
+  }
+}
+
+template <int CD, bool POLY>
+__global__ void __launch_bounds__(32 * kBatchWarps) k_pair_b64(
+    int64_t n, int nr, const float4 *__restrict__ pos32, const float2 *__restrict__ fb,
+    const int32_t *__restrict__ cnt, int W, const uint32_t *__restrict__ list, PolyAB P,
+    const Rec32 *__restrict__ tab, float inv_ds, float hx, float hy, float hz, double self_c,
+    const double *__restrict__ f, double *__restrict__ u) {
+  __shared__ float4 s_geo[kBatchWarps][32];   // dx, dy, dz, A
+  __shared__ float2 s_bj[kBatchWarps][32];    // B, source slot bits
+  __shared__ float2 s_out[kBatchWarps][kBatchR][3];  // float-float results
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t s = blockIdx.x * (int64_t)kBatchWarps + w;
+  const bool act = s < n;
+  float2 sum[3], cmp[3], blk[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) sum[c] = cmp[c] = blk[c] = make_float2(0.f, 0.f);
+  if (act) {
+    const float4 pi = pos32[s];
+    const int64_t b = s * (int64_t)W;
+    const int e = cnt[s];
+    int nb = 0;
+    for (int m0 = 0; m0 < e; m0 += 32) {
+      const int np = min(32, e - m0);
+      if (lane < np) {
+        const uint32_t en = __ldg(list + b + m0 + lane);
+        const uint32_t j = en >> kCodeBits;
+        const float4 pj = __ldg(pos32 + j);
+        float ox, oy, oz;
+        decode_shift<CD>(en, hx, hy, hz, ox, oy, oz);
+        const float dx = (pj.x - pi.x) + ox, dy = (pj.y - pi.y) + oy, dz = (pj.z - pi.z) + oz;
+        const float s2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+        float A, B;
+        tensor_ab32<POLY>(s2, P, tab, inv_ds, A, B);
+        s_geo[w][lane] = make_float4(dx, dy, dz, A);
+        s_bj[w][lane] = make_float2(B, __uint_as_float(j));
+      }
+      __syncwarp();
+      for (int p = 0; p < np; ++p) {
+        const float4 g = s_geo[w][p];
+        const float2 bj = s_bj[w][p];
+        const float2 *fj = fb + (int64_t)__float_as_uint(bj.y) * (3 * 32);
+        const float2 fx = __ldg(fj + lane), fy = __ldg(fj + 32 + lane), fz = __ldg(fj + 64 + lane);
+        const float2 dx2 = make_float2(g.x, g.x), dy2 = make_float2(g.y, g.y),
+                     dz2 = make_float2(g.z, g.z), A2 = make_float2(g.w, g.w);
+        // (x.f) B for both right-hand sides, then A f + B (x.f) x
+        float2 d = __ffma2_rn(dz2, fz, __ffma2_rn(dy2, fy, __fmul2_rn(dx2, fx)));
+        d = __fmul2_rn(make_float2(bj.x, bj.x), d);
+        blk[0] = __ffma2_rn(d, dx2, __ffma2_rn(A2, fx, blk[0]));
+        blk[1] = __ffma2_rn(d, dy2, __ffma2_rn(A2, fy, blk[1]));
+        blk[2] = __ffma2_rn(d, dz2, __ffma2_rn(A2, fz, blk[2]));
+        if (++nb == 8) {
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            kahan_add(sum[c].x, cmp[c].x, blk[c].x);
+            kahan_add(sum[c].y, cmp[c].y, blk[c].y);
+            blk[c] = make_float2(0.f, 0.f);
+          }
+          nb = 0;
+        }
+      }
+      __syncwarp();
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    kahan_add(sum[c].x, cmp[c].x, blk[c].x);
+    kahan_add(sum[c].y, cmp[c].y, blk[c].y);
+    s_out[w][2 * lane][c] = make_float2(sum[c].x, -cmp[c].x);
+    s_out[w][2 * lane + 1][c] = make_float2(sum[c].y, -cmp[c].y);
+  }
+  __syncthreads();
+  // coalesced FP64 write-out: per right-hand side, the CTA's targets'
+  // 3 components are consecutive doubles
+  const int64_t s0 = blockIdx.x * (int64_t)kBatchWarps;
+  const int ns = (int)(n - s0 < kBatchWarps ? n - s0 : kBatchWarps);
+  for (int k = threadIdx.x; k < nr * ns * 3; k += blockDim.x) {
+    const int r = k / (ns * 3), q = k - r * (ns * 3);
+    const int t = q / 3, c = q - t * 3;
+    const float2 v = s_out[t][r][c];
+    const int64_t idx = ((int64_t)r * n + s0) * 3 + q;
+    u[idx] = fma(self_c, f[idx], f2d_bits(v.x) + f2d_bits(v.y));
+  }
+}
+
 __global__ void k_slots_to_f32(int64_t n, int nrhs, const double *__restrict__ f,
                                float4 *__restrict__ f32) {
   const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -524,6 +641,39 @@ void launch_cheb(ggem_ctx *c, const Rec32 *src, Rec32 *next, double self_c, doub
       c->n, src, c->nb_cnt.p, c->nb_w, c->nb_list.p, poly_of(c),
       reinterpret_cast<const Rec32 *>(c->tab.p), c->tab_inv_ds, g.h32[0], g.h32[1], g.h32[2],
       self_c, two_da, two_db, coef, x0, x1, xm, dw, next);
+}
+
+template <int CD, bool POLY>
+void launch_b64_t(ggem_ctx *c, int nr, const double *f, double *u, double self_c) {
+  const Grid &g = c->grid;
+  const unsigned grid = (unsigned)((c->n + kBatchWarps - 1) / kBatchWarps);
+  k_pair_b64<CD, POLY><<<grid, 32 * kBatchWarps, 0, c->stream>>>(
+      c->n, nr, c->pos32.p, reinterpret_cast<const float2 *>(c->w_fb.p), c->nb_cnt.p, c->nb_w,
+      c->nb_list.p, poly_of(c), reinterpret_cast<const Rec32 *>(c->tab.p), c->tab_inv_ds,
+      g.h32[0], g.h32[1], g.h32[2], self_c, f, u);
+}
+
+// many right-hand sides: passes of 64 (k_stage_b64 + k_pair_b64)
+int matvec_b64(ggem_ctx *c, int nrhs, const double *f, double *u, double self_c) {
+  const int64_t n = c->n;
+  cudaError_t e = c->w_fb.ensure((size_t)n * 3 * kBatchR);
+  if (e) return cuda_fail(c, e, "batched staging");
+  const bool cd2 = c->prm.cell_div == 2;
+  for (int r0 = 0; r0 < nrhs; r0 += kBatchR) {
+    const int nr = std::min(kBatchR, nrhs - r0);
+    const double *fr = f + (int64_t)r0 * n * 3;
+    double *ur = u + (int64_t)r0 * n * 3;
+    k_stage_b64<<<(unsigned)((n + 31) / 32), 256, 0, c->stream>>>(n, nr, fr, c->w_fb.p);
+    if (int rc = check_launch(c, "batched staging")) return rc;
+    kt_start(c, kKPairF32);
+    if (c->use_poly) cd2 ? launch_b64_t<2, true>(c, nr, fr, ur, self_c)
+                         : launch_b64_t<1, true>(c, nr, fr, ur, self_c);
+    else cd2 ? launch_b64_t<2, false>(c, nr, fr, ur, self_c)
+             : launch_b64_t<1, false>(c, nr, fr, ur, self_c);
+    kt_stop(c, kKPairF32);
+    if (int rc = check_launch(c, "pair f32 batched")) return rc;
+  }
+  return GGEM_OK;
 }
 
 template <int CD, bool POLY, int NR>
@@ -623,6 +773,7 @@ int matvec_slots(ggem_ctx *c, int nrhs, const double *f, double *u, int self_mod
     return GGEM_OK;
   }
   if (nrhs == 1) return launch_f32_r1(c, f, u, self_coefficient(c, self_mode));
+  if (nrhs >= kBatchMinRhs) return matvec_b64(c, nrhs, f, u, self_coefficient(c, self_mode));
   cudaError_t e = c->w_f32.ensure((size_t)c->n * nrhs);
   if (e) return cuda_fail(c, e, "f32 staging");
   const int64_t tot = c->n * nrhs;

@@ -167,7 +167,7 @@ def test_fp64_matvec_reference_mode_non_periodic_axis():
     assert rel(got, want) <= FP64_TOL
 
 
-@pytest.mark.parametrize("nrhs", [1, 5, 8])
+@pytest.mark.parametrize("nrhs", [1, 5, 8, 20, 64, 70])
 @pytest.mark.parametrize("cell_div", [1, 2])
 def test_fp32_matvec_error(nrhs, cell_div):
     xyz, L = suspension(5000, 0.1, 31)
@@ -422,3 +422,35 @@ def test_fused_chebyshev_terms_match_unfused_path():
     # here, below the FP32 pair-sum error, so only the FP32 runs agree closely
     assert r2[0]["err1"] == pytest.approx(r1[0]["err1"], rel=1e-6)
     assert 0.5 * rep_o.err1 <= r2[0]["err1"] <= 2.0 * rep_o.err1
+
+
+def test_batched_64_rhs_chains_matvec_and_chebyshev():
+    """The polymer workload's shape at a small size: 20-bead chains, phi=0.05,
+    64 noise right-hand sides through the batched pair kernel (lanes over
+    right-hand sides) and the adaptive Chebyshev; each checked against the
+    FP64 oracle."""
+    xyz, L = G.make_chains(11, 100, 20, 2.0, 0.05)
+    n = len(xyz)
+    box = O.make_box([0] * 3, [L] * 3, [1, 1, 1])
+    c = O.constants(alpha=0.5)
+    nb = O.neighbors_cutoff(box, xyz, 7.0)
+    f = np.random.default_rng(9).standard_normal((64, n, 3))
+    want = O.local_matvec(c, box, xyz, nb, f, O.SELF_BEAD, nthreads=8)
+    xi = np.random.default_rng(10).standard_normal((64, 3 * n))
+    with G.Context(box_hi=(L,) * 3, rc=7.0, precision=G.FP32) as ctx:
+        ctx.set_particles(xyz)
+        ctx.build_cells()
+        got = ctx.local_matvec(f, G.SELF_BEAD)
+        lo, hi = ctx.lanczos_bounds(k=40, seed=2)
+        y, reps = ctx.cheb_inv_sqrt(xi, 50, lo / 1.05, hi * 1.05, 1e-3, check_every=0)
+    assert rel(got, want) <= FP32_TOL
+    for r in range(64):
+        assert rel(got[r], want[r]) <= FP32_TOL
+    assert all(rp["converged"] and rp["err1"] <= 1e-3 for rp in reps)
+    op = O.Operator(matvec=(c, box, xyz, nb, O.SELF_BEAD, 8))
+    for r in (0, 31, 63):
+        # the oracle checks every term and may stop earlier than the adaptive
+        # schedule; both series meet err1 <= 1e-3
+        y_o, rep_o = O.cheb_inv_sqrt(op, xi[r], 50, lo / 1.05, hi * 1.05, 1e-3)
+        assert rep_o.converged and rep_o.n_terms <= reps[r]["n_terms"]
+        assert rel(y.reshape(64, -1)[r], y_o) <= 5e-3
