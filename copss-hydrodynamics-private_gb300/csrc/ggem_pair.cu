@@ -463,22 +463,76 @@ __global__ void __launch_bounds__(256) k_stage_b64(int64_t n, int nr, const doub
   }
 }
 
+// forces of row entry q (clamped to the last one) for the two right-hand
+// sides of this lane: fw = fb + lane, jw = the warp's source slots
+__device__ __forceinline__ void b64_fetch(const float2 *__restrict__ fw, const uint32_t *jw, int q,
+                                          int np, float2 &x, float2 &y, float2 &z) {
+  const float2 *fp = fw + (int64_t)jw[min(q, np - 1)] * (3 * 32);
+  x = __ldg(fp);
+  y = __ldg(fp + 32);
+  z = __ldg(fp + 64);
+}
+
+// blk += A f + B (x.f) x for both right-hand sides of the lane (packed)
+__device__ __forceinline__ void b64_accumulate(const float4 &g0, const float4 &g1,
+                                               const float2 &g2, const float2 &fx,
+                                               const float2 &fy, const float2 &fz, float2 &b0,
+                                               float2 &b1, float2 &b2) {
+  const float2 dx2 = make_float2(g0.x, g0.y), dy2 = make_float2(g0.z, g0.w);
+  const float2 dz2 = make_float2(g1.x, g1.y), A2 = make_float2(g1.z, g1.w);
+  float2 d = __ffma2_rn(dz2, fz, __ffma2_rn(dy2, fy, __fmul2_rn(dx2, fx)));
+  d = __fmul2_rn(g2, d);
+  b0 = __ffma2_rn(d, dx2, __ffma2_rn(A2, fx, b0));
+  b1 = __ffma2_rn(d, dy2, __ffma2_rn(A2, fy, b1));
+  b2 = __ffma2_rn(d, dz2, __ffma2_rn(A2, fz, b2));
+}
+
+// block sums into the Kahan pairs, blocks cleared
+__device__ __forceinline__ void b64_flush(float2 (&sum)[3], float2 (&cmp)[3], float2 &b0,
+                                          float2 &b1, float2 &b2) {
+  kahan_add(sum[0].x, cmp[0].x, b0.x);
+  kahan_add(sum[0].y, cmp[0].y, b0.y);
+  kahan_add(sum[1].x, cmp[1].x, b1.x);
+  kahan_add(sum[1].y, cmp[1].y, b1.y);
+  kahan_add(sum[2].x, cmp[2].x, b2.x);
+  kahan_add(sum[2].y, cmp[2].y, b2.y);
+  b0 = b1 = b2 = make_float2(0.f, 0.f);
+}
+
 template <int CD, bool POLY>
-__global__ void __launch_bounds__(32 * kBatchWarps) k_pair_b64(
+__global__ void __launch_bounds__(32 * kBatchWarps, 3) k_pair_b64(
     int64_t n, int nr, const float4 *__restrict__ pos32, const float2 *__restrict__ fb,
     const int32_t *__restrict__ cnt, int W, const uint32_t *__restrict__ list, PolyAB P,
-    const Rec32 *__restrict__ tab, float inv_ds, float hx, float hy, float hz, double self_c,
-    const double *__restrict__ f, double *__restrict__ u) {
-  __shared__ float4 s_geo[kBatchWarps][32];   // dx, dy, dz, A
-  __shared__ float2 s_bj[kBatchWarps][32];    // B, source slot bits
+    const Rec32 *__restrict__ tab, float inv_ds, float hx, float hy, float hz, float self_hi,
+    float self_lo, double *__restrict__ u) {
+  // per entry, pre-duplicated for the packed arithmetic:
+  // g0 = (dx, dx, dy, dy), g1 = (dz, dz, A, A), g2 = (B, B), source slot
+  __shared__ float4 s_g0[kBatchWarps][32], s_g1[kBatchWarps][32];
+  __shared__ float2 s_g2[kBatchWarps][32];
+  __shared__ uint32_t s_j[kBatchWarps][32];
   __shared__ float2 s_out[kBatchWarps][kBatchR][3];  // float-float results
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t s = blockIdx.x * (int64_t)kBatchWarps + w;
   const bool act = s < n;
-  float2 sum[3], cmp[3], blk[3];
+  float2 sum[3], cmp[3];
+  float2 blk0 = make_float2(0.f, 0.f), blk1 = blk0, blk2 = blk0;
 #pragma unroll
-  for (int c = 0; c < 3; ++c) sum[c] = cmp[c] = blk[c] = make_float2(0.f, 0.f);
+  for (int c = 0; c < 3; ++c) sum[c] = cmp[c] = make_float2(0.f, 0.f);
   if (act) {
+    // self term from the target's own staged forces, as a float-float
+    // product with self_c = self_hi + self_lo
+    {
+      const float2 *fo = fb + s * (3 * 32);
+      const float2 ch = make_float2(self_hi, self_hi), cl = make_float2(self_lo, self_lo);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const float2 v = __ldg(fo + 32 * c + lane);
+        const float2 pr = __fmul2_rn(ch, v);
+        const float2 er = __ffma2_rn(cl, v, __ffma2_rn(ch, v, make_float2(-pr.x, -pr.y)));
+        sum[c] = pr;
+        cmp[c] = make_float2(-er.x, -er.y);  // Kahan keeps value = sum - cmp
+      }
+    }
     const float4 pi = pos32[s];
     const int64_t b = s * (int64_t)W;
     const int e = cnt[s];
@@ -495,54 +549,59 @@ __global__ void __launch_bounds__(32 * kBatchWarps) k_pair_b64(
         const float s2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
         float A, B;
         tensor_ab32<POLY>(s2, P, tab, inv_ds, A, B);
-        s_geo[w][lane] = make_float4(dx, dy, dz, A);
-        s_bj[w][lane] = make_float2(B, __uint_as_float(j));
+        s_g0[w][lane] = make_float4(dx, dx, dy, dy);
+        s_g1[w][lane] = make_float4(dz, dz, A, A);
+        s_g2[w][lane] = make_float2(B, B);
+        s_j[w][lane] = j;
       }
       __syncwarp();
-      for (int p = 0; p < np; ++p) {
-        const float4 g = s_geo[w][p];
-        const float2 bj = s_bj[w][p];
-        const float2 *fj = fb + (int64_t)__float_as_uint(bj.y) * (3 * 32);
-        const float2 fx = __ldg(fj + lane), fy = __ldg(fj + 32 + lane), fz = __ldg(fj + 64 + lane);
-        const float2 dx2 = make_float2(g.x, g.x), dy2 = make_float2(g.y, g.y),
-                     dz2 = make_float2(g.z, g.z), A2 = make_float2(g.w, g.w);
-        // (x.f) B for both right-hand sides, then A f + B (x.f) x
-        float2 d = __ffma2_rn(dz2, fz, __ffma2_rn(dy2, fy, __fmul2_rn(dx2, fx)));
-        d = __fmul2_rn(make_float2(bj.x, bj.x), d);
-        blk[0] = __ffma2_rn(d, dx2, __ffma2_rn(A2, fx, blk[0]));
-        blk[1] = __ffma2_rn(d, dy2, __ffma2_rn(A2, fy, blk[1]));
-        blk[2] = __ffma2_rn(d, dz2, __ffma2_rn(A2, fz, blk[2]));
-        if (++nb == 8) {
-#pragma unroll
-          for (int c = 0; c < 3; ++c) {
-            kahan_add(sum[c].x, cmp[c].x, blk[c].x);
-            kahan_add(sum[c].y, cmp[c].y, blk[c].y);
-            blk[c] = make_float2(0.f, 0.f);
-          }
+      // three force slots in flight: each is refilled with the entry three
+      // ahead right after its own entry is used (no register rotation)
+      const float2 *fw = fb + lane;
+      const uint32_t *jw = s_j[w];
+      float2 ax, ay, az, bx, by, bz, cx, cy, cz;
+      b64_fetch(fw, jw, 0, np, ax, ay, az);
+      b64_fetch(fw, jw, 1, np, bx, by, bz);
+      b64_fetch(fw, jw, 2, np, cx, cy, cz);
+      for (int p = 0; p < np; p += 3) {
+        b64_accumulate(s_g0[w][p], s_g1[w][p], s_g2[w][p], ax, ay, az, blk0, blk1, blk2);
+        b64_fetch(fw, jw, p + 3, np, ax, ay, az);
+        if (p + 1 < np) {
+          b64_accumulate(s_g0[w][p + 1], s_g1[w][p + 1], s_g2[w][p + 1], bx, by, bz, blk0, blk1,
+                         blk2);
+          b64_fetch(fw, jw, p + 4, np, bx, by, bz);
+        }
+        if (p + 2 < np) {
+          b64_accumulate(s_g0[w][p + 2], s_g1[w][p + 2], s_g2[w][p + 2], cx, cy, cz, blk0, blk1,
+                         blk2);
+          b64_fetch(fw, jw, p + 5, np, cx, cy, cz);
+        }
+        if (++nb == 3) {  // every 9 entries into the compensated sums
+          b64_flush(sum, cmp, blk0, blk1, blk2);
           nb = 0;
         }
       }
       __syncwarp();
     }
   }
+  b64_flush(sum, cmp, blk0, blk1, blk2);
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
-    kahan_add(sum[c].x, cmp[c].x, blk[c].x);
-    kahan_add(sum[c].y, cmp[c].y, blk[c].y);
     s_out[w][2 * lane][c] = make_float2(sum[c].x, -cmp[c].x);
     s_out[w][2 * lane + 1][c] = make_float2(sum[c].y, -cmp[c].y);
   }
   __syncthreads();
   // coalesced FP64 write-out: per right-hand side, the CTA's targets'
-  // 3 components are consecutive doubles
+  // 3 components are consecutive doubles; one FP64 add per value
   const int64_t s0 = blockIdx.x * (int64_t)kBatchWarps;
   const int ns = (int)(n - s0 < kBatchWarps ? n - s0 : kBatchWarps);
-  for (int k = threadIdx.x; k < nr * ns * 3; k += blockDim.x) {
-    const int r = k / (ns * 3), q = k - r * (ns * 3);
+  constexpr int kRow = 3 * kBatchWarps;
+  for (int k = threadIdx.x; k < nr * kRow; k += blockDim.x) {
+    const int r = k / kRow, q = k - r * kRow;
     const int t = q / 3, c = q - t * 3;
+    if (t >= ns) continue;
     const float2 v = s_out[t][r][c];
-    const int64_t idx = ((int64_t)r * n + s0) * 3 + q;
-    u[idx] = fma(self_c, f[idx], f2d_bits(v.x) + f2d_bits(v.y));
+    u[((int64_t)r * n + s0) * 3 + q] = f2d_bits(v.x) + f2d_bits(v.y);
   }
 }
 
@@ -650,7 +709,7 @@ void launch_b64_t(ggem_ctx *c, int nr, const double *f, double *u, double self_c
   k_pair_b64<CD, POLY><<<grid, 32 * kBatchWarps, 0, c->stream>>>(
       c->n, nr, c->pos32.p, reinterpret_cast<const float2 *>(c->w_fb.p), c->nb_cnt.p, c->nb_w,
       c->nb_list.p, poly_of(c), reinterpret_cast<const Rec32 *>(c->tab.p), c->tab_inv_ds,
-      g.h32[0], g.h32[1], g.h32[2], self_c, f, u);
+      g.h32[0], g.h32[1], g.h32[2], (float)self_c, (float)(self_c - (double)(float)self_c), u);
 }
 
 // many right-hand sides: passes of 64 (k_stage_b64 + k_pair_b64)
