@@ -396,67 +396,16 @@ struct OverlapGrid {
 
 }  // namespace
 
-extern "C" int ggem_make_suspension(uint64_t seed, int64_t n, double phi, double radius,
-                                    double *xyz, double *box_length) {
-  if (n <= 0 || !(phi > 0.0 && phi < 0.35) || !(radius > 0) || !xyz || !box_length)
-    return GGEM_ERR_BAD_ARG;
-  const double L = std::cbrt((double)n * 4.0 / 3.0 * ggem::kPi * radius * radius * radius / phi);
-  *box_length = L;
-  SplitMix rng(seed);
-  const double min_sep = 2.0 * radius, min2 = min_sep * min_sep;
-  OverlapGrid g(L, min_sep, xyz);
-  if (g.nc < 3) {
-    // tiny boxes: brute force
-    for (int64_t i = 0; i < n; ++i) {
-      int64_t tries = 0;
-      for (;;) {
-        if (++tries > 1000000) return GGEM_ERR_BAD_ARG;
-        for (int d = 0; d < 3; ++d) xyz[3 * i + d] = rng.uniform() * L;
-        bool ok = true;
-        for (int64_t j = 0; j < i && ok; ++j) {
-          double r2 = 0;
-          for (int d = 0; d < 3; ++d) {
-            double v = xyz[3 * j + d] - xyz[3 * i + d];
-            v -= L * std::nearbyint(v / L);
-            r2 += v * v;
-          }
-          ok = r2 >= min2;
-        }
-        if (ok) break;
-      }
-    }
-    return GGEM_OK;
-  }
-  for (int64_t i = 0; i < n; ++i) {
-    int64_t tries = 0;
-    for (;;) {
-      if (++tries > 1000000) return GGEM_ERR_BAD_ARG;
-      for (int d = 0; d < 3; ++d) xyz[3 * i + d] = rng.uniform() * L;
-      if (!g.overlaps(xyz + 3 * i, min2, -1)) break;
-    }
-    g.insert(i);
-  }
-  return GGEM_OK;
-}
+namespace {
 
-extern "C" int ggem_make_chains(uint64_t seed, int64_t n_chains, int beads_per_chain,
-                                double bond, double phi, double radius, double *xyz,
-                                double *box_length) {
-  if (n_chains <= 0 || beads_per_chain <= 0 || !(bond > 0) || !(phi > 0.0 && phi < 0.35) ||
-      !(radius > 0) || !xyz || !box_length)
-    return GGEM_ERR_BAD_ARG;
-  const int64_t n = n_chains * (int64_t)beads_per_chain;
-  const double L = std::cbrt((double)n * 4.0 / 3.0 * ggem::kPi * radius * radius * radius / phi);
-  *box_length = L;
-  SplitMix rng(seed);
-  const double min_sep = 2.0 * radius;
-  // beads closer than min_sep are rejected; the bonded predecessor sits at
-  // exactly `bond` and is skipped in the test
-  const double min2 = min_sep * min_sep * (1.0 - 1e-12);
-  OverlapGrid g(L, min_sep, xyz);
-  if (g.nc < 3) return GGEM_ERR_BAD_ARG;
+// grows n_chains self-avoiding random-walk chains (bond length `bond`,
+// beads closer than sqrt(min2) rejected, the bonded predecessor skipped) at
+// indices [base, base + n_chains * beads); a chain that runs into a dead end
+// is removed and grown again
+int grow_chains(SplitMix &rng, OverlapGrid &g, double *xyz, double L, int64_t base0,
+                int64_t n_chains, int beads_per_chain, double bond, double min2) {
   for (int64_t c = 0; c < n_chains; ++c) {
-    const int64_t base = c * beads_per_chain;
+    const int64_t base = base0 + c * beads_per_chain;
     int64_t restarts = 0;
   restart:
     if (++restarts > 10000) return GGEM_ERR_BAD_ARG;
@@ -500,6 +449,97 @@ extern "C" int ggem_make_chains(uint64_t seed, int64_t n_chains, int beads_per_c
     }
   }
   return GGEM_OK;
+}
+
+// random sequential addition of free beads at indices [base, base + count)
+int place_free(SplitMix &rng, OverlapGrid &g, double *xyz, double L, int64_t base, int64_t count,
+               double min2) {
+  for (int64_t i = base; i < base + count; ++i) {
+    int64_t tries = 0;
+    for (;;) {
+      if (++tries > 1000000) return GGEM_ERR_BAD_ARG;
+      for (int d = 0; d < 3; ++d) xyz[3 * i + d] = rng.uniform() * L;
+      if (!g.overlaps(xyz + 3 * i, min2, -1)) break;
+    }
+    g.insert(i);
+  }
+  return GGEM_OK;
+}
+
+}  // namespace
+
+extern "C" int ggem_make_suspension(uint64_t seed, int64_t n, double phi, double radius,
+                                    double *xyz, double *box_length) {
+  if (n <= 0 || !(phi > 0.0 && phi < 0.35) || !(radius > 0) || !xyz || !box_length)
+    return GGEM_ERR_BAD_ARG;
+  const double L = std::cbrt((double)n * 4.0 / 3.0 * ggem::kPi * radius * radius * radius / phi);
+  *box_length = L;
+  SplitMix rng(seed);
+  const double min_sep = 2.0 * radius, min2 = min_sep * min_sep;
+  OverlapGrid g(L, min_sep, xyz);
+  if (g.nc < 3) {
+    // tiny boxes: brute force
+    for (int64_t i = 0; i < n; ++i) {
+      int64_t tries = 0;
+      for (;;) {
+        if (++tries > 1000000) return GGEM_ERR_BAD_ARG;
+        for (int d = 0; d < 3; ++d) xyz[3 * i + d] = rng.uniform() * L;
+        bool ok = true;
+        for (int64_t j = 0; j < i && ok; ++j) {
+          double r2 = 0;
+          for (int d = 0; d < 3; ++d) {
+            double v = xyz[3 * j + d] - xyz[3 * i + d];
+            v -= L * std::nearbyint(v / L);
+            r2 += v * v;
+          }
+          ok = r2 >= min2;
+        }
+        if (ok) break;
+      }
+    }
+    return GGEM_OK;
+  }
+  return place_free(rng, g, xyz, L, 0, n, min2);
+}
+
+extern "C" int ggem_make_chains(uint64_t seed, int64_t n_chains, int beads_per_chain,
+                                double bond, double phi, double radius, double *xyz,
+                                double *box_length) {
+  if (n_chains <= 0 || beads_per_chain <= 0 || !(bond > 0) || !(phi > 0.0 && phi < 0.35) ||
+      !(radius > 0) || !xyz || !box_length)
+    return GGEM_ERR_BAD_ARG;
+  const int64_t n = n_chains * (int64_t)beads_per_chain;
+  const double L = std::cbrt((double)n * 4.0 / 3.0 * ggem::kPi * radius * radius * radius / phi);
+  *box_length = L;
+  SplitMix rng(seed);
+  const double min_sep = 2.0 * radius;
+  // beads closer than min_sep are rejected; the bonded predecessor sits at
+  // exactly `bond` and is skipped in the test
+  const double min2 = min_sep * min_sep * (1.0 - 1e-12);
+  OverlapGrid g(L, min_sep, xyz);
+  if (g.nc < 3) return GGEM_ERR_BAD_ARG;
+  return grow_chains(rng, g, xyz, L, 0, n_chains, beads_per_chain, bond, min2);
+}
+
+extern "C" int ggem_make_mixture(uint64_t seed, int64_t n_chains, int beads_per_chain,
+                                 int64_t n_free, double bond, double phi, double radius,
+                                 double *xyz, double *box_length) {
+  if (n_chains < 0 || n_free < 0 || n_chains + n_free <= 0 ||
+      (n_chains > 0 && beads_per_chain <= 0) || !(bond > 0) || !(phi > 0.0 && phi < 0.35) ||
+      !(radius > 0) || !xyz || !box_length)
+    return GGEM_ERR_BAD_ARG;
+  const int64_t nc_beads = n_chains * (int64_t)std::max(beads_per_chain, 0);
+  const int64_t n = nc_beads + n_free;
+  const double L = std::cbrt((double)n * 4.0 / 3.0 * ggem::kPi * radius * radius * radius / phi);
+  *box_length = L;
+  SplitMix rng(seed);
+  const double min_sep = 2.0 * radius;
+  OverlapGrid g(L, min_sep, xyz);
+  if (g.nc < 3) return GGEM_ERR_BAD_ARG;
+  if (int rc = grow_chains(rng, g, xyz, L, 0, n_chains, beads_per_chain, bond,
+                           min_sep * min_sep * (1.0 - 1e-12)))
+    return rc;
+  return place_free(rng, g, xyz, L, nc_beads, n_free, min_sep * min_sep);
 }
 
 extern "C" int ggem_make_normals(uint64_t seed, int64_t n, double *out) {

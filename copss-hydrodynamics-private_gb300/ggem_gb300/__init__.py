@@ -113,6 +113,19 @@ def lib():
         "ggem_make_suspension": (i, [C.c_uint64, i64, d, d, vp, P(d)]),
         "ggem_make_chains": (i, [C.c_uint64, i64, i, d, d, d, vp, P(d)]),
         "ggem_make_normals": (i, [C.c_uint64, i64, vp]),
+        "ggem_make_mixture": (i, [C.c_uint64, i64, i, i64, d, d, d, vp, P(d)]),
+        "ggem_surrogate_create": (vp, [i, C.c_uint64]),
+        "ggem_surrogate_destroy": (None, [vp]),
+        "ggem_surrogate_last_error": (C.c_char_p, [vp]),
+        "ggem_surrogate_set_norm": (i, [vp, vp]),
+        "ggem_surrogate_get_norm": (i, [vp, vp]),
+        "ggem_surrogate_set_params": (i, [vp, vp]),
+        "ggem_surrogate_get_params": (i, [vp, vp]),
+        "ggem_surrogate_train": (i, [vp, vp, vp, i64, i, i, C.c_float, C.c_uint64, vp]),
+        "ggem_surrogate_predict": (i, [vp, vp, i64, vp]),
+        "ggem_surrogate_gradient": (i, [vp, vp, vp, i64, P(C.c_float), vp]),
+        "ggem_surrogate_features": (i, [vp, d, vp]),
+        "ggem_surrogate_interval": (i, [vp, vp, d, d, d, P(d), P(d)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -155,6 +168,113 @@ def make_suspension(seed, n, phi, radius=1.0):
     if rc:
         raise GGEMError(rc, "suspension generation failed")
     return xyz, L.value
+
+
+def make_mixture(seed, n_chains, beads, n_free, bond=2.0, phi=0.05, radius=1.0):
+    """n_chains chains of `beads` beads followed by n_free free beads."""
+    xyz = np.zeros((n_chains * beads + n_free, 3))
+    L = C.c_double()
+    rc = lib().ggem_make_mixture(int(seed), int(n_chains), int(beads), int(n_free), float(bond),
+                                 float(phi), float(radius), _p(xyz), C.byref(L))
+    if rc:
+        raise GGEMError(rc, "mixture generation failed")
+    return xyz, L.value
+
+
+SUR_FEATURES, SUR_OUTPUTS, SUR_HIST_BINS = 35, 2, 32
+SUR_PARAMS = 128 * 48 + 128 + 3 * (128 * 128 + 128)
+SUR_NORM = 2 * SUR_FEATURES + 2 * SUR_OUTPUTS
+
+
+class Surrogate:
+    """The eigen-interval network (include/ggem_surrogate.h): BF16 MLP
+    35 -> 128 -> 128 -> 128 -> 2 trained and evaluated by the library's
+    tensor-core kernels."""
+
+    def __init__(self, device=0, seed=1):
+        self.h = lib().ggem_surrogate_create(int(device), int(seed))
+        if not self.h:
+            raise GGEMError(ERR_NO_DEVICE, "surrogate: no usable CUDA device")
+
+    def close(self):
+        if self.h:
+            lib().ggem_surrogate_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc:
+            raise GGEMError(rc, (lib().ggem_surrogate_last_error(self.h) or b"").decode())
+
+    @property
+    def norm(self) -> np.ndarray:
+        out = np.zeros(SUR_NORM, dtype=np.float32)
+        self._check(lib().ggem_surrogate_get_norm(self.h, _p(out)))
+        return out
+
+    @norm.setter
+    def norm(self, v):
+        v = np.ascontiguousarray(v, dtype=np.float32)
+        assert v.size == SUR_NORM
+        self._check(lib().ggem_surrogate_set_norm(self.h, _p(v)))
+
+    def fit_norm(self, X, Y):
+        """Feature and output mean / std from a training set."""
+        X = np.asarray(X, dtype=np.float64)
+        Y = np.asarray(Y, dtype=np.float64)
+        sd = X.std(axis=0)
+        sd[sd < 1e-6] = 1.0
+        ysd = Y.std(axis=0)
+        ysd[ysd < 1e-6] = 1.0
+        self.norm = np.concatenate([X.mean(axis=0), sd, Y.mean(axis=0), ysd])
+
+    @property
+    def params(self) -> np.ndarray:
+        out = np.zeros(SUR_PARAMS, dtype=np.float32)
+        self._check(lib().ggem_surrogate_get_params(self.h, _p(out)))
+        return out
+
+    @params.setter
+    def params(self, v):
+        v = np.ascontiguousarray(v, dtype=np.float32)
+        assert v.size == SUR_PARAMS
+        self._check(lib().ggem_surrogate_set_params(self.h, _p(v)))
+
+    def train(self, X, Y, epochs, batch=256, lr=1e-3, seed=0):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        Y = np.ascontiguousarray(Y, dtype=np.float32)
+        loss = np.zeros(epochs, dtype=np.float32)
+        self._check(lib().ggem_surrogate_train(self.h, _p(X), _p(Y), len(X), int(epochs),
+                                               int(batch), float(lr), int(seed), _p(loss)))
+        return loss
+
+    def predict(self, X) -> np.ndarray:
+        X = np.ascontiguousarray(np.atleast_2d(X), dtype=np.float32)
+        Y = np.zeros((len(X), SUR_OUTPUTS), dtype=np.float32)
+        self._check(lib().ggem_surrogate_predict(self.h, _p(X), len(X), _p(Y)))
+        return Y
+
+    def gradient(self, X, Y):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        Y = np.ascontiguousarray(Y, dtype=np.float32)
+        g = np.zeros(SUR_PARAMS, dtype=np.float32)
+        loss = C.c_float()
+        self._check(lib().ggem_surrogate_gradient(self.h, _p(X), _p(Y), len(X), C.byref(loss),
+                                                  _p(g)))
+        return loss.value, g
+
+    def save(self, path):
+        np.savez(path, params=self.params, norm=self.norm)
+
+    def load(self, path):
+        d = np.load(path)
+        self.norm = d["norm"]
+        self.params = d["params"]
 
 
 def make_chains(seed, n_chains, beads, bond=2.0, phi=0.05, radius=1.0):
@@ -363,6 +483,18 @@ class Context:
     def lanczos_bounds(self, k=30, seed=1):
         lo, hi = C.c_double(), C.c_double()
         self._check(lib().ggem_lanczos_bounds(self.h, int(k), int(seed), C.byref(lo), C.byref(hi)))
+        return lo.value, hi.value
+
+    def surrogate_features(self, chain_fraction=0.0) -> np.ndarray:
+        f = np.zeros(SUR_FEATURES, dtype=np.float32)
+        self._check(lib().ggem_surrogate_features(self.h, float(chain_fraction), _p(f)))
+        return f
+
+    def surrogate_interval(self, sur, chain_fraction=0.0, margin_lo=0.0, margin_hi=0.0):
+        lo, hi = C.c_double(), C.c_double()
+        self._check(lib().ggem_surrogate_interval(self.h, sur.h, float(chain_fraction),
+                                                  float(margin_lo), float(margin_hi),
+                                                  C.byref(lo), C.byref(hi)))
         return lo.value, hi.value
 
     def power_iteration(self, tol=1e-3, maxits=50):

@@ -25,6 +25,12 @@ int ggem_make_suspension(uint64_t seed, int64_t n, double phi, double radius, do
 int ggem_make_chains(uint64_t seed, int64_t n_chains, int beads_per_chain, double bond,
                      double phi, double radius, double *xyz, double *box_length);
 /* n iid N(0,1) values */
+/* n_chains chains of beads_per_chain beads (grown as in ggem_make_chains)
+ * followed by n_free free beads placed by random sequential addition, all
+ * non-overlapping, in the periodic cube of volume fraction phi; beads
+ * [0, n_chains * beads_per_chain) are the chains */
+int ggem_make_mixture(uint64_t seed, int64_t n_chains, int beads_per_chain, int64_t n_free,
+                      double bond, double phi, double radius, double *xyz, double *box_length);
 int ggem_make_normals(uint64_t seed, int64_t n, double *out);
 
 #ifdef __cplusplus

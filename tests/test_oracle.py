@@ -244,3 +244,39 @@ def test_philox_known_answer():
     r = np.sqrt(-2 * np.log(u1))
     assert out[0] == pytest.approx(r * np.cos(2 * np.pi * u2), rel=1e-14)
     assert out[1] == pytest.approx(r * np.sin(2 * np.pi * u2), rel=1e-14)
+
+
+def test_mlp_oracle_gradient_matches_finite_differences():
+    """The network oracle's backward formulas, in exact float64 arithmetic,
+    against central differences of its own loss."""
+    import mlp_oracle as M
+    rng = np.random.default_rng(4)
+    n = 7
+    P = (rng.standard_normal(55808) * 0.05)
+    X = rng.standard_normal((n, M.IN))
+    Y = rng.standard_normal((n, M.OUT))
+    norm = np.concatenate([np.zeros(M.IN), np.ones(M.IN), np.zeros(2), np.ones(2)])
+    loss, g = M.loss_and_grad(P, norm, X, Y, exact=True)
+    # a sample of parameters from every layer (weights and biases)
+    offs = [0, 48 * 128, 48 * 128 + 128, 48 * 128 + 128 + 16384, 48 * 128 + 256 + 2 * 16384,
+            48 * 128 + 384 + 3 * 16384]
+    picks = [offs[0] + 5, offs[0] + 130, offs[1] + 3, offs[2] + 777, offs[3] + 11,
+             offs[4] + 129, offs[4] + 5, offs[5] + 1]
+    for k in picks:
+        h = 1e-6
+        Pp, Pm = P.copy(), P.copy()
+        Pp[k] += h
+        Pm[k] -= h
+        fd = (M.loss_and_grad(Pp, norm, X, Y, exact=True)[0] -
+              M.loss_and_grad(Pm, norm, X, Y, exact=True)[0]) / (2 * h)
+        assert abs(fd - g[k]) <= 1e-6 + 1e-5 * abs(g[k]), (k, fd, g[k])
+
+
+def test_bf16_rounding_is_nearest_even():
+    import mlp_oracle as M
+    x = np.array([1.0, 1.0 + 2 ** -8, 1.0 + 3 * 2 ** -8, 1.0 + 2 ** -9, -2.5, 0.0],
+                 dtype=np.float32)
+    got = M.bf16(x)
+    want = np.array([1.0, 1.0, 1.0 + 4 * 2 ** -8, 1.0, -2.5, 0.0], dtype=np.float32)
+    # 1 + 2^-8 is a tie between 1 and 1 + 2^-7: even mantissa -> 1
+    assert np.array_equal(got, want)
