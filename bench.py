@@ -193,19 +193,34 @@ def run_gb300(args, rank, world):
     d_xi = torch.empty(3 * N_BEADS, dtype=torch.float64, device="cuda")
     d_dw = torch.empty_like(d_xi)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
-    state = {"bounds": None, "lanczos_calls": 0, "reports": []}
+    state = {"bounds": None, "lanczos_calls": 0, "surrogate_calls": 0, "reports": [],
+             "source": None}
+    from ggem_gb300 import surrogate_data as SD
+    sur_loaded = None if args.no_surrogate else SD.load_default(device=dev)
+    sur, sur_margins = (sur_loaded[0], sur_loaded[1]) if sur_loaded else (None, None)
 
-    def bounds(c):
+    def lanczos(c):
         lo, hi = c.lanczos_bounds(k=24, seed=7)
         state["lanczos_calls"] += 1
         return lo / 1.05, hi * 1.05  # eig_factor widening, copss.C:1607
+
+    def bounds(c, retry):
+        # the network's interval first; Lanczos when the Chebyshev check
+        # rejected the previous interval (the reference recomputes its
+        # eigenvalues when the series fails, copss.C:1598-1671)
+        if sur is not None and not retry:
+            state["surrogate_calls"] += 1
+            state["source"] = "surrogate"
+            return c.surrogate_interval(sur, 0.0, sur_margins[0], sur_margins[1])
+        state["source"] = "lanczos"
+        return lanczos(c)
 
     def device_step(step_id):
         ctx.set_particles_dev(d_xyz.data_ptr(), N_BEADS)
         ctx.build_cells()
         ctx.philox_normals_dev(SEED, step_id, 3 * N_BEADS, d_xi.data_ptr())
         if state["bounds"] is None:
-            state["bounds"] = bounds(ctx)
+            state["bounds"] = bounds(ctx, False)
         for attempt in range(2):
             lo, hi = state["bounds"]
             rc, rep = ctx.brownian_displacement_dev(d_xi.data_ptr(), d_dw.data_ptr(), 1,
@@ -214,7 +229,7 @@ def run_gb300(args, rank, world):
             if rc == 0:
                 state["reports"].append(rep[0])
                 return
-            state["bounds"] = bounds(ctx)  # recompute and retry once
+            state["bounds"] = bounds(ctx, True)  # recompute and retry once
         raise RuntimeError(f"Chebyshev failed twice: {rep}")
 
     def timed(fn, steps, warmup, flush_l2=True):
@@ -366,6 +381,41 @@ def run_gb300(args, rank, world):
                         "every term, one RHS, no graphs"}
     ctx64.close()
 
+    # ---- eigen bounds refreshed every step: network vs Lanczos ----------
+    per_step = None
+    if sur is not None:
+        def refresh_step(step_id, use_sur):
+            ctx.set_particles_dev(d_xyz.data_ptr(), N_BEADS)
+            ctx.build_cells()
+            ctx.philox_normals_dev(SEED, step_id, 3 * N_BEADS, d_xi.data_ptr())
+            if use_sur:
+                lo, hi = ctx.surrogate_interval(sur, 0.0, sur_margins[0], sur_margins[1])
+            else:
+                lo, hi = lanczos(ctx)
+            rc, rep = ctx.brownian_displacement_dev(d_xi.data_ptr(), d_dw.data_ptr(), 1,
+                                                    CHEB_MAX, lo, hi, CHEB_TOL,
+                                                    check_every=args.check_every)
+            if rc != 0:  # rejected interval: Lanczos fallback
+                lo, hi = lanczos(ctx)
+                rc, rep = ctx.brownian_displacement_dev(d_xi.data_ptr(), d_dw.data_ptr(), 1,
+                                                        CHEB_MAX, lo, hi, CHEB_TOL,
+                                                        check_every=args.check_every)
+            return rc == 0, rep[0]["n_terms"]
+
+        per_step = {}
+        for name, use_sur in (("surrogate", True), ("lanczos24", False)):
+            for s_ in range(2):
+                refresh_step(s_, use_sur)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            oks = [refresh_step(100 + s_, use_sur) for s_ in range(max(5, args.steps))]
+            ctx.synchronize()
+            dt = (time.perf_counter() - t0) / len(oks)
+            per_step[name] = {"steps_per_s": 1.0 / dt, "ms_per_step": dt * 1e3,
+                              "converged": all(o for o, _ in oks),
+                              "cheb_terms": sorted({t for _, t in oks})}
+        per_step["surrogate_margins_log"] = [float(x) for x in sur_margins]
+
     # ---- polymer suspension, 64 batched noise right-hand sides ----------
     poly = None if args.skip_polymer else polymer_leg(G, torch, dev, flush, peak_fn=None)
 
@@ -402,7 +452,10 @@ def run_gb300(args, rank, world):
         "velocity_rel_err_fp32_vs_fp64": rel_err, "velocity_max_component_err": comp_err,
         "cheb": {"terms": [r["n_terms"] for r in reps], "err1_max": max(r["err1"] for r in reps),
                  "converged": all(r["converged"] for r in reps),
+                 "bounds_source": state["source"],
+                 "surrogate_calls": state["surrogate_calls"],
                  "lanczos_calls": state["lanczos_calls"]},
+        "bounds_every_step": per_step,
         "roofline": {"bound": "fp32", "kernel": names[dom],
                      "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak if peak else None,
@@ -573,6 +626,7 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--reference-max-steps", type=int, default=6)
     ap.add_argument("--skip-polymer", action="store_true")
+    ap.add_argument("--no-surrogate", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
 

@@ -26,6 +26,7 @@ import argparse
 import json
 import time
 from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
 
 import numpy as np
 
@@ -111,6 +112,17 @@ def save(path, sur, summary, loss):
     np.savez(path, params=sur.params, norm=sur.norm,
              margins=np.asarray(summary["margins_log"], np.float64), loss=loss,
              summary=json.dumps(summary))
+
+
+DEFAULT_WEIGHTS = Path(__file__).resolve().parent / "data" / "eigen_surrogate.npz"
+
+
+def load_default(device=0):
+    """The network trained by this module's command line on 20000 + 2000
+    configurations (None when the file is absent)."""
+    if not DEFAULT_WEIGHTS.exists():
+        return None
+    return load(DEFAULT_WEIGHTS, device=device)
 
 
 def load(path, device=0):
