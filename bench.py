@@ -50,6 +50,16 @@ RC = 7.0
 CHEB_MAX = 50
 CHEB_TOL = 1e-3
 SEED = 20261203
+# DRAM bytes (read + write) per launch of the dominant pair kernel from one
+# ncu capture of this bench's workload (profiles/, the kernel's summary file)
+PAIR_TRAFFIC = {}
+
+
+def measured_peaks():
+    try:
+        return json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+    except (OSError, ValueError):
+        return {}
 
 
 def workload_config(extra=None):
@@ -424,17 +434,44 @@ def run_gb300(args, rank, world):
     # term (k_pair_cheb) or the plain pair sum (k_pair_r1), whichever took
     # more time; both do the same pair work per launch
     peak = ctx.probe_fp32_peak()
-    names = {"pair_cheb": "k_pair_cheb (CSR pair-list sum + fused FP64 Chebyshev term)",
-             "pair_fp32": "k_pair_r1 (CSR pair-list sum, one RHS)"}
+    row_width, stored = ctx.pair_storage()
+    if stored:
+        names = {"pair_cheb": "k_pair_cheb_t (stored pair tensors + fused FP64 Chebyshev term)",
+                 "pair_fp32": "k_pair_r1t (stored pair tensors, one RHS)"}
+    else:
+        names = {"pair_cheb": "k_pair_cheb (pair list, tensors per pair + fused Chebyshev term)",
+                 "pair_fp32": "k_pair_r1 (pair list, tensors per pair, one RHS)"}
     dom = max(names, key=lambda k: kt[k][0])
     pair_ms, pair_n = kt[dom]
     avg_pair_ms = pair_ms / max(pair_n, 1)
     flops_per_launch = n_pairs * (28 + 19 * 1)
+    # algorithmic bytes with stored tensors: 4 B entry + 16 B tensor per pair,
+    # and per bead 16 B force + 4 B row count + the FP64 vectors the kernel
+    # reads and writes (plain: f 24 + u 24; fused term: x0, x1, dw in, dw,
+    # x_{k+1} out 5 x 24, next forces 16)
+    per_bead = {"pair_fp32": 16 + 4 + 48, "pair_cheb": 16 + 4 + 120 + 16}
+    bytes_per_launch = n_pairs * 20 + N_BEADS * per_bead[dom]
     achieved = flops_per_launch / (avg_pair_ms * 1e-3) / 1e12
     others = {k: {"avg_launch_ms": kt[k][0] / max(kt[k][1], 1), "launches": kt[k][1],
                   "tflops": (flops_per_launch / (kt[k][0] / kt[k][1] * 1e-3) / 1e12)
                   if kt[k][1] else None} for k in names}
     ctx.close()
+    if stored:
+        gbs = bytes_per_launch / (avg_pair_ms * 1e-3) / 1e9
+        hbm_peak = measured_peaks().get("hbm_gbs")
+        roof = {"bound": "hbm", "kernel": names[dom], "achieved": gbs, "peak": hbm_peak,
+                "unit": "GB/s", "frac": gbs / hbm_peak if hbm_peak else None,
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy), of measured",
+                "bytes_per_launch": bytes_per_launch, "fp32_tflops": achieved,
+                "fp32_frac_of_live_peak": achieved / peak if peak else None}
+    else:
+        roof = {"bound": "fp32", "kernel": names[dom], "achieved": achieved, "peak": peak,
+                "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
+                "peak_source": "measured live: FP32 FMA-chain probe on this GPU "
+                               "(MEASURED_PEAKS.json has no FP32 figure)"}
+    roof.update({"flops_per_launch": flops_per_launch, "pairs": n_pairs, "row_width": row_width,
+                 "avg_launch_ms": avg_pair_ms, "launches_timed": pair_n,
+                 "pair_kernels": others, "traffic": PAIR_TRAFFIC.get(names[dom].split()[0])})
 
     result = {
         "metric": METRIC, "value": steps_per_s, "unit": "Brownian steps/s", "n_gpus": world,
@@ -456,14 +493,7 @@ def run_gb300(args, rank, world):
                  "surrogate_calls": state["surrogate_calls"],
                  "lanczos_calls": state["lanczos_calls"]},
         "bounds_every_step": per_step,
-        "roofline": {"bound": "fp32", "kernel": names[dom],
-                     "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                     "frac": achieved / peak if peak else None,
-                     "peak_source": "measured live: FP32 FMA-chain probe on this GPU "
-                                    "(MEASURED_PEAKS.json has no FP32 figure)",
-                     "flops_per_launch": flops_per_launch, "pairs": n_pairs,
-                     "avg_launch_ms": avg_pair_ms, "launches_timed": pair_n,
-                     "pair_kernels": others, "traffic": None},
+        "roofline": roof,
         "kernel_ms_in_timed_region": {k: v[0] for k, v in kt.items()},
         "gpu_launches": int(lc1 - lc0),
         "clocks": clk.summary(), "wall_s_timed": t_wall,

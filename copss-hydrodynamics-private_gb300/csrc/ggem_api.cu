@@ -239,6 +239,7 @@ int validate_and_setup(ggem_ctx *c) {
       // FP32 evaluation error stays within 1e-6 of the tensor scale
       c->use_poly = fit_tensor_poly(c->cst, s_max, c->poly_a, c->poly_b, &c->poly_x0,
                                     &c->poly_x1, c->poly_e, &c->poly_max_err) == 0;
+      c->use_pretensor = tensor_b_nonnegative(c->cst, s_max);
     }
   } else {
     return fail(c, GGEM_ERR_BAD_ARG, "nb_mode must be GGEM_NB_REFERENCE or GGEM_NB_CUTOFF");
@@ -400,7 +401,10 @@ extern "C" int ggem_build_cells(ggem_ctx *ctx) {
   // checks then share the list's single host readback
   const bool with_list = ctx->prm.precision == GGEM_FP32 && ctx->prm.nb_mode == GGEM_NB_CUTOFF;
   if (int rc = build_cells(ctx, with_list)) return rc;
-  if (with_list) return build_pair_list(ctx);
+  if (with_list) {
+    if (int rc = build_pair_list(ctx)) return rc;
+    return build_pair_tensors(ctx);
+  }
   return GGEM_OK;
 }
 

@@ -388,6 +388,7 @@ int build_cells(ggem_ctx *c, bool defer_flags) {
   }
   c->cells_built = false;
   c->list_built = false;
+  c->pretensor_ok = false;
   if (!defer_flags) {
     int flags = 0;
     if (int rc = read_error_flags(c, &flags)) return rc;

@@ -109,6 +109,20 @@ extern "C" int ggem_get_pair_count(const ggem_ctx *ctx, int64_t *count) {
   return GGEM_OK;
 }
 
+extern "C" int ggem_get_pair_storage(const ggem_ctx *ctx, int *row_width, int *tensors_stored) {
+  if (!ctx || !row_width || !tensors_stored) return GGEM_ERR_BAD_ARG;
+  if (!ctx->list_built) return GGEM_ERR_BAD_ARG;
+  *row_width = ctx->nb_w;
+  *tensors_stored = ctx->pretensor_ok ? 1 : 0;
+  return GGEM_OK;
+}
+
+extern "C" int ggem_set_pair_tensors(ggem_ctx *ctx, int enable) {
+  if (!ctx) return GGEM_ERR_BAD_ARG;
+  ctx->allow_pretensor = enable != 0;
+  return GGEM_OK;
+}
+
 extern "C" int ggem_set_kernel_timing(ggem_ctx *ctx, int enable) {
   if (!ctx) return GGEM_ERR_BAD_ARG;
   if (int rc = drain(ctx)) return rc;

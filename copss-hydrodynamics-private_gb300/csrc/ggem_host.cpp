@@ -150,6 +150,18 @@ int fit_tensor_table(const ggem_constants &c, double s_max, int nt, std::vector<
 // measured with FP32 arithmetic (fused multiply-adds, as on the device) on a
 // dense grid, relative to |A| + |B| s; the caller falls back to the table when
 // it is too large.
+// B(s) >= 0 on [0, s_max] (sampled densely in FP64): the condition under
+// which a pair's tensor packs as (A, sqrt(B) x)
+bool tensor_b_nonnegative(const ggem_constants &c, double s_max) {
+  const int m = 20000;
+  for (int k = 0; k <= m; ++k) {
+    double A, B, sc;
+    tensor_ab(c, s_max * k / m, &A, &B, &sc);
+    if (!(B >= 0.0)) return false;
+  }
+  return true;
+}
+
 int fit_tensor_poly(const ggem_constants &c, double s_max, float *a, float *b, float *x0,
                     float *x1, float *e_coef, double *max_err) {
   const int deg = kPolyDeg;

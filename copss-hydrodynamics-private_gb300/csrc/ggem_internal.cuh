@@ -134,6 +134,14 @@ struct ggem_ctx {
   // records of x_k in w_rec[rec_cur], those of x_{k+1} written to the other)
   ggem::DevBuf<float4> w_src;
   ggem::DevBuf<float4> w_rec[2];
+  // per-pair tensors (A, sqrt(B) x) in the list's row layout, computed once
+  // per configuration when B >= 0 on [0, rc^2]; forces then travel as one
+  // float4 per slot (w_f4, w_f4n for the fused Chebyshev chain)
+  bool use_pretensor = false;   // B >= 0 holds for these constants
+  bool allow_pretensor = true;  // ggem_set_pair_tensors
+  bool pretensor_ok = false;
+  ggem::DevBuf<float4> pair_ten;
+  ggem::DevBuf<float4> w_f4[2];
   int rec_cur = 0;
   int cheb_pred_terms = 0;             // degree the last adaptive Chebyshev needed
 
@@ -183,6 +191,7 @@ int fit_tensor_table(const ggem_constants &c, double s_max, int nt, std::vector<
                      double *max_err);
 int fit_tensor_poly(const ggem_constants &c, double s_max, float *a, float *b, float *x0,
                     float *x1, float *e_coef, double *max_err);
+bool tensor_b_nonnegative(const ggem_constants &c, double s_max);
 void tridiag_extremes(int k, const double *a, const double *b, double *lmin, double *lmax);
 void cheb_coeffs_host(int N, double da, double db, int method, double *coef);
 
@@ -200,6 +209,7 @@ int matvec_slots(ggem_ctx *c, int nrhs, const double *d_f_slot, double *d_u_slot
 int matvec_f32_staged(ggem_ctx *c, int nrhs, const double *d_f_slot, double *d_u_slot,
                       int self_mode);
 double self_coefficient(const ggem_ctx *c, int self_mode);
+int build_pair_tensors(ggem_ctx *c);
 int pair_cheb_term(ggem_ctx *c, bool records_fresh, const double *x0, const double *x1,
                    double *xm, double *dw, double two_da, double two_db, double coef,
                    int self_mode);

@@ -378,6 +378,131 @@ __global__ void __launch_bounds__(256) k_pair_cheb(
   }
 }
 
+// ---- precomputed pair tensors ---------------------------------------------
+//
+// Once per configuration (after the list build), every listed pair's tensor
+// is stored as t = (A, sqrt(B) x) in the list's row layout, valid when
+// B >= 0 on [0, rc^2] (checked at context creation).  A matvec then streams
+// 20 B per pair (entry + tensor, evict-first) and gathers a 16-byte force:
+// G f = A f + (x~ . f) x~ with x~ = sqrt(B) x, no position gathers and no
+// polynomial per pair and matvec.
+template <int CD, bool POLY>
+__global__ void __launch_bounds__(256) k_pair_tensor(
+    int64_t n, const float4 *__restrict__ pos32, const int32_t *__restrict__ cnt, int W,
+    const uint32_t *__restrict__ list, PolyAB P, const Rec32 *__restrict__ tab, float inv_ds,
+    float hx, float hy, float hz, float4 *__restrict__ ten) {
+  const int64_t gid = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / kGroup;
+  const int sub = (int)(threadIdx.x % kGroup);
+  if (gid >= n) return;
+  const int64_t s = gid;
+  const float4 pi = pos32[s];
+  const int64_t b = s * (int64_t)W, e = b + cnt[s];
+  for (int64_t m = b + sub; m < e; m += kGroup) {
+    const uint32_t en = __ldg(list + m);
+    const float4 pj = __ldg(pos32 + (en >> kCodeBits));
+    float ox, oy, oz;
+    decode_shift<CD>(en, hx, hy, hz, ox, oy, oz);
+    const float dx = (pj.x - pi.x) + ox, dy = (pj.y - pi.y) + oy, dz = (pj.z - pi.z) + oz;
+    const float s2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+    float A, B;
+    tensor_ab32<POLY>(s2, P, tab, inv_ds, A, B);
+    const float q = sqrtf(fmaxf(B, 0.f));
+    ten[m] = make_float4(A, q * dx, q * dy, q * dz);
+  }
+}
+
+// forces of one right-hand side as one float4 per slot (w = 0)
+__global__ void k_stage_f4(int64_t n, const double *__restrict__ f, float4 *__restrict__ f4) {
+  const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  f4[s] = make_float4((float)f[3 * s], (float)f[3 * s + 1], (float)f[3 * s + 2], 0.f);
+}
+
+// the pair loop over precomputed tensors (cf. pair_sum_r1)
+__device__ __forceinline__ PairSum pair_sum_t(int64_t s, bool act, int sub,
+                                              const float4 *__restrict__ f4,
+                                              const int32_t *__restrict__ cnt, int W,
+                                              const uint32_t *__restrict__ list,
+                                              const float4 *__restrict__ ten) {
+  const int64_t b = s * (int64_t)W, e = act ? b + cnt[s] : b;
+  float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
+  float2 bxy = make_float2(0.f, 0.f);
+  float bz = 0.f;
+  int blk = 0;
+  for (int64_t m = b + sub; m < e; m += kGroup) {
+    const uint32_t en = __ldcs(list + m);
+    const float4 t = __ldcs(ten + m);
+    const float4 fj = __ldg(f4 + (en >> kCodeBits));
+    const float2 txy = make_float2(t.y, t.z), fxy = make_float2(fj.x, fj.y);
+    const float2 p = __fmul2_rn(txy, fxy);
+    const float d = fmaf(t.w, fj.z, p.x + p.y);
+    bxy = __fadd2_rn(bxy, __ffma2_rn(make_float2(t.x, t.x), fxy, __fmul2_rn(make_float2(d, d), txy)));
+    bz += fmaf(t.x, fj.z, d * t.w);
+    if (++blk == 8) {
+      kahan_add(sx, cx, bxy.x);
+      kahan_add(sy, cy, bxy.y);
+      kahan_add(sz, cz, bz);
+      bxy = make_float2(0.f, 0.f);
+      bz = 0.f;
+      blk = 0;
+    }
+  }
+  kahan_add(sx, cx, bxy.x);
+  kahan_add(sy, cy, bxy.y);
+  kahan_add(sz, cz, bz);
+  PairSum r{sx, -cx, sy, -cy, sz, -cz};
+  group_ff(r.hx, r.lx);
+  group_ff(r.hy, r.ly);
+  group_ff(r.hz, r.lz);
+  return r;
+}
+
+// u = M f from precomputed tensors, single right-hand side
+__global__ void __launch_bounds__(256) k_pair_r1t(int64_t n, const float4 *__restrict__ f4,
+                                                  const int32_t *__restrict__ cnt, int W,
+                                                  const uint32_t *__restrict__ list,
+                                                  const float4 *__restrict__ ten, double self_c,
+                                                  const double *__restrict__ f,
+                                                  double *__restrict__ u) {
+  const int64_t gid = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / kGroup;
+  const int sub = (int)(threadIdx.x % kGroup);
+  const bool act = gid < n;
+  const int64_t s = act ? gid : n - 1;
+  const PairSum r = pair_sum_t(s, act, sub, f4, cnt, W, list, ten);
+  group_store(act, sub, s, r.hx, r.lx, r.hy, r.ly, r.hz, r.lz, self_c, f, u);
+}
+
+// one Chebyshev term from precomputed tensors (cf. k_pair_cheb); f4 holds
+// the FP32 forces of x1, next receives those of xm
+__global__ void __launch_bounds__(256) k_pair_cheb_t(
+    int64_t n, const float4 *__restrict__ f4, const int32_t *__restrict__ cnt, int W,
+    const uint32_t *__restrict__ list, const float4 *__restrict__ ten, double self_c,
+    double two_da, double two_db, double coef, const double *__restrict__ x0,
+    const double *__restrict__ x1, double *__restrict__ xm, double *__restrict__ dw,
+    float4 *__restrict__ next) {
+  const int64_t gid = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / kGroup;
+  const int sub = (int)(threadIdx.x % kGroup);
+  const bool act = gid < n;
+  const int64_t s = act ? gid : n - 1;
+  const PairSum r = pair_sum_t(s, act, sub, f4, cnt, W, list, ten);
+  if (!act) return;
+  float *nf = reinterpret_cast<float *>(next + s);
+  if (sub < 3) {
+    const float h = sub == 0 ? r.hx : (sub == 1 ? r.hy : r.hz);
+    const float l = sub == 0 ? r.lx : (sub == 1 ? r.ly : r.lz);
+    const int64_t k = 3 * s + sub;
+    const double xk = x1[k];
+    const double m = fma(self_c, xk, f2d_bits(h) + f2d_bits(l));
+    double v = two_db * xk + two_da * m;
+    v -= x0[k];
+    xm[k] = v;
+    dw[k] = dw[k] + coef * v;
+    nf[sub] = __double2float_rn(v);
+  } else {
+    nf[3] = 0.f;
+  }
+}
+
 // NR right-hand sides r0 .. r0+NR-1: f32 is [r][n] float4, u [r][n][3]
 template <int CD, bool POLY, int NR>
 __global__ void __launch_bounds__(256) k_pair_nr(
@@ -678,6 +803,17 @@ void launch_r1(ggem_ctx *c, const Rec32 *src, const double *f, double *u, double
 int launch_f32_r1(ggem_ctx *c, const double *f, double *u, double self_c) {
   const int64_t n = c->n;
   cudaError_t e;
+  if (c->pretensor_ok) {
+    if ((e = c->w_f4[0].ensure((size_t)n))) return cuda_fail(c, e, "pair forces");
+    k_stage_f4<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(n, f, c->w_f4[0].p);
+    if (int rc = check_launch(c, "pair forces")) return rc;
+    kt_start(c, kKPairF32);
+    const int64_t threads = n * kGroup;
+    k_pair_r1t<<<(unsigned)((threads + 255) / 256), 256, 0, c->stream>>>(
+        n, c->w_f4[0].p, c->nb_cnt.p, c->nb_w, c->nb_list.p, c->pair_ten.p, self_c, f, u);
+    kt_stop(c, kKPairF32);
+    return check_launch(c, "pair f32 r1 (tensors)");
+  }
   if ((e = c->w_src.ensure(2 * (size_t)n))) return cuda_fail(c, e, "pair records");
   Rec32 *src = reinterpret_cast<Rec32 *>(c->w_src.p);
   k_build_src<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(n, c->pos32.p, f, src);
@@ -787,6 +923,24 @@ int pair_cheb_term(ggem_ctx *c, bool records_fresh, const double *x0, const doub
   const int64_t n = c->n;
   if (n == 0) return GGEM_OK;
   cudaError_t e;
+  const double self_c0 = self_coefficient(c, self_mode);
+  if (c->pretensor_ok) {
+    if ((e = c->w_f4[0].ensure((size_t)n)) || (e = c->w_f4[1].ensure((size_t)n)))
+      return cuda_fail(c, e, "chebyshev forces");
+    float4 *cur = c->w_f4[c->rec_cur].p, *nxt = c->w_f4[c->rec_cur ^ 1].p;
+    if (!records_fresh) {
+      k_stage_f4<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(n, x1, cur);
+      if (int rc = check_launch(c, "chebyshev forces")) return rc;
+    }
+    kt_start(c, kKPairCheb);
+    const int64_t threads = n * kGroup;
+    k_pair_cheb_t<<<(unsigned)((threads + 255) / 256), 256, 0, c->stream>>>(
+        n, cur, c->nb_cnt.p, c->nb_w, c->nb_list.p, c->pair_ten.p, self_c0, two_da, two_db, coef,
+        x0, x1, xm, dw, nxt);
+    kt_stop(c, kKPairCheb);
+    c->rec_cur ^= 1;
+    return check_launch(c, "pair chebyshev term (tensors)");
+  }
   if ((e = c->w_rec[0].ensure(2 * (size_t)n)) || (e = c->w_rec[1].ensure(2 * (size_t)n)))
     return cuda_fail(c, e, "chebyshev records");
   Rec32 *cur = reinterpret_cast<Rec32 *>(c->w_rec[c->rec_cur].p);
@@ -808,6 +962,52 @@ int pair_cheb_term(ggem_ctx *c, bool records_fresh, const double *x0, const doub
   kt_stop(c, kKPairCheb);
   c->rec_cur ^= 1;
   return check_launch(c, "pair chebyshev term");
+}
+
+// the per-pair tensors of the current list (k_pair_tensor)
+int build_pair_tensors(ggem_ctx *c) {
+  c->pretensor_ok = false;
+  if (!c->use_pretensor || !c->allow_pretensor || !c->list_built) return GGEM_OK;
+  const int64_t n = c->n;
+  if (n == 0) {
+    c->pretensor_ok = true;
+    return GGEM_OK;
+  }
+  cudaError_t e = c->pair_ten.ensure((size_t)n * c->nb_w);
+  if (e) {
+    // no room for the tensors: the pair kernels evaluate them on the fly
+    cudaGetLastError();
+    return GGEM_OK;
+  }
+  const Grid &g = c->grid;
+  const int64_t threads = n * kGroup;
+  const unsigned grid = (unsigned)((threads + 255) / 256);
+  const bool cd2 = c->prm.cell_div == 2;
+  const Rec32 *tab = reinterpret_cast<const Rec32 *>(c->tab.p);
+  kt_start(c, kKListBuild);
+  if (c->use_poly) {
+    if (cd2)
+      k_pair_tensor<2, true><<<grid, 256, 0, c->stream>>>(n, c->pos32.p, c->nb_cnt.p, c->nb_w,
+                                                          c->nb_list.p, poly_of(c), tab, c->tab_inv_ds,
+                                                          g.h32[0], g.h32[1], g.h32[2], c->pair_ten.p);
+    else
+      k_pair_tensor<1, true><<<grid, 256, 0, c->stream>>>(n, c->pos32.p, c->nb_cnt.p, c->nb_w,
+                                                          c->nb_list.p, poly_of(c), tab, c->tab_inv_ds,
+                                                          g.h32[0], g.h32[1], g.h32[2], c->pair_ten.p);
+  } else {
+    if (cd2)
+      k_pair_tensor<2, false><<<grid, 256, 0, c->stream>>>(n, c->pos32.p, c->nb_cnt.p, c->nb_w,
+                                                           c->nb_list.p, poly_of(c), tab, c->tab_inv_ds,
+                                                           g.h32[0], g.h32[1], g.h32[2], c->pair_ten.p);
+    else
+      k_pair_tensor<1, false><<<grid, 256, 0, c->stream>>>(n, c->pos32.p, c->nb_cnt.p, c->nb_w,
+                                                           c->nb_list.p, poly_of(c), tab, c->tab_inv_ds,
+                                                           g.h32[0], g.h32[1], g.h32[2], c->pair_ten.p);
+  }
+  kt_stop(c, kKListBuild);
+  if (int rc = check_launch(c, "pair tensors")) return rc;
+  c->pretensor_ok = true;
+  return GGEM_OK;
 }
 
 double self_coefficient(const ggem_ctx *c, int self_mode) {

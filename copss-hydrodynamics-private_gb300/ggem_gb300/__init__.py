@@ -103,6 +103,8 @@ def lib():
         "ggem_brownian_displacement_dev": (i, [vp, i, i, d, d, d, i, vp, vp, P(ChebReport)]),
         "ggem_get_launch_count": (i, [vp, P(i64)]),
         "ggem_get_pair_count": (i, [vp, P(i64)]),
+        "ggem_get_pair_storage": (i, [vp, P(i), P(i)]),
+        "ggem_set_pair_tensors": (i, [vp, i]),
         "ggem_probe_fp32_peak": (i, [vp, P(d)]),
         "ggem_set_kernel_timing": (i, [vp, i]),
         "ggem_get_kernel_timing": (i, [vp, i, P(d), P(i64)]),
@@ -469,6 +471,15 @@ class Context:
 
     def set_kernel_timing(self, enable: bool):
         self._check(lib().ggem_set_kernel_timing(self.h, int(bool(enable))))
+
+    def set_pair_tensors(self, enable: bool):
+        self._check(lib().ggem_set_pair_tensors(self.h, 1 if enable else 0))
+
+    def pair_storage(self):
+        """(row width, whether per-pair tensors are stored)"""
+        w, t = C.c_int(), C.c_int()
+        self._check(lib().ggem_get_pair_storage(self.h, C.byref(w), C.byref(t)))
+        return w.value, bool(t.value)
 
     def kernel_timing(self, kernel: int):
         t, n = C.c_double(), C.c_int64()

@@ -21,6 +21,13 @@ int ggem_get_launch_count(const ggem_ctx *ctx, int64_t *count);
 /* ordered in-cutoff pairs of the current FP32 pair list (the work unit of
  * the pair kernel) */
 int ggem_get_pair_count(const ggem_ctx *ctx, int64_t *count);
+/* storage of the current FP32 pair list: row width (entries per row) and
+ * whether per-pair tensors are stored (1: the pair kernels stream 20 B per
+ * pair, 0: they evaluate the tensor per pair and matvec) */
+int ggem_get_pair_storage(const ggem_ctx *ctx, int *row_width, int *tensors_stored);
+/* allow (1, the default when B(s) >= 0 on [0, rc^2]) or forbid (0) stored
+ * pair tensors; takes effect at the next ggem_build_cells */
+int ggem_set_pair_tensors(ggem_ctx *ctx, int enable);
 /* dense FP32 FMA throughput of this device in TFLOP/s (FMA = 2 flops),
  * measured with CUDA events over a register-resident FMA chain kernel on the
  * context's stream */

@@ -454,3 +454,30 @@ def test_batched_64_rhs_chains_matvec_and_chebyshev():
         y_o, rep_o = O.cheb_inv_sqrt(op, xi[r], 50, lo / 1.05, hi * 1.05, 1e-3)
         assert rep_o.converged and rep_o.n_terms <= reps[r]["n_terms"]
         assert rel(y.reshape(64, -1)[r], y_o) <= 5e-3
+
+
+@pytest.mark.parametrize("stored", [True, False])
+def test_pair_tensor_storage_modes(stored):
+    """Stored per-pair tensors (streamed) and per-matvec tensors (computed)
+    give the same velocities within the FP32 contract, and the same
+    fused-Chebyshev displacement."""
+    xyz, L = suspension(4000, 0.1, 71)
+    box = O.make_box([0] * 3, [L] * 3, [1, 1, 1])
+    c = O.constants(alpha=0.5)
+    nb = O.neighbors_cutoff(box, xyz, 7.0)
+    f = np.random.default_rng(8).standard_normal((1, len(xyz), 3))
+    want = O.local_matvec(c, box, xyz, nb, f, O.SELF_BEAD, nthreads=8)
+    xi = np.random.default_rng(9).standard_normal(3 * len(xyz))
+    with G.Context(box_hi=(L,) * 3, rc=7.0, precision=G.FP32) as ctx:
+        ctx.set_pair_tensors(stored)
+        ctx.set_particles(xyz)
+        ctx.build_cells()
+        W, st = ctx.pair_storage()
+        assert st == stored and W % 8 == 0
+        got = ctx.local_matvec(f, G.SELF_BEAD)
+        lo, hi = ctx.lanczos_bounds(k=30, seed=3)
+        y, rep = ctx.cheb_inv_sqrt(xi, 12, lo / 1.05, hi * 1.05, 0.0, check_every=11)
+    assert rel(got, want) <= FP32_TOL
+    op = O.Operator(matvec=(c, box, xyz, nb, O.SELF_BEAD, 8))
+    y_o, _ = O.cheb_inv_sqrt(op, xi, 12, lo / 1.05, hi * 1.05, 0.0)
+    assert rel(y, y_o) <= 1e-5
