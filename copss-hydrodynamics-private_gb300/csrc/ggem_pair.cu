@@ -397,17 +397,24 @@ __global__ void __launch_bounds__(256) k_pair_tensor(
   const int64_t s = gid;
   const float4 pi = pos32[s];
   const int64_t b = s * (int64_t)W, e = b + cnt[s];
-  for (int64_t m = b + sub; m < e; m += kGroup) {
-    const uint32_t en = __ldg(list + m);
-    const float4 pj = __ldg(pos32 + (en >> kCodeBits));
-    float ox, oy, oz;
-    decode_shift<CD>(en, hx, hy, hz, ox, oy, oz);
-    const float dx = (pj.x - pi.x) + ox, dy = (pj.y - pi.y) + oy, dz = (pj.z - pi.z) + oz;
-    const float s2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-    float A, B;
-    tensor_ab32<POLY>(s2, P, tab, inv_ds, A, B);
-    const float q = sqrtf(fmaxf(B, 0.f));
-    ten[m] = make_float4(A, q * dx, q * dy, q * dz);
+  for (int64_t m = b + sub; m < e; m += 2 * kGroup) {
+    const bool two = m + kGroup < e;
+    const uint32_t en0 = __ldg(list + m), en1 = two ? __ldg(list + m + kGroup) : en0;
+    const float4 pj0 = __ldg(pos32 + (en0 >> kCodeBits)), pj1 = __ldg(pos32 + (en1 >> kCodeBits));
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      if (q == 1 && !two) break;
+      const uint32_t en = q ? en1 : en0;
+      const float4 pj = q ? pj1 : pj0;
+      float ox, oy, oz;
+      decode_shift<CD>(en, hx, hy, hz, ox, oy, oz);
+      const float dx = (pj.x - pi.x) + ox, dy = (pj.y - pi.y) + oy, dz = (pj.z - pi.z) + oz;
+      const float s2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+      float A, B;
+      tensor_ab32<POLY>(s2, P, tab, inv_ds, A, B);
+      const float w = sqrtf(fmaxf(B, 0.f));
+      __stcs(ten + m + q * kGroup, make_float4(A, w * dx, w * dy, w * dz));
+    }
   }
 }
 
@@ -418,27 +425,43 @@ __global__ void k_stage_f4(int64_t n, const double *__restrict__ f, float4 *__re
   f4[s] = make_float4((float)f[3 * s], (float)f[3 * s + 1], (float)f[3 * s + 2], 0.f);
 }
 
-// the pair loop over precomputed tensors (cf. pair_sum_r1)
+// the pair loop over precomputed tensors (cf. pair_sum_r1).  Four entries
+// per lane and iteration are loaded before any is used, so that each lane
+// keeps four streaming loads and four force gathers in flight; an entry past
+// the row end reads a zero tensor and adds exactly zero.
 __device__ __forceinline__ PairSum pair_sum_t(int64_t s, bool act, int sub,
                                               const float4 *__restrict__ f4,
                                               const int32_t *__restrict__ cnt, int W,
                                               const uint32_t *__restrict__ list,
                                               const float4 *__restrict__ ten) {
+  constexpr int U = 4;
   const int64_t b = s * (int64_t)W, e = act ? b + cnt[s] : b;
   float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
   float2 bxy = make_float2(0.f, 0.f);
   float bz = 0.f;
   int blk = 0;
-  for (int64_t m = b + sub; m < e; m += kGroup) {
-    const uint32_t en = __ldcs(list + m);
-    const float4 t = __ldcs(ten + m);
-    const float4 fj = __ldg(f4 + (en >> kCodeBits));
-    const float2 txy = make_float2(t.y, t.z), fxy = make_float2(fj.x, fj.y);
-    const float2 p = __fmul2_rn(txy, fxy);
-    const float d = fmaf(t.w, fj.z, p.x + p.y);
-    bxy = __fadd2_rn(bxy, __ffma2_rn(make_float2(t.x, t.x), fxy, __fmul2_rn(make_float2(d, d), txy)));
-    bz += fmaf(t.x, fj.z, d * t.w);
-    if (++blk == 8) {
+  for (int64_t m = b + sub; m < e; m += U * kGroup) {
+    uint32_t en[U];
+    float4 t[U], fj[U];
+#pragma unroll
+    for (int q = 0; q < U; ++q) {
+      const int64_t mq = m + q * kGroup;
+      const bool ok = mq < e;
+      en[q] = ok ? __ldcs(list + mq) : 0u;
+      t[q] = ok ? __ldcs(ten + mq) : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+#pragma unroll
+    for (int q = 0; q < U; ++q) fj[q] = __ldg(f4 + (en[q] >> kCodeBits));
+#pragma unroll
+    for (int q = 0; q < U; ++q) {
+      const float2 txy = make_float2(t[q].y, t[q].z), fxy = make_float2(fj[q].x, fj[q].y);
+      const float2 p = __fmul2_rn(txy, fxy);
+      const float d = fmaf(t[q].w, fj[q].z, p.x + p.y);
+      bxy = __fadd2_rn(bxy, __ffma2_rn(make_float2(t[q].x, t[q].x), fxy,
+                                       __fmul2_rn(make_float2(d, d), txy)));
+      bz += fmaf(t[q].x, fj[q].z, d * t[q].w);
+    }
+    if (++blk == 2) {  // every 8 entries into the compensated sums
       kahan_add(sx, cx, bxy.x);
       kahan_add(sy, cy, bxy.y);
       kahan_add(sz, cz, bz);
@@ -1060,3 +1083,78 @@ int matvec_f32_staged(ggem_ctx *c, int nrhs, const double *f, double *u, int sel
 }
 
 }  // namespace ggem
+
+
+using namespace ggem;
+
+extern "C" int ggem_autotune_pair_storage(ggem_ctx *ctx, int reps, double matvecs_per_build,
+                                          int *use_stored, double *ms_computed,
+                                          double *ms_stored) {
+  if (!ctx || reps < 1 || !(matvecs_per_build > 0) || !use_stored || !ms_computed || !ms_stored)
+    return GGEM_ERR_BAD_ARG;
+  if (ctx->prm.precision != GGEM_FP32 || !ctx->list_built)
+    return fail(ctx, GGEM_ERR_BAD_ARG, "autotune needs a built FP32 pair list");
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev != ctx->device) cudaSetDevice(ctx->device);
+  const int64_t n = ctx->n;
+  cudaError_t e;
+  if ((e = ctx->w_in.ensure((size_t)3 * std::max<int64_t>(n, 1))) ||
+      (e = ctx->w_out.ensure((size_t)3 * std::max<int64_t>(n, 1))))
+    return cuda_fail(ctx, e, "autotune buffers");
+  if (n > 0 && (e = cudaMemsetAsync(ctx->w_in.p, 0, sizeof(double) * 3 * n, ctx->stream)))
+    return cuda_fail(ctx, e, "autotune buffers");
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  const bool timing = ctx->timing;
+  ctx->timing = false;
+  auto time_matvecs = [&](double *ms) -> int {
+    if (int rc = matvec_slots(ctx, 1, ctx->w_in.p, ctx->w_out.p, GGEM_SELF_BEAD)) return rc;
+    cudaEventRecord(a, ctx->stream);
+    for (int r = 0; r < reps; ++r)
+      if (int rc = matvec_slots(ctx, 1, ctx->w_in.p, ctx->w_out.p, GGEM_SELF_BEAD)) return rc;
+    cudaEventRecord(b, ctx->stream);
+    cudaEventSynchronize(b);
+    float t = 0.f;
+    cudaEventElapsedTime(&t, a, b);
+    *ms = t / reps;
+    return GGEM_OK;
+  };
+  int rc = GGEM_OK;
+  double t_comp = 0.0, t_store = 1e30;
+  const bool allow = ctx->allow_pretensor;
+  // tensors evaluated per pair and matvec
+  ctx->pretensor_ok = false;
+  rc = time_matvecs(&t_comp);
+  if (!rc && ctx->use_pretensor) {
+    ctx->allow_pretensor = true;
+    cudaEventRecord(a, ctx->stream);
+    rc = build_pair_tensors(ctx);
+    cudaEventRecord(b, ctx->stream);
+    cudaEventSynchronize(b);
+    float t_pass = 0.f;
+    cudaEventElapsedTime(&t_pass, a, b);
+    if (!rc && ctx->pretensor_ok) {
+      double t_mv = 0.0;
+      rc = time_matvecs(&t_mv);
+      t_store = t_mv + t_pass / matvecs_per_build;
+    }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  ctx->timing = timing;
+  if (rc) {
+    ctx->allow_pretensor = allow;
+    if (dev != ctx->device) cudaSetDevice(dev);
+    return rc;
+  }
+  const bool stored = t_store < t_comp;
+  ctx->allow_pretensor = stored;
+  if (!stored) ctx->pretensor_ok = false;  // the stored tensors stay allocated but unused
+  *use_stored = stored ? 1 : 0;
+  *ms_computed = t_comp;
+  *ms_stored = ctx->use_pretensor ? t_store : -1.0;
+  if (dev != ctx->device) cudaSetDevice(dev);
+  return GGEM_OK;
+}

@@ -28,6 +28,14 @@ int ggem_get_pair_storage(const ggem_ctx *ctx, int *row_width, int *tensors_stor
 /* allow (1, the default when B(s) >= 0 on [0, rc^2]) or forbid (0) stored
  * pair tensors; takes effect at the next ggem_build_cells */
 int ggem_set_pair_tensors(ggem_ctx *ctx, int enable);
+/* autotune the pair storage on the current configuration (cells and list
+ * built, FP32): times `reps` single-RHS matvecs with tensors evaluated per
+ * pair and with stored tensors (plus the one tensor pass per build,
+ * amortised over matvecs_per_build matvecs) by CUDA events on the context's
+ * stream, keeps the faster variant for this context and reports both costs
+ * in ms per matvec (the stored one with its amortised pass) */
+int ggem_autotune_pair_storage(ggem_ctx *ctx, int reps, double matvecs_per_build,
+                               int *use_stored, double *ms_computed, double *ms_stored);
 /* dense FP32 FMA throughput of this device in TFLOP/s (FMA = 2 flops),
  * measured with CUDA events over a register-resident FMA chain kernel on the
  * context's stream */
