@@ -129,6 +129,16 @@ def lib():
         "ggem_surrogate_gradient": (i, [vp, vp, vp, i64, P(C.c_float), vp]),
         "ggem_surrogate_features": (i, [vp, d, vp]),
         "ggem_surrogate_interval": (i, [vp, vp, d, d, d, P(d), P(d)]),
+        "ggem_ensemble_create": (i, [P(Params), i, vp, P(vp)]),
+        "ggem_ensemble_destroy": (None, [vp]),
+        "ggem_ensemble_last_error": (C.c_char_p, [vp]),
+        "ggem_ensemble_set_particles_dev": (i, [vp, vp, vp]),
+        "ggem_ensemble_sizes": (i, [vp, P(i64), P(i64)]),
+        "ggem_ensemble_matvec_dev": (i, [vp, i, vp, vp, i]),
+        "ggem_ensemble_brownian_dev": (i, [vp, i, i, vp, vp, d, vp, vp, P(ChebReport)]),
+        "ggem_ensemble_intervals": (i, [vp, vp, vp, d, d, vp, vp]),
+        "ggem_ensemble_lanczos": (i, [vp, i, i, C.c_uint64, P(d), P(d)]),
+        "ggem_ensemble_autotune": (i, [vp, i, P(i), P(d)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -525,3 +535,92 @@ class Context:
     def philox_normals_dev(self, seed, stream, n, d_out):
         self._check(lib().ggem_philox_normals_dev(self.h, int(seed), int(stream), int(n),
                                                   C.c_void_p(d_out)))
+
+
+class Ensemble:
+    """K periodic suspensions as one block-diagonal operator
+    (include/ggem_ensemble.h).  Vectors are device arrays [bead][nrhs][3]
+    float64 in ensemble order (the suspensions' beads concatenated)."""
+
+    def __init__(self, box_lengths, *, alpha=0.5, mu=None, br0=1.0, point_type=POLYMER_BEAD,
+                 rc=7.0, cell_div=0, device=0):
+        p = default_params()
+        if mu is not None:
+            p.mu = float(mu)
+        p.alpha, p.br0, p.point_type = float(alpha), float(br0), int(point_type)
+        p.rc, p.cell_div, p.device = float(rc), int(cell_div), int(device)
+        p.precision, p.nb_mode = FP32, NB_CUTOFF
+        self.box = np.ascontiguousarray(box_lengths, dtype=np.float64)
+        self.K = len(self.box)
+        h = C.c_void_p()
+        rc_ = lib().ggem_ensemble_create(C.byref(p), self.K, _p(self.box), C.byref(h))
+        if rc_:
+            raise GGEMError(rc_, lib().ggem_strerror(rc_).decode())
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().ggem_ensemble_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, rc):
+        if rc:
+            raise GGEMError(rc, (lib().ggem_ensemble_last_error(self.h) or b"").decode())
+        return rc
+
+    def set_particles_dev(self, n, d_xyz):
+        self.n = np.ascontiguousarray(n, dtype=np.int64)
+        self._check(lib().ggem_ensemble_set_particles_dev(self.h, _p(self.n), C.c_void_p(d_xyz)))
+
+    def sizes(self):
+        b, q = C.c_int64(), C.c_int64()
+        self._check(lib().ggem_ensemble_sizes(self.h, C.byref(b), C.byref(q)))
+        return b.value, q.value
+
+    def matvec_dev(self, nrhs, d_f, d_u, self_mode=SELF_BEAD):
+        self._check(lib().ggem_ensemble_matvec_dev(self.h, int(nrhs), C.c_void_p(d_f),
+                                                   C.c_void_p(d_u), int(self_mode)))
+
+    def brownian_dev(self, nrhs, N, eig_min, eig_max, tol, d_xi, d_dw):
+        """(return code, reports [K][nrhs]); GGEM_ERR_CHEB_NOT_CONVERGED is
+        returned, not raised, so that the caller can fall back to Lanczos"""
+        lo = np.ascontiguousarray(eig_min, dtype=np.float64)
+        hi = np.ascontiguousarray(eig_max, dtype=np.float64)
+        reps = (ChebReport * (self.K * nrhs))()
+        rc = lib().ggem_ensemble_brownian_dev(self.h, int(nrhs), int(N), _p(lo), _p(hi),
+                                              float(tol), C.c_void_p(d_xi), C.c_void_p(d_dw),
+                                              reps)
+        if rc and rc != ERR_CHEB_NOT_CONVERGED:
+            self._check(rc)
+        return rc, [[reps[b * nrhs + r].as_dict() for r in range(nrhs)] for b in range(self.K)]
+
+    def intervals(self, sur, chain_fraction=None, margin_lo=0.0, margin_hi=0.0):
+        cf = np.zeros(self.K) if chain_fraction is None else \
+            np.ascontiguousarray(chain_fraction, dtype=np.float64)
+        lo, hi = np.zeros(self.K), np.zeros(self.K)
+        self._check(lib().ggem_ensemble_intervals(self.h, sur.h, _p(cf), float(margin_lo),
+                                                  float(margin_hi), _p(lo), _p(hi)))
+        return lo, hi
+
+    def lanczos(self, b, k=24, seed=7):
+        lo, hi = C.c_double(), C.c_double()
+        self._check(lib().ggem_ensemble_lanczos(self.h, int(b), int(k), int(seed), C.byref(lo),
+                                                C.byref(hi)))
+        return lo.value, hi.value
+
+    def autotune(self, nrhs=8):
+        t, ms = C.c_int(), C.c_double()
+        self._check(lib().ggem_ensemble_autotune(self.h, int(nrhs), C.byref(t), C.byref(ms)))
+        return t.value, ms.value

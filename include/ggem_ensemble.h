@@ -1,0 +1,81 @@
+/*
+ * ggem_ensemble.h -- many independent suspensions of uneven size through
+ * one set of launches.
+ *
+ * The reference runs one suspension per COPSS job (Copss::fixman_integrate,
+ * copss.C:1560-1686, with its own GGEMStokes, PointMesh and BrownianSystem).
+ * An ensemble holds K periodic suspensions with their own boxes and bead
+ * counts: each is built as an ordinary context (cell list, pair list,
+ * stored pair tensors), and their lists are concatenated into one
+ * block-diagonal operator, so that a matvec or a Chebyshev term of all K
+ * suspensions and up to 8 right-hand sides each is a single kernel launch.
+ * The unchecked stretch of Chebyshev terms is captured once as a CUDA graph
+ * and replayed.  Every series keeps its own eigen interval, coefficients,
+ * error estimators and stopping decision (brownian_system.C:967-1178).
+ *
+ * Vector layout: [bead][rhs][3] float64, beads in ensemble order (the K
+ * suspensions' particles concatenated, each in its caller order).
+ */
+#ifndef GGEM_ENSEMBLE_H
+#define GGEM_ENSEMBLE_H
+
+#include <stdint.h>
+
+#include "ggem_gb300.h"
+#include "ggem_surrogate.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GGEM_ENSEMBLE_MAX_RHS 8
+
+typedef struct ggem_ensemble ggem_ensemble;
+
+/* K suspensions sharing base's physics (mu, alpha, br0, point type, rc,
+ * cell_div, device); suspension b is the periodic cube [0, box_length[b])^3
+ * (FP32 pair sums, cut-off lists, FP64 recurrence) */
+int ggem_ensemble_create(const ggem_params *base, int k, const double *box_length,
+                         ggem_ensemble **out);
+void ggem_ensemble_destroy(ggem_ensemble *e);
+const char *ggem_ensemble_last_error(const ggem_ensemble *e);
+
+/* positions of all suspensions (device, [sum n][3], ensemble order) with
+ * n[b] beads in suspension b: cell lists, pair lists and pair tensors of
+ * every suspension, then the concatenated operator */
+int ggem_ensemble_set_particles_dev(ggem_ensemble *e, const int64_t *n, const double *d_xyz);
+/* total beads and ordered in-cutoff pairs of the current configuration */
+int ggem_ensemble_sizes(const ggem_ensemble *e, int64_t *beads, int64_t *pairs);
+
+/* u = M f for every suspension, nrhs <= 8, device vectors [bead][nrhs][3] */
+int ggem_ensemble_matvec_dev(ggem_ensemble *e, int nrhs, const double *d_f, double *d_u,
+                             int self_mode);
+
+/* Brownian displacements dw = M M^{-1/2} xi of every suspension and
+ * right-hand side: Chebyshev of at most N terms on [eig_min[b], eig_max[b]]
+ * with the adaptive schedule of ggem_brownian_displacement (check_every 0),
+ * err1 <= tol; rep[b * nrhs + r] per series.  Returns
+ * GGEM_ERR_CHEB_NOT_CONVERGED when some series failed (its dw is still
+ * written); the caller recomputes those intervals (Lanczos) and repeats. */
+int ggem_ensemble_brownian_dev(ggem_ensemble *e, int nrhs, int N, const double *eig_min,
+                               const double *eig_max, double tol, const double *d_xi,
+                               double *d_dw, ggem_cheb_report *rep);
+
+/* eigen intervals of all suspensions: features of each (pair-distance
+ * histograms on the GPU) and one batched forward pass of the network */
+int ggem_ensemble_intervals(ggem_ensemble *e, ggem_surrogate *s, const double *chain_fraction,
+                            double margin_lo, double margin_hi, double *eig_min,
+                            double *eig_max);
+/* Lanczos bounds of suspension b (the fallback) */
+int ggem_ensemble_lanczos(ggem_ensemble *e, int b, int k, uint64_t seed, double *eig_min,
+                          double *eig_max);
+
+/* autotune the ensemble kernels' block size on the current configuration
+ * (candidates 128, 256, 512 threads; CUDA-event timing of the fused term);
+ * the choice is kept and reported */
+int ggem_ensemble_autotune(ggem_ensemble *e, int nrhs, int *block_threads, double *ms_per_term);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

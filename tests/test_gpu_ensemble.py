@@ -1,0 +1,137 @@
+"""Uneven ensembles of suspensions through one block-diagonal operator,
+against the FP64 oracle of every suspension."""
+import numpy as np
+import pytest
+
+import ggem_gb300 as G
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+FP32_TOL = 1e-6
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    from ggem_gb300 import build as B
+    B.build()
+    O.build_oracle(with_ref=False)
+
+
+def rel(a, b):
+    return np.linalg.norm(np.asarray(a) - np.asarray(b)) / np.linalg.norm(np.asarray(b))
+
+
+def _ensemble(K, seed, n_range=(500, 3000)):
+    rng = np.random.default_rng(seed)
+    sus = []
+    for b in range(K):
+        n = int(np.exp(rng.uniform(np.log(n_range[0]), np.log(n_range[1]))))
+        phi = float(rng.uniform(0.02, 0.2))
+        xyz, L = G.make_suspension(seed * 1000 + b, n, phi)
+        sus.append((xyz, L))
+    return sus
+
+
+def _device(a):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).cuda()
+
+
+def test_ensemble_matvec_matches_every_suspension():
+    import torch
+    sus = _ensemble(6, 3)
+    R = 8
+    f = [np.random.default_rng(b).standard_normal((len(x), R, 3)) for b, (x, _) in enumerate(sus)]
+    with G.Ensemble([L for _, L in sus]) as ens:
+        d_xyz = _device(np.concatenate([x for x, _ in sus]))
+        ens.set_particles_dev([len(x) for x, _ in sus], d_xyz.data_ptr())
+        beads, pairs = ens.sizes()
+        assert beads == sum(len(x) for x, _ in sus)
+        d_f = _device(np.concatenate(f))
+        d_u = torch.empty_like(d_f)
+        ens.matvec_dev(R, d_f.data_ptr(), d_u.data_ptr(), G.SELF_BEAD)
+        u = d_u.cpu().numpy()
+    c = O.constants(alpha=0.5)
+    off = 0
+    n_pairs = 0
+    for b, (xyz, L) in enumerate(sus):
+        n = len(xyz)
+        box = O.make_box([0] * 3, [L] * 3, [1, 1, 1])
+        nb = O.neighbors_cutoff(box, xyz, 7.0)
+        n_pairs += nb.offsets[-1]
+        fb = np.transpose(f[b], (1, 0, 2))          # [r][n][3]
+        want = O.local_matvec(c, box, xyz, nb, fb, O.SELF_BEAD, nthreads=8)
+        got = np.transpose(u[off:off + n], (1, 0, 2))
+        assert rel(got, want) <= FP32_TOL, b
+        off += n
+    assert pairs == n_pairs
+
+
+def test_ensemble_brownian_matches_oracle_series():
+    import torch
+    sus = _ensemble(5, 7)
+    R = 8
+    xi = [np.random.default_rng(100 + b).standard_normal((len(x), R, 3))
+          for b, (x, _) in enumerate(sus)]
+    with G.Ensemble([L for _, L in sus]) as ens:
+        d_xyz = _device(np.concatenate([x for x, _ in sus]))
+        ens.set_particles_dev([len(x) for x, _ in sus], d_xyz.data_ptr())
+        block, ms = ens.autotune(R)
+        assert block in (128, 256, 512) and ms > 0
+        bounds = [ens.lanczos(b, k=40, seed=1) for b in range(len(sus))]
+        lo = np.array([x[0] for x in bounds]) / 1.05
+        hi = np.array([x[1] for x in bounds]) * 1.05
+        d_xi = _device(np.concatenate(xi))
+        d_dw = torch.empty_like(d_xi)
+        results = []
+        for _ in range(3):  # the second and third calls replay the captured terms
+            rc, reps = ens.brownian_dev(R, 50, lo, hi, 1e-3, d_xi.data_ptr(), d_dw.data_ptr())
+            assert rc == 0
+            results.append((d_dw.cpu().numpy(), reps))
+    c = O.constants(alpha=0.5)
+    for dw, reps in results:
+        off = 0
+        for b, (xyz, L) in enumerate(sus):
+            n = len(xyz)
+            box = O.make_box([0] * 3, [L] * 3, [1, 1, 1])
+            nb = O.neighbors_cutoff(box, xyz, 7.0)
+            op = O.Operator(matvec=(c, box, xyz, nb, O.SELF_BEAD, 8))
+            for r in (0, 5):
+                assert reps[b][r]["converged"] and reps[b][r]["err1"] <= 1e-3
+                y_o, rep_o = O.cheb_inv_sqrt(op, xi[b][:, r, :].reshape(-1), 50, lo[b], hi[b],
+                                             1e-3)
+                dw_o = O.local_matvec(c, box, xyz, nb, y_o.reshape(1, n, 3), O.SELF_BEAD,
+                                      nthreads=8)
+                assert rel(dw[off:off + n, r, :], dw_o[0]) <= 5e-3, (b, r)
+            off += n
+
+
+def test_ensemble_intervals_from_the_network():
+    """All intervals from one batched forward pass; series the check rejects
+    fall back to Lanczos."""
+    import torch
+    from ggem_gb300 import surrogate_data as SD
+    loaded = SD.load_default()
+    if loaded is None:
+        pytest.skip("no trained network shipped")
+    sur, margins, _ = loaded
+    sus = _ensemble(8, 13, n_range=(1000, 5000))
+    R = 8
+    with G.Ensemble([L for _, L in sus]) as ens:
+        d_xyz = _device(np.concatenate([x for x, _ in sus]))
+        ens.set_particles_dev([len(x) for x, _ in sus], d_xyz.data_ptr())
+        lo, hi = ens.intervals(sur, None, margins[0], margins[1])
+        assert np.all(lo > 0) and np.all(hi > lo)
+        xi = np.random.default_rng(5).standard_normal((sum(len(x) for x, _ in sus), R, 3))
+        d_xi = _device(xi)
+        d_dw = torch.empty_like(d_xi)
+        rc, reps = ens.brownian_dev(R, 50, lo, hi, 1e-3, d_xi.data_ptr(), d_dw.data_ptr())
+        failed = [b for b in range(len(sus)) if not all(r["converged"] for r in reps[b])]
+        for b in failed:
+            lo[b], hi[b] = (v * f for v, f in zip(ens.lanczos(b, 24, 7), (1 / 1.05, 1.05)))
+        if failed:
+            rc, reps = ens.brownian_dev(R, 50, lo, hi, 1e-3, d_xi.data_ptr(), d_dw.data_ptr())
+        assert rc == 0
+        assert len(failed) <= 2
+        assert all(r["converged"] for rb in reps for r in rb)
+    sur.close()
