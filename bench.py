@@ -436,6 +436,7 @@ def run_gb300(args, rank, world):
 
     # ---- polymer suspension, 64 batched noise right-hand sides ----------
     poly = None if args.skip_polymer else polymer_leg(G, torch, dev, flush, peak_fn=None)
+    ens_res = None if args.skip_ensemble else ensemble_leg(G, torch, dev, flush, sur, sur_margins)
 
     # ---- roofline of the dominant kernel --------------------------------
     # the dominant kernel of the timed steps: the fused pair-sum + Chebyshev
@@ -506,6 +507,7 @@ def run_gb300(args, rank, world):
         "gpu_launches": int(lc1 - lc0),
         "clocks": clk.summary(), "wall_s_timed": t_wall,
         "polymer_64rhs": poly,
+        "ensemble_512x8": ens_res,
     }
     if rank == 0 and not args.no_cpu_baseline and world == 1:
         result["cpu_baseline"] = cpu_baseline(xyz, L, state["bounds"], args)
@@ -593,6 +595,112 @@ def polymer_leg(G, torch, dev, flush, peak_fn=None, reps=5):
 
 
 # --------------------------------------------------------------------------
+# uneven ensemble: 512 suspensions, 8 noise right-hand sides each
+# --------------------------------------------------------------------------
+ENS_K, ENS_NRHS = 512, 8
+
+
+def ensemble_leg(G, torch, dev, flush, sur, margins, reps=3):
+    """512 periodic suspensions, N log-uniform in [500, 20000], phi uniform
+    in [0.02, 0.2], 8 noise vectors each, through one block-diagonal
+    operator: build, autotune, eigen intervals (one batched forward pass of
+    the network vs Lanczos(24) per suspension), and the Brownian step of
+    all 4096 series (device resident, L2 flushed before each timed step)."""
+    from concurrent.futures import ThreadPoolExecutor
+    rng = np.random.default_rng(SEED + 11)
+    ns = np.exp(rng.uniform(np.log(500), np.log(20000), ENS_K)).astype(np.int64)
+    phis = rng.uniform(0.02, 0.2, ENS_K)
+    with ThreadPoolExecutor(16) as ex:
+        sus = list(ex.map(lambda b: G.make_suspension(SEED * 7 + b, int(ns[b]), float(phis[b])),
+                          range(ENS_K)))
+    t0 = time.perf_counter()
+    ens = G.Ensemble([L for _, L in sus], device=dev)
+    d_xyz = torch.from_numpy(np.concatenate([x for x, _ in sus]).reshape(-1)).cuda()
+    torch.cuda.synchronize()
+    ens.set_particles_dev(ns, d_xyz.data_ptr())
+    t_build = time.perf_counter() - t0
+    beads, pairs = ens.sizes()
+    block, ms_term = ens.autotune(ENS_NRHS)
+    t0 = time.perf_counter()
+    lz = [ens.lanczos(b, 24, 7) for b in range(ENS_K)]
+    t_lz = time.perf_counter() - t0
+    lo = np.array([x[0] for x in lz]) / 1.05
+    hi = np.array([x[1] for x in lz]) * 1.05
+    t_sur = None
+    if sur is not None:
+        t0 = time.perf_counter()
+        lo, hi = ens.intervals(sur, None, margins[0], margins[1])
+        t_sur = time.perf_counter() - t0
+    xi = torch.randn(beads * ENS_NRHS * 3, dtype=torch.float64, device="cuda")
+    dw = torch.empty_like(xi)
+    torch.cuda.synchronize()
+    fallbacks = 0
+
+    def step():
+        nonlocal fallbacks
+        rc, rp = ens.brownian_dev(ENS_NRHS, CHEB_MAX, lo, hi, CHEB_TOL, xi.data_ptr(),
+                                  dw.data_ptr())
+        if rc:
+            for b in range(ENS_K):  # rejected intervals: Lanczos, then again
+                if not all(r["converged"] for r in rp[b]):
+                    fallbacks += 1
+                    l_, h_ = ens.lanczos(b, 24, 7)
+                    lo[b], hi[b] = l_ / 1.05, h_ * 1.05
+            rc, rp = ens.brownian_dev(ENS_NRHS, CHEB_MAX, lo, hi, CHEB_TOL, xi.data_ptr(),
+                                      dw.data_ptr())
+        return rc, rp
+
+    for _ in range(2):
+        step()
+    ts, terms, ok = [], [], True
+    for _ in range(reps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        rc, rp = step()
+        torch.cuda.synchronize()
+        ts.append(time.perf_counter() - t0)
+        ok = ok and rc == 0
+        terms.append(max(r["n_terms"] for rb in rp for r in rb))
+    f = torch.randn(beads * ENS_NRHS * 3, dtype=torch.float64, device="cuda")
+    u = torch.empty_like(f)
+    ens.matvec_dev(ENS_NRHS, f.data_ptr(), u.data_ptr())
+    mv = []
+    for _ in range(5):
+        flush.zero_()
+        torch.cuda.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        b_ = torch.cuda.Event(enable_timing=True)
+        a.record()
+        ens.matvec_dev(ENS_NRHS, f.data_ptr(), u.data_ptr())
+        b_.record()
+        b_.synchronize()
+        mv.append(a.elapsed_time(b_))
+    ens.close()
+    step_s = float(np.mean(ts))
+    # algorithmic bytes of one fused term: 20 B per pair (entry + tensor) and
+    # per bead 8 x (16 B force + 3 x 8 B x0, x1, dw in, dw, x_{k+1} out, 16 B
+    # next force) + 4 B row count
+    term_bytes = pairs * 20 + beads * (ENS_NRHS * (16 + 5 * 24 + 16) + 4)
+    peak = measured_peaks().get("hbm_gbs")
+    return {"workload": f"{ENS_K} periodic suspensions, N log-uniform in [500, 20000] "
+                        f"(sum {beads}), phi uniform in [0.02, 0.2], {ENS_NRHS} noise vectors each",
+            "beads": beads, "pairs": pairs, "build_s": t_build,
+            "autotune": {"block_threads": block, "ms_per_term": ms_term},
+            "intervals_s": {"network_one_batch": t_sur, "lanczos24_per_suspension": t_lz},
+            "lanczos_fallbacks": fallbacks,
+            "brownian_step_ms": step_s * 1e3,
+            "series_steps_per_s": ENS_K * ENS_NRHS / step_s,
+            "cheb_terms_max": terms, "converged": ok,
+            "matvec_8rhs_ms": float(np.mean(mv)),
+            "term_kernel": {"kernel": "k_ens_pair<true> (stored tensors, 8 lanes per slot)",
+                            "bytes": term_bytes, "ms": ms_term,
+                            "gbs": term_bytes / (ms_term * 1e-3) / 1e9,
+                            "frac_of_hbm": (term_bytes / (ms_term * 1e-3) / 1e9 / peak)
+                            if peak else None}}
+
+
+# --------------------------------------------------------------------------
 # CPU baseline / reference arm: the FP64 oracle on the host cores
 # --------------------------------------------------------------------------
 def _oracle_step(O, c, box, xyz, xi, lo, hi, nthreads):
@@ -665,6 +773,7 @@ def main():
     ap.add_argument("--reference-max-steps", type=int, default=6)
     ap.add_argument("--skip-polymer", action="store_true")
     ap.add_argument("--no-surrogate", action="store_true")
+    ap.add_argument("--skip-ensemble", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
 
