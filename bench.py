@@ -153,6 +153,26 @@ class ClockSampler:
 
 
 # --------------------------------------------------------------------------
+# replicas: every rank runs its own suspension, no collective on the data path
+# --------------------------------------------------------------------------
+def replica_throughput(ms_step, world, device="cuda"):
+    """(max-over-ranks step time in ms, whole-job steps/s of `world`
+    replicas); the only collective is this one scalar reduction."""
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([float(ms_step)], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_step = float(t.item())
+    return ms_step, 1e3 / ms_step * world
+
+
+def replica_seed(rank):
+    """each rank's suspension is an independent replica"""
+    return SEED + rank
+
+
+# --------------------------------------------------------------------------
 # GB300 arm
 # --------------------------------------------------------------------------
 def run_gb300(args, rank, world):
@@ -166,7 +186,7 @@ def run_gb300(args, rank, world):
     L_lib = G.lib()
     import ctypes as C
 
-    xyz, L = G.make_suspension(SEED + rank, N_BEADS, PHI)
+    xyz, L = G.make_suspension(replica_seed(rank), N_BEADS, PHI)
     box = (L, L, L)
 
     def make_ctx(prec, div=1):
@@ -287,12 +307,7 @@ def run_gb300(args, rank, world):
           ((G.KERNEL_PAIR_FP32, "pair_fp32"), (G.KERNEL_PAIR_CHEB, "pair_cheb"),
            (G.KERNEL_CHEB_TERM, "cheb_term"), (G.KERNEL_LIST_BUILD, "list_build"))}
     ctx.set_kernel_timing(False)
-    ms_step = float(np.mean(ts))
-    if world > 1:
-        t = torch.tensor([ms_step], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms_step = float(t.item())
-    steps_per_s = 1e3 / ms_step * world  # replicas: every rank runs its own suspension
+    ms_step, steps_per_s = replica_throughput(float(np.mean(ts)), world)
     n_pairs = ctx.pair_count()
     reps = state["reports"][-args.steps:]
 
