@@ -144,6 +144,10 @@ struct ggem_ctx {
   ggem::DevBuf<float4> w_f4[2];
   int rec_cur = 0;
   int cheb_pred_terms = 0;             // degree the last adaptive Chebyshev needed
+  // polymer bonds as a per-bead adjacency (caller ids, bond order)
+  int64_t bond_n = -1;                 // particle count the bonds were set for
+  ggem::DevBuf<int64_t> bond_off;      // [n+1]
+  ggem::DevBuf<int32_t> bond_nbr;      // [2m]
 
   // scan scratch (one per recursion level)
   std::vector<ggem::DevBuf<int64_t> *> scan_scratch;

@@ -29,6 +29,7 @@ ERR_NOT_SPD, ERR_CHEB_NOT_CONVERGED, ERR_SURROGATE_REJECTED = -5, -6, -7
 ERR_OUT_OF_DOMAIN, ERR_NO_DEVICE, ERR_OOM, ERR_INVALID_RANGE = -8, -9, -10, -11
 KERNEL_PAIR_FP32, KERNEL_PAIR_FP64, KERNEL_CHEB_TERM, KERNEL_LIST_BUILD, KERNEL_PAIR_CHEB = (
     0, 1, 2, 3, 4)
+SPRING_WLS, SPRING_FENE, SPRING_UD, SPRING_LHS = 0, 1, 2, 3
 
 
 class Params(C.Structure):
@@ -129,6 +130,11 @@ def lib():
         "ggem_surrogate_gradient": (i, [vp, vp, vp, i64, P(C.c_float), vp]),
         "ggem_surrogate_features": (i, [vp, d, vp]),
         "ggem_surrogate_interval": (i, [vp, vp, d, d, d, P(d), P(d)]),
+        "ggem_ev_gaussian_forces": (i, [vp, d, d, vp, i]),
+        "ggem_ev_gaussian_forces_dev": (i, [vp, d, d, vp, i]),
+        "ggem_set_bonds": (i, [vp, i64, vp]),
+        "ggem_spring_forces": (i, [vp, i, d, d, vp, i]),
+        "ggem_spring_forces_dev": (i, [vp, i, d, d, vp, i]),
         "ggem_ensemble_create": (i, [P(Params), i, vp, P(vp)]),
         "ggem_ensemble_destroy": (None, [vp]),
         "ggem_ensemble_last_error": (C.c_char_p, [vp]),
@@ -514,6 +520,24 @@ class Context:
         lo, hi = C.c_double(), C.c_double()
         self._check(lib().ggem_lanczos_bounds(self.h, int(k), int(seed), C.byref(lo), C.byref(hi)))
         return lo.value, hi.value
+
+    def ev_gaussian_forces(self, c1, c2, f=None):
+        """excluded-volume forces [n][3], added to f when given"""
+        out = np.zeros((self.n, 3)) if f is None else _f64(f).reshape(self.n, 3).copy()
+        self._check(lib().ggem_ev_gaussian_forces(self.h, float(c1), float(c2), _p(out),
+                                                  0 if f is None else 1))
+        return out
+
+    def set_bonds(self, bonds):
+        b = np.ascontiguousarray(bonds, dtype=np.int64).reshape(-1, 2)
+        self._check(lib().ggem_set_bonds(self.h, len(b), _p(b)))
+
+    def spring_forces(self, kind, c1, Ls, f=None):
+        """bonded spring forces [n][3], added to f when given"""
+        out = np.zeros((self.n, 3)) if f is None else _f64(f).reshape(self.n, 3).copy()
+        self._check(lib().ggem_spring_forces(self.h, int(kind), float(c1), float(Ls), _p(out),
+                                             0 if f is None else 1))
+        return out
 
     def surrogate_features(self, chain_fraction=0.0) -> np.ndarray:
         f = np.zeros(SUR_FEATURES, dtype=np.float32)

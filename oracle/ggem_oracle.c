@@ -918,3 +918,66 @@ void orc_philox_normals(uint64_t seed, uint64_t stream, int64_t n, double *out) 
     if (2 * p + 1 < n) out[2 * p + 1] = r * sin(two_pi * u2);
   }
 }
+
+
+/* ---- force fixes ------------------------------------------------------- */
+
+/* fix/fix_base.C:150-162: -c1 c2 exp(-c2 |r|^2) r, |r| from its norm */
+void orc_ev_gaussian(const orc_box *b, int64_t n, const double *xyz, const orc_nblist *nb,
+                     double c1, double c2, double *f) {
+  for (int64_t i = 0; i < n; ++i) {
+    double acc[3] = {0.0, 0.0, 0.0};
+    for (int64_t k = nb->offsets[i]; k < nb->offsets[i + 1]; ++k) {
+      const int64_t j = nb->ids[k];
+      double r[3];
+      orc_point_vector(b, xyz + 3 * i, xyz + 3 * j, r);
+      const double len = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+      const double w = -c1 * c2 * exp(-c2 * len * len);
+      for (int d = 0; d < 3; ++d) acc[d] += w * r[d];
+    }
+    for (int d = 0; d < 3; ++d) f[3 * i + d] += acc[d];
+  }
+}
+
+/* fix/fix_base.C:55-148, tol = 1e-3 (fix/fix_base.h:50) */
+void orc_spring_force(int kind, const double R_ij[3], double c1, double Ls, double F[3]) {
+  const double tol = 1e-3;
+  const double R = sqrt(R_ij[0] * R_ij[0] + R_ij[1] * R_ij[1] + R_ij[2] * R_ij[2]);
+  double scale;
+  if (kind == 0) {         /* worm-like spring, :55-74 */
+    const double ratio = R / Ls;
+    double v0 = 1.0 - ratio;
+    if (fabs(v0) < tol) v0 = v0 / fabs(v0) * tol;
+    scale = c1 * (1.0 / (v0 * v0) - 1.0 + 4.0 * ratio) / R;
+  } else if (kind == 1) {  /* FENE, :77-96 */
+    const double ratio = R / Ls;
+    double v0 = 1.0 - ratio * ratio;
+    if (fabs(v0) < tol) v0 = v0 / fabs(v0) * tol * tol;
+    scale = c1 * ratio / v0 / R;
+  } else if (kind == 2) {  /* Underhill-Doyle, :99-124 */
+    const double ratio = R / Ls, r2 = ratio * ratio, cc = c1 * c1;
+    const double a1 = 1.0, a2 = -7.0 * c1, a3 = 3.0 / 32.0 - 0.75 * c1 - 6.0 * cc;
+    const double a4 = (13.0 / 32.0 + 0.8172 * c1 - 14.79 * cc) / (1.0 - 4.225 * c1 + 4.87 * cc);
+    const double T4 = 1.0 - r2, T2 = 1.0 / T4, T1 = T2 / T4;
+    scale = (a1 * T1 + a2 * T2 + a3 + a4 * T4) / R;
+  } else {                 /* linear Hookean spring, :127-148 */
+    scale = Ls * (R - c1) / R;
+  }
+  for (int d = 0; d < 3; ++d) F[d] = scale * R_ij[d];
+}
+
+/* fix/fix_point_wls.C:66-92 */
+void orc_spring_forces(const orc_box *b, int64_t n, const double *xyz, int64_t m,
+                       const int64_t *bonds, int kind, double c1, double Ls, double *f) {
+  (void)n;
+  for (int64_t k = 0; k < m; ++k) {
+    const int64_t i = bonds[2 * k], j = bonds[2 * k + 1];
+    double R[3], F[3];
+    orc_point_vector(b, xyz + 3 * i, xyz + 3 * j, R);
+    orc_spring_force(kind, R, c1, Ls, F);
+    for (int d = 0; d < 3; ++d) {
+      f[3 * i + d] += F[d];
+      f[3 * j + d] -= F[d];
+    }
+  }
+}

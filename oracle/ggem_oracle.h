@@ -161,6 +161,21 @@ void orc_std_normal_vector(uint64_t seed, int64_t skip_vectors, int64_t n,
  * checking the device noise generator bit-for-bit */
 void orc_philox_normals(uint64_t seed, uint64_t stream, int64_t n, double *out);
 
+/* excluded-volume Gaussian force, FixPointGaussianDNA::compute
+ * (fix/fix_point_gaussian_dna.C:69-84) with FixBase::gaussian_force
+ * (fix/fix_base.C:150-162): f_i += sum over nb(i) of -c1 c2 exp(-c2 r^2) r_ij,
+ * r_ij = point_vector(x_i, x_j) (minimum image) */
+void orc_ev_gaussian(const orc_box *b, int64_t n, const double *xyz, const orc_nblist *nb,
+                     double c1, double c2, double *f);
+/* the FixBase spring laws (fix/fix_base.C:55-148): the force on bead i from
+ * R_ij = x_j - x_i; kind 0 WLS, 1 FENE, 2 Underhill-Doyle, 3 LHS (c1 = l0,
+ * Ls = k0) */
+void orc_spring_force(int kind, const double R_ij[3], double c1, double Ls, double F[3]);
+/* FixPointWLS::compute (fix/fix_point_wls.C:66-92) for any law: bonds m x 2,
+ * F_ij to bead bonds[k][0] and -F_ij to bonds[k][1], in bond order */
+void orc_spring_forces(const orc_box *b, int64_t n, const double *xyz, int64_t m,
+                       const int64_t *bonds, int kind, double c1, double Ls, double *f);
+
 #ifdef __cplusplus
 }
 #endif

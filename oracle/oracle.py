@@ -115,6 +115,9 @@ def lib():
         L.orc_power_iteration.restype = C.c_int
         L.orc_std_normal_vector.argtypes = [C.c_uint64, i64, i64, d, d, vp]
         L.orc_philox_normals.argtypes = [C.c_uint64, C.c_uint64, i64, vp]
+        L.orc_ev_gaussian.argtypes = [C.POINTER(Box), i64, vp, C.POINTER(NbList), d, d, vp]
+        L.orc_spring_force.argtypes = [C.c_int, vp, d, d, vp]
+        L.orc_spring_forces.argtypes = [C.POINTER(Box), i64, vp, i64, vp, C.c_int, d, d, vp]
         _lib = L
     return _lib
 
@@ -378,3 +381,22 @@ def philox_normals(seed, stream, n):
     out = np.zeros(n)
     lib().orc_philox_normals(int(seed), int(stream), int(n), _p(out))
     return out
+
+
+def ev_gaussian(box: Box, xyz, nbrs: "Neighbors", c1, c2) -> np.ndarray:
+    """excluded-volume forces [n][3] (fix_point_gaussian_dna.C:69-84)"""
+    xyz = _f64(xyz)
+    f = np.zeros_like(xyz)
+    lib().orc_ev_gaussian(C.byref(box), len(xyz), _p(xyz), C.byref(nbrs.nb), float(c1),
+                          float(c2), _p(f))
+    return f
+
+
+def spring_forces(box: Box, xyz, bonds, kind, c1, Ls) -> np.ndarray:
+    """bonded spring forces [n][3] (fix_point_wls.C:66-92 with the law `kind`)"""
+    xyz = _f64(xyz)
+    b = np.ascontiguousarray(bonds, dtype=np.int64)
+    f = np.zeros_like(xyz)
+    lib().orc_spring_forces(C.byref(box), len(xyz), _p(xyz), len(b), _p(b), int(kind),
+                            float(c1), float(Ls), _p(f))
+    return f

@@ -481,3 +481,46 @@ def test_pair_tensor_storage_modes(stored):
     op = O.Operator(matvec=(c, box, xyz, nb, O.SELF_BEAD, 8))
     y_o, _ = O.cheb_inv_sqrt(op, xi, 12, lo / 1.05, hi * 1.05, 0.0)
     assert rel(y, y_o) <= 1e-5
+
+
+@pytest.mark.parametrize("mode", ["cutoff", "reference"])
+def test_excluded_volume_forces_match_oracle(mode):
+    xyz, L = suspension(3000, 0.1, 81)
+    box = O.make_box([0] * 3, [L] * 3, [1, 1, 1])
+    c1, c2 = 0.37, 0.21
+    if mode == "cutoff":
+        nb = O.neighbors_cutoff(box, xyz, 7.0)
+        kw = dict(rc=7.0, precision=G.FP64)
+    else:
+        nm = 12
+        sre = 0.5 * L / nm + 8.0 + 1e-3
+        nb = O.neighbors_reference(box, O.make_mesh(nm, nm, nm, sre), xyz)
+        kw = dict(nb_mode=G.NB_REFERENCE, n_mesh=(nm,) * 3, search_radius_e=sre,
+                  precision=G.FP64)
+    want = O.ev_gaussian(box, xyz, nb, c1, c2)
+    with G.Context(box_hi=(L,) * 3, **kw) as ctx:
+        ctx.set_particles(xyz)
+        ctx.build_cells()
+        got = ctx.ev_gaussian_forces(c1, c2)
+        base = np.ones_like(got)
+        got2 = ctx.ev_gaussian_forces(c1, c2, f=base)
+    assert rel(got, want) <= 1e-12
+    assert rel(got2 - base, want) <= 1e-12
+
+
+@pytest.mark.parametrize("kind", [G.SPRING_WLS, G.SPRING_FENE, G.SPRING_UD, G.SPRING_LHS])
+def test_spring_forces_match_oracle(kind):
+    n_chains, beads = 60, 20
+    xyz, L = G.make_chains(17, n_chains, beads, 2.0, 0.05)
+    bonds = np.array([[c * beads + k, c * beads + k + 1] for c in range(n_chains)
+                      for k in range(beads - 1)])
+    box = O.make_box([0] * 3, [L] * 3, [1, 1, 1])
+    params = {G.SPRING_WLS: (0.25, 4.0), G.SPRING_FENE: (0.8, 3.0), G.SPRING_UD: (0.05, 5.0),
+              G.SPRING_LHS: (1.9, 2.5)}[kind]
+    want = O.spring_forces(box, xyz, bonds, kind, *params)
+    with G.Context(box_hi=(L,) * 3, rc=7.0, precision=G.FP32) as ctx:
+        ctx.set_particles(xyz)
+        ctx.build_cells()
+        ctx.set_bonds(bonds)
+        got = ctx.spring_forces(kind, *params)
+    assert rel(got, want) <= 1e-12

@@ -280,3 +280,33 @@ def test_bf16_rounding_is_nearest_even():
     want = np.array([1.0, 1.0, 1.0 + 4 * 2 ** -8, 1.0, -2.5, 0.0], dtype=np.float32)
     # 1 + 2^-8 is a tie between 1 and 1 + 2^-7: even mantissa -> 1
     assert np.array_equal(got, want)
+
+
+def test_force_oracle_laws_and_action_reaction():
+    """The spring laws of the force fixes (fix_base.C:55-148) on known
+    points, and Newton's third law of the pairwise oracle forces."""
+    import oracle as O
+    O.build_oracle(with_ref=False)
+    box = O.make_box([0] * 3, [30.0] * 3, [1, 1, 1])
+    # LHS: zero at the rest length, k0 (R - l0) along R beyond it
+    xyz = np.array([[1.0, 1.0, 1.0], [4.0, 1.0, 1.0]])
+    f = O.spring_forces(box, xyz, [[0, 1]], 3, 2.0, 5.0)
+    assert np.allclose(f[0], [5.0, 0, 0]) and np.allclose(f[1], [-5.0, 0, 0])
+    f = O.spring_forces(box, xyz, [[0, 1]], 3, 3.0, 5.0)
+    assert np.allclose(f, 0.0)
+    # WLS at R/Ls = 1/2: c1 (1/(1/2)^2 - 1 + 2) = 5 c1 along R
+    f = O.spring_forces(box, xyz, [[0, 1]], 0, 0.7, 6.0)
+    assert np.allclose(f[0], [0.7 * 5.0, 0, 0])
+    # minimum image: the partner across the boundary pulls backwards
+    xyz2 = np.array([[0.5, 1.0, 1.0], [29.0, 1.0, 1.0]])
+    f = O.spring_forces(box, xyz2, [[0, 1]], 3, 0.0, 1.0)
+    assert np.allclose(f[0], [-1.5, 0, 0])
+    rng = np.random.default_rng(2)
+    pts = rng.uniform(0, 30.0, (300, 3))
+    nb = O.neighbors_cutoff(box, pts, 7.0)
+    ev = O.ev_gaussian(box, pts, nb, 0.3, 0.2)
+    assert np.abs(ev.sum(axis=0)).max() < 1e-12 * np.abs(ev).max() * len(pts)
+    bonds = np.stack([np.arange(299), np.arange(1, 300)], 1)
+    for kind in range(4):
+        sp = O.spring_forces(box, pts, bonds, kind, 0.2, 40.0)
+        assert np.abs(sp.sum(axis=0)).max() < 1e-9 * max(1.0, np.abs(sp).max())
