@@ -56,6 +56,17 @@ class ChebReport(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class PolymerData(C.Structure):
+    _fields_ = [("n_beads", C.c_int64), ("n_bonds", C.c_int64), ("n_bead_types", C.c_int),
+                ("n_bond_types", C.c_int), ("n_chains", C.c_int), ("has_box", C.c_int),
+                ("box_lo", C.c_double * 3), ("box_hi", C.c_double * 3),
+                ("xyz", C.POINTER(C.c_double)), ("chain_id", C.POINTER(C.c_int32)),
+                ("bead_type", C.POINTER(C.c_int32)), ("rot", C.POINTER(C.c_double)),
+                ("const_force", C.POINTER(C.c_double)), ("charge", C.POINTER(C.c_double)),
+                ("mass", C.POINTER(C.c_double)), ("bonds", C.POINTER(C.c_int64)),
+                ("bond_type", C.POINTER(C.c_int32))]
+
+
 class GGEMError(RuntimeError):
     def __init__(self, code, msg):
         super().__init__(f"ggem error {code}: {msg}")
@@ -135,6 +146,13 @@ def lib():
         "ggem_set_bonds": (i, [vp, i64, vp]),
         "ggem_spring_forces": (i, [vp, i, d, d, vp, i]),
         "ggem_spring_forces_dev": (i, [vp, i, d, d, vp, i]),
+        "ggem_read_polymer_data": (i, [C.c_char_p, P(PolymerData)]),
+        "ggem_read_polymer_vtk": (i, [C.c_char_p, P(PolymerData)]),
+        "ggem_free_polymer_data": (None, [P(PolymerData)]),
+        "ggem_write_polymer_vtk": (i, [C.c_char_p, i64, vp, i64, vp, vp, i]),
+        "ggem_write_bead_csv": (i, [C.c_char_p, i64, vp, vp, vp, i]),
+        "ggem_write_petsc_vec": (i, [C.c_char_p, i64, vp]),
+        "ggem_read_petsc_vec": (i, [C.c_char_p, i64, vp, P(i64)]),
         "ggem_ensemble_create": (i, [P(Params), i, vp, P(vp)]),
         "ggem_ensemble_destroy": (None, [vp]),
         "ggem_ensemble_last_error": (C.c_char_p, [vp]),
@@ -648,3 +666,89 @@ class Ensemble:
         t, ms = C.c_int(), C.c_double()
         self._check(lib().ggem_ensemble_autotune(self.h, int(nrhs), C.byref(t), C.byref(ms)))
         return t.value, ms.value
+
+
+# ---- particle files (include/ggem_io.h) ----------------------------------
+def _take_polymer(d: PolymerData) -> dict:
+    n, m = d.n_beads, d.n_bonds
+
+    def arr(ptr, count, shape=None):
+        a = np.ctypeslib.as_array(ptr, shape=(count,)).copy()
+        return a.reshape(shape) if shape else a
+    out = {"n_beads": n, "n_bonds": m, "n_chains": d.n_chains,
+           "n_bead_types": d.n_bead_types, "n_bond_types": d.n_bond_types,
+           "xyz": arr(d.xyz, 3 * n, (n, 3)) if n else np.zeros((0, 3)),
+           "chain_id": arr(d.chain_id, n) if n else np.zeros(0, np.int32),
+           "bead_type": arr(d.bead_type, n) if n else np.zeros(0, np.int32),
+           "bonds": arr(d.bonds, 2 * m, (m, 2)) if m else np.zeros((0, 2), np.int64),
+           "bond_type": arr(d.bond_type, m) if m else np.zeros(0, np.int32)}
+    if d.const_force and n:
+        out["const_force"] = arr(d.const_force, 3 * n, (n, 3))
+        out["charge"] = arr(d.charge, n)
+        out["rot"] = arr(d.rot, 3 * n, (n, 3))
+    if d.mass and d.n_bead_types:
+        out["mass"] = arr(d.mass, d.n_bead_types)
+    if d.has_box:
+        out["box_lo"], out["box_hi"] = tuple(d.box_lo), tuple(d.box_hi)
+    return out
+
+
+def _read_polymer(fn, path) -> dict:
+    d = PolymerData()
+    rc = fn(str(path).encode(), C.byref(d))
+    if rc:
+        raise GGEMError(rc, f"cannot read {path}")
+    try:
+        return _take_polymer(d)
+    finally:
+        lib().ggem_free_polymer_data(C.byref(d))
+
+
+def read_polymer_data(path) -> dict:
+    """LAMMPS-style polymer data file (polymer_chain.C:61-226), 0-based ids"""
+    return _read_polymer(lib().ggem_read_polymer_data, path)
+
+
+def read_polymer_vtk(path) -> dict:
+    """polymer VTK written by write_polymer_vtk (polymer_chain.C:396-494)"""
+    return _read_polymer(lib().ggem_read_polymer_vtk, path)
+
+
+def write_polymer_vtk(path, xyz, bonds, chain_id=None, precision=6):
+    xyz = _f64(xyz).reshape(-1, 3)
+    b = np.ascontiguousarray(bonds, dtype=np.int64).reshape(-1, 2)
+    c = None if chain_id is None else np.ascontiguousarray(chain_id, dtype=np.int32)
+    rc = lib().ggem_write_polymer_vtk(str(path).encode(), len(xyz), _p(xyz), len(b), _p(b),
+                                      None if c is None else _p(c), int(precision))
+    if rc:
+        raise GGEMError(rc, f"cannot write {path}")
+
+
+def write_bead_csv(path, xyz, vel=None, force=None, precision=6):
+    xyz = _f64(xyz).reshape(-1, 3)
+    v = None if vel is None else _f64(vel).reshape(-1, 3)
+    f = None if force is None else _f64(force).reshape(-1, 3)
+    rc = lib().ggem_write_bead_csv(str(path).encode(), len(xyz), _p(xyz),
+                                   None if v is None else _p(v), None if f is None else _p(f),
+                                   int(precision))
+    if rc:
+        raise GGEMError(rc, f"cannot write {path}")
+
+
+def write_petsc_vec(path, v):
+    v = _f64(v).reshape(-1)
+    rc = lib().ggem_write_petsc_vec(str(path).encode(), len(v), _p(v))
+    if rc:
+        raise GGEMError(rc, f"cannot write {path}")
+
+
+def read_petsc_vec(path) -> np.ndarray:
+    n = C.c_int64()
+    rc = lib().ggem_read_petsc_vec(str(path).encode(), -1, None, C.byref(n))
+    if rc:
+        raise GGEMError(rc, f"cannot read {path}")
+    v = np.zeros(n.value)
+    rc = lib().ggem_read_petsc_vec(str(path).encode(), n.value, _p(v), C.byref(n))
+    if rc:
+        raise GGEMError(rc, f"cannot read {path}")
+    return v

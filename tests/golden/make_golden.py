@@ -12,6 +12,9 @@ GGEM_REFERENCE_ROOT).  Two fixtures come out:
   analytical_solution_stokes.C:66-102).  Columns are taken by position
   (0, 7-9, 10-12); the files predate the csv writer at
   pm_system_stokes.C:669-674.
+* polymer_bd_hi_data.in, polymer_bd_hi_output_0.vtk -- the reference's
+  PointParticle_Polymer_BD_HI particle data file and the VTK of its initial
+  configuration written by the reference (pins the particle-file formats).
 * ref_chebyshev_coeffs.json -- Chebyshev coefficients produced by the
   reference's own src/chebyshev.C (compiled into oracle/_ref by
   oracle/Makefile) for a grid of orders, intervals and quadrature methods,
@@ -73,10 +76,27 @@ def cheb_coeffs() -> dict:
     return {"source": "src/chebyshev.C via oracle/_ref", "cases": cases}
 
 
+POLYMER_DIR = (REF_ROOT / "tests" / "integration_tests" / "resources"
+               / "PointParticle_Polymer_BD_HI")
+
+
+def polymer_files() -> None:
+    """The reference's PointParticle_Polymer_BD_HI input data file and the
+    VTK its writer produced for that initial configuration, copied verbatim:
+    a reader / writer round trip through the library must reproduce the VTK
+    byte for byte (polymer_chain.C:61-226, :1096-1154)."""
+    (HERE / "polymer_bd_hi_data.in").write_bytes(
+        (POLYMER_DIR / "point_particle_data.in").read_bytes())
+    (HERE / "polymer_bd_hi_output_0.vtk").write_bytes(
+        (POLYMER_DIR / "output" / "output_polymer_0.vtk").read_bytes())
+
+
 def main() -> None:
     (HERE / "ggem_profile_3P.json").write_text(json.dumps(profiles()))
     (HERE / "ref_chebyshev_coeffs.json").write_text(json.dumps(cheb_coeffs(), indent=1))
-    print("wrote", HERE / "ggem_profile_3P.json", HERE / "ref_chebyshev_coeffs.json")
+    polymer_files()
+    print("wrote", HERE / "ggem_profile_3P.json", HERE / "ref_chebyshev_coeffs.json",
+          HERE / "polymer_bd_hi_data.in", HERE / "polymer_bd_hi_output_0.vtk")
 
 
 if __name__ == "__main__":
