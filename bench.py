@@ -223,7 +223,8 @@ def run_gb300(args, rank, world):
     ctx.build_cells()
     use_stored, ms_comp, ms_store = ctx.autotune_pair_storage(reps=10, matvecs_per_build=12.0)
     tuning = {"cell_div": cell_div, "pair_tensors_stored": use_stored,
-              "ms_per_matvec_computed": ms_comp, "ms_per_matvec_stored_amortised": ms_store}
+              "ms_per_matvec_computed": ms_comp, "ms_per_matvec_stored_amortised": ms_store,
+              "stored_variant": ctx.stored_variant}
     stream = torch.cuda.Stream(device=dev)
     ctx.set_stream(stream.cuda_stream)
 
@@ -318,6 +319,7 @@ def run_gb300(args, rank, world):
                for s in range(args.steps + args.warmup)]
     ctx_e = make_ctx(G.FP32, cell_div)
     ctx_e.set_pair_tensors(use_stored)
+    ctx_e.set_pair_variant(ctx.stored_variant)
     ctx_e.set_particles(xyz)
     ctx_e.build_cells()
     e_bounds = state["bounds"]

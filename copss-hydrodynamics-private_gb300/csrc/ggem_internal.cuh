@@ -140,6 +140,7 @@ struct ggem_ctx {
   bool use_pretensor = false;   // B >= 0 holds for these constants
   bool allow_pretensor = true;  // ggem_set_pair_tensors
   bool pretensor_ok = false;
+  int stored_variant = 0;         // shape of the stored-tensor pair kernels (autotuned)
   ggem::DevBuf<float4> pair_ten;
   ggem::DevBuf<float4> w_f4[2];
   int rec_cur = 0;

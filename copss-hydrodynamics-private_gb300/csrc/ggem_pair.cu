@@ -425,43 +425,86 @@ __global__ void k_stage_f4(int64_t n, const double *__restrict__ f, float4 *__re
   f4[s] = make_float4((float)f[3 * s], (float)f[3 * s + 1], (float)f[3 * s + 2], 0.f);
 }
 
-// the pair loop over precomputed tensors (cf. pair_sum_r1).  Four entries
-// per lane and iteration are loaded before any is used, so that each lane
-// keeps four streaming loads and four force gathers in flight; an entry past
-// the row end reads a zero tensor and adds exactly zero.
-__device__ __forceinline__ PairSum pair_sum_t(int64_t s, bool act, int sub,
-                                              const float4 *__restrict__ f4,
-                                              const int32_t *__restrict__ cnt, int W,
-                                              const uint32_t *__restrict__ list,
-                                              const float4 *__restrict__ ten) {
-  constexpr int U = 4;
+// float-float sum over the G lanes of a target's group
+template <int G>
+__device__ __forceinline__ void group_ff_g(float &hi, float &lo) {
+#pragma unroll
+  for (int o = G / 2; o > 0; o >>= 1) {
+    const float h2 = __shfl_xor_sync(0xffffffffu, hi, o);
+    const float l2 = __shfl_xor_sync(0xffffffffu, lo, o);
+    ff_add(hi, lo, h2, l2);
+  }
+}
+
+// blk += G f over one entry: A f + (x~ . f) x~, x and y packed (FFMA2)
+__device__ __forceinline__ void tensor_apply(const float4 &t, const float4 &fj, float2 &bxy,
+                                             float &bz) {
+  const float2 txy = make_float2(t.y, t.z), fxy = make_float2(fj.x, fj.y);
+  const float2 p = __fmul2_rn(txy, fxy);
+  const float d = fmaf(t.w, fj.z, p.x + p.y);
+  bxy = __fadd2_rn(bxy, __ffma2_rn(make_float2(t.x, t.x), fxy, __fmul2_rn(make_float2(d, d), txy)));
+  bz += fmaf(t.x, fj.z, d * t.w);
+}
+
+// The pair loop over stored tensors for one target slot s (cf. pair_sum_r1):
+// G lanes share the target and take every G-th entry, U entries per lane and
+// iteration are loaded before any is used (an entry past the row end reads a
+// zero tensor and adds exactly zero).  PIPE: the streamed entries and tensors
+// of the next iteration are requested before the current iteration's force
+// gathers are used, so that the HBM latency of the stream overlaps the L2
+// latency of the gathers.  Variants are picked by ggem_autotune_pair_storage.
+template <int G, int U, bool PIPE>
+__device__ __forceinline__ PairSum pair_sum_tv(int64_t s, bool act, int sub,
+                                               const float4 *__restrict__ f4,
+                                               const int32_t *__restrict__ cnt, int W,
+                                               const uint32_t *__restrict__ list,
+                                               const float4 *__restrict__ ten) {
+  constexpr int FLUSH = (8 + U - 1) / U;  // iterations per Kahan flush (~8 entries)
   const int64_t b = s * (int64_t)W, e = act ? b + cnt[s] : b;
   float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
   float2 bxy = make_float2(0.f, 0.f);
   float bz = 0.f;
   int blk = 0;
-  for (int64_t m = b + sub; m < e; m += U * kGroup) {
-    uint32_t en[U];
-    float4 t[U], fj[U];
+  uint32_t en[U];
+  float4 t[U];
+  int64_t m = b + sub;
+  if (PIPE) {
 #pragma unroll
     for (int q = 0; q < U; ++q) {
-      const int64_t mq = m + q * kGroup;
+      const int64_t mq = m + q * G;
       const bool ok = mq < e;
       en[q] = ok ? __ldcs(list + mq) : 0u;
       t[q] = ok ? __ldcs(ten + mq) : make_float4(0.f, 0.f, 0.f, 0.f);
     }
+  }
+  for (; m < e; m += U * G) {
+    if (!PIPE) {
+#pragma unroll
+      for (int q = 0; q < U; ++q) {
+        const int64_t mq = m + q * G;
+        const bool ok = mq < e;
+        en[q] = ok ? __ldcs(list + mq) : 0u;
+        t[q] = ok ? __ldcs(ten + mq) : make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+    }
+    float4 fj[U];
 #pragma unroll
     for (int q = 0; q < U; ++q) fj[q] = __ldg(f4 + (en[q] >> kCodeBits));
+    float4 tc[U];
 #pragma unroll
-    for (int q = 0; q < U; ++q) {
-      const float2 txy = make_float2(t[q].y, t[q].z), fxy = make_float2(fj[q].x, fj[q].y);
-      const float2 p = __fmul2_rn(txy, fxy);
-      const float d = fmaf(t[q].w, fj[q].z, p.x + p.y);
-      bxy = __fadd2_rn(bxy, __ffma2_rn(make_float2(t[q].x, t[q].x), fxy,
-                                       __fmul2_rn(make_float2(d, d), txy)));
-      bz += fmaf(t[q].x, fj[q].z, d * t[q].w);
+    for (int q = 0; q < U; ++q) tc[q] = t[q];
+    if (PIPE) {
+#pragma unroll
+      for (int q = 0; q < U; ++q) {
+        const int64_t mq = m + U * G + q * G;
+        const bool ok = mq < e;
+        en[q] = ok ? __ldcs(list + mq) : 0u;
+        t[q] = ok ? __ldcs(ten + mq) : make_float4(0.f, 0.f, 0.f, 0.f);
+      }
     }
-    if (++blk == 2) {  // every 8 entries into the compensated sums
+#pragma unroll
+    for (int q = 0; q < U; ++q) tensor_apply(tc[q], fj[q], bxy, bz);
+    if (++blk == FLUSH) {
       kahan_add(sx, cx, bxy.x);
       kahan_add(sy, cy, bxy.y);
       kahan_add(sz, cz, bz);
@@ -474,40 +517,42 @@ __device__ __forceinline__ PairSum pair_sum_t(int64_t s, bool act, int sub,
   kahan_add(sy, cy, bxy.y);
   kahan_add(sz, cz, bz);
   PairSum r{sx, -cx, sy, -cy, sz, -cz};
-  group_ff(r.hx, r.lx);
-  group_ff(r.hy, r.ly);
-  group_ff(r.hz, r.lz);
+  group_ff_g<G>(r.hx, r.lx);
+  group_ff_g<G>(r.hy, r.ly);
+  group_ff_g<G>(r.hz, r.lz);
   return r;
 }
 
-// u = M f from precomputed tensors, single right-hand side
-__global__ void __launch_bounds__(256) k_pair_r1t(int64_t n, const float4 *__restrict__ f4,
-                                                  const int32_t *__restrict__ cnt, int W,
-                                                  const uint32_t *__restrict__ list,
-                                                  const float4 *__restrict__ ten, double self_c,
-                                                  const double *__restrict__ f,
-                                                  double *__restrict__ u) {
-  const int64_t gid = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / kGroup;
-  const int sub = (int)(threadIdx.x % kGroup);
+// u = M f from stored tensors, single right-hand side
+template <int G, int U, bool PIPE>
+__global__ void __launch_bounds__(256) k_pair_r1tv(int64_t n, const float4 *__restrict__ f4,
+                                                   const int32_t *__restrict__ cnt, int W,
+                                                   const uint32_t *__restrict__ list,
+                                                   const float4 *__restrict__ ten, double self_c,
+                                                   const double *__restrict__ f,
+                                                   double *__restrict__ u) {
+  const int64_t gid = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / G;
+  const int sub = (int)(threadIdx.x % G);
   const bool act = gid < n;
   const int64_t s = act ? gid : n - 1;
-  const PairSum r = pair_sum_t(s, act, sub, f4, cnt, W, list, ten);
+  const PairSum r = pair_sum_tv<G, U, PIPE>(s, act, sub, f4, cnt, W, list, ten);
   group_store(act, sub, s, r.hx, r.lx, r.hy, r.ly, r.hz, r.lz, self_c, f, u);
 }
 
-// one Chebyshev term from precomputed tensors (cf. k_pair_cheb); f4 holds
-// the FP32 forces of x1, next receives those of xm
-__global__ void __launch_bounds__(256) k_pair_cheb_t(
+// one Chebyshev term from stored tensors (cf. k_pair_cheb); f4 holds the
+// FP32 forces of x1, next receives those of xm
+template <int G, int U, bool PIPE>
+__global__ void __launch_bounds__(256) k_pair_cheb_tv(
     int64_t n, const float4 *__restrict__ f4, const int32_t *__restrict__ cnt, int W,
     const uint32_t *__restrict__ list, const float4 *__restrict__ ten, double self_c,
     double two_da, double two_db, double coef, const double *__restrict__ x0,
     const double *__restrict__ x1, double *__restrict__ xm, double *__restrict__ dw,
     float4 *__restrict__ next) {
-  const int64_t gid = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / kGroup;
-  const int sub = (int)(threadIdx.x % kGroup);
+  const int64_t gid = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / G;
+  const int sub = (int)(threadIdx.x % G);
   const bool act = gid < n;
   const int64_t s = act ? gid : n - 1;
-  const PairSum r = pair_sum_t(s, act, sub, f4, cnt, W, list, ten);
+  const PairSum r = pair_sum_tv<G, U, PIPE>(s, act, sub, f4, cnt, W, list, ten);
   if (!act) return;
   float *nf = reinterpret_cast<float *>(next + s);
   if (sub < 3) {
@@ -521,8 +566,56 @@ __global__ void __launch_bounds__(256) k_pair_cheb_t(
     xm[k] = v;
     dw[k] = dw[k] + coef * v;
     nf[sub] = __double2float_rn(v);
-  } else {
+  } else if (sub == 3) {
     nf[3] = 0.f;
+  }
+}
+
+// the stored-tensor variants the autotuner chooses from: lanes per target,
+// entries in flight per lane, pipelined stream
+struct StoredVariant {
+  int G, U;
+  bool pipe;
+};
+constexpr StoredVariant kStoredVariants[] = {{4, 4, false}, {4, 2, true}, {8, 2, true}, {8, 4, false}};
+constexpr int kNumStoredVariants = 4;
+
+template <int V>
+void launch_stored_r1(ggem_ctx *c, const float4 *f4, double self_c, const double *f, double *u) {
+  constexpr StoredVariant sv = kStoredVariants[V];
+  const int64_t threads = c->n * sv.G;
+  k_pair_r1tv<sv.G, sv.U, sv.pipe><<<(unsigned)((threads + 255) / 256), 256, 0, c->stream>>>(
+      c->n, f4, c->nb_cnt.p, c->nb_w, c->nb_list.p, c->pair_ten.p, self_c, f, u);
+}
+
+template <int V>
+void launch_stored_cheb(ggem_ctx *c, const float4 *f4, double self_c, double two_da,
+                        double two_db, double coef, const double *x0, const double *x1,
+                        double *xm, double *dw, float4 *next) {
+  constexpr StoredVariant sv = kStoredVariants[V];
+  const int64_t threads = c->n * sv.G;
+  k_pair_cheb_tv<sv.G, sv.U, sv.pipe><<<(unsigned)((threads + 255) / 256), 256, 0, c->stream>>>(
+      c->n, f4, c->nb_cnt.p, c->nb_w, c->nb_list.p, c->pair_ten.p, self_c, two_da, two_db, coef,
+      x0, x1, xm, dw, next);
+}
+
+void dispatch_stored_r1(ggem_ctx *c, const float4 *f4, double self_c, const double *f, double *u) {
+  switch (c->stored_variant) {
+    case 1: launch_stored_r1<1>(c, f4, self_c, f, u); break;
+    case 2: launch_stored_r1<2>(c, f4, self_c, f, u); break;
+    case 3: launch_stored_r1<3>(c, f4, self_c, f, u); break;
+    default: launch_stored_r1<0>(c, f4, self_c, f, u); break;
+  }
+}
+
+void dispatch_stored_cheb(ggem_ctx *c, const float4 *f4, double self_c, double two_da,
+                          double two_db, double coef, const double *x0, const double *x1,
+                          double *xm, double *dw, float4 *next) {
+  switch (c->stored_variant) {
+    case 1: launch_stored_cheb<1>(c, f4, self_c, two_da, two_db, coef, x0, x1, xm, dw, next); break;
+    case 2: launch_stored_cheb<2>(c, f4, self_c, two_da, two_db, coef, x0, x1, xm, dw, next); break;
+    case 3: launch_stored_cheb<3>(c, f4, self_c, two_da, two_db, coef, x0, x1, xm, dw, next); break;
+    default: launch_stored_cheb<0>(c, f4, self_c, two_da, two_db, coef, x0, x1, xm, dw, next); break;
   }
 }
 
@@ -831,9 +924,7 @@ int launch_f32_r1(ggem_ctx *c, const double *f, double *u, double self_c) {
     k_stage_f4<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(n, f, c->w_f4[0].p);
     if (int rc = check_launch(c, "pair forces")) return rc;
     kt_start(c, kKPairF32);
-    const int64_t threads = n * kGroup;
-    k_pair_r1t<<<(unsigned)((threads + 255) / 256), 256, 0, c->stream>>>(
-        n, c->w_f4[0].p, c->nb_cnt.p, c->nb_w, c->nb_list.p, c->pair_ten.p, self_c, f, u);
+    dispatch_stored_r1(c, c->w_f4[0].p, self_c, f, u);
     kt_stop(c, kKPairF32);
     return check_launch(c, "pair f32 r1 (tensors)");
   }
@@ -956,10 +1047,7 @@ int pair_cheb_term(ggem_ctx *c, bool records_fresh, const double *x0, const doub
       if (int rc = check_launch(c, "chebyshev forces")) return rc;
     }
     kt_start(c, kKPairCheb);
-    const int64_t threads = n * kGroup;
-    k_pair_cheb_t<<<(unsigned)((threads + 255) / 256), 256, 0, c->stream>>>(
-        n, cur, c->nb_cnt.p, c->nb_w, c->nb_list.p, c->pair_ten.p, self_c0, two_da, two_db, coef,
-        x0, x1, xm, dw, nxt);
+    dispatch_stored_cheb(c, cur, self_c0, two_da, two_db, coef, x0, x1, xm, dw, nxt);
     kt_stop(c, kKPairCheb);
     c->rec_cur ^= 1;
     return check_launch(c, "pair chebyshev term (tensors)");
@@ -1087,10 +1175,17 @@ int matvec_f32_staged(ggem_ctx *c, int nrhs, const double *f, double *u, int sel
 
 using namespace ggem;
 
+extern "C" int ggem_set_pair_variant(ggem_ctx *ctx, int variant) {
+  if (!ctx || variant < 0 || variant >= kNumStoredVariants) return GGEM_ERR_BAD_ARG;
+  ctx->stored_variant = variant;
+  return GGEM_OK;
+}
+
 extern "C" int ggem_autotune_pair_storage(ggem_ctx *ctx, int reps, double matvecs_per_build,
                                           int *use_stored, double *ms_computed,
-                                          double *ms_stored) {
-  if (!ctx || reps < 1 || !(matvecs_per_build > 0) || !use_stored || !ms_computed || !ms_stored)
+                                          double *ms_stored, int *stored_variant) {
+  if (!ctx || reps < 1 || !(matvecs_per_build > 0) || !use_stored || !ms_computed ||
+      !ms_stored || !stored_variant)
     return GGEM_ERR_BAD_ARG;
   if (ctx->prm.precision != GGEM_FP32 || !ctx->list_built)
     return fail(ctx, GGEM_ERR_BAD_ARG, "autotune needs a built FP32 pair list");
@@ -1136,9 +1231,20 @@ extern "C" int ggem_autotune_pair_storage(ggem_ctx *ctx, int reps, double matvec
     float t_pass = 0.f;
     cudaEventElapsedTime(&t_pass, a, b);
     if (!rc && ctx->pretensor_ok) {
-      double t_mv = 0.0;
-      rc = time_matvecs(&t_mv);
-      t_store = t_mv + t_pass / matvecs_per_build;
+      // every stored-tensor kernel shape; the fastest stays selected
+      int best_v = 0;
+      double best_mv = 1e30;
+      for (int v = 0; v < kNumStoredVariants && !rc; ++v) {
+        ctx->stored_variant = v;
+        double t_mv = 0.0;
+        rc = time_matvecs(&t_mv);
+        if (!rc && t_mv < best_mv) {
+          best_mv = t_mv;
+          best_v = v;
+        }
+      }
+      ctx->stored_variant = best_v;
+      t_store = best_mv + t_pass / matvecs_per_build;
     }
   }
   cudaEventDestroy(a);
@@ -1155,6 +1261,7 @@ extern "C" int ggem_autotune_pair_storage(ggem_ctx *ctx, int reps, double matvec
   *use_stored = stored ? 1 : 0;
   *ms_computed = t_comp;
   *ms_stored = ctx->use_pretensor ? t_store : -1.0;
+  *stored_variant = ctx->stored_variant;
   if (dev != ctx->device) cudaSetDevice(dev);
   return GGEM_OK;
 }

@@ -117,7 +117,8 @@ def lib():
         "ggem_get_pair_count": (i, [vp, P(i64)]),
         "ggem_get_pair_storage": (i, [vp, P(i), P(i)]),
         "ggem_set_pair_tensors": (i, [vp, i]),
-        "ggem_autotune_pair_storage": (i, [vp, i, d, P(i), P(d), P(d)]),
+        "ggem_autotune_pair_storage": (i, [vp, i, d, P(i), P(d), P(d), P(i)]),
+        "ggem_set_pair_variant": (i, [vp, i]),
         "ggem_probe_fp32_peak": (i, [vp, P(d)]),
         "ggem_set_kernel_timing": (i, [vp, i]),
         "ggem_get_kernel_timing": (i, [vp, i, P(d), P(i64)]),
@@ -513,10 +514,15 @@ class Context:
     def autotune_pair_storage(self, reps=10, matvecs_per_build=12.0):
         """(use_stored, ms per matvec computed, ms per matvec stored incl. the
         amortised tensor pass); the faster variant stays selected"""
-        u, a, b = C.c_int(), C.c_double(), C.c_double()
+        u, a, b, v = C.c_int(), C.c_double(), C.c_double(), C.c_int()
         self._check(lib().ggem_autotune_pair_storage(self.h, int(reps), float(matvecs_per_build),
-                                                     C.byref(u), C.byref(a), C.byref(b)))
+                                                     C.byref(u), C.byref(a), C.byref(b),
+                                                     C.byref(v)))
+        self.stored_variant = v.value
         return bool(u.value), a.value, b.value
+
+    def set_pair_variant(self, v):
+        self._check(lib().ggem_set_pair_variant(self.h, int(v)))
 
     def pair_storage(self):
         """(row width, whether per-pair tensors are stored)"""

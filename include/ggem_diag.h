@@ -32,10 +32,15 @@ int ggem_set_pair_tensors(ggem_ctx *ctx, int enable);
  * built, FP32): times `reps` single-RHS matvecs with tensors evaluated per
  * pair and with stored tensors (plus the one tensor pass per build,
  * amortised over matvecs_per_build matvecs) by CUDA events on the context's
- * stream, keeps the faster variant for this context and reports both costs
- * in ms per matvec (the stored one with its amortised pass) */
+ * stream; the stored form is timed for each of its kernel shapes (lanes per
+ * target, entries in flight, pipelined stream).  The fastest stays selected
+ * for this context; both costs are reported in ms per matvec (the stored
+ * one with its amortised pass), with the chosen stored shape */
 int ggem_autotune_pair_storage(ggem_ctx *ctx, int reps, double matvecs_per_build,
-                               int *use_stored, double *ms_computed, double *ms_stored);
+                               int *use_stored, double *ms_computed, double *ms_stored,
+                               int *stored_variant);
+/* select the stored-tensor kernel shape directly (0 .. 3) */
+int ggem_set_pair_variant(ggem_ctx *ctx, int variant);
 /* dense FP32 FMA throughput of this device in TFLOP/s (FMA = 2 flops),
  * measured with CUDA events over a register-resident FMA chain kernel on the
  * context's stream */

@@ -456,8 +456,9 @@ def test_batched_64_rhs_chains_matvec_and_chebyshev():
         assert rel(y.reshape(64, -1)[r], y_o) <= 5e-3
 
 
-@pytest.mark.parametrize("stored", [True, False])
-def test_pair_tensor_storage_modes(stored):
+@pytest.mark.parametrize("stored,variant", [(False, 0), (True, 0), (True, 1), (True, 2),
+                                            (True, 3)])
+def test_pair_tensor_storage_modes(stored, variant):
     """Stored per-pair tensors (streamed) and per-matvec tensors (computed)
     give the same velocities within the FP32 contract, and the same
     fused-Chebyshev displacement."""
@@ -470,6 +471,7 @@ def test_pair_tensor_storage_modes(stored):
     xi = np.random.default_rng(9).standard_normal(3 * len(xyz))
     with G.Context(box_hi=(L,) * 3, rc=7.0, precision=G.FP32) as ctx:
         ctx.set_pair_tensors(stored)
+        ctx.set_pair_variant(variant)
         ctx.set_particles(xyz)
         ctx.build_cells()
         W, st = ctx.pair_storage()
