@@ -224,9 +224,12 @@ def run_gb300(args, rank, world):
     use_stored, ms_comp, ms_store = ctx.autotune_pair_storage(reps=10, matvecs_per_build=12.0)
     tuning = {"cell_div": cell_div, "pair_tensors_stored": use_stored,
               "ms_per_matvec_computed": ms_comp, "ms_per_matvec_stored_amortised": ms_store,
-              "stored_variant": ctx.stored_variant}
+              "pair_variants_computed_stored": list(ctx.pair_variants)}
     stream = torch.cuda.Stream(device=dev)
     ctx.set_stream(stream.cuda_stream)
+    # rebuilds return without waiting for the device; the list statistics
+    # are read with the Chebyshev error check of the same step
+    ctx.set_deferred_checks(True)
 
     d_xi = torch.empty(3 * N_BEADS, dtype=torch.float64, device="cuda")
     d_dw = torch.empty_like(d_xi)
@@ -319,9 +322,10 @@ def run_gb300(args, rank, world):
                for s in range(args.steps + args.warmup)]
     ctx_e = make_ctx(G.FP32, cell_div)
     ctx_e.set_pair_tensors(use_stored)
-    ctx_e.set_pair_variant(ctx.stored_variant)
+    ctx_e.set_pair_variant(*ctx.pair_variants)
     ctx_e.set_particles(xyz)
     ctx_e.build_cells()
+    ctx_e.set_deferred_checks(True)
     e_bounds = state["bounds"]
     RepArr = G.ChebReport * 1
 

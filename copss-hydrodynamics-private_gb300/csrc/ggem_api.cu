@@ -248,7 +248,10 @@ int validate_and_setup(ggem_ctx *c) {
   // (larger) reference-mode element stencil is only swept in FP64
   if (p.precision == GGEM_FP32 && (int)c->stencil.size() > kMaxCode)
     return fail(c, GGEM_ERR_BAD_ARG, "stencil larger than the pair-entry code space");
-  for (int d = 0; d < 3; ++d) g.h32[d] = (float)g.h[d];
+  for (int d = 0; d < 3; ++d) {
+    g.h32[d] = (float)g.h[d];
+    g.inv_h[d] = 1.0 / g.h[d];
+  }
   return upload_stencil(c);
 }
 
@@ -383,6 +386,7 @@ static int set_particles_common(ggem_ctx *ctx, int64_t n, const double *xyz, boo
   ctx->n = n;
   ctx->cells_built = false;
   ctx->list_built = false;
+  ctx->list_unchecked = false;  // the pending statistics describe the old positions
   return GGEM_OK;
 }
 
@@ -394,9 +398,20 @@ extern "C" int ggem_set_particles_dev(ggem_ctx *ctx, int64_t n, const double *d_
   return set_particles_common(ctx, n, d_xyz, true);
 }
 
+extern "C" int ggem_set_deferred_checks(ggem_ctx *ctx, int enable) {
+  if (!ctx) return GGEM_ERR_BAD_ARG;
+  DeviceGuard dg(ctx->device);
+  if (!enable)
+    if (int rc = settle_list(ctx)) return rc;
+  ctx->defer_checks = enable != 0;
+  return GGEM_OK;
+}
+
 extern "C" int ggem_build_cells(ggem_ctx *ctx) {
   if (!ctx) return GGEM_ERR_BAD_ARG;
   DeviceGuard dg(ctx->device);
+  // statistics of an earlier deferred build that nothing has read yet
+  if (int rc = settle_list(ctx)) return rc;
   // the FP32 path builds its pair list right after the cells; both error
   // checks then share the list's single host readback
   const bool with_list = ctx->prm.precision == GGEM_FP32 && ctx->prm.nb_mode == GGEM_NB_CUTOFF;
@@ -409,6 +424,7 @@ extern "C" int ggem_build_cells(ggem_ctx *ctx) {
 }
 
 static int require_built(ggem_ctx *ctx) {
+  if (int rc = settle_list(ctx)) return rc;
   if (!ctx->cells_built)
     return fail(ctx, GGEM_ERR_BAD_ARG, "call ggem_build_cells after setting particles");
   if (ctx->prm.precision == GGEM_FP32 && !ctx->list_built)
@@ -434,6 +450,7 @@ extern "C" int ggem_neighbor_pair_count(ggem_ctx *ctx, int64_t *count) {
 
 extern "C" int ggem_get_cell_of_particles(ggem_ctx *ctx, int32_t *cell) {
   if (!ctx || (!cell && ctx->n)) return GGEM_ERR_BAD_ARG;
+  if (int rc = settle_list(ctx)) return rc;
   if (!ctx->cells_built) return fail(ctx, GGEM_ERR_BAD_ARG, "cells not built");
   DeviceGuard dg(ctx->device);
   if (ctx->n == 0) return GGEM_OK;

@@ -40,17 +40,26 @@ __global__ void k_assign(int64_t n, const double *__restrict__ xyz, Grid g,
   for (int d = 0; d < 3; ++d) {
     double x = xyz[3 * i + d];
     double t = x - g.lo[d];
+    // (FP64 runs at a small fraction of the FP32 rate: fmod and the division
+    // are taken only where they can change the result)
     if (g.periodic[d]) {
-      t = fmod(t, g.L[d]);
-      if (t < 0) t += g.L[d];
-      if (t >= g.L[d]) t = 0.0;
-      // keep the caller's value when it already lies in the box
-      if (!(x >= g.lo[d] && x < g.lo[d] + g.L[d])) x = g.lo[d] + t;
+      if (!(t >= 0.0 && t < g.L[d])) {  // inside, fmod(t, L) == t
+        t = fmod(t, g.L[d]);
+        if (t < 0) t += g.L[d];
+        if (t >= g.L[d]) t = 0.0;
+        // keep the caller's value when it already lies in the box
+        if (!(x >= g.lo[d] && x < g.lo[d] + g.L[d])) x = g.lo[d] + t;
+      }
     } else if (!(t >= 0.0 && t <= g.L[d])) {
       bad = true;
     }
     p[d] = x;
-    int k = (int)floor(t / g.h[d]);
+    // floor(t / h): t * (1/h) is within a few ulps of t / h, so its floor is
+    // the same unless it lies within 1e-9 of an integer (|t / h| < 1e6)
+    const double q = t * g.inv_h[d];
+    double fq = floor(q);
+    if (q - fq < 1e-9 || (fq + 1.0) - q < 1e-9 || !(fabs(q) < 1e6)) fq = floor(t / g.h[d]);
+    int k = (int)fq;
     c[d] = k < 0 ? 0 : (k >= g.nc[d] ? g.nc[d] - 1 : k);
   }
   if (bad) atomicOr(err, kErrOutOfDomain);
@@ -149,12 +158,34 @@ __global__ void k_scatter(int64_t n, const int32_t *__restrict__ cell_of,
 }
 
 // ascending particle id inside each cell (deterministic slot order, and the
-// order of build_elem_point_containing_list, point_mesh.C:585-631)
+// order of build_elem_point_containing_list, point_mesh.C:585-631): cells of
+// up to 16 particles are sorted in registers by an odd-even transposition
+// network, larger ones by insertion in place
 __global__ void k_sort_cells(int64_t ncell, const int32_t *__restrict__ start,
                              int32_t *__restrict__ order) {
   const int64_t cidx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (cidx >= ncell) return;
   const int32_t b = start[cidx], e = start[cidx + 1];
+  const int32_t m = e - b;
+  if (m <= 1) return;
+  if (m <= 16) {
+    int32_t v[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) v[k] = k < m ? order[b + k] : 0x7fffffff;
+#pragma unroll
+    for (int r = 0; r < 16; ++r) {
+#pragma unroll
+      for (int k = r & 1; k + 1 < 16; k += 2) {
+        const int32_t lo = min(v[k], v[k + 1]), hi = max(v[k], v[k + 1]);
+        v[k] = lo;
+        v[k + 1] = hi;
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 16; ++k)
+      if (k < m) order[b + k] = v[k];
+    return;
+  }
   for (int32_t k = b + 1; k < e; ++k) {
     const int32_t v = order[k];
     int32_t m = k - 1;
@@ -327,7 +358,7 @@ __global__ void __launch_bounds__(32 * kListWarps) k_pair_list_warp(
       }
     }
     if (own_ok) {
-      count[own] = own_cnt;
+      count[own] = min(own_cnt, W);  // the stored entries; the full length goes to stat
       cell_total += (unsigned long long)own_cnt;
       cell_max = max(cell_max, own_cnt);
     }
@@ -430,10 +461,28 @@ int build_pair_list(ggem_ctx *c) {
   }
   const int nst = (int)c->stencil.size();
   if (nst > kMaxStencil) return fail(c, GGEM_ERR_BAD_ARG, "stencil too large for the list builder");
+  const unsigned cb = (unsigned)((c->grid.ncell + kListWarps - 1) / kListWarps);
+  if (c->defer_checks && c->list_checked_once) {
+    // keep the width of the previous build; a longer row is stored clipped
+    // (counts never exceed W) and found when the statistics are read
+    if ((e = c->nb_list.ensure((size_t)n * c->nb_w))) return cuda_fail(c, e, "pair list");
+    if ((e = cudaMemsetAsync(c->nb_stat.p, 0, 2 * sizeof(unsigned long long), st)))
+      return cuda_fail(c, e, "memset");
+    kt_start(c, kKListBuild);
+    k_pair_list_warp<<<cb, 32 * kListWarps, 0, st>>>(
+        c->grid, c->d_stencil.p, nst, c->d_shift.p, c->cell_start.p, c->pos32.p, c->pos64.p,
+        c->rc2_lo, c->rc2_hi, c->rc2, c->nb_w, c->nb_cnt.p, c->nb_list.p, c->nb_stat.p, c->err.p);
+    kt_stop(c, kKListBuild);
+    if (int rc = check_launch(c, "pair list")) return rc;
+    c->cells_built = true;
+    c->list_built = true;
+    c->list_unchecked = true;
+    c->n_pairs = -1;
+    return GGEM_OK;
+  }
   // The error word still holds the cell build's flags; they come back with
   // the list statistics in one host synchronisation.  A row longer than the
   // current width makes the host widen the rows and fill once more.
-  const unsigned cb = (unsigned)((c->grid.ncell + kListWarps - 1) / kListWarps);
   unsigned long long *h = reinterpret_cast<unsigned long long *>(c->h_red);
   for (int attempt = 0; attempt < 2; ++attempt) {
     const int W = c->nb_w;
@@ -458,6 +507,7 @@ int build_pair_list(ggem_ctx *c) {
     if (!(flags & kErrListCapacity)) {
       c->n_pairs = (int64_t)h[0];
       c->list_built = true;
+      c->list_checked_once = true;
       return GGEM_OK;
     }
     const unsigned long long longest = h[1];
@@ -465,6 +515,55 @@ int build_pair_list(ggem_ctx *c) {
     if ((e = cudaMemsetAsync(c->err.p, 0, sizeof(int), st))) return cuda_fail(c, e, "memset");
   }
   return fail(c, GGEM_ERR_CELL_OVERFLOW, "pair list rows exceeded their width twice");
+}
+
+int enqueue_list_check(ggem_ctx *c) {
+  if (!c->list_unchecked) return GGEM_OK;
+  unsigned long long *h = reinterpret_cast<unsigned long long *>(c->h_red + kListStatSlot);
+  h[2] = 0;
+  cudaError_t e = cudaMemcpyAsync(h, c->nb_stat.p, 2 * sizeof(unsigned long long),
+                                  cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(&h[2], c->err.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+  if (e) return cuda_fail(c, e, "list statistics");
+  return GGEM_OK;
+}
+
+int finish_list_check(ggem_ctx *c, bool *rebuilt) {
+  if (rebuilt) *rebuilt = false;
+  if (!c->list_unchecked) return GGEM_OK;
+  c->list_unchecked = false;
+  const unsigned long long *h = reinterpret_cast<unsigned long long *>(c->h_red + kListStatSlot);
+  const int flags = (int)h[2];
+  if (int rc = cell_flag_error(c, flags)) {
+    c->list_built = false;
+    return rc;
+  }
+  if (!(flags & kErrListCapacity)) {
+    c->n_pairs = (int64_t)h[0];
+    return GGEM_OK;
+  }
+  // rows overflowed: widen them and rebuild with the synchronous path
+  const unsigned long long longest = h[1];
+  c->nb_w = (int)std::min<unsigned long long>((longest + longest / 8 + 8 + 7) / 8 * 8, 1u << 24);
+  cudaError_t e = cudaMemsetAsync(c->err.p, 0, sizeof(int), c->stream);
+  if (e) return cuda_fail(c, e, "memset");
+  const bool defer = c->defer_checks;
+  c->defer_checks = false;
+  int rc = build_pair_list(c);
+  c->defer_checks = defer;
+  if (rc) return rc;
+  if ((rc = build_pair_tensors(c))) return rc;
+  if (rebuilt) *rebuilt = true;
+  return GGEM_OK;
+}
+
+int settle_list(ggem_ctx *c) {
+  if (!c->list_unchecked) return GGEM_OK;
+  if (int rc = enqueue_list_check(c)) return rc;
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e) return cuda_fail(c, e, "list statistics");
+  return finish_list_check(c, nullptr);
 }
 
 }  // namespace ggem

@@ -206,23 +206,29 @@ __device__ __forceinline__ void philox10(uint32_t c[4], uint32_t k0, uint32_t k1
   }
 }
 
+// Counter (p, stream) gives elements 4p .. 4p+3: words (c0, c1) and (c2, c3)
+// each make one Box-Muller pair from u1 = (c0 + 1/2) 2^-32 (rounded to
+// FP32) and u2 = (floor(c1 / 2^9) + 1/2) 2^-23 (exact), transformed in FP32
+// (the FP64 transcendentals would run at 1/64 of the FP32 rate); the tail
+// reaches 6.8 sigma.
 __global__ void k_philox_normals(int64_t n, uint64_t seed, uint64_t stream,
                                  double *__restrict__ out) {
   const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (2 * p >= n) return;
+  if (4 * p >= n) return;
   uint32_t c[4] = {(uint32_t)p, (uint32_t)((uint64_t)p >> 32), (uint32_t)stream,
                    (uint32_t)(stream >> 32)};
   philox10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
-  const uint64_t a = ((uint64_t)c[0] << 21) ^ (c[1] >> 11);
-  const uint64_t b = ((uint64_t)c[2] << 21) ^ (c[3] >> 11);
-  const double u1 = ((double)a + 0.5) * 0x1.0p-53;
-  const double u2 = ((double)b + 0.5) * 0x1.0p-53;
-  const double r = sqrt(-2.0 * log(u1));
-  const double two_pi = 6.283185307179586476925286766559;
-  double sn, cs;
-  sincos(two_pi * u2, &sn, &cs);
-  out[2 * p] = r * cs;
-  if (2 * p + 1 < n) out[2 * p + 1] = r * sn;
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const float u1 = fmaf(__uint2float_rn(c[2 * h]), 0x1p-32f, 0x1p-33f);
+    const float u2 = fmaf((float)(c[2 * h + 1] >> 9), 0x1p-23f, 0x1p-24f);
+    const float r = sqrtf(-2.f * logf(u1));
+    float sn, cs;
+    sincospif(2.f * u2, &sn, &cs);
+    const int64_t k = 4 * p + 2 * h;
+    if (k < n) out[k] = (double)(r * cs);
+    if (k + 1 < n) out[k + 1] = (double)(r * sn);
+  }
 }
 
 struct DeviceGuard {
@@ -281,6 +287,10 @@ int ensure_cheb_buffers(ggem_ctx *c, size_t len) {
   return GGEM_OK;
 }
 
+// cheb_slots' answer when a deferred list build turned out to have
+// overflowing rows: the list has been rebuilt and the series must restart
+constexpr int kRestartCheb = 1;
+
 // Chebyshev on slot-ordered xi (c->w_in); leaves y in c->w_y.
 //
 // check_every = 1: the reference's loop (brownian_system.C:1089-1155): the
@@ -337,7 +347,16 @@ int cheb_slots(ggem_ctx *c, int nrhs, int N, double eig_min, double eig_max, dou
     if (int rc = matvec_slots(c, nrhs, dw, dm, sm)) return rc;
     k_dot_partials<<<dim3(G, nrhs), kVecThreads, 0, st>>>(D, dm, dm, p_dm);
     if (int rc = check_launch(c, "dm norm")) return rc;
+    // a deferred list build is checked in the same synchronisation
+    const bool pending = c->list_unchecked;
+    if (pending)
+      if (int rc = enqueue_list_check(c)) return rc;
     if (int rc = finalize_to_host(c, 4 * nrhs, G, h)) return rc;
+    if (pending) {
+      bool rebuilt = false;
+      if (int rc = finish_list_check(c, &rebuilt)) return rc;
+      if (rebuilt) return kRestartCheb;
+    }
     for (int r = 0; r < nrhs; ++r) {
       if (!active[r]) continue;
       const double aux4 = std::sqrt(h[r]);
@@ -399,7 +418,7 @@ int cheb_slots(ggem_ctx *c, int nrhs, int N, double eig_min, double eig_max, dou
       }
     *dm_is_my = false;
     if (check) {
-      if (int rc = check_now(std::fabs(X[i + 1]), true)) return rc;
+      if (int rc = check_now(std::fabs(X[i + 1]), true)) return rc;  // incl. kRestartCheb
       *dm_is_my = true;
       if (first_check < 0) first_check = i + 1;
     }
@@ -446,8 +465,10 @@ extern "C" int ggem_cheb_inv_sqrt_dev(ggem_ctx *ctx, int nrhs, int N, double eig
   if (int rc = ensure_cheb_buffers(ctx, len)) return rc;
   if (int rc = permute_to_slots(ctx, nrhs, d_xi, ctx->w_in.p)) return rc;
   bool dm_is_my = false;
-  if (int rc = cheb_slots(ctx, nrhs, N, eig_min, eig_max, tol_cheb, check_every, rep, &dm_is_my))
-    return rc;
+  int rc = cheb_slots(ctx, nrhs, N, eig_min, eig_max, tol_cheb, check_every, rep, &dm_is_my);
+  if (rc == kRestartCheb)  // the deferred list was rebuilt wider: run the series again
+    rc = cheb_slots(ctx, nrhs, N, eig_min, eig_max, tol_cheb, check_every, rep, &dm_is_my);
+  if (rc) return rc;
   return permute_from_slots(ctx, nrhs, ctx->w_y.p, d_xi);
 }
 
@@ -502,8 +523,10 @@ extern "C" int ggem_brownian_displacement_dev(ggem_ctx *ctx, int nrhs, int N, do
   if (int rc = ensure_cheb_buffers(ctx, len)) return rc;
   if (int rc = permute_to_slots(ctx, nrhs, d_xi, ctx->w_in.p)) return rc;
   bool dm_is_my = false;
-  if (int rc = cheb_slots(ctx, nrhs, N, eig_min, eig_max, tol_cheb, check_every, rep, &dm_is_my))
-    return rc;
+  int rc = cheb_slots(ctx, nrhs, N, eig_min, eig_max, tol_cheb, check_every, rep, &dm_is_my);
+  if (rc == kRestartCheb)  // the deferred list was rebuilt wider: run the series again
+    rc = cheb_slots(ctx, nrhs, N, eig_min, eig_max, tol_cheb, check_every, rep, &dm_is_my);
+  if (rc) return rc;
   bool all = true;
   for (int r = 0; r < nrhs; ++r) all = all && rep[r].converged;
   if (!all)
@@ -522,6 +545,7 @@ extern "C" int ggem_lanczos_bounds(ggem_ctx *ctx, int k, uint64_t seed, double *
                                    double *eig_max) {
   if (!ctx || !eig_min || !eig_max) return GGEM_ERR_BAD_ARG;
   if (k < 2 || k > 512) return ggem::fail(ctx, GGEM_ERR_BAD_ARG, "Lanczos steps must be in [2, 512]");
+  if (int rc = settle_list(ctx)) return rc;
   if (!ctx->cells_built || (ctx->prm.precision == GGEM_FP32 && !ctx->list_built))
     return ggem::fail(ctx, GGEM_ERR_BAD_ARG, "call ggem_build_cells first");
   DeviceGuard dg(ctx->device);
@@ -537,7 +561,7 @@ extern "C" int ggem_lanczos_bounds(ggem_ctx *ctx, int k, uint64_t seed, double *
   const int G = vec_blocks(D);
   double *Q = ctx->lz_Q.p, *w = ctx->w_out.p, *h = ctx->h_red;
   // start vector: N(0,1) from the counter-based generator
-  k_philox_normals<<<(unsigned)((D / 2 + 256) / 256), 256, 0, st>>>(D, seed, 0x4C414E43ull, Q);
+  k_philox_normals<<<(unsigned)(((D + 3) / 4 + 255) / 256), 256, 0, st>>>(D, seed, 0x4C414E43ull, Q);
   if (int rc = check_launch(ctx, "lanczos start")) return rc;
   if (int rc = sumsq_to_host(ctx, 1, D, Q, h)) return rc;
   k_scale<<<grid1(D), 256, 0, st>>>(D, 1.0 / std::sqrt(h[0]), Q, Q);
@@ -577,6 +601,7 @@ extern "C" int ggem_lanczos_bounds(ggem_ctx *ctx, int k, uint64_t seed, double *
 
 extern "C" int ggem_power_iteration(ggem_ctx *ctx, double tol, int maxits, double *eig) {
   if (!ctx || !(tol > 0) || maxits < 1 || !eig) return GGEM_ERR_BAD_ARG;
+  if (int rc = settle_list(ctx)) return rc;
   if (!ctx->cells_built || (ctx->prm.precision == GGEM_FP32 && !ctx->list_built))
     return ggem::fail(ctx, GGEM_ERR_BAD_ARG, "call ggem_build_cells first");
   DeviceGuard dg(ctx->device);
@@ -616,7 +641,7 @@ extern "C" int ggem_philox_normals_dev(ggem_ctx *ctx, uint64_t seed, uint64_t st
   if (!ctx || n < 0 || (n > 0 && !d_out)) return GGEM_ERR_BAD_ARG;
   if (n == 0) return GGEM_OK;
   DeviceGuard dg(ctx->device);
-  const int64_t pairs = (n + 1) / 2;
-  k_philox_normals<<<(unsigned)((pairs + 255) / 256), 256, 0, ctx->stream>>>(n, seed, stream, d_out);
+  const int64_t quads = (n + 3) / 4;
+  k_philox_normals<<<(unsigned)((quads + 255) / 256), 256, 0, ctx->stream>>>(n, seed, stream, d_out);
   return check_launch(ctx, "philox");
 }

@@ -104,6 +104,8 @@ extern "C" int ggem_get_launch_count(const ggem_ctx *ctx, int64_t *count) {
 
 extern "C" int ggem_get_pair_count(const ggem_ctx *ctx, int64_t *count) {
   if (!ctx || !count) return GGEM_ERR_BAD_ARG;
+  // reading pending statistics of a deferred build updates only cached state
+  if (int rc = settle_list(const_cast<ggem_ctx *>(ctx))) return rc;
   if (!ctx->list_built) return GGEM_ERR_BAD_ARG;
   *count = ctx->n_pairs;
   return GGEM_OK;
@@ -111,6 +113,7 @@ extern "C" int ggem_get_pair_count(const ggem_ctx *ctx, int64_t *count) {
 
 extern "C" int ggem_get_pair_storage(const ggem_ctx *ctx, int *row_width, int *tensors_stored) {
   if (!ctx || !row_width || !tensors_stored) return GGEM_ERR_BAD_ARG;
+  if (int rc = settle_list(const_cast<ggem_ctx *>(ctx))) return rc;
   if (!ctx->list_built) return GGEM_ERR_BAD_ARG;
   *row_width = ctx->nb_w;
   *tensors_stored = ctx->pretensor_ok ? 1 : 0;

@@ -175,6 +175,7 @@ using namespace ggem;
 extern "C" int ggem_ev_gaussian_forces_dev(ggem_ctx *ctx, double c1, double c2, double *d_f,
                                            int accumulate) {
   if (!ctx || (!d_f && ctx->n)) return GGEM_ERR_BAD_ARG;
+  if (int rc = settle_list(ctx)) return rc;
   if (!ctx->cells_built) return fail(ctx, GGEM_ERR_BAD_ARG, "call ggem_build_cells first");
   FGuard g(ctx->device);
   if (ctx->n == 0) return GGEM_OK;
@@ -189,6 +190,7 @@ extern "C" int ggem_ev_gaussian_forces_dev(ggem_ctx *ctx, double c1, double c2, 
 extern "C" int ggem_ev_gaussian_forces(ggem_ctx *ctx, double c1, double c2, double *f,
                                        int accumulate) {
   if (!ctx || (!f && ctx->n)) return GGEM_ERR_BAD_ARG;
+  if (int rc = settle_list(ctx)) return rc;
   if (!ctx->cells_built) return fail(ctx, GGEM_ERR_BAD_ARG, "call ggem_build_cells first");
   FGuard g(ctx->device);
   return with_host_forces(ctx, f, accumulate, [&](double *d) {
@@ -233,6 +235,7 @@ extern "C" int ggem_spring_forces_dev(ggem_ctx *ctx, int kind, double c1, double
                                       int accumulate) {
   if (!ctx || (!d_f && ctx->n) || kind < GGEM_SPRING_WLS || kind > GGEM_SPRING_LHS)
     return GGEM_ERR_BAD_ARG;
+  if (int rc = settle_list(ctx)) return rc;
   if (!ctx->cells_built) return fail(ctx, GGEM_ERR_BAD_ARG, "call ggem_build_cells first");
   if (ctx->bond_n != ctx->n) return fail(ctx, GGEM_ERR_BAD_ARG, "set the bonds for these particles");
   FGuard g(ctx->device);
@@ -246,6 +249,7 @@ extern "C" int ggem_spring_forces_dev(ggem_ctx *ctx, int kind, double c1, double
 extern "C" int ggem_spring_forces(ggem_ctx *ctx, int kind, double c1, double Ls, double *f,
                                   int accumulate) {
   if (!ctx || (!f && ctx->n)) return GGEM_ERR_BAD_ARG;
+  if (int rc = settle_list(ctx)) return rc;
   if (!ctx->cells_built) return fail(ctx, GGEM_ERR_BAD_ARG, "call ggem_build_cells first");
   FGuard g(ctx->device);
   return with_host_forces(ctx, f, accumulate, [&](double *d) {

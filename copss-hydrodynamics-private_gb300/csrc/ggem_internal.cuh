@@ -53,6 +53,7 @@ struct DevConsts {
 // uniform cell grid over the box (cells == elements in reference mode)
 struct Grid {
   double lo[3], L[3], h[3];
+  double inv_h[3];  // 1 / h, for the fast path of the cell index
   float h32[3];
   int nc[3];
   int periodic[3];
@@ -115,6 +116,12 @@ struct ggem_ctx {
 
   // FP32 pair list
   bool list_built = false;
+  // deferred checks (ggem_set_deferred_checks): a build after the first one
+  // keeps the row width and leaves its statistics and error word on the
+  // device; the next synchronising call reads them (list_unchecked)
+  bool defer_checks = false;
+  bool list_checked_once = false;
+  bool list_unchecked = false;
   int64_t n_pairs = 0;
   ggem::DevBuf<int32_t> nb_cnt;       // entries per target row
   ggem::DevBuf<unsigned long long> nb_stat;  // [0] total entries, [1] longest row
@@ -141,6 +148,7 @@ struct ggem_ctx {
   bool allow_pretensor = true;  // ggem_set_pair_tensors
   bool pretensor_ok = false;
   int stored_variant = 0;         // shape of the stored-tensor pair kernels (autotuned)
+  int computed_variant = 0;       // loop shape of the per-matvec-tensor kernels (autotuned)
   ggem::DevBuf<float4> pair_ten;
   ggem::DevBuf<float4> w_f4[2];
   int rec_cur = 0;
@@ -205,6 +213,15 @@ void cheb_coeffs_host(int N, double da, double db, int method, double *coef);
 int build_cells(ggem_ctx *c, bool defer_flags = false);
 int cell_flag_error(ggem_ctx *c, int flags);
 int build_pair_list(ggem_ctx *c);
+// deferred builds: copy the list statistics and the error word to the host
+// mirror (asynchronous), then, after the stream has synchronised, evaluate
+// them; *rebuilt is set when the rows had overflowed and the list (and the
+// stored pair tensors) were rebuilt wider: results computed since the
+// build are void.  settle_list does both with its own synchronisation.
+int enqueue_list_check(ggem_ctx *c);
+int finish_list_check(ggem_ctx *c, bool *rebuilt);
+int settle_list(ggem_ctx *c);
+constexpr int kListStatSlot = 4088;  // h_red[4088 .. 4090]: deferred list statistics
 int device_exclusive_scan_i32(ggem_ctx *c, const int32_t *in, int32_t *out, int64_t n);
 int device_exclusive_scan_i64(ggem_ctx *c, const int64_t *in, int64_t *out, int64_t n);
 

@@ -265,37 +265,111 @@ __global__ void k_build_src(int64_t n, const float4 *__restrict__ pos32,
   src[s] = r;
 }
 
-// float-float sum of one target's pair terms, complete on every lane of the group
+// float-float sum of one target's pair terms
 struct PairSum {
   float hx, lx, hy, ly, hz, lz;
 };
 
-// the pair loop of one target slot s over its CSR entries (one right-hand
+// 2^x on the special-function unit (PTX ex2.approx.ftz.f32); the argument
+// range of the tensor, [-alpha^2 rc^2 log2(e), 0], keeps results normal
+__device__ __forceinline__ float ex2_sfu(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+// one 32-byte record in a single 256-bit read-only load (sm_100+): the
+// position and the force of a source share one sector, so one request per
+// warp touches each sector once instead of twice
+__device__ __forceinline__ Rec32 ld_rec32(const Rec32 *p) {
+  Rec32 r;
+  asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+      : "=f"(r.a.x), "=f"(r.a.y), "=f"(r.a.z), "=f"(r.a.w), "=f"(r.b.x), "=f"(r.b.y),
+        "=f"(r.b.z), "=f"(r.b.w)
+      : "l"(p));
+  return r;
+}
+
+// the FP32 cell shift of every entry code, staged per block in shared
+// memory (one 16-byte load per pair instead of decoding the code); the
+// table holds (float)(k h) for offsets |k| <= 2, which equals the FP32
+// product k * (float)h that the list build and decode_shift use
+__device__ __forceinline__ void stage_shifts(float4 *sh, const float4 *__restrict__ shift) {
+  for (int k = threadIdx.x; k < kMaxCode; k += blockDim.x) sh[k] = shift[k];
+  __syncthreads();
+}
+
+// reduce-scatter of the group's float-float sums: afterwards lane sub
+// (0, 1, 2) holds component sub of the target's total, summed in the same
+// tree as the all-reduce ((lane 0 + lane 2) + (lane 1 + lane 3))
+__device__ __forceinline__ void group_scatter3(int sub, const PairSum &r, float &h, float &l) {
+  const bool up = sub & 2;
+  // lanes 0, 1 keep (x, y) and send z; lanes 2, 3 keep z and send (x, y)
+  float k1h = up ? r.hz : r.hx, k1l = up ? r.lz : r.lx;
+  float k2h = up ? 0.f : r.hy, k2l = up ? 0.f : r.ly;
+  const float s1h = up ? r.hx : r.hz, s1l = up ? r.lx : r.lz;
+  const float s2h = up ? r.hy : 0.f, s2l = up ? r.ly : 0.f;
+  const float a1h = __shfl_xor_sync(0xffffffffu, s1h, 2), a1l = __shfl_xor_sync(0xffffffffu, s1l, 2);
+  const float a2h = __shfl_xor_sync(0xffffffffu, s2h, 2), a2l = __shfl_xor_sync(0xffffffffu, s2l, 2);
+  ff_add(k1h, k1l, a1h, a1l);
+  ff_add(k2h, k2l, a2h, a2l);
+  // lane 0 keeps x, lane 1 keeps y, lane 2 keeps z (lane 3: zero)
+  const bool odd = sub & 1;
+  h = odd ? k2h : k1h;
+  l = odd ? k2l : k1l;
+  const float th = odd ? k1h : k2h, tl = odd ? k1l : k2l;
+  const float bh = __shfl_xor_sync(0xffffffffu, th, 1), bl = __shfl_xor_sync(0xffffffffu, tl, 1);
+  ff_add(h, l, bh, bl);
+}
+
+// the pair loop of one target slot s over its list entries (one right-hand
 // side, 32-byte source records); lanes sub = 0..kGroup-1 take every
-// kGroup-th entry, so a group reads consecutive list words
-template <int CD, bool POLY>
+// kGroup-th entry, so a group reads consecutive list words.  The next entry
+// of the lane is loaded while the current pair is evaluated.  (Prefetching
+// the next source record into registers or L1 as well measured no faster.)
+template <bool POLY>
 __device__ __forceinline__ PairSum pair_sum_r1(int64_t s, bool act, int sub, const Rec32 &ri,
                                                const Rec32 *__restrict__ src,
                                                const int32_t *__restrict__ cnt, int W,
                                                const uint32_t *__restrict__ list,
                                                const PolyAB &P, const Rec32 *__restrict__ tab,
-                                               float inv_ds, float hx, float hy, float hz) {
-  const int64_t b = s * (int64_t)W, e = act ? b + cnt[s] : b;
+                                               float inv_ds, const float4 *sh) {
+  const uint32_t *lp = list + s * (int64_t)W + sub;
+  int left = (act ? cnt[s] : 0) - sub;  // entries lp[0], lp[kGroup], ... while left > 0
   float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
   float2 bxy = make_float2(0.f, 0.f);
   float bz = 0.f;
   int blk = 0;
-  for (int64_t m = b + sub; m < e; m += kGroup) {
-    const uint32_t en = __ldg(list + m);
-    const Rec32 rj = src[en >> kCodeBits];
-    float ox, oy, oz;
-    decode_shift<CD>(en, hx, hy, hz, ox, oy, oz);
-    const float dx = (rj.a.x - ri.a.x) + ox;
-    const float dy = (rj.a.y - ri.a.y) + oy;
-    const float dz = (rj.a.z - ri.a.z) + oz;
+  uint32_t nxt = left > 0 ? __ldg(lp) : 0u;
+  while (left > 0) {
+    const uint32_t en = nxt;
+    left -= kGroup;
+    lp += kGroup;
+    if (left > 0) nxt = __ldg(lp);
+    const Rec32 rj = ld_rec32(src + (en >> kCodeBits));
+    const float4 o = sh[en & (kMaxCode - 1)];
+    const float dx = (rj.a.x - ri.a.x) + o.x;
+    const float dy = (rj.a.y - ri.a.y) + o.y;
+    const float dz = (rj.a.z - ri.a.z) + o.z;
     const float s2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
     float A, B;
-    tensor_ab32<POLY>(s2, P, tab, inv_ds, A, B);
+    if (POLY) {
+      const float x = fmaf(s2, P.x1, P.x0);
+      const float2 xx = make_float2(x, x);
+      float2 ab = P.ab[kPolyDeg];
+#pragma unroll
+      for (int q = kPolyDeg - 1; q >= 0; --q) ab = __ffma2_rn(ab, xx, P.ab[q]);
+      // e^{-alpha^2 s} = 2^{p + r}, p = s e_hi rounded, r its residual plus s e_lo
+      const float p = s2 * P.e_hi;
+      const float r = fmaf(s2, P.e_lo, fmaf(s2, P.e_hi, -p));
+      const float E0 = ex2_sfu(p);
+      const float E = fmaf(E0, r * 0.6931471805599453f, E0);
+      ab = __fmul2_rn(ab, make_float2(E, E));
+      A = ab.x;
+      B = ab.y;
+    } else {
+      tensor_ab32<false>(s2, P, tab, inv_ds, A, B);
+    }
     // G f = A f + B (x.f) x, the x and y components packed (FFMA2)
     const float2 dxy = make_float2(dx, dy), fxy = make_float2(rj.b.x, rj.b.y);
     const float2 pxy = __fmul2_rn(dxy, fxy);
@@ -316,61 +390,67 @@ __device__ __forceinline__ PairSum pair_sum_r1(int64_t s, bool act, int sub, con
   kahan_add(sy, cy, bxy.y);
   kahan_add(sz, cz, bz);
   // Kahan keeps sum = s - c: the float-float value is (s, -c)
-  PairSum r{sx, -cx, sy, -cy, sz, -cz};
-  group_ff(r.hx, r.lx);
-  group_ff(r.hy, r.ly);
-  group_ff(r.hz, r.lz);
-  return r;
+  return PairSum{sx, -cx, sy, -cy, sz, -cz};
 }
 
+// the per-matvec-tensor kernel shapes the autotuner chooses from: blocks of
+// 256 threads per SM that the register cap allows (6 at 40 registers, 8 at 32
+// with a few spills outside the pair loop)
+constexpr int kComputedMinBlocks[] = {6, 8};
+constexpr int kNumComputedVariants = 2;
+
 // u = M f, single right-hand side
-template <int CD, bool POLY>
-__global__ void __launch_bounds__(256) k_pair_r1(
+template <bool POLY, int V>
+__global__ void __launch_bounds__(256, kComputedMinBlocks[V]) k_pair_r1(
     int64_t n, const Rec32 *__restrict__ src, const int32_t *__restrict__ cnt, int W,
     const uint32_t *__restrict__ list, PolyAB P, const Rec32 *__restrict__ tab, float inv_ds,
-    float hx, float hy, float hz, double self_c, const double *__restrict__ f,
+    const float4 *__restrict__ shift, double self_c, const double *__restrict__ f,
     double *__restrict__ u) {
+  __shared__ float4 sh[kMaxCode];
+  stage_shifts(sh, shift);
   const int64_t gid = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / kGroup;
   const int sub = (int)(threadIdx.x % kGroup);
   const bool act = gid < n;
   const int64_t s = act ? gid : n - 1;
   const Rec32 ri = src[s];
-  const PairSum r =
-      pair_sum_r1<CD, POLY>(s, act, sub, ri, src, cnt, W, list, P, tab, inv_ds, hx, hy, hz);
-  group_store(act, sub, s, r.hx, r.lx, r.hy, r.ly, r.hz, r.lz, self_c, f, u);
+  const PairSum r = pair_sum_r1<POLY>(s, act, sub, ri, src, cnt, W, list, P, tab, inv_ds, sh);
+  float h, l;
+  group_scatter3(sub, r, h, l);
+  if (!act || sub >= 3) return;
+  const int64_t k = 3 * s + sub;
+  u[k] = fma(self_c, f[k], f2d_bits(h) + f2d_bits(l));
 }
 
 // One Chebyshev term with the pair sum (brownian_system.C:1091-1108 for one
 // right-hand side, without the norms of the error estimators):
 //   m = M x1 (pair sum + self term),  xm = (2db x1 + 2da m) - x0,
 //   dw += coef xm,  and the 32-byte records of xm for the next term.
+// With c1 = 2db + 2da self_c this is xm = 2da (pair sum) + (c1 x1 - x0).
 // src holds the records of x1; next must be a different buffer.
-template <int CD, bool POLY>
-__global__ void __launch_bounds__(256) k_pair_cheb(
+template <bool POLY, int V>
+__global__ void __launch_bounds__(256, kComputedMinBlocks[V]) k_pair_cheb(
     int64_t n, const Rec32 *__restrict__ src, const int32_t *__restrict__ cnt, int W,
     const uint32_t *__restrict__ list, PolyAB P, const Rec32 *__restrict__ tab, float inv_ds,
-    float hx, float hy, float hz, double self_c, double two_da, double two_db, double coef,
+    const float4 *__restrict__ shift, double two_da, double c1, double coef,
     const double *__restrict__ x0, const double *__restrict__ x1, double *__restrict__ xm,
     double *__restrict__ dw, Rec32 *__restrict__ next) {
+  __shared__ float4 sh[kMaxCode];
+  stage_shifts(sh, shift);
   const int64_t gid = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / kGroup;
   const int sub = (int)(threadIdx.x % kGroup);
   const bool act = gid < n;
   const int64_t s = act ? gid : n - 1;
   const Rec32 ri = src[s];
-  const PairSum r =
-      pair_sum_r1<CD, POLY>(s, act, sub, ri, src, cnt, W, list, P, tab, inv_ds, hx, hy, hz);
+  const PairSum r = pair_sum_r1<POLY>(s, act, sub, ri, src, cnt, W, list, P, tab, inv_ds, sh);
+  float h, l;
+  group_scatter3(sub, r, h, l);
   if (!act) return;
   float *nf = reinterpret_cast<float *>(next + s);
   if (sub < 3) {
-    const float h = sub == 0 ? r.hx : (sub == 1 ? r.hy : r.hz);
-    const float l = sub == 0 ? r.lx : (sub == 1 ? r.ly : r.lz);
     const int64_t k = 3 * s + sub;
-    const double xk = x1[k];
-    const double m = fma(self_c, xk, f2d_bits(h) + f2d_bits(l));
-    double v = two_db * xk + two_da * m;
-    v -= x0[k];
+    const double v = fma(two_da, f2d_bits(h) + f2d_bits(l), fma(c1, x1[k], -x0[k]));
     xm[k] = v;
-    dw[k] = dw[k] + coef * v;
+    dw[k] = fma(coef, v, dw[k]);
     nf[4 + sub] = __double2float_rn(v);
   } else {
     reinterpret_cast<float4 *>(nf)[0] = ri.a;  // the target's position record
@@ -905,14 +985,18 @@ PolyAB poly_of(const ggem_ctx *c) {
   return P;
 }
 
-template <int CD, bool POLY>
+template <bool POLY, int V>
 void launch_r1(ggem_ctx *c, const Rec32 *src, const double *f, double *u, double self_c) {
   const int64_t threads = c->n * kGroup;
-  const Grid &g = c->grid;
-  k_pair_r1<CD, POLY><<<(unsigned)((threads + 255) / 256), 256, 0, c->stream>>>(
+  k_pair_r1<POLY, V><<<(unsigned)((threads + 255) / 256), 256, 0, c->stream>>>(
       c->n, src, c->nb_cnt.p, c->nb_w, c->nb_list.p, poly_of(c),
-      reinterpret_cast<const Rec32 *>(c->tab.p), c->tab_inv_ds, g.h32[0], g.h32[1], g.h32[2],
-      self_c, f, u);
+      reinterpret_cast<const Rec32 *>(c->tab.p), c->tab_inv_ds, c->d_shift.p, self_c, f, u);
+}
+
+template <bool POLY>
+void dispatch_r1(ggem_ctx *c, const Rec32 *src, const double *f, double *u, double self_c) {
+  if (c->computed_variant == 1) launch_r1<POLY, 1>(c, src, f, u, self_c);
+  else launch_r1<POLY, 0>(c, src, f, u, self_c);
 }
 
 // single right-hand side: records from FP64 slot-order f, then the pair sum
@@ -933,23 +1017,28 @@ int launch_f32_r1(ggem_ctx *c, const double *f, double *u, double self_c) {
   k_build_src<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(n, c->pos32.p, f, src);
   if (int rc = check_launch(c, "pair records")) return rc;
   kt_start(c, kKPairF32);
-  const bool cd2 = c->prm.cell_div == 2;
-  if (c->use_poly) cd2 ? launch_r1<2, true>(c, src, f, u, self_c) : launch_r1<1, true>(c, src, f, u, self_c);
-  else cd2 ? launch_r1<2, false>(c, src, f, u, self_c) : launch_r1<1, false>(c, src, f, u, self_c);
+  if (c->use_poly) dispatch_r1<true>(c, src, f, u, self_c);
+  else dispatch_r1<false>(c, src, f, u, self_c);
   kt_stop(c, kKPairF32);
   return check_launch(c, "pair f32 r1");
 }
 
-template <int CD, bool POLY>
-void launch_cheb(ggem_ctx *c, const Rec32 *src, Rec32 *next, double self_c, double two_da,
-                 double two_db, double coef, const double *x0, const double *x1, double *xm,
-                 double *dw) {
+// c1 = 2db + 2da self_c folds the self term into the x1 coefficient
+template <bool POLY, int V>
+void launch_cheb(ggem_ctx *c, const Rec32 *src, Rec32 *next, double two_da, double c1,
+                 double coef, const double *x0, const double *x1, double *xm, double *dw) {
   const int64_t threads = c->n * kGroup;
-  const Grid &g = c->grid;
-  k_pair_cheb<CD, POLY><<<(unsigned)((threads + 255) / 256), 256, 0, c->stream>>>(
+  k_pair_cheb<POLY, V><<<(unsigned)((threads + 255) / 256), 256, 0, c->stream>>>(
       c->n, src, c->nb_cnt.p, c->nb_w, c->nb_list.p, poly_of(c),
-      reinterpret_cast<const Rec32 *>(c->tab.p), c->tab_inv_ds, g.h32[0], g.h32[1], g.h32[2],
-      self_c, two_da, two_db, coef, x0, x1, xm, dw, next);
+      reinterpret_cast<const Rec32 *>(c->tab.p), c->tab_inv_ds, c->d_shift.p, two_da, c1, coef,
+      x0, x1, xm, dw, next);
+}
+
+template <bool POLY>
+void dispatch_cheb(ggem_ctx *c, const Rec32 *src, Rec32 *next, double two_da, double c1,
+                   double coef, const double *x0, const double *x1, double *xm, double *dw) {
+  if (c->computed_variant == 1) launch_cheb<POLY, 1>(c, src, next, two_da, c1, coef, x0, x1, xm, dw);
+  else launch_cheb<POLY, 0>(c, src, next, two_da, c1, coef, x0, x1, xm, dw);
 }
 
 template <int CD, bool POLY>
@@ -1060,16 +1149,10 @@ int pair_cheb_term(ggem_ctx *c, bool records_fresh, const double *x0, const doub
     k_build_src<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(n, c->pos32.p, x1, cur);
     if (int rc = check_launch(c, "chebyshev records")) return rc;
   }
-  const double self_c = self_coefficient(c, self_mode);
+  const double c1 = two_db + two_da * self_c0;
   kt_start(c, kKPairCheb);
-  const bool cd2 = c->prm.cell_div == 2;
-  if (c->use_poly) {
-    if (cd2) launch_cheb<2, true>(c, cur, nxt, self_c, two_da, two_db, coef, x0, x1, xm, dw);
-    else launch_cheb<1, true>(c, cur, nxt, self_c, two_da, two_db, coef, x0, x1, xm, dw);
-  } else {
-    if (cd2) launch_cheb<2, false>(c, cur, nxt, self_c, two_da, two_db, coef, x0, x1, xm, dw);
-    else launch_cheb<1, false>(c, cur, nxt, self_c, two_da, two_db, coef, x0, x1, xm, dw);
-  }
+  if (c->use_poly) dispatch_cheb<true>(c, cur, nxt, two_da, c1, coef, x0, x1, xm, dw);
+  else dispatch_cheb<false>(c, cur, nxt, two_da, c1, coef, x0, x1, xm, dw);
   kt_stop(c, kKPairCheb);
   c->rec_cur ^= 1;
   return check_launch(c, "pair chebyshev term");
@@ -1175,18 +1258,22 @@ int matvec_f32_staged(ggem_ctx *c, int nrhs, const double *f, double *u, int sel
 
 using namespace ggem;
 
-extern "C" int ggem_set_pair_variant(ggem_ctx *ctx, int variant) {
-  if (!ctx || variant < 0 || variant >= kNumStoredVariants) return GGEM_ERR_BAD_ARG;
-  ctx->stored_variant = variant;
+extern "C" int ggem_set_pair_variant(ggem_ctx *ctx, int computed, int stored) {
+  if (!ctx || computed < 0 || computed >= kNumComputedVariants || stored < 0 ||
+      stored >= kNumStoredVariants)
+    return GGEM_ERR_BAD_ARG;
+  ctx->computed_variant = computed;
+  ctx->stored_variant = stored;
   return GGEM_OK;
 }
 
 extern "C" int ggem_autotune_pair_storage(ggem_ctx *ctx, int reps, double matvecs_per_build,
                                           int *use_stored, double *ms_computed,
-                                          double *ms_stored, int *stored_variant) {
+                                          double *ms_stored, int *variants) {
   if (!ctx || reps < 1 || !(matvecs_per_build > 0) || !use_stored || !ms_computed ||
-      !ms_stored || !stored_variant)
+      !ms_stored || !variants)
     return GGEM_ERR_BAD_ARG;
+  if (int rc = settle_list(ctx)) return rc;
   if (ctx->prm.precision != GGEM_FP32 || !ctx->list_built)
     return fail(ctx, GGEM_ERR_BAD_ARG, "autotune needs a built FP32 pair list");
   int dev = 0;
@@ -1219,9 +1306,22 @@ extern "C" int ggem_autotune_pair_storage(ggem_ctx *ctx, int reps, double matvec
   int rc = GGEM_OK;
   double t_comp = 0.0, t_store = 1e30;
   const bool allow = ctx->allow_pretensor;
-  // tensors evaluated per pair and matvec
+  // tensors evaluated per pair and matvec, each loop shape; the fastest stays
   ctx->pretensor_ok = false;
-  rc = time_matvecs(&t_comp);
+  {
+    int best_v = 0;
+    t_comp = 1e30;
+    for (int v = 0; v < kNumComputedVariants && !rc; ++v) {
+      ctx->computed_variant = v;
+      double t_mv = 0.0;
+      rc = time_matvecs(&t_mv);
+      if (!rc && t_mv < t_comp) {
+        t_comp = t_mv;
+        best_v = v;
+      }
+    }
+    ctx->computed_variant = best_v;
+  }
   if (!rc && ctx->use_pretensor) {
     ctx->allow_pretensor = true;
     cudaEventRecord(a, ctx->stream);
@@ -1261,7 +1361,8 @@ extern "C" int ggem_autotune_pair_storage(ggem_ctx *ctx, int reps, double matvec
   *use_stored = stored ? 1 : 0;
   *ms_computed = t_comp;
   *ms_stored = ctx->use_pretensor ? t_store : -1.0;
-  *stored_variant = ctx->stored_variant;
+  variants[0] = ctx->computed_variant;
+  variants[1] = ctx->stored_variant;
   if (dev != ctx->device) cudaSetDevice(dev);
   return GGEM_OK;
 }

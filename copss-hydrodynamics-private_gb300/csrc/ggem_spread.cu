@@ -338,6 +338,7 @@ extern "C" int ggem_green_tensor_local(ggem_ctx *ctx, int64_t m, const double *x
 extern "C" int ggem_local_field(ggem_ctx *ctx, int64_t nt, const double *targets, const double *f,
                                 double *u) {
   if (!ctx || nt < 0 || (nt > 0 && (!targets || !u)) || (ctx->n > 0 && !f)) return GGEM_ERR_BAD_ARG;
+  if (int rc = ggem::settle_list(ctx)) return rc;
   if (!ctx->cells_built) return ggem::fail(ctx, GGEM_ERR_BAD_ARG, "call ggem_build_cells first");
   DeviceGuard dg(ctx->device);
   if (int rc = stage_common(ctx, nt, targets, f)) return rc;
@@ -358,6 +359,7 @@ static double spread_radius(const ggem_ctx *ctx, double spread_rc) {
 extern "C" int ggem_spread_qp(ggem_ctx *ctx, int64_t nq, const double *qxyz, const int32_t *qp_elem,
                               const double *f, double spread_rc, double *rho) {
   if (!ctx || nq < 0 || (nq > 0 && (!qxyz || !rho)) || (ctx->n > 0 && !f)) return GGEM_ERR_BAD_ARG;
+  if (int rc = ggem::settle_list(ctx)) return rc;
   if (!ctx->cells_built) return ggem::fail(ctx, GGEM_ERR_BAD_ARG, "call ggem_build_cells first");
   const bool ref = ctx->prm.nb_mode == GGEM_NB_REFERENCE;
   if (ref && !qp_elem && nq > 0)
@@ -386,6 +388,7 @@ extern "C" int ggem_element_rhs(ggem_ctx *ctx, int64_t n_elem, int nq_per_elem, 
   if (!ctx || n_elem < 0 || nq_per_elem < 1 || n_u < 1 ||
       (n_elem > 0 && (!qxyz || !int_force || !Fe)) || (ctx->n > 0 && !f))
     return GGEM_ERR_BAD_ARG;
+  if (int rc = ggem::settle_list(ctx)) return rc;
   if (!ctx->cells_built) return ggem::fail(ctx, GGEM_ERR_BAD_ARG, "call ggem_build_cells first");
   const bool ref = ctx->prm.nb_mode == GGEM_NB_REFERENCE;
   if (ref && n_elem != ctx->grid.ncell)

@@ -793,6 +793,7 @@ extern "C" int ggem_surrogate_gradient(ggem_surrogate *s, const float *X, const 
 
 extern "C" int ggem_surrogate_features(ggem_ctx *ctx, double chain_fraction, float *features) {
   if (!ctx || !features) return GGEM_ERR_BAD_ARG;
+  if (int rc = ggem::settle_list(ctx)) return rc;
   if (ctx->prm.precision != GGEM_FP32 || !ctx->list_built)
     return fail(ctx, GGEM_ERR_BAD_ARG, "features need the FP32 pair list (build cells first)");
   SurDeviceGuard dg(ctx->device);

@@ -99,6 +99,7 @@ def lib():
         "ggem_set_particles": (i, [vp, i64, vp]),
         "ggem_set_particles_dev": (i, [vp, i64, vp]),
         "ggem_build_cells": (i, [vp]),
+        "ggem_set_deferred_checks": (i, [vp, i]),
         "ggem_neighbor_pair_count": (i, [vp, P(i64)]),
         "ggem_get_neighbors": (i, [vp, vp, vp, i64]),
         "ggem_get_cell_of_particles": (i, [vp, vp]),
@@ -118,7 +119,7 @@ def lib():
         "ggem_get_pair_storage": (i, [vp, P(i), P(i)]),
         "ggem_set_pair_tensors": (i, [vp, i]),
         "ggem_autotune_pair_storage": (i, [vp, i, d, P(i), P(d), P(d), P(i)]),
-        "ggem_set_pair_variant": (i, [vp, i]),
+        "ggem_set_pair_variant": (i, [vp, i, i]),
         "ggem_probe_fp32_peak": (i, [vp, P(d)]),
         "ggem_set_kernel_timing": (i, [vp, i]),
         "ggem_get_kernel_timing": (i, [vp, i, P(d), P(i64)]),
@@ -410,6 +411,11 @@ class Context:
     def build_cells(self):
         self._check(lib().ggem_build_cells(self.h))
 
+    def set_deferred_checks(self, enable: bool):
+        """builds after the first keep the row width and return without
+        waiting; their statistics are read by the next synchronising call"""
+        self._check(lib().ggem_set_deferred_checks(self.h, 1 if enable else 0))
+
     def pair_count(self) -> int:
         v = C.c_int64()
         self._check(lib().ggem_neighbor_pair_count(self.h, C.byref(v)))
@@ -513,16 +519,18 @@ class Context:
 
     def autotune_pair_storage(self, reps=10, matvecs_per_build=12.0):
         """(use_stored, ms per matvec computed, ms per matvec stored incl. the
-        amortised tensor pass); the faster variant stays selected"""
-        u, a, b, v = C.c_int(), C.c_double(), C.c_double(), C.c_int()
+        amortised tensor pass); the faster form and the fastest kernel shape
+        of each stay selected (``pair_variants``: computed, stored)"""
+        u, a, b, v = C.c_int(), C.c_double(), C.c_double(), (C.c_int * 2)()
         self._check(lib().ggem_autotune_pair_storage(self.h, int(reps), float(matvecs_per_build),
-                                                     C.byref(u), C.byref(a), C.byref(b),
-                                                     C.byref(v)))
-        self.stored_variant = v.value
+                                                     C.byref(u), C.byref(a), C.byref(b), v))
+        self.pair_variants = (v[0], v[1])
         return bool(u.value), a.value, b.value
 
-    def set_pair_variant(self, v):
-        self._check(lib().ggem_set_pair_variant(self.h, int(v)))
+    def set_pair_variant(self, computed=0, stored=0):
+        """kernel shapes: computed 0 (registers capped for 6) or 1 (for 8
+        blocks per SM); stored 0 .. 3"""
+        self._check(lib().ggem_set_pair_variant(self.h, int(computed), int(stored)))
 
     def pair_storage(self):
         """(row width, whether per-pair tensors are stored)"""

@@ -32,15 +32,17 @@ int ggem_set_pair_tensors(ggem_ctx *ctx, int enable);
  * built, FP32): times `reps` single-RHS matvecs with tensors evaluated per
  * pair and with stored tensors (plus the one tensor pass per build,
  * amortised over matvecs_per_build matvecs) by CUDA events on the context's
- * stream; the stored form is timed for each of its kernel shapes (lanes per
- * target, entries in flight, pipelined stream).  The fastest stays selected
- * for this context; both costs are reported in ms per matvec (the stored
- * one with its amortised pass), with the chosen stored shape */
+ * stream; each form is timed for each of its kernel shapes (per-matvec
+ * tensors: registers capped for 6 or for 8 blocks per SM; stored
+ * tensors: lanes per target, entries in flight, pipelined stream).  The
+ * fastest stays selected for this context; both costs are reported in ms
+ * per matvec (the stored one with its amortised pass) and variants[0],
+ * variants[1] receive the chosen computed and stored shapes */
 int ggem_autotune_pair_storage(ggem_ctx *ctx, int reps, double matvecs_per_build,
                                int *use_stored, double *ms_computed, double *ms_stored,
-                               int *stored_variant);
-/* select the stored-tensor kernel shape directly (0 .. 3) */
-int ggem_set_pair_variant(ggem_ctx *ctx, int variant);
+                               int *variants);
+/* select the kernel shapes directly: computed 0 .. 1, stored 0 .. 3 */
+int ggem_set_pair_variant(ggem_ctx *ctx, int computed, int stored);
 /* dense FP32 FMA throughput of this device in TFLOP/s (FMA = 2 flops),
  * measured with CUDA events over a register-resident FMA chain kernel on the
  * context's stream */

@@ -132,6 +132,16 @@ int ggem_synchronize(ggem_ctx *ctx);
 int ggem_set_particles(ggem_ctx *ctx, int64_t n, const double *xyz);
 int ggem_set_particles_dev(ggem_ctx *ctx, int64_t n, const double *d_xyz);
 int ggem_build_cells(ggem_ctx *ctx);
+/* deferred checks: with enable = 1, a build after the first one keeps the
+ * pair-list row width and returns without waiting for the device; its row
+ * statistics and error word (a particle outside a non-periodic axis, a row
+ * longer than the width) are read at the next synchronising call.  The
+ * Chebyshev calls read them with their first error check and, when the rows
+ * overflowed, rebuild the list wider and run the series again; every other
+ * call that uses the cells or the list reads them on entry.  Errors of a
+ * build are therefore reported by the call that reads them.  Off (0) by
+ * default; switching it off reads any pending statistics. */
+int ggem_set_deferred_checks(ggem_ctx *ctx, int enable);
 /* number of ordered neighbour pairs (self excluded) of the current build */
 int ggem_neighbor_pair_count(ggem_ctx *ctx, int64_t *count);
 /* per-particle neighbour lists in original particle ids, ascending,
@@ -214,8 +224,9 @@ int ggem_power_iteration(ggem_ctx *ctx, double tol, int maxits, double *eig);
  * length n are drawn first (restart fast-forward, copss.C:1544-1555) */
 int ggem_std_random_vector(uint64_t seed, int64_t skip_vectors, int64_t n, double mean,
                            double stddev, double *out);
-/* counter-based N(0,1) noise on the device (Philox4x32-10 + Box-Muller) for
- * batched right-hand sides: element 2p, 2p+1 from counter (p, stream) */
+/* counter-based N(0,1) noise on the device (Philox4x32-10 + Box-Muller in
+ * FP32, FP64 output) for batched right-hand sides: elements 4p .. 4p+3 from
+ * counter (p, stream) */
 int ggem_philox_normals_dev(ggem_ctx *ctx, uint64_t seed, uint64_t stream, int64_t n,
                             double *d_out);
 

@@ -903,19 +903,24 @@ static void philox10(uint32_t c[4], uint32_t k0, uint32_t k1) {
   }
 }
 
+/* counter (p, stream) -> elements 4p .. 4p+3; the uniforms are formed in
+ * FP32 exactly as on the device (u1 rounded once, u2 exact), the transform
+ * runs in FP64 here: the device's FP32 transform agrees to a few FP32 ulps */
 void orc_philox_normals(uint64_t seed, uint64_t stream, int64_t n, double *out) {
   const double two_pi = 2.0 * ORC_PI;
-  for (int64_t p = 0; 2 * p < n; ++p) {
+  for (int64_t p = 0; 4 * p < n; ++p) {
     uint32_t c[4] = {(uint32_t)p, (uint32_t)((uint64_t)p >> 32), (uint32_t)stream,
                      (uint32_t)(stream >> 32)};
     philox10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
-    const uint64_t a = ((uint64_t)c[0] << 21) ^ (c[1] >> 11);
-    const uint64_t bq = ((uint64_t)c[2] << 21) ^ (c[3] >> 11);
-    const double u1 = ((double)a + 0.5) * 0x1.0p-53;
-    const double u2 = ((double)bq + 0.5) * 0x1.0p-53;
-    const double r = sqrt(-2.0 * log(u1));
-    out[2 * p] = r * cos(two_pi * u2);
-    if (2 * p + 1 < n) out[2 * p + 1] = r * sin(two_pi * u2);
+    for (int h = 0; h < 2; ++h) {
+      /* (float)c0 * 2^-32 is exact, so the sum is the device's single fmaf rounding */
+      const float u1 = (float)c[2 * h] * 0x1p-32f + 0x1p-33f;
+      const float u2 = (float)(c[2 * h + 1] >> 9) * 0x1p-23f + 0x1p-24f;
+      const double r = sqrt(-2.0 * log((double)u1));
+      const int64_t k = 4 * p + 2 * h;
+      if (k < n) out[k] = r * cos(two_pi * (double)u2);
+      if (k + 1 < n) out[k + 1] = r * sin(two_pi * (double)u2);
+    }
   }
 }
 

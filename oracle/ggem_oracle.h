@@ -158,7 +158,8 @@ void orc_std_normal_vector(uint64_t seed, int64_t skip_vectors, int64_t n,
                            double mean, double stddev, double *out);
 
 /* Philox4x32-10 (Salmon et al., SC'11) counter-based normals, restated for
- * checking the device noise generator bit-for-bit */
+ * checking the device noise generator: the counter words bit-for-bit, the
+ * FP32 Box-Muller transform to a few FP32 ulps */
 void orc_philox_normals(uint64_t seed, uint64_t stream, int64_t n, double *out);
 
 /* excluded-volume Gaussian force, FixPointGaussianDNA::compute

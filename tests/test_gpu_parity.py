@@ -326,7 +326,8 @@ def test_philox_noise_matches_oracle():
         ctx.synchronize()
     got = d.cpu().numpy()
     want = O.philox_normals(99, 7, n)
-    assert np.abs(got - want).max() <= 1e-13
+    # counter words bit-exact; the FP32 transform within a few FP32 ulps
+    assert np.all(np.abs(got - want) <= 1e-6 * (1.0 + np.abs(want)))
     assert abs(got.mean()) < 0.05 and abs(got.std() - 1) < 0.05
 
 
@@ -456,8 +457,8 @@ def test_batched_64_rhs_chains_matvec_and_chebyshev():
         assert rel(y.reshape(64, -1)[r], y_o) <= 5e-3
 
 
-@pytest.mark.parametrize("stored,variant", [(False, 0), (True, 0), (True, 1), (True, 2),
-                                            (True, 3)])
+@pytest.mark.parametrize("stored,variant", [(False, 0), (False, 1), (True, 0), (True, 1),
+                                            (True, 2), (True, 3)])
 def test_pair_tensor_storage_modes(stored, variant):
     """Stored per-pair tensors (streamed) and per-matvec tensors (computed)
     give the same velocities within the FP32 contract, and the same
@@ -471,7 +472,8 @@ def test_pair_tensor_storage_modes(stored, variant):
     xi = np.random.default_rng(9).standard_normal(3 * len(xyz))
     with G.Context(box_hi=(L,) * 3, rc=7.0, precision=G.FP32) as ctx:
         ctx.set_pair_tensors(stored)
-        ctx.set_pair_variant(variant)
+        ctx.set_pair_variant(computed=0 if stored else variant,
+                             stored=variant if stored else 0)
         ctx.set_particles(xyz)
         ctx.build_cells()
         W, st = ctx.pair_storage()

@@ -236,14 +236,15 @@ def test_std_normal_stream_is_reproducible_and_normal():
 def test_philox_known_answer():
     # Philox4x32-10 known-answer vector (Random123 kat_vectors: counter 0,
     # key 0 -> 6627e8d5 e169c58d bc57ac4c 9b00dbd8)
-    out = O.philox_normals(0, 0, 2)
-    u53a = (0x6627e8d5 << 21) ^ (0xe169c58d >> 11)
-    u53b = (0xbc57ac4c << 21) ^ (0x9b00dbd8 >> 11)
-    u1 = (u53a + 0.5) * 2.0 ** -53
-    u2 = (u53b + 0.5) * 2.0 ** -53
-    r = np.sqrt(-2 * np.log(u1))
-    assert out[0] == pytest.approx(r * np.cos(2 * np.pi * u2), rel=1e-14)
-    assert out[1] == pytest.approx(r * np.sin(2 * np.pi * u2), rel=1e-14)
+    out = O.philox_normals(0, 0, 4)
+    words = [0x6627e8d5, 0xe169c58d, 0xbc57ac4c, 0x9b00dbd8]
+    for h in range(2):
+        u1 = float(np.float32(np.float32(words[2 * h]) * np.float32(2.0 ** -32)
+                              + np.float32(2.0 ** -33)))
+        u2 = float(np.float32((words[2 * h + 1] >> 9) * 2.0 ** -23 + 2.0 ** -24))
+        r = np.sqrt(-2 * np.log(u1))
+        assert out[2 * h] == pytest.approx(r * np.cos(2 * np.pi * u2), rel=1e-14)
+        assert out[2 * h + 1] == pytest.approx(r * np.sin(2 * np.pi * u2), rel=1e-14)
 
 
 def test_mlp_oracle_gradient_matches_finite_differences():
