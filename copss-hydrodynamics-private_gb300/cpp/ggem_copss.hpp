@@ -8,6 +8,8 @@
 //   BrownianSystem  brownian_system.h:72-260 (Chebyshev approximation,
 //                                          eigen bounds, power iteration,
 //                                          noise, hi_ewald)
+//   PMSystemStokes  pm_system_stokes.h      (compute_point_velocity: FEM
+//                                          point values + local velocity)
 // Vectors keep the reference's PETSc layout [f1x, f1y, f1z, f2x, ...].
 // Errors follow the reference: a failing call that the reference ends with
 // libmesh_error() throws ggem_copss::Error; calls that return a
@@ -22,6 +24,7 @@
 #include <string>
 #include <vector>
 
+#include "ggem_fem.h"
 #include "ggem_gb300.h"
 
 namespace ggem_copss {
@@ -205,6 +208,43 @@ class BrownianSystem {
  private:
   ParticleSystem &ps_;
   std::default_random_engine engine_;
+};
+
+// PMSystemStokes::compute_point_velocity (pm_system_stokes.C:383-500): the
+// FEM solution at every particle (point_value of u, v, w on the HEX20 mesh)
+// plus, for option "disturbed", the local velocity with the bead self term
+// (U = U_global + U_local - coeff_1 f + f).  The mesh's dof map
+// ([n_elem][u, v, w][20 nodes], DofMap::dof_indices per element in libMesh's
+// Hex20 node order) is uploaded once.
+class PMSystemStokes {
+ public:
+  PMSystemStokes(ParticleSystem &ps, const std::array<int, 3> &n_elem, const Point &lo,
+                 const Point &hi, int64_t n_dofs, const std::vector<int64_t> &elem_dofs)
+      : ps_(ps) {
+    check(ggem_fem_create(ps.ctx(), n_elem.data(), lo.data(), hi.data(), n_dofs,
+                          elem_dofs.data(), &fem_),
+          ps.ctx());
+  }
+  ~PMSystemStokes() { ggem_fem_destroy(fem_); }
+  PMSystemStokes(const PMSystemStokes &) = delete;
+  PMSystemStokes &operator=(const PMSystemStokes &) = delete;
+
+  void compute_point_velocity(const std::vector<double> &solution, const std::vector<double> &f,
+                              const std::string &option, std::vector<double> &pv) const {
+    pv.assign(3 * ps_.num_particles(), 0.0);
+    if (option == "disturbed") {
+      check(ggem_local_matvec(ps_.ctx(), 1, f.data(), pv.data(), GGEM_SELF_BEAD), ps_.ctx());
+      check(ggem_fem_point_values(fem_, solution.data(), pv.data(), 1), ps_.ctx());
+    } else if (option == "undisturbed") {
+      check(ggem_fem_point_values(fem_, solution.data(), pv.data(), 0), ps_.ctx());
+    } else {
+      throw Error(GGEM_ERR_BAD_ARG, "compute_point_velocity: option must be disturbed or undisturbed");
+    }
+  }
+
+ private:
+  ParticleSystem &ps_;
+  ggem_fem *fem_ = nullptr;
 };
 
 }  // namespace ggem_copss

@@ -155,6 +155,11 @@ def lib():
         "ggem_write_bead_csv": (i, [C.c_char_p, i64, vp, vp, vp, i]),
         "ggem_write_petsc_vec": (i, [C.c_char_p, i64, vp]),
         "ggem_read_petsc_vec": (i, [C.c_char_p, i64, vp, P(i64)]),
+        "ggem_fem_create": (i, [vp, vp, vp, vp, i64, vp, P(vp)]),
+        "ggem_fem_destroy": (None, [vp]),
+        "ggem_fem_point_values": (i, [vp, vp, vp, i]),
+        "ggem_fem_point_values_dev": (i, [vp, vp, vp, i]),
+        "ggem_fem_hex20_shape": (None, [vp, vp]),
         "ggem_ensemble_create": (i, [P(Params), i, vp, P(vp)]),
         "ggem_ensemble_destroy": (None, [vp]),
         "ggem_ensemble_last_error": (C.c_char_p, [vp]),
@@ -591,6 +596,61 @@ class Context:
     def philox_normals_dev(self, seed, stream, n, d_out):
         self._check(lib().ggem_philox_normals_dev(self.h, int(seed), int(stream), int(n),
                                                   C.c_void_p(d_out)))
+
+
+def hex20_shape(xi):
+    """the 20 serendipity shape functions at reference point xi (include/ggem_fem.h)"""
+    x = np.ascontiguousarray(xi, dtype=np.float64)
+    n = np.zeros(20)
+    lib().ggem_fem_hex20_shape(_p(x), _p(n))
+    return n
+
+
+class Fem:
+    """The HEX20 mesh of the FEM velocity (include/ggem_fem.h): point values
+    of u, v, w at the particles of `ctx`.  elem_dofs is [n_elem][3][20]."""
+
+    def __init__(self, ctx, n_elem, lo, hi, n_dofs, elem_dofs):
+        self.ctx = ctx
+        ne = np.ascontiguousarray(n_elem, dtype=np.int32)
+        self._lo = np.ascontiguousarray(lo, dtype=np.float64)
+        self._hi = np.ascontiguousarray(hi, dtype=np.float64)
+        dofs = np.ascontiguousarray(elem_dofs, dtype=np.int64)
+        self.n_dofs = int(n_dofs)
+        h = C.c_void_p()
+        ctx._check(lib().ggem_fem_create(ctx.h, _p(ne), _p(self._lo), _p(self._hi),
+                                         self.n_dofs, _p(dofs), C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().ggem_fem_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def point_values(self, solution, u=None, accumulate=False):
+        """U_global [n][3] at the context's particles (added to u when
+        accumulate)"""
+        sol = _f64(solution)
+        out = np.zeros((self.ctx.n, 3)) if u is None else _f64(u).reshape(self.ctx.n, 3).copy()
+        self.ctx._check(lib().ggem_fem_point_values(self.h, _p(sol), _p(out),
+                                                    1 if accumulate else 0))
+        return out
+
+    def point_values_dev(self, d_solution, d_u, accumulate=False):
+        self.ctx._check(lib().ggem_fem_point_values_dev(self.h, C.c_void_p(d_solution),
+                                                        C.c_void_p(d_u), 1 if accumulate else 0))
 
 
 class Ensemble:

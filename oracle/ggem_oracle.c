@@ -986,3 +986,62 @@ void orc_spring_forces(const orc_box *b, int64_t n, const double *xyz, int64_t m
     }
   }
 }
+
+
+/* ---- FEM velocity at points -------------------------------------------- */
+
+/* libMesh Hex20 nodes on [-1, 1]^3: corners 0-7, then the edge midpoints of
+ * edges 0-1, 1-2, 2-3, 3-0, 0-4, 1-5, 2-6, 3-7, 4-5, 5-6, 6-7, 7-4 */
+static const int HEX20_X[20] = {-1, 1, 1, -1, -1, 1, 1, -1, 0, 1, 0, -1, -1, 1, 1, -1, 0, 1, 0, -1};
+static const int HEX20_Y[20] = {-1, -1, 1, 1, -1, -1, 1, 1, -1, 0, 1, 0, -1, -1, 1, 1, -1, 0, 1, 0};
+static const int HEX20_Z[20] = {-1, -1, -1, -1, 1, 1, 1, 1, -1, -1, -1, -1, 0, 0, 0, 0, 1, 1, 1, 1};
+
+void orc_hex20_shape(double x, double y, double z, double n[20]) {
+  for (int k = 0; k < 20; ++k) {
+    const double a = HEX20_X[k], b = HEX20_Y[k], c = HEX20_Z[k];
+    if (k < 8)
+      n[k] = (1.0 + a * x) * (1.0 + b * y) * (1.0 + c * z) * (a * x + b * y + c * z - 2.0) / 8.0;
+    else if (a == 0.0)
+      n[k] = (1.0 - x * x) * (1.0 + b * y) * (1.0 + c * z) / 4.0;
+    else if (b == 0.0)
+      n[k] = (1.0 + a * x) * (1.0 - y * y) * (1.0 + c * z) / 4.0;
+    else
+      n[k] = (1.0 + a * x) * (1.0 + b * y) * (1.0 - z * z) / 4.0;
+  }
+}
+
+/* element containing x on the uniform mesh (floor((x - lo) / h), periodic
+ * axes wrapped first, clamped to the mesh) and the reference coordinate */
+int64_t orc_fem_point_values(int64_t n, const double *xyz, const int ne[3], const double lo[3],
+                             const double hi[3], const int periodic[3],
+                             const int64_t *elem_dofs, const double *sol, double *u) {
+  int64_t outside = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    int e[3];
+    double xi[3];
+    for (int d = 0; d < 3; ++d) {
+      const double L = hi[d] - lo[d], h = L / ne[d];
+      double t = xyz[3 * i + d] - lo[d];
+      if (periodic[d]) {
+        t = fmod(t, L);
+        if (t < 0) t += L;
+        if (t >= L) t = 0.0;
+      } else if (!(t >= 0.0 && t <= L)) {
+        ++outside;
+      }
+      int k = (int)floor(t / h);
+      k = k < 0 ? 0 : (k >= ne[d] ? ne[d] - 1 : k);
+      e[d] = k;
+      xi[d] = 2.0 * (t - k * h) / h - 1.0;
+    }
+    double nf[20];
+    orc_hex20_shape(xi[0], xi[1], xi[2], nf);
+    const int64_t elem = e[0] + (int64_t)ne[0] * (e[1] + (int64_t)ne[1] * e[2]);
+    for (int v = 0; v < 3; ++v) {
+      double s = 0.0;
+      for (int k = 0; k < 20; ++k) s += nf[k] * sol[elem_dofs[elem * 60 + 20 * v + k]];
+      u[3 * i + v] = s;
+    }
+  }
+  return outside;
+}

@@ -177,6 +177,16 @@ void orc_spring_force(int kind, const double R_ij[3], double c1, double Ls, doub
 void orc_spring_forces(const orc_box *b, int64_t n, const double *xyz, int64_t m,
                        const int64_t *bonds, int kind, double c1, double Ls, double *f);
 
+/* the global (FEM) velocity at points: libMesh System::point_value of the
+ * SECOND-order u, v, w on the HEX20 build_cube mesh
+ * (pm_system_stokes.C:437-441), restated from the 20-node serendipity
+ * element (libMesh Hex20 node order); elem_dofs [ne][3][20].  Returns the
+ * number of points outside a non-periodic axis (clamped to the mesh). */
+void orc_hex20_shape(double x, double y, double z, double n[20]);
+int64_t orc_fem_point_values(int64_t n, const double *xyz, const int ne[3], const double lo[3],
+                             const double hi[3], const int periodic[3],
+                             const int64_t *elem_dofs, const double *sol, double *u);
+
 #ifdef __cplusplus
 }
 #endif

@@ -118,6 +118,9 @@ def lib():
         L.orc_ev_gaussian.argtypes = [C.POINTER(Box), i64, vp, C.POINTER(NbList), d, d, vp]
         L.orc_spring_force.argtypes = [C.c_int, vp, d, d, vp]
         L.orc_spring_forces.argtypes = [C.POINTER(Box), i64, vp, i64, vp, C.c_int, d, d, vp]
+        L.orc_hex20_shape.argtypes = [d, d, d, vp]
+        L.orc_fem_point_values.restype = i64
+        L.orc_fem_point_values.argtypes = [i64, vp, vp, vp, vp, vp, vp, vp, vp]
         _lib = L
     return _lib
 
@@ -400,3 +403,26 @@ def spring_forces(box: Box, xyz, bonds, kind, c1, Ls) -> np.ndarray:
     lib().orc_spring_forces(C.byref(box), len(xyz), _p(xyz), len(b), _p(b), int(kind),
                             float(c1), float(Ls), _p(f))
     return f
+
+
+def hex20_shape(xi):
+    """the 20 serendipity shape functions at reference point xi (Hex20 order)"""
+    n = np.zeros(20)
+    lib().orc_hex20_shape(float(xi[0]), float(xi[1]), float(xi[2]), _p(n))
+    return n
+
+
+def fem_point_values(xyz, n_elem, lo, hi, periodic, elem_dofs, solution):
+    """(U_global [n][3], number of points outside a non-periodic axis):
+    point_value of u, v, w on the HEX20 mesh (pm_system_stokes.C:437-441)"""
+    xyz = _f64(xyz)
+    ne = np.ascontiguousarray(n_elem, dtype=np.int32)
+    lo = _f64(lo)
+    hi = _f64(hi)
+    per = np.ascontiguousarray(periodic, dtype=np.int32)
+    dofs = np.ascontiguousarray(elem_dofs, dtype=np.int64)
+    sol = _f64(solution)
+    u = np.zeros((len(xyz), 3))
+    out = lib().orc_fem_point_values(len(xyz), _p(xyz), _p(ne), _p(lo), _p(hi), _p(per),
+                                     _p(dofs), _p(sol), _p(u))
+    return u, int(out)

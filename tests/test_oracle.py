@@ -311,3 +311,31 @@ def test_force_oracle_laws_and_action_reaction():
     for kind in range(4):
         sp = O.spring_forces(box, pts, bonds, kind, 0.2, 40.0)
         assert np.abs(sp.sum(axis=0)).max() < 1e-9 * max(1.0, np.abs(sp).max())
+
+
+def test_hex20_shape_functions_kronecker_partition_and_quadratics():
+    """the serendipity element: N_i(node_j) = delta_ij, sum N = 1, and the
+    20-node space reproduces every quadratic polynomial exactly"""
+    from fem_mesh import HEX20
+    for j, node in enumerate(HEX20):
+        n = O.hex20_shape(node.astype(float))
+        assert np.allclose(n, np.eye(20)[j], atol=1e-15)
+    rng = np.random.default_rng(0)
+    for xi in rng.uniform(-1, 1, (50, 3)):
+        n = O.hex20_shape(xi)
+        assert abs(n.sum() - 1.0) < 1e-14
+        for mono in (lambda p: p[..., 0] * p[..., 1], lambda p: p[..., 2] ** 2,
+                     lambda p: p[..., 1] - 0.5 * p[..., 0] * p[..., 2]):
+            assert abs(n @ mono(HEX20.astype(float)) - mono(xi)) < 1e-14
+
+
+def test_fem_point_values_oracle_reproduces_quadratic_fields():
+    from fem_mesh import hex20_mesh, quadratic
+    ne, lo, hi = (4, 3, 5), (-2.0, 0.0, 1.0), (6.0, 3.0, 11.0)
+    dofs, nd, dpos, dvar = hex20_mesh(ne, lo, hi, seed=1)
+    sol = np.array([quadratic(dpos[k], dvar[k]) for k in range(nd)])
+    pts = np.random.default_rng(2).uniform(lo, hi, (300, 3))
+    u, outside = O.fem_point_values(pts, ne, lo, hi, (0, 0, 0), dofs, sol)
+    assert outside == 0
+    want = np.stack([quadratic(pts, v) for v in range(3)], axis=1)
+    assert np.abs(u - want).max() <= 1e-12 * np.abs(want).max()
