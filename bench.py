@@ -51,8 +51,9 @@ CHEB_MAX = 50
 CHEB_TOL = 1e-3
 SEED = 20261203
 # DRAM bytes (read + write) per launch of the dominant pair kernel from one
-# ncu capture of this bench's workload (profiles/, the kernel's summary file)
-PAIR_TRAFFIC = {}
+# ncu capture of this bench's workload (profiles/k_pair_cheb_N200k.md; ncu
+# flushes the caches before the launch, so this is the cold-cache figure)
+PAIR_TRAFFIC = {"k_pair_cheb": 72.76e6}
 
 
 def measured_peaks():
@@ -328,6 +329,7 @@ def run_gb300(args, rank, world):
     ctx_e.set_deferred_checks(True)
     e_bounds = state["bounds"]
     RepArr = G.ChebReport * 1
+    e_stats = {"lanczos_fallbacks": 0, "terms": []}
 
     def e2e_step(step_id):
         nonlocal e_bounds
@@ -341,7 +343,9 @@ def run_gb300(args, rank, world):
                                                    C.c_void_p(h_xi.data_ptr()),
                                                    C.c_void_p(h_dw.data_ptr()), rep)
             if rc2 == 0:
+                e_stats["terms"].append(rep[0].n_terms)
                 break
+            e_stats["lanczos_fallbacks"] += 1
             lo, hi = ctx_e.lanczos_bounds(k=24, seed=7)
             e_bounds = (lo / 1.05, hi * 1.05)
         if rc or rc2:
@@ -360,6 +364,8 @@ def run_gb300(args, rank, world):
         e_ts.append((t1 - t0) * 1e3)
         clk.mark(t0, t1)
     e2e_ms = float(np.mean(e_ts))
+    e_stats["ms_per_step_median"] = float(np.median(e_ts))
+    e_stats["ms_per_step_max"] = float(np.max(e_ts))
     ctx_e.close()
 
     # ---- mobility matvec throughput (FP32, device resident) ------------
@@ -466,8 +472,8 @@ def run_gb300(args, rank, world):
     peak = ctx.probe_fp32_peak()
     row_width, stored = ctx.pair_storage()
     if stored:
-        names = {"pair_cheb": "k_pair_cheb_t (stored pair tensors + fused FP64 Chebyshev term)",
-                 "pair_fp32": "k_pair_r1t (stored pair tensors, one RHS)"}
+        names = {"pair_cheb": "k_pair_cheb_tv (stored pair tensors + fused FP64 Chebyshev term)",
+                 "pair_fp32": "k_pair_r1tv (stored pair tensors, one RHS)"}
     else:
         names = {"pair_cheb": "k_pair_cheb (pair list, tensors per pair + fused Chebyshev term)",
                  "pair_fp32": "k_pair_r1 (pair list, tensors per pair, one RHS)"}
@@ -481,6 +487,12 @@ def run_gb300(args, rank, world):
     # x_{k+1} out 5 x 24, next forces 16)
     per_bead = {"pair_fp32": 16 + 4 + 48, "pair_cheb": 16 + 4 + 120 + 16}
     bytes_per_launch = n_pairs * 20 + N_BEADS * per_bead[dom]
+    if not stored:
+        # tensors evaluated per pair: 4 B entry per pair; per bead the 32-byte
+        # source record, the row count and the FP64 vectors (plain: f, u; fused
+        # term: x0, x1, dw in, dw, x_{k+1} out) and the next 32-byte record
+        per_bead = {"pair_fp32": 32 + 4 + 48, "pair_cheb": 32 + 4 + 120 + 32}
+        bytes_per_launch = n_pairs * 4 + N_BEADS * per_bead[dom]
     achieved = flops_per_launch / (avg_pair_ms * 1e-3) / 1e12
     others = {k: {"avg_launch_ms": kt[k][0] / max(kt[k][1], 1), "launches": kt[k][1],
                   "tflops": (flops_per_launch / (kt[k][0] / kt[k][1] * 1e-3) / 1e12)
@@ -495,10 +507,14 @@ def run_gb300(args, rank, world):
                 "bytes_per_launch": bytes_per_launch, "fp32_tflops": achieved,
                 "fp32_frac_of_live_peak": achieved / peak if peak else None}
     else:
+        gbs = bytes_per_launch / (avg_pair_ms * 1e-3) / 1e9
+        hbm_peak = measured_peaks().get("hbm_gbs")
         roof = {"bound": "fp32", "kernel": names[dom], "achieved": achieved, "peak": peak,
                 "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
                 "peak_source": "measured live: FP32 FMA-chain probe on this GPU "
-                               "(MEASURED_PEAKS.json has no FP32 figure)"}
+                               "(MEASURED_PEAKS.json has no FP32 figure)",
+                "bytes_per_launch": bytes_per_launch, "hbm_gbs": gbs,
+                "hbm_frac_of_measured": gbs / hbm_peak if hbm_peak else None}
     roof.update({"flops_per_launch": flops_per_launch, "pairs": n_pairs, "row_width": row_width,
                  "avg_launch_ms": avg_pair_ms, "launches_timed": pair_n,
                  "pair_kernels": others, "traffic": PAIR_TRAFFIC.get(names[dom].split()[0])})
@@ -511,7 +527,7 @@ def run_gb300(args, rank, world):
         "config": workload_config({"parallelism": f"replicas x{world}", "cell_div": cell_div,
                                    "check_every": args.check_every, "autotune": tuning}),
         "e2e": {"value": 1e3 / e2e_ms * world, "unit": "Brownian steps/s",
-                "ms_per_step": e2e_ms, "h2d_bytes_per_step": 2 * 24 * N_BEADS,
+                "ms_per_step": e2e_ms, "detail": e_stats, "h2d_bytes_per_step": 2 * 24 * N_BEADS,
                 "d2h_bytes_per_step": 24 * N_BEADS},
         "matvecs_per_s": matvecs_per_s, "matvec_ms": float(np.mean(mv_ts)),
         "plain_fp64_gpu": fp64,

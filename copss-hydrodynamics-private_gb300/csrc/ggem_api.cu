@@ -36,6 +36,7 @@ int cuda_fail(ggem_ctx *c, cudaError_t e, const char *what) {
 
 int check_launch(ggem_ctx *c, const char *what) {
   ++c->launches;
+  if (c->trace) trace_mark(c, what);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(c, e, what);
   return GGEM_OK;

@@ -529,22 +529,20 @@ int enqueue_list_check(ggem_ctx *c) {
   return GGEM_OK;
 }
 
-int finish_list_check(ggem_ctx *c, bool *rebuilt) {
+int finish_list_check(ggem_ctx *c, unsigned long long total, unsigned long long longest, int flags,
+                      bool *rebuilt) {
   if (rebuilt) *rebuilt = false;
   if (!c->list_unchecked) return GGEM_OK;
   c->list_unchecked = false;
-  const unsigned long long *h = reinterpret_cast<unsigned long long *>(c->h_red + kListStatSlot);
-  const int flags = (int)h[2];
   if (int rc = cell_flag_error(c, flags)) {
     c->list_built = false;
     return rc;
   }
   if (!(flags & kErrListCapacity)) {
-    c->n_pairs = (int64_t)h[0];
+    c->n_pairs = (int64_t)total;
     return GGEM_OK;
   }
   // rows overflowed: widen them and rebuild with the synchronous path
-  const unsigned long long longest = h[1];
   c->nb_w = (int)std::min<unsigned long long>((longest + longest / 8 + 8 + 7) / 8 * 8, 1u << 24);
   cudaError_t e = cudaMemsetAsync(c->err.p, 0, sizeof(int), c->stream);
   if (e) return cuda_fail(c, e, "memset");
@@ -563,7 +561,8 @@ int settle_list(ggem_ctx *c) {
   if (int rc = enqueue_list_check(c)) return rc;
   cudaError_t e = cudaStreamSynchronize(c->stream);
   if (e) return cuda_fail(c, e, "list statistics");
-  return finish_list_check(c, nullptr);
+  const unsigned long long *h = reinterpret_cast<unsigned long long *>(c->h_red + kListStatSlot);
+  return finish_list_check(c, h[0], h[1], (int)h[2], nullptr);
 }
 
 }  // namespace ggem

@@ -7,6 +7,8 @@
 // 40 B x 3n per right-hand side per term of algorithmic traffic.
 #include <cuda_runtime.h>
 
+#include <cstring>
+
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -59,15 +61,25 @@ __global__ void __launch_bounds__(kVecThreads) k_dot_partials(int64_t D, const d
   if (threadIdx.x == 0) partial[(int64_t)r * gridDim.x + blockIdx.x] = t;
 }
 
-// out[q] = sum_b partial[q][b], fixed order (deterministic)
+// out[q] = sum_b partial[q][b], fixed order (deterministic).  With stat and
+// err given, out[nq .. nq+2] also receive the pair-list statistics (total
+// and longest row, as bit patterns) and the error word of a deferred build,
+// so that one readback carries both.
 __global__ void __launch_bounds__(kVecThreads) k_finalize(int G, const double *__restrict__ partial,
-                                                          double *__restrict__ out) {
+                                                          double *__restrict__ out, int nq,
+                                                          const unsigned long long *__restrict__ stat,
+                                                          const int *__restrict__ err) {
   __shared__ double sh[32];
   const int q = blockIdx.x;
   double acc = 0.0;
   for (int b = threadIdx.x; b < G; b += blockDim.x) acc += partial[(int64_t)q * G + b];
   const double t = block_sum(acc, sh);
   if (threadIdx.x == 0) out[q] = t;
+  if (stat && q == 0 && threadIdx.x == 0) {
+    out[nq] = __longlong_as_double((long long)stat[0]);
+    out[nq + 1] = __longlong_as_double((long long)stat[1]);
+    out[nq + 2] = (double)*err;
+  }
 }
 
 // x1 = db * x0 + da * x1   (VecAXPBY(x1, db, da, x0), brownian_system.C:1041)
@@ -246,12 +258,16 @@ int grid1(int64_t tot) {
   return (int)std::max<int64_t>(1, std::min<int64_t>((tot + 255) / 256, 4096));
 }
 
-// results[q] of the partial arrays, copied to the pinned host mirror
-int finalize_to_host(ggem_ctx *c, int nq, int G, double *host) {
+// results[q] of the partial arrays, copied to the pinned host mirror; with
+// list_stats, host[nq .. nq+2] receive a deferred build's statistics too
+int finalize_to_host(ggem_ctx *c, int nq, int G, double *host, bool list_stats = false) {
   double *out = c->w_red.p + (size_t)nq * G;
-  k_finalize<<<nq, kVecThreads, 0, c->stream>>>(G, c->w_red.p, out);
+  k_finalize<<<nq, kVecThreads, 0, c->stream>>>(G, c->w_red.p, out, nq,
+                                                list_stats ? c->nb_stat.p : nullptr,
+                                                list_stats ? c->err.p : nullptr);
   if (int rc = check_launch(c, "finalize")) return rc;
-  cudaError_t e = cudaMemcpyAsync(host, out, sizeof(double) * nq, cudaMemcpyDeviceToHost, c->stream);
+  const int nv = nq + (list_stats ? 3 : 0);
+  cudaError_t e = cudaMemcpyAsync(host, out, sizeof(double) * nv, cudaMemcpyDeviceToHost, c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   if (e) return cuda_fail(c, e, "reduction readback");
   return GGEM_OK;
@@ -291,7 +307,8 @@ int ensure_cheb_buffers(ggem_ctx *c, size_t len) {
 // overflowing rows: the list has been rebuilt and the series must restart
 constexpr int kRestartCheb = 1;
 
-// Chebyshev on slot-ordered xi (c->w_in); leaves y in c->w_y.
+// Chebyshev on xi (caller order, device; left unchanged); leaves y in c->w_y
+// (slot order).
 //
 // check_every = 1: the reference's loop (brownian_system.C:1089-1155): the
 //   error-check matvec dw_mid = M dw and both estimators every term.
@@ -304,12 +321,27 @@ constexpr int kRestartCheb = 1;
 // whether c->w_out holds M y for every right-hand side (the last check ran
 // on the final y), which the Brownian displacement reuses.
 int cheb_slots(ggem_ctx *c, int nrhs, int N, double eig_min, double eig_max, double tol,
-               int check_every, ggem_cheb_report *rep, bool *dm_is_my) {
+               int check_every, const double *xi, ggem_cheb_report *rep, bool *dm_is_my) {
   const int64_t D = 3 * c->n;
-  const int64_t tot = D * nrhs;
   const int sm = brownian_self_mode(c);
-  const int G = vec_blocks(D);
+  const bool faithful = check_every == 1;
+  // Terms that no error check follows need neither norm: on the FP32
+  // single-RHS path they run as one fused pair-sum + recurrence kernel that
+  // also writes the FP32 records of the next x1 (records_fresh).  With
+  // per-matvec pair tensors outside the reference-faithful mode the whole
+  // series is fused: the first step is one pair kernel (x1, dw, xi.M.xi),
+  // checked terms add their two norms in the same kernel and the check
+  // matvec sums |M dw|^2; their partial sums then have one entry per pair
+  // kernel block.
+  const bool can_fuse = nrhs == 1 && c->prm.precision == GGEM_FP32 &&
+                        c->prm.nb_mode == GGEM_NB_CUTOFF;
+  const bool fused = can_fuse && !faithful && !c->pretensor_ok && c->n > 0;
+  const int G = fused ? pair_grid_blocks(c) : vec_blocks(D);
   cudaStream_t st = c->stream;
+  if (fused) {
+    cudaError_t e = c->w_red.ensure((size_t)4 * G + 16);
+    if (e) return cuda_fail(c, e, "chebyshev partial sums");
+  }
   double *x0 = c->w_c.p, *x1 = c->w_d.p, *xm = c->w_e.p, *dw = c->w_y.p, *dm = c->w_out.p;
   // reduction regions: term norms [2 nrhs][G], |dm|^2 [nrhs][G], xi.M.xi
   // [nrhs][G], then the 4 nrhs finalized values
@@ -325,36 +357,47 @@ int cheb_slots(ggem_ctx *c, int nrhs, int N, double eig_min, double eig_max, dou
   std::vector<int> active(nrhs, 1);
   for (int r = 0; r < nrhs; ++r) rep[r] = ggem_cheb_report{0, 1, 0, 0.0, 0.0};
   double *h = c->h_red;
-  const bool faithful = check_every == 1;
   const int k_first = (check_every == 0) ? std::max(2, c->cheb_pred_terms > 0 ? c->cheb_pred_terms : 8)
                                          : 0;
   *dm_is_my = false;
   // x0 = xi; x1 = M x0; aux2 = x1.x0; x1 = db x0 + da x1   (:1036-1041)
-  k_copy<<<grid1(tot), 256, 0, st>>>(tot, c->w_in.p, x0);
-  if (int rc = check_launch(c, "copy")) return rc;
-  if (int rc = matvec_slots(c, nrhs, x0, x1, sm)) return rc;
-  k_dot_partials<<<dim3(G, nrhs), kVecThreads, 0, st>>>(D, x1, x0, p_aux2);
-  if (int rc = check_launch(c, "aux2")) return rc;
-  k_cheb_first<<<grid1(tot), 256, 0, st>>>(D, nrhs, da, db, x0, x1);
-  if (int rc = check_launch(c, "cheb first")) return rc;
-  // dw = c0 x0, dw += c1 x1 with both norms   (:1050-1056)
-  k_cheb_init<<<dim3(G, nrhs), kVecThreads, 0, st>>>(D, X[0], X[1], x0, x1, dw, p_term);
-  if (int rc = check_launch(c, "cheb init")) return rc;
+  // dw = c0 x0, dw += c1 x1 (with both norms unless fused)  (:1050-1056)
+  bool records_fresh = false;
+  if (fused) {
+    if (int rc = cheb_start_fused(c, xi, x0, x1, dw, da, db, X[0], X[1], p_aux2, sm)) return rc;
+    records_fresh = true;
+  } else {
+    if (int rc = permute_to_slots(c, nrhs, xi, x0)) return rc;
+    if (int rc = matvec_slots(c, nrhs, x0, x1, sm)) return rc;
+    k_dot_partials<<<dim3(G, nrhs), kVecThreads, 0, st>>>(D, x1, x0, p_aux2);
+    if (int rc = check_launch(c, "aux2")) return rc;
+    k_cheb_first<<<grid1(D * nrhs), 256, 0, st>>>(D, nrhs, da, db, x0, x1);
+    if (int rc = check_launch(c, "cheb first")) return rc;
+    k_cheb_init<<<dim3(G, nrhs), kVecThreads, 0, st>>>(D, X[0], X[1], x0, x1, dw, p_term);
+    if (int rc = check_launch(c, "cheb init")) return rc;
+  }
   for (int r = 0; r < nrhs; ++r) rep[r].n_matvecs = 1;
 
   // evaluate err1 / err2 of the current dw for the active right-hand sides
   auto check_now = [&](double coef_abs, bool apply_rules) -> int {
-    if (int rc = matvec_slots(c, nrhs, dw, dm, sm)) return rc;
-    k_dot_partials<<<dim3(G, nrhs), kVecThreads, 0, st>>>(D, dm, dm, p_dm);
-    if (int rc = check_launch(c, "dm norm")) return rc;
-    // a deferred list build is checked in the same synchronisation
+    if (fused) {
+      if (int rc = matvec_dot(c, dw, dm, sm, p_dm)) return rc;
+    } else {
+      if (int rc = matvec_slots(c, nrhs, dw, dm, sm)) return rc;
+      k_dot_partials<<<dim3(G, nrhs), kVecThreads, 0, st>>>(D, dm, dm, p_dm);
+      if (int rc = check_launch(c, "dm norm")) return rc;
+    }
+    // a deferred list build is checked in the same readback
     const bool pending = c->list_unchecked;
-    if (pending)
-      if (int rc = enqueue_list_check(c)) return rc;
-    if (int rc = finalize_to_host(c, 4 * nrhs, G, h)) return rc;
+    if (int rc = finalize_to_host(c, 4 * nrhs, G, h, pending)) return rc;
     if (pending) {
+      const double *v = h + 4 * nrhs;
       bool rebuilt = false;
-      if (int rc = finish_list_check(c, &rebuilt)) return rc;
+      unsigned long long total = 0, longest = 0;
+      std::memcpy(&total, &v[0], sizeof total);
+      std::memcpy(&longest, &v[1], sizeof longest);
+      if (int rc = finish_list_check(c, total, longest, (int)v[2], &rebuilt))
+        return rc;
       if (rebuilt) return kRestartCheb;
     }
     for (int r = 0; r < nrhs; ++r) {
@@ -382,12 +425,6 @@ int cheb_slots(ggem_ctx *c, int nrhs, int N, double eig_min, double eig_max, dou
   }
   const double two_da = 2. * da, two_db = 2. * db;
   int first_check = -1;
-  // Terms that no error check follows need neither norm: on the FP32
-  // single-RHS path they run as one fused pair-sum + recurrence kernel that
-  // also writes the FP32 records of the next x1 (records_fresh).
-  const bool can_fuse = nrhs == 1 && c->prm.precision == GGEM_FP32 &&
-                        c->prm.nb_mode == GGEM_NB_CUTOFF;
-  bool records_fresh = false;
   for (int i = 1; i < N; ++i) {
     int n_active = 0;
     for (int r = 0; r < nrhs; ++r) n_active += active[r];
@@ -396,8 +433,9 @@ int cheb_slots(ggem_ctx *c, int nrhs, int N, double eig_min, double eig_max, dou
     if (faithful) check = true;
     else if (check_every > 1) check = (i % check_every == 0) || (i == N - 1);
     else check = (i + 1 >= k_first) || (i == N - 1);
-    if (can_fuse && !check) {
-      if (int rc = pair_cheb_term(c, records_fresh, x0, x1, xm, dw, two_da, two_db, X[i + 1], sm))
+    if (can_fuse && (!check || fused)) {
+      if (int rc = pair_cheb_term(c, records_fresh, x0, x1, xm, dw, two_da, two_db, X[i + 1], sm,
+                                  check ? p_term : nullptr))
         return rc;
       records_fresh = true;
     } else {
@@ -463,11 +501,10 @@ extern "C" int ggem_cheb_inv_sqrt_dev(ggem_ctx *ctx, int nrhs, int N, double eig
   DeviceGuard dg(ctx->device);
   const size_t len = (size_t)ctx->n * 3 * nrhs;
   if (int rc = ensure_cheb_buffers(ctx, len)) return rc;
-  if (int rc = permute_to_slots(ctx, nrhs, d_xi, ctx->w_in.p)) return rc;
   bool dm_is_my = false;
-  int rc = cheb_slots(ctx, nrhs, N, eig_min, eig_max, tol_cheb, check_every, rep, &dm_is_my);
+  int rc = cheb_slots(ctx, nrhs, N, eig_min, eig_max, tol_cheb, check_every, d_xi, rep, &dm_is_my);
   if (rc == kRestartCheb)  // the deferred list was rebuilt wider: run the series again
-    rc = cheb_slots(ctx, nrhs, N, eig_min, eig_max, tol_cheb, check_every, rep, &dm_is_my);
+    rc = cheb_slots(ctx, nrhs, N, eig_min, eig_max, tol_cheb, check_every, d_xi, rep, &dm_is_my);
   if (rc) return rc;
   return permute_from_slots(ctx, nrhs, ctx->w_y.p, d_xi);
 }
@@ -521,11 +558,10 @@ extern "C" int ggem_brownian_displacement_dev(ggem_ctx *ctx, int nrhs, int N, do
   DeviceGuard dg(ctx->device);
   const size_t len = (size_t)ctx->n * 3 * nrhs;
   if (int rc = ensure_cheb_buffers(ctx, len)) return rc;
-  if (int rc = permute_to_slots(ctx, nrhs, d_xi, ctx->w_in.p)) return rc;
   bool dm_is_my = false;
-  int rc = cheb_slots(ctx, nrhs, N, eig_min, eig_max, tol_cheb, check_every, rep, &dm_is_my);
+  int rc = cheb_slots(ctx, nrhs, N, eig_min, eig_max, tol_cheb, check_every, d_xi, rep, &dm_is_my);
   if (rc == kRestartCheb)  // the deferred list was rebuilt wider: run the series again
-    rc = cheb_slots(ctx, nrhs, N, eig_min, eig_max, tol_cheb, check_every, rep, &dm_is_my);
+    rc = cheb_slots(ctx, nrhs, N, eig_min, eig_max, tol_cheb, check_every, d_xi, rep, &dm_is_my);
   if (rc) return rc;
   bool all = true;
   for (int r = 0; r < nrhs; ++r) all = all && rep[r].converged;
@@ -576,7 +612,7 @@ extern "C" int ggem_lanczos_bounds(ggem_ctx *ctx, int k, uint64_t seed, double *
     for (int pass = 0; pass < 2; ++pass) {
       k_multi_dot<<<dim3(G, j + 1), kVecThreads, 0, st>>>(D, Q, w, ctx->w_red.p);
       if (int rc = check_launch(ctx, "lanczos dots")) return rc;
-      k_finalize<<<j + 1, kVecThreads, 0, st>>>(G, ctx->w_red.p, hdev);
+      k_finalize<<<j + 1, kVecThreads, 0, st>>>(G, ctx->w_red.p, hdev, j + 1, nullptr, nullptr);
       if (int rc = check_launch(ctx, "lanczos finalize")) return rc;
       k_sub_proj<<<grid1(D), 256, 0, st>>>(D, j + 1, Q, hdev, w);
       if (int rc = check_launch(ctx, "lanczos project")) return rc;

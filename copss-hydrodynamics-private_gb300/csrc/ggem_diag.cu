@@ -48,6 +48,14 @@ void kt_stop(ggem_ctx *c, int kind) {
   t.ev.push_back(e);
 }
 
+void trace_mark(ggem_ctx *c, const char *what) {
+  if (c->trace_ev.size() >= 100000) return;
+  cudaEvent_t e = take_event(c);
+  if (!e) return;
+  cudaEventRecord(e, c->stream);
+  c->trace_ev.emplace_back(what, e);
+}
+
 static int drain(ggem_ctx *c) {
   cudaError_t err = cudaStreamSynchronize(c->stream);
   if (err) return cuda_fail(c, err, "timing sync");
@@ -178,5 +186,35 @@ extern "C" int ggem_probe_fp32_peak(ggem_ctx *ctx, double *tflops) {
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   *tflops = best;
+  return GGEM_OK;
+}
+
+extern "C" int ggem_set_launch_trace(ggem_ctx *ctx, int enable) {
+  if (!ctx) return GGEM_ERR_BAD_ARG;
+  cudaError_t err = cudaStreamSynchronize(ctx->stream);
+  if (err) return cuda_fail(ctx, err, "trace sync");
+  for (auto &t : ctx->trace_ev) ctx->ev_pool.push_back(t.second);
+  ctx->trace_ev.clear();
+  ctx->trace = enable != 0;
+  if (ctx->trace) trace_mark(ctx, "trace start");
+  return GGEM_OK;
+}
+
+extern "C" int ggem_get_launch_trace(ggem_ctx *ctx, int64_t max, double *t_ms,
+                                     const char **names, int64_t *count) {
+  if (!ctx || !count || (max > 0 && (!t_ms || !names))) return GGEM_ERR_BAD_ARG;
+  cudaError_t err = cudaStreamSynchronize(ctx->stream);
+  if (err) return cuda_fail(ctx, err, "trace sync");
+  const int64_t n = (int64_t)ctx->trace_ev.size();
+  *count = n;
+  for (int64_t k = 0; k < n && k < max; ++k) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, ctx->trace_ev[0].second, ctx->trace_ev[k].second) != cudaSuccess) {
+      cudaGetLastError();
+      ms = -1.f;
+    }
+    t_ms[k] = ms;
+    names[k] = ctx->trace_ev[k].first;
+  }
   return GGEM_OK;
 }

@@ -22,6 +22,7 @@
 
 #include <cstdint>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "ggem_gb300.h"
@@ -180,6 +181,9 @@ struct ggem_ctx {
     int64_t count = 0;
   } ktimer[5];
   std::vector<cudaEvent_t> ev_pool;
+  // launch trace (ggem_set_launch_trace): one event after every launch
+  bool trace = false;
+  std::vector<std::pair<const char *, cudaEvent_t>> trace_ev;
 
   ~ggem_ctx();
 };
@@ -191,6 +195,7 @@ enum : int { kKPairF32 = 0, kKPairF64 = 1, kKChebTerm = 2, kKListBuild = 3, kKPa
 
 void kt_start(ggem_ctx *c, int kind);
 void kt_stop(ggem_ctx *c, int kind);
+void trace_mark(ggem_ctx *c, const char *what);
 
 int fail(ggem_ctx *c, int code, const std::string &msg);
 int cuda_fail(ggem_ctx *c, cudaError_t e, const char *what);
@@ -219,7 +224,8 @@ int build_pair_list(ggem_ctx *c);
 // stored pair tensors) were rebuilt wider: results computed since the
 // build are void.  settle_list does both with its own synchronisation.
 int enqueue_list_check(ggem_ctx *c);
-int finish_list_check(ggem_ctx *c, bool *rebuilt);
+int finish_list_check(ggem_ctx *c, unsigned long long total, unsigned long long longest, int flags,
+                      bool *rebuilt);
 int settle_list(ggem_ctx *c);
 constexpr int kListStatSlot = 4088;  // h_red[4088 .. 4090]: deferred list statistics
 int device_exclusive_scan_i32(ggem_ctx *c, const int32_t *in, int32_t *out, int64_t n);
@@ -232,9 +238,18 @@ int matvec_f32_staged(ggem_ctx *c, int nrhs, const double *d_f_slot, double *d_u
                       int self_mode);
 double self_coefficient(const ggem_ctx *c, int self_mode);
 int build_pair_tensors(ggem_ctx *c);
+// part: nullptr, or where the blocks' shares of |dw|^2 (before the update)
+// and |xm|^2 go ([2][pair_grid_blocks]); per-matvec pair tensors only
 int pair_cheb_term(ggem_ctx *c, bool records_fresh, const double *x0, const double *x1,
                    double *xm, double *dw, double two_da, double two_db, double coef,
-                   int self_mode);
+                   int self_mode, double *part);
+// blocks of the single-RHS pair kernels (the length of their partial sums)
+int pair_grid_blocks(const ggem_ctx *c);
+// the fused first step (xi in caller order) and the check matvec with |u|^2
+int cheb_start_fused(ggem_ctx *c, const double *xi, double *x0, double *x1, double *dw,
+                     double da, double db, double c0, double c1, double *part_aux2,
+                     int self_mode);
+int matvec_dot(ggem_ctx *c, const double *f, double *u, int self_mode, double *part);
 int permute_to_slots(ggem_ctx *c, int nrhs, const double *d_orig, double *d_slot);
 int permute_from_slots(ggem_ctx *c, int nrhs, const double *d_slot, double *d_orig);
 

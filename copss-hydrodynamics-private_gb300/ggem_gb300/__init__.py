@@ -122,6 +122,8 @@ def lib():
         "ggem_set_pair_variant": (i, [vp, i, i]),
         "ggem_probe_fp32_peak": (i, [vp, P(d)]),
         "ggem_set_kernel_timing": (i, [vp, i]),
+        "ggem_set_launch_trace": (i, [vp, i]),
+        "ggem_get_launch_trace": (i, [vp, i64, vp, vp, P(i64)]),
         "ggem_get_kernel_timing": (i, [vp, i, P(d), P(i64)]),
         "ggem_lanczos_bounds": (i, [vp, i, C.c_uint64, P(d), P(d)]),
         "ggem_power_iteration": (i, [vp, d, i, P(d)]),
@@ -518,6 +520,18 @@ class Context:
 
     def set_kernel_timing(self, enable: bool):
         self._check(lib().ggem_set_kernel_timing(self.h, int(bool(enable))))
+
+    def set_launch_trace(self, enable: bool):
+        self._check(lib().ggem_set_launch_trace(self.h, int(bool(enable))))
+
+    def launch_trace(self, max_events=100000):
+        """[(ms from the trace start, launch name)] of the traced launches"""
+        t = np.zeros(max_events)
+        names = (C.c_char_p * max_events)()
+        n = C.c_int64()
+        self._check(lib().ggem_get_launch_trace(self.h, max_events, _p(t), names, C.byref(n)))
+        m = min(n.value, max_events)
+        return [(float(t[k]), names[k].decode()) for k in range(m)]
 
     def set_pair_tensors(self, enable: bool):
         self._check(lib().ggem_set_pair_tensors(self.h, 1 if enable else 0))

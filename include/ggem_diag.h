@@ -16,6 +16,15 @@
 extern "C" {
 #endif
 
+/* launch trace: with enable = 1 every kernel launch of the context is
+ * followed by an event on its stream (the first marks the start); reading
+ * returns, for up to max launches, the event times in ms from the start and
+ * the launch names (static strings), and the number recorded in *count.
+ * The differences of consecutive times are a kernel's duration plus the
+ * idle gap before it.  Setting it (on or off) clears the trace. */
+int ggem_set_launch_trace(ggem_ctx *ctx, int enable);
+int ggem_get_launch_trace(ggem_ctx *ctx, int64_t max, double *t_ms, const char **names,
+                          int64_t *count);
 /* number of CUDA kernels this context has launched so far */
 int ggem_get_launch_count(const ggem_ctx *ctx, int64_t *count);
 /* ordered in-cutoff pairs of the current FP32 pair list (the work unit of
