@@ -149,6 +149,29 @@ __global__ void __launch_bounds__(kVecThreads) k_cheb_term(int64_t D, double two
   }
 }
 
+// the norms of a fused term (k_cheb_term's q0, q1 for one right-hand side):
+// |dw - coef xm|^2 (the dw before the term) and |xm|^2
+__global__ void __launch_bounds__(kVecThreads) k_term_norms(int64_t D, double coef,
+                                                            const double *__restrict__ xm,
+                                                            const double *__restrict__ dw,
+                                                            double *__restrict__ partial) {
+  __shared__ double sh[32];
+  double a4 = 0.0, a3 = 0.0;
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < D;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    const double v = xm[k];
+    const double y = dw[k] - coef * v;
+    a4 += y * y;
+    a3 += v * v;
+  }
+  const double s4 = block_sum(a4, sh);
+  const double s3 = block_sum(a3, sh);
+  if (threadIdx.x == 0) {
+    partial[blockIdx.x] = s4;
+    partial[gridDim.x + blockIdx.x] = s3;
+  }
+}
+
 __global__ void k_copy(int64_t tot, const double *__restrict__ a, double *__restrict__ b) {
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < tot;
        k += (int64_t)gridDim.x * blockDim.x)
@@ -316,7 +339,8 @@ constexpr int kRestartCheb = 1;
 //   last); the norms of a term come from the fused term kernel.
 // check_every = 0: the first check is at the degree the previous call
 //   converged at (8 on the first call), then every term; the prediction is
-//   lowered by one whenever the first check already passes.
+//   lowered by one when the first check passed with room for one degree
+//   less (see the end of cheb_slots).
 // Only check points synchronise with the host.  On return *dm_is_my tells
 // whether c->w_out holds M y for every right-hand side (the last check ran
 // on the final y), which the Brownian displacement reuses.
@@ -329,19 +353,13 @@ int cheb_slots(ggem_ctx *c, int nrhs, int N, double eig_min, double eig_max, dou
   // single-RHS path they run as one fused pair-sum + recurrence kernel that
   // also writes the FP32 records of the next x1 (records_fresh).  With
   // per-matvec pair tensors outside the reference-faithful mode the whole
-  // series is fused: the first step is one pair kernel (x1, dw, xi.M.xi),
-  // checked terms add their two norms in the same kernel and the check
-  // matvec sums |M dw|^2; their partial sums then have one entry per pair
-  // kernel block.
+  // series is fused: the first step is one pair kernel (m = M x0, x1, dw)
+  // and a checked term is a fused term followed by its two norms.
   const bool can_fuse = nrhs == 1 && c->prm.precision == GGEM_FP32 &&
                         c->prm.nb_mode == GGEM_NB_CUTOFF;
   const bool fused = can_fuse && !faithful && !c->pretensor_ok && c->n > 0;
-  const int G = fused ? pair_grid_blocks(c) : vec_blocks(D);
+  const int G = vec_blocks(D);
   cudaStream_t st = c->stream;
-  if (fused) {
-    cudaError_t e = c->w_red.ensure((size_t)4 * G + 16);
-    if (e) return cuda_fail(c, e, "chebyshev partial sums");
-  }
   double *x0 = c->w_c.p, *x1 = c->w_d.p, *xm = c->w_e.p, *dw = c->w_y.p, *dm = c->w_out.p;
   // reduction regions: term norms [2 nrhs][G], |dm|^2 [nrhs][G], xi.M.xi
   // [nrhs][G], then the 4 nrhs finalized values
@@ -364,7 +382,10 @@ int cheb_slots(ggem_ctx *c, int nrhs, int N, double eig_min, double eig_max, dou
   // dw = c0 x0, dw += c1 x1 (with both norms unless fused)  (:1050-1056)
   bool records_fresh = false;
   if (fused) {
-    if (int rc = cheb_start_fused(c, xi, x0, x1, dw, da, db, X[0], X[1], p_aux2, sm)) return rc;
+    // dm holds m = M x0 until the first check
+    if (int rc = cheb_start_fused(c, xi, x0, dm, x1, dw, da, db, X[0], X[1], sm)) return rc;
+    k_dot_partials<<<dim3(G, 1), kVecThreads, 0, st>>>(D, dm, x0, p_aux2);
+    if (int rc = check_launch(c, "aux2")) return rc;
     records_fresh = true;
   } else {
     if (int rc = permute_to_slots(c, nrhs, xi, x0)) return rc;
@@ -380,13 +401,9 @@ int cheb_slots(ggem_ctx *c, int nrhs, int N, double eig_min, double eig_max, dou
 
   // evaluate err1 / err2 of the current dw for the active right-hand sides
   auto check_now = [&](double coef_abs, bool apply_rules) -> int {
-    if (fused) {
-      if (int rc = matvec_dot(c, dw, dm, sm, p_dm)) return rc;
-    } else {
-      if (int rc = matvec_slots(c, nrhs, dw, dm, sm)) return rc;
-      k_dot_partials<<<dim3(G, nrhs), kVecThreads, 0, st>>>(D, dm, dm, p_dm);
-      if (int rc = check_launch(c, "dm norm")) return rc;
-    }
+    if (int rc = matvec_slots(c, nrhs, dw, dm, sm)) return rc;
+    k_dot_partials<<<dim3(G, nrhs), kVecThreads, 0, st>>>(D, dm, dm, p_dm);
+    if (int rc = check_launch(c, "dm norm")) return rc;
     // a deferred list build is checked in the same readback
     const bool pending = c->list_unchecked;
     if (int rc = finalize_to_host(c, 4 * nrhs, G, h, pending)) return rc;
@@ -434,10 +451,13 @@ int cheb_slots(ggem_ctx *c, int nrhs, int N, double eig_min, double eig_max, dou
     else if (check_every > 1) check = (i % check_every == 0) || (i == N - 1);
     else check = (i + 1 >= k_first) || (i == N - 1);
     if (can_fuse && (!check || fused)) {
-      if (int rc = pair_cheb_term(c, records_fresh, x0, x1, xm, dw, two_da, two_db, X[i + 1], sm,
-                                  check ? p_term : nullptr))
+      if (int rc = pair_cheb_term(c, records_fresh, x0, x1, xm, dw, two_da, two_db, X[i + 1], sm))
         return rc;
       records_fresh = true;
+      if (check) {
+        k_term_norms<<<G, kVecThreads, 0, st>>>(D, X[i + 1], xm, dw, p_term);
+        if (int rc = check_launch(c, "term norms")) return rc;
+      }
     } else {
       if (int rc = matvec_slots(c, nrhs, x1, xm, sm)) return rc;
       RhsCoef cf;
@@ -473,7 +493,18 @@ int cheb_slots(ggem_ctx *c, int nrhs, int N, double eig_min, double eig_max, dou
       all = all && rep[r].converged;
       worst = std::max(worst, rep[r].n_terms);
     }
-    if (all) c->cheb_pred_terms = (worst == first_check) ? std::max(2, worst - 1) : worst;
+    // The series error shrinks by about rho = (sqrt(k) - 1) / (sqrt(k) + 1)
+    // per degree (k = eig_max / eig_min, the Chebyshev rate for x^(-1/2));
+    // the next call tries one degree less only when the first check passed
+    // with that much room, so a workload converging at a steady degree does
+    // not pay a failing check (an extra matvec and host round trip) every
+    // other call.
+    double e1 = 0.0;
+    for (int r = 0; r < nrhs; ++r) e1 = std::max(e1, rep[r].err1);
+    const double kap = eig_min > 0 ? eig_max / eig_min : 1e30;
+    const double rho = (std::sqrt(kap) - 1.0) / (std::sqrt(kap) + 1.0);
+    const bool lower = worst == first_check && e1 <= 0.8 * rho * tol;
+    if (all) c->cheb_pred_terms = lower ? std::max(2, worst - 1) : worst;
   }
   return GGEM_OK;
 }

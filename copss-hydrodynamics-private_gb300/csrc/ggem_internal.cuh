@@ -238,18 +238,14 @@ int matvec_f32_staged(ggem_ctx *c, int nrhs, const double *d_f_slot, double *d_u
                       int self_mode);
 double self_coefficient(const ggem_ctx *c, int self_mode);
 int build_pair_tensors(ggem_ctx *c);
-// part: nullptr, or where the blocks' shares of |dw|^2 (before the update)
-// and |xm|^2 go ([2][pair_grid_blocks]); per-matvec pair tensors only
 int pair_cheb_term(ggem_ctx *c, bool records_fresh, const double *x0, const double *x1,
                    double *xm, double *dw, double two_da, double two_db, double coef,
-                   int self_mode, double *part);
-// blocks of the single-RHS pair kernels (the length of their partial sums)
+                   int self_mode);
+// blocks of the single-RHS pair kernels
 int pair_grid_blocks(const ggem_ctx *c);
-// the fused first step (xi in caller order) and the check matvec with |u|^2
-int cheb_start_fused(ggem_ctx *c, const double *xi, double *x0, double *x1, double *dw,
-                     double da, double db, double c0, double c1, double *part_aux2,
-                     int self_mode);
-int matvec_dot(ggem_ctx *c, const double *f, double *u, int self_mode, double *part);
+// the fused first step of a series (xi in caller order; m = M x0 is kept)
+int cheb_start_fused(ggem_ctx *c, const double *xi, double *x0, double *m, double *x1,
+                     double *dw, double da, double db, double c0, double c1, int self_mode);
 int permute_to_slots(ggem_ctx *c, int nrhs, const double *d_orig, double *d_slot);
 int permute_from_slots(ggem_ctx *c, int nrhs, const double *d_slot, double *d_orig);
 

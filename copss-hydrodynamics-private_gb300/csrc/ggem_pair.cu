@@ -394,37 +394,19 @@ __device__ __forceinline__ PairSum pair_sum_r1(int64_t s, bool act, int sub, con
 }
 
 // the per-matvec-tensor kernel shapes the autotuner chooses from: blocks of
-// 256 threads per SM that the register cap allows (6 at 40 registers, 8 at 32
-// with a few spills outside the pair loop)
-constexpr int kComputedMinBlocks[] = {6, 8};
+// 256 threads per SM that the register cap allows (6 at 40 registers, with a
+// few spilled epilogue values in some kernels; 5 at 48 without)
+constexpr int kComputedMinBlocks[] = {6, 5};
 constexpr int kNumComputedVariants = 2;
 
-// sum over the block of one FP64 value per thread, in a fixed order (the
-// Chebyshev estimators' partial norms); every thread of the 256 must call
-// it; the result is valid in thread 0
-__device__ __forceinline__ double pair_block_sum(double v, double *sh) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  if (lane == 0) sh[warp] = v;
-  __syncthreads();
-  double t = 0.0;
-  if (threadIdx.x == 0)
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += sh[w];
-  __syncthreads();
-  return t;
-}
-
-// u = M f, single right-hand side; with DOT, part[blockIdx.x] also receives
-// the block's share of |u|^2 (the check matvec of the Chebyshev estimator)
-template <bool POLY, int V, bool DOT>
+// u = M f, single right-hand side
+template <bool POLY, int V>
 __global__ void __launch_bounds__(256, kComputedMinBlocks[V]) k_pair_r1(
     int64_t n, const Rec32 *__restrict__ src, const int32_t *__restrict__ cnt, int W,
     const uint32_t *__restrict__ list, PolyAB P, const Rec32 *__restrict__ tab, float inv_ds,
     const float4 *__restrict__ shift, double self_c, const double *__restrict__ f,
-    double *__restrict__ u, double *__restrict__ part) {
+    double *__restrict__ u) {
   __shared__ float4 sh[kMaxCode];
-  __shared__ double red[8];
   stage_shifts(sh, shift);
   const int64_t gid = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / kGroup;
   const int sub = (int)(threadIdx.x % kGroup);
@@ -434,31 +416,25 @@ __global__ void __launch_bounds__(256, kComputedMinBlocks[V]) k_pair_r1(
   const PairSum r = pair_sum_r1<POLY>(s, act, sub, ri, src, cnt, W, list, P, tab, inv_ds, sh);
   float h, l;
   group_scatter3(sub, r, h, l);
-  double uk = 0.0;
-  if (act && sub < 3) {
-    const int64_t k = 3 * s + sub;
-    uk = fma(self_c, f[k], f2d_bits(h) + f2d_bits(l));
-    u[k] = uk;
-  }
-  if (DOT) {
-    const double t = pair_block_sum(uk * uk, red);
-    if (threadIdx.x == 0) part[blockIdx.x] = t;
-  }
+  if (!act || sub >= 3) return;
+  const int64_t k = 3 * s + sub;
+  u[k] = fma(self_c, f[k], f2d_bits(h) + f2d_bits(l));
 }
 
 // The first Chebyshev step in one pass (brownian_system.C:1036-1056 for one
-// right-hand side): m = M x0 (src holds the records of x0), the block's share
-// of aux2 = m . x0 into part_aux2, x1 = db x0 + da m, dw = c0 x0 + c1 x1, and
-// the 32-byte records of x1 for the first term.
+// right-hand side): m = M x0 (src holds the records of x0, m is kept for
+// the dot xi . M xi), x1 = db x0 + da m, dw = c0 x0 + c1 x1, and the 32-byte
+// records of x1 for the first term.  (The estimator sums stay in separate
+// vector kernels: a block-wide FP64 reduction here costs more than the
+// launch it saves, FP64 being 1/64 of the FP32 rate.)
 template <bool POLY, int V>
 __global__ void __launch_bounds__(256, kComputedMinBlocks[V]) k_pair_first(
     int64_t n, const Rec32 *__restrict__ src, const int32_t *__restrict__ cnt, int W,
     const uint32_t *__restrict__ list, PolyAB P, const Rec32 *__restrict__ tab, float inv_ds,
     const float4 *__restrict__ shift, double self_c, double da, double db, double c0, double c1,
-    const double *__restrict__ x0, double *__restrict__ x1, double *__restrict__ dw,
-    Rec32 *__restrict__ next, double *__restrict__ part_aux2) {
+    const double *__restrict__ x0, double *__restrict__ m, double *__restrict__ x1,
+    double *__restrict__ dw, Rec32 *__restrict__ next) {
   __shared__ float4 sh[kMaxCode];
-  __shared__ double red[8];
   stage_shifts(sh, shift);
   const int64_t gid = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / kGroup;
   const int sub = (int)(threadIdx.x % kGroup);
@@ -468,43 +444,37 @@ __global__ void __launch_bounds__(256, kComputedMinBlocks[V]) k_pair_first(
   const PairSum r = pair_sum_r1<POLY>(s, act, sub, ri, src, cnt, W, list, P, tab, inv_ds, sh);
   float h, l;
   group_scatter3(sub, r, h, l);
-  double pdot = 0.0;
+  if (!act) return;
   float *nf = reinterpret_cast<float *>(next + s);
-  if (act && sub < 3) {
+  if (sub < 3) {
     const int64_t k = 3 * s + sub;
     const double xk = x0[k];
     const double mk = fma(self_c, xk, f2d_bits(h) + f2d_bits(l));
-    pdot = mk * xk;
+    m[k] = mk;
     const double x1k = db * xk + da * mk;
     x1[k] = x1k;
     dw[k] = c0 * xk + c1 * x1k;
     nf[4 + sub] = __double2float_rn(x1k);
-  } else if (act) {
+  } else {
     reinterpret_cast<float4 *>(nf)[0] = ri.a;
     nf[7] = 0.f;
   }
-  const double t = pair_block_sum(pdot, red);
-  if (threadIdx.x == 0) part_aux2[blockIdx.x] = t;
 }
 
 // One Chebyshev term with the pair sum (brownian_system.C:1091-1108 for one
-// right-hand side):
+// right-hand side, without the norms of the error estimators):
 //   m = M x1 (pair sum + self term),  xm = (2db x1 + 2da m) - x0,
 //   dw += coef xm,  and the 32-byte records of xm for the next term.
 // With c1 = 2db + 2da self_c this is xm = 2da (pair sum) + (c1 x1 - x0).
-// With NORMS the block's shares of |dw|^2 (before the update) and |xm|^2 go
-// to part[blockIdx.x] and part[gridDim.x + blockIdx.x] (the estimators of a
-// checked term).  src holds the records of x1; next must be a different
-// buffer.
-template <bool POLY, int V, bool NORMS>
+// src holds the records of x1; next must be a different buffer.
+template <bool POLY, int V>
 __global__ void __launch_bounds__(256, kComputedMinBlocks[V]) k_pair_cheb(
     int64_t n, const Rec32 *__restrict__ src, const int32_t *__restrict__ cnt, int W,
     const uint32_t *__restrict__ list, PolyAB P, const Rec32 *__restrict__ tab, float inv_ds,
     const float4 *__restrict__ shift, double two_da, double c1, double coef,
     const double *__restrict__ x0, const double *__restrict__ x1, double *__restrict__ xm,
-    double *__restrict__ dw, Rec32 *__restrict__ next, double *__restrict__ part) {
+    double *__restrict__ dw, Rec32 *__restrict__ next) {
   __shared__ float4 sh[kMaxCode];
-  __shared__ double red[8];
   stage_shifts(sh, shift);
   const int64_t gid = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / kGroup;
   const int sub = (int)(threadIdx.x % kGroup);
@@ -514,28 +484,17 @@ __global__ void __launch_bounds__(256, kComputedMinBlocks[V]) k_pair_cheb(
   const PairSum r = pair_sum_r1<POLY>(s, act, sub, ri, src, cnt, W, list, P, tab, inv_ds, sh);
   float h, l;
   group_scatter3(sub, r, h, l);
-  double a4 = 0.0, a3 = 0.0;
+  if (!act) return;
   float *nf = reinterpret_cast<float *>(next + s);
-  if (act && sub < 3) {
+  if (sub < 3) {
     const int64_t k = 3 * s + sub;
     const double v = fma(two_da, f2d_bits(h) + f2d_bits(l), fma(c1, x1[k], -x0[k]));
-    const double y = dw[k];
     xm[k] = v;
-    dw[k] = fma(coef, v, y);
+    dw[k] = fma(coef, v, dw[k]);
     nf[4 + sub] = __double2float_rn(v);
-    a4 = y * y;
-    a3 = v * v;
-  } else if (act) {
+  } else {
     reinterpret_cast<float4 *>(nf)[0] = ri.a;  // the target's position record
     nf[7] = 0.f;
-  }
-  if (NORMS) {
-    const double t4 = pair_block_sum(a4, red);
-    const double t3 = pair_block_sum(a3, red);
-    if (threadIdx.x == 0) {
-      part[blockIdx.x] = t4;
-      part[gridDim.x + blockIdx.x] = t3;
-    }
   }
 }
 
@@ -1083,33 +1042,24 @@ PolyAB poly_of(const ggem_ctx *c) {
   return P;
 }
 
-template <bool POLY, int V, bool DOT>
-void launch_r1(ggem_ctx *c, const Rec32 *src, const double *f, double *u, double self_c,
-               double *part) {
-  k_pair_r1<POLY, V, DOT><<<(unsigned)pair_grid_blocks(c), 256, 0, c->stream>>>(
+template <bool POLY, int V>
+void launch_r1(ggem_ctx *c, const Rec32 *src, const double *f, double *u, double self_c) {
+  k_pair_r1<POLY, V><<<(unsigned)pair_grid_blocks(c), 256, 0, c->stream>>>(
       c->n, src, c->nb_cnt.p, c->nb_w, c->nb_list.p, poly_of(c),
-      reinterpret_cast<const Rec32 *>(c->tab.p), c->tab_inv_ds, c->d_shift.p, self_c, f, u, part);
+      reinterpret_cast<const Rec32 *>(c->tab.p), c->tab_inv_ds, c->d_shift.p, self_c, f, u);
 }
 
 template <bool POLY>
-void dispatch_r1(ggem_ctx *c, const Rec32 *src, const double *f, double *u, double self_c,
-                 double *part) {
-  if (part) {
-    if (c->computed_variant == 1) launch_r1<POLY, 1, true>(c, src, f, u, self_c, part);
-    else launch_r1<POLY, 0, true>(c, src, f, u, self_c, part);
-  } else {
-    if (c->computed_variant == 1) launch_r1<POLY, 1, false>(c, src, f, u, self_c, nullptr);
-    else launch_r1<POLY, 0, false>(c, src, f, u, self_c, nullptr);
-  }
+void dispatch_r1(ggem_ctx *c, const Rec32 *src, const double *f, double *u, double self_c) {
+  if (c->computed_variant == 1) launch_r1<POLY, 1>(c, src, f, u, self_c);
+  else launch_r1<POLY, 0>(c, src, f, u, self_c);
 }
 
-// single right-hand side: records from FP64 slot-order f, then the pair sum;
-// part (per-matvec tensors only) receives the blocks' shares of |u|^2
-int launch_f32_r1(ggem_ctx *c, const double *f, double *u, double self_c, double *part) {
+// single right-hand side: records from FP64 slot-order f, then the pair sum
+int launch_f32_r1(ggem_ctx *c, const double *f, double *u, double self_c) {
   const int64_t n = c->n;
   cudaError_t e;
   if (c->pretensor_ok) {
-    if (part) return fail(c, GGEM_ERR_BAD_ARG, "matvec norms need per-matvec pair tensors");
     if ((e = c->w_f4[0].ensure((size_t)n))) return cuda_fail(c, e, "pair forces");
     k_stage_f4<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(n, f, c->w_f4[0].p);
     if (int rc = check_launch(c, "pair forces")) return rc;
@@ -1123,45 +1073,37 @@ int launch_f32_r1(ggem_ctx *c, const double *f, double *u, double self_c, double
   k_build_src<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(n, c->pos32.p, f, src);
   if (int rc = check_launch(c, "pair records")) return rc;
   kt_start(c, kKPairF32);
-  if (c->use_poly) dispatch_r1<true>(c, src, f, u, self_c, part);
-  else dispatch_r1<false>(c, src, f, u, self_c, part);
+  if (c->use_poly) dispatch_r1<true>(c, src, f, u, self_c);
+  else dispatch_r1<false>(c, src, f, u, self_c);
   kt_stop(c, kKPairF32);
   return check_launch(c, "pair f32 r1");
 }
 
 // c1 = 2db + 2da self_c folds the self term into the x1 coefficient
-template <bool POLY, int V, bool NORMS>
+template <bool POLY, int V>
 void launch_cheb(ggem_ctx *c, const Rec32 *src, Rec32 *next, double two_da, double c1,
-                 double coef, const double *x0, const double *x1, double *xm, double *dw,
-                 double *part) {
-  k_pair_cheb<POLY, V, NORMS><<<(unsigned)pair_grid_blocks(c), 256, 0, c->stream>>>(
+                 double coef, const double *x0, const double *x1, double *xm, double *dw) {
+  k_pair_cheb<POLY, V><<<(unsigned)pair_grid_blocks(c), 256, 0, c->stream>>>(
       c->n, src, c->nb_cnt.p, c->nb_w, c->nb_list.p, poly_of(c),
       reinterpret_cast<const Rec32 *>(c->tab.p), c->tab_inv_ds, c->d_shift.p, two_da, c1, coef,
-      x0, x1, xm, dw, next, part);
+      x0, x1, xm, dw, next);
 }
 
 template <bool POLY>
 void dispatch_cheb(ggem_ctx *c, const Rec32 *src, Rec32 *next, double two_da, double c1,
-                   double coef, const double *x0, const double *x1, double *xm, double *dw,
-                   double *part) {
-  const bool v1 = c->computed_variant == 1;
-  if (part) {
-    if (v1) launch_cheb<POLY, 1, true>(c, src, next, two_da, c1, coef, x0, x1, xm, dw, part);
-    else launch_cheb<POLY, 0, true>(c, src, next, two_da, c1, coef, x0, x1, xm, dw, part);
-  } else {
-    if (v1) launch_cheb<POLY, 1, false>(c, src, next, two_da, c1, coef, x0, x1, xm, dw, nullptr);
-    else launch_cheb<POLY, 0, false>(c, src, next, two_da, c1, coef, x0, x1, xm, dw, nullptr);
-  }
+                   double coef, const double *x0, const double *x1, double *xm, double *dw) {
+  if (c->computed_variant == 1) launch_cheb<POLY, 1>(c, src, next, two_da, c1, coef, x0, x1, xm, dw);
+  else launch_cheb<POLY, 0>(c, src, next, two_da, c1, coef, x0, x1, xm, dw);
 }
 
 template <bool POLY, int V>
 void launch_first(ggem_ctx *c, const Rec32 *src, Rec32 *next, double self_c, double da,
-                  double db, double c0, double c1, const double *x0, double *x1, double *dw,
-                  double *part_aux2) {
+                  double db, double c0, double c1, const double *x0, double *m, double *x1,
+                  double *dw) {
   k_pair_first<POLY, V><<<(unsigned)pair_grid_blocks(c), 256, 0, c->stream>>>(
       c->n, src, c->nb_cnt.p, c->nb_w, c->nb_list.p, poly_of(c),
       reinterpret_cast<const Rec32 *>(c->tab.p), c->tab_inv_ds, c->d_shift.p, self_c, da, db, c0,
-      c1, x0, x1, dw, next, part_aux2);
+      c1, x0, m, x1, dw, next);
 }
 
 template <int CD, bool POLY>
@@ -1245,13 +1187,12 @@ int permute_from_slots(ggem_ctx *c, int nrhs, const double *d_slot, double *d_or
 // previous fused term wrote them); otherwise they are built here first.
 int pair_cheb_term(ggem_ctx *c, bool records_fresh, const double *x0, const double *x1,
                    double *xm, double *dw, double two_da, double two_db, double coef,
-                   int self_mode, double *part) {
+                   int self_mode) {
   const int64_t n = c->n;
   if (n == 0) return GGEM_OK;
   cudaError_t e;
   const double self_c0 = self_coefficient(c, self_mode);
   if (c->pretensor_ok) {
-    if (part) return fail(c, GGEM_ERR_BAD_ARG, "term norms need per-matvec pair tensors");
     if ((e = c->w_f4[0].ensure((size_t)n)) || (e = c->w_f4[1].ensure((size_t)n)))
       return cuda_fail(c, e, "chebyshev forces");
     float4 *cur = c->w_f4[c->rec_cur].p, *nxt = c->w_f4[c->rec_cur ^ 1].p;
@@ -1275,8 +1216,8 @@ int pair_cheb_term(ggem_ctx *c, bool records_fresh, const double *x0, const doub
   }
   const double c1 = two_db + two_da * self_c0;
   kt_start(c, kKPairCheb);
-  if (c->use_poly) dispatch_cheb<true>(c, cur, nxt, two_da, c1, coef, x0, x1, xm, dw, part);
-  else dispatch_cheb<false>(c, cur, nxt, two_da, c1, coef, x0, x1, xm, dw, part);
+  if (c->use_poly) dispatch_cheb<true>(c, cur, nxt, two_da, c1, coef, x0, x1, xm, dw);
+  else dispatch_cheb<false>(c, cur, nxt, two_da, c1, coef, x0, x1, xm, dw);
   kt_stop(c, kKPairCheb);
   c->rec_cur ^= 1;
   return check_launch(c, "pair chebyshev term");
@@ -1287,11 +1228,10 @@ int pair_grid_blocks(const ggem_ctx *c) {
 }
 
 // The first step of a fused series: xi (caller order) into slot order (x0)
-// with its records, then k_pair_first (x1, dw, records of x1 for the first
-// term and the blocks' shares of xi . M xi in part_aux2).
-int cheb_start_fused(ggem_ctx *c, const double *xi, double *x0, double *x1, double *dw,
-                     double da, double db, double c0, double c1, double *part_aux2,
-                     int self_mode) {
+// with its records, then k_pair_first (m = M x0, x1, dw and the records of
+// x1 for the first term).
+int cheb_start_fused(ggem_ctx *c, const double *xi, double *x0, double *m, double *x1,
+                     double *dw, double da, double db, double c0, double c1, int self_mode) {
   const int64_t n = c->n;
   if (n == 0) return GGEM_OK;
   if (c->pretensor_ok) return fail(c, GGEM_ERR_BAD_ARG, "fused start needs per-matvec pair tensors");
@@ -1307,21 +1247,15 @@ int cheb_start_fused(ggem_ctx *c, const double *xi, double *x0, double *x1, doub
   kt_start(c, kKPairF32);
   const bool v1 = c->computed_variant == 1;
   if (c->use_poly) {
-    if (v1) launch_first<true, 1>(c, cur, nxt, self_c, da, db, c0, c1, x0, x1, dw, part_aux2);
-    else launch_first<true, 0>(c, cur, nxt, self_c, da, db, c0, c1, x0, x1, dw, part_aux2);
+    if (v1) launch_first<true, 1>(c, cur, nxt, self_c, da, db, c0, c1, x0, m, x1, dw);
+    else launch_first<true, 0>(c, cur, nxt, self_c, da, db, c0, c1, x0, m, x1, dw);
   } else {
-    if (v1) launch_first<false, 1>(c, cur, nxt, self_c, da, db, c0, c1, x0, x1, dw, part_aux2);
-    else launch_first<false, 0>(c, cur, nxt, self_c, da, db, c0, c1, x0, x1, dw, part_aux2);
+    if (v1) launch_first<false, 1>(c, cur, nxt, self_c, da, db, c0, c1, x0, m, x1, dw);
+    else launch_first<false, 0>(c, cur, nxt, self_c, da, db, c0, c1, x0, m, x1, dw);
   }
   kt_stop(c, kKPairF32);
   c->rec_cur ^= 1;
   return check_launch(c, "pair first step");
-}
-
-// u = M f (one right-hand side, slot order) with the blocks' shares of |u|^2
-int matvec_dot(ggem_ctx *c, const double *f, double *u, int self_mode, double *part) {
-  if (c->n == 0) return GGEM_OK;
-  return launch_f32_r1(c, f, u, self_coefficient(c, self_mode), part);
 }
 
 // the per-pair tensors of the current list (k_pair_tensor)
@@ -1391,7 +1325,7 @@ int matvec_slots(ggem_ctx *c, int nrhs, const double *f, double *u, int self_mod
     }
     return GGEM_OK;
   }
-  if (nrhs == 1) return launch_f32_r1(c, f, u, self_coefficient(c, self_mode), nullptr);
+  if (nrhs == 1) return launch_f32_r1(c, f, u, self_coefficient(c, self_mode));
   if (nrhs >= kBatchMinRhs) return matvec_b64(c, nrhs, f, u, self_coefficient(c, self_mode));
   cudaError_t e = c->w_f32.ensure((size_t)c->n * nrhs);
   if (e) return cuda_fail(c, e, "f32 staging");

@@ -547,7 +547,7 @@ class Context:
         return bool(u.value), a.value, b.value
 
     def set_pair_variant(self, computed=0, stored=0):
-        """kernel shapes: computed 0 (registers capped for 6) or 1 (for 8
+        """kernel shapes: computed 0 (registers capped for 6) or 1 (for 5
         blocks per SM); stored 0 .. 3"""
         self._check(lib().ggem_set_pair_variant(self.h, int(computed), int(stored)))
 

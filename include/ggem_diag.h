@@ -42,7 +42,7 @@ int ggem_set_pair_tensors(ggem_ctx *ctx, int enable);
  * pair and with stored tensors (plus the one tensor pass per build,
  * amortised over matvecs_per_build matvecs) by CUDA events on the context's
  * stream; each form is timed for each of its kernel shapes (per-matvec
- * tensors: registers capped for 6 or for 8 blocks per SM; stored
+ * tensors: registers capped for 6 or for 5 blocks of 256 per SM; stored
  * tensors: lanes per target, entries in flight, pipelined stream).  The
  * fastest stays selected for this context; both costs are reported in ms
  * per matvec (the stored one with its amortised pass) and variants[0],
