@@ -243,6 +243,9 @@ int pair_cheb_term(ggem_ctx *c, bool records_fresh, const double *x0, const doub
                    int self_mode);
 // blocks of the single-RHS pair kernels
 int pair_grid_blocks(const ggem_ctx *c);
+// u = M f, one right-hand side, caller order in and out (FP32 list with
+// per-matvec tensors only); f_slot receives f in slot order
+int matvec_orig_fused(ggem_ctx *c, const double *f, double *u, double *f_slot, int self_mode);
 // the fused first step of a series (xi in caller order; m = M x0 is kept)
 int cheb_start_fused(ggem_ctx *c, const double *xi, double *x0, double *m, double *x1,
                      double *dw, double da, double db, double c0, double c1, int self_mode);

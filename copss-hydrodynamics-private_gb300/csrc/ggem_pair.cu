@@ -399,13 +399,14 @@ __device__ __forceinline__ PairSum pair_sum_r1(int64_t s, bool act, int sub, con
 constexpr int kComputedMinBlocks[] = {6, 5};
 constexpr int kNumComputedVariants = 2;
 
-// u = M f, single right-hand side
-template <bool POLY, int V>
+// u = M f, single right-hand side; with ORIG, u is written in the caller's
+// particle order (u[order[s]]) instead of slot order
+template <bool POLY, int V, bool ORIG>
 __global__ void __launch_bounds__(256, kComputedMinBlocks[V]) k_pair_r1(
     int64_t n, const Rec32 *__restrict__ src, const int32_t *__restrict__ cnt, int W,
     const uint32_t *__restrict__ list, PolyAB P, const Rec32 *__restrict__ tab, float inv_ds,
     const float4 *__restrict__ shift, double self_c, const double *__restrict__ f,
-    double *__restrict__ u) {
+    double *__restrict__ u, const int32_t *__restrict__ order) {
   __shared__ float4 sh[kMaxCode];
   stage_shifts(sh, shift);
   const int64_t gid = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / kGroup;
@@ -418,7 +419,9 @@ __global__ void __launch_bounds__(256, kComputedMinBlocks[V]) k_pair_r1(
   group_scatter3(sub, r, h, l);
   if (!act || sub >= 3) return;
   const int64_t k = 3 * s + sub;
-  u[k] = fma(self_c, f[k], f2d_bits(h) + f2d_bits(l));
+  const double v = fma(self_c, f[k], f2d_bits(h) + f2d_bits(l));
+  if (ORIG) u[3 * (int64_t)order[s] + sub] = v;
+  else u[k] = v;
 }
 
 // The first Chebyshev step in one pass (brownian_system.C:1036-1056 for one
@@ -1042,17 +1045,18 @@ PolyAB poly_of(const ggem_ctx *c) {
   return P;
 }
 
-template <bool POLY, int V>
+template <bool POLY, int V, bool ORIG>
 void launch_r1(ggem_ctx *c, const Rec32 *src, const double *f, double *u, double self_c) {
-  k_pair_r1<POLY, V><<<(unsigned)pair_grid_blocks(c), 256, 0, c->stream>>>(
+  k_pair_r1<POLY, V, ORIG><<<(unsigned)pair_grid_blocks(c), 256, 0, c->stream>>>(
       c->n, src, c->nb_cnt.p, c->nb_w, c->nb_list.p, poly_of(c),
-      reinterpret_cast<const Rec32 *>(c->tab.p), c->tab_inv_ds, c->d_shift.p, self_c, f, u);
+      reinterpret_cast<const Rec32 *>(c->tab.p), c->tab_inv_ds, c->d_shift.p, self_c, f, u,
+      c->order.p);
 }
 
-template <bool POLY>
+template <bool POLY, bool ORIG = false>
 void dispatch_r1(ggem_ctx *c, const Rec32 *src, const double *f, double *u, double self_c) {
-  if (c->computed_variant == 1) launch_r1<POLY, 1>(c, src, f, u, self_c);
-  else launch_r1<POLY, 0>(c, src, f, u, self_c);
+  if (c->computed_variant == 1) launch_r1<POLY, 1, ORIG>(c, src, f, u, self_c);
+  else launch_r1<POLY, 0, ORIG>(c, src, f, u, self_c);
 }
 
 // single right-hand side: records from FP64 slot-order f, then the pair sum
@@ -1256,6 +1260,29 @@ int cheb_start_fused(ggem_ctx *c, const double *xi, double *x0, double *m, doubl
   kt_stop(c, kKPairF32);
   c->rec_cur ^= 1;
   return check_launch(c, "pair first step");
+}
+
+// u = M f for one right-hand side with f and u in the caller's particle
+// order (FP32 list, per-matvec tensors): the slot permutation of f is fused
+// with its records (k_to_slots_rec) and the pair kernel writes u in caller
+// order, so a matvec is two launches.  f_slot receives f in slot order (the
+// self term reads it).
+int matvec_orig_fused(ggem_ctx *c, const double *f, double *u, double *f_slot, int self_mode) {
+  const int64_t n = c->n;
+  if (n == 0) return GGEM_OK;
+  if (c->pretensor_ok) return fail(c, GGEM_ERR_BAD_ARG, "fused matvec needs per-matvec pair tensors");
+  cudaError_t e = c->w_src.ensure(2 * (size_t)n);
+  if (e) return cuda_fail(c, e, "pair records");
+  Rec32 *src = reinterpret_cast<Rec32 *>(c->w_src.p);
+  k_to_slots_rec<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(n, c->order.p, c->pos32.p,
+                                                                     f, f_slot, src);
+  if (int rc = check_launch(c, "to slots + records")) return rc;
+  const double self_c = self_coefficient(c, self_mode);
+  kt_start(c, kKPairF32);
+  if (c->use_poly) dispatch_r1<true, true>(c, src, f_slot, u, self_c);
+  else dispatch_r1<false, true>(c, src, f_slot, u, self_c);
+  kt_stop(c, kKPairF32);
+  return check_launch(c, "pair f32 r1");
 }
 
 // the per-pair tensors of the current list (k_pair_tensor)
