@@ -304,7 +304,11 @@ def run_gb300(args, rank, world):
     ctx.set_kernel_timing(True)
     lc0 = ctx.launch_count()
     t_wall0 = time.perf_counter()
+    # an NVTX range around the timed device steps lets a profiler select
+    # exactly their launches (ncu --nvtx --nvtx-include "brownian_steps/")
+    torch.cuda.nvtx.range_push("brownian_steps")
     ts = timed(device_step, args.steps, 0)
+    torch.cuda.nvtx.range_pop()
     t_wall = time.perf_counter() - t_wall0
     clk.mark(t_wall0, t_wall0 + t_wall)
     lc1 = ctx.launch_count()
