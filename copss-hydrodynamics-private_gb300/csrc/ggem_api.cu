@@ -75,9 +75,6 @@ struct DeviceGuard {
   }
 };
 
-bool finite3(const double *v) {
-  return std::isfinite(v[0]) && std::isfinite(v[1]) && std::isfinite(v[2]);
-}
 
 // reference-mode element stencil: every element offset whose centroid lies
 // within search_radius_e (minimum image) of the element's own centroid,
@@ -373,10 +370,8 @@ static int set_particles_common(ggem_ctx *ctx, int64_t n, const double *xyz, boo
   if (n >= ((int64_t)1 << (32 - kCodeBits)))
     return fail(ctx, GGEM_ERR_BAD_ARG, "at most 2^25 particles per context");
   DeviceGuard dg(ctx->device);
-  if (!dev) {
-    for (int64_t i = 0; i < n; ++i)
-      if (!finite3(xyz + 3 * i)) return fail(ctx, GGEM_ERR_BAD_ARG, "non-finite position");
-  }
+  // non-finite coordinates are found by the cell build on the device (a host
+  // scan of the positions cost more than the copy itself)
   cudaError_t e = ctx->xyz_in.ensure((size_t)std::max<int64_t>(3 * n, 1));
   if (e) return cuda_fail(ctx, e, "positions");
   if (n > 0) {

@@ -36,9 +36,13 @@ __global__ void k_assign(int64_t n, const double *__restrict__ xyz, Grid g,
   if (i >= n) return;
   double p[3];
   int c[3];
-  bool bad = false;
+  bool bad = false, nonfinite = false;
   for (int d = 0; d < 3; ++d) {
     double x = xyz[3 * i + d];
+    if (!isfinite(x)) {  // reported as a bad argument; the cell index stays in range
+      nonfinite = true;
+      x = g.lo[d];
+    }
     double t = x - g.lo[d];
     // (FP64 runs at a small fraction of the FP32 rate: fmod and the division
     // are taken only where they can change the result)
@@ -63,6 +67,7 @@ __global__ void k_assign(int64_t n, const double *__restrict__ xyz, Grid g,
     c[d] = k < 0 ? 0 : (k >= g.nc[d] ? g.nc[d] - 1 : k);
   }
   if (bad) atomicOr(err, kErrOutOfDomain);
+  if (nonfinite) atomicOr(err, kErrNonFinite);
   const int32_t id = c[0] + g.nc[0] * (c[1] + g.nc[1] * c[2]);
   cell_of[i] = id;
   atomicAdd(&count[id], 1);
@@ -430,6 +435,10 @@ int build_cells(ggem_ctx *c, bool defer_flags) {
 }
 
 int cell_flag_error(ggem_ctx *c, int flags) {
+  if (flags & kErrNonFinite) {
+    c->cells_built = false;
+    return fail(c, GGEM_ERR_BAD_ARG, "non-finite position");
+  }
   if (flags & kErrOutOfDomain) {
     c->cells_built = false;
     return fail(c, GGEM_ERR_OUT_OF_DOMAIN,

@@ -43,6 +43,7 @@ enum : int {
   kErrTimeout = 4,
   kErrBadIndex = 8,
   kErrListCapacity = 16,  // speculative list fill ran past the allocated list
+  kErrNonFinite = 32,     // a particle position is NaN or infinite
 };
 
 // derived GGEM constants (ggem_stokes.C:39-114) in FP64

@@ -131,6 +131,8 @@ int ggem_synchronize(ggem_ctx *ctx);
  * cell assignment, sorted cell list and (FP32) the cached pair list */
 int ggem_set_particles(ggem_ctx *ctx, int64_t n, const double *xyz);
 int ggem_set_particles_dev(ggem_ctx *ctx, int64_t n, const double *d_xyz);
+/* (a NaN or infinite coordinate is reported by the cell build, or with
+ * deferred checks by the call that reads its flags, as GGEM_ERR_BAD_ARG) */
 int ggem_build_cells(ggem_ctx *ctx);
 /* deferred checks: with enable = 1, a build after the first one keeps the
  * pair-list row width and returns without waiting for the device; its row

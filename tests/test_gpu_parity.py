@@ -331,6 +331,20 @@ def test_philox_noise_matches_oracle():
     assert abs(got.mean()) < 0.05 and abs(got.std() - 1) < 0.05
 
 
+def test_non_finite_position_reported_by_the_build():
+    xyz, L = suspension(500, 0.05, 9)
+    bad = xyz.copy()
+    bad[3, 1] = np.nan
+    with G.Context(box_hi=(L,) * 3, rc=7.0, precision=G.FP32) as ctx:
+        ctx.set_particles(bad)
+        with pytest.raises(G.GGEMError) as ei:
+            ctx.build_cells()
+        assert ei.value.code == G.ERR_BAD_ARG
+        ctx.set_particles(xyz)  # the context stays usable
+        ctx.build_cells()
+        assert ctx.pair_count() > 0
+
+
 def test_errors_are_reported_not_raised_on_device():
     with G.Context(box_hi=(20.0,) * 3, periodic=(0, 0, 0), precision=G.FP64) as ctx:
         ctx.set_particles(np.array([[1.0, 1.0, 1.0], [25.0, 1.0, 1.0]]))
