@@ -15,6 +15,8 @@ ggem_ctx::~ggem_ctx() {
   for (auto &t : ktimer)
     for (cudaEvent_t e : t.ev) cudaEventDestroy(e);
   for (cudaEvent_t e : ev_pool) cudaEventDestroy(e);
+  for (auto &t : trace_ev) cudaEventDestroy(t.second);
+  if (ev_readback) cudaEventDestroy(ev_readback);
   for (auto *b : scan_scratch) delete b;
   if (h_red) cudaFreeHost(h_red);
   if (h_stage) cudaFreeHost(h_stage);

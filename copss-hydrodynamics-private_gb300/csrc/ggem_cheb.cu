@@ -282,8 +282,12 @@ int grid1(int64_t tot) {
 }
 
 // results[q] of the partial arrays, copied to the pinned host mirror; with
-// list_stats, host[nq .. nq+2] receive a deferred build's statistics too
-int finalize_to_host(ggem_ctx *c, int nq, int G, double *host, bool list_stats = false) {
+// list_stats, host[nq .. nq+2] receive a deferred build's statistics too.
+// before_wait (optional) queues more work behind the readback before the
+// host waits for it.
+template <typename F>
+int finalize_to_host_then(ggem_ctx *c, int nq, int G, double *host, bool list_stats,
+                          F &&before_wait) {
   double *out = c->w_red.p + (size_t)nq * G;
   k_finalize<<<nq, kVecThreads, 0, c->stream>>>(G, c->w_red.p, out, nq,
                                                 list_stats ? c->nb_stat.p : nullptr,
@@ -291,9 +295,19 @@ int finalize_to_host(ggem_ctx *c, int nq, int G, double *host, bool list_stats =
   if (int rc = check_launch(c, "finalize")) return rc;
   const int nv = nq + (list_stats ? 3 : 0);
   cudaError_t e = cudaMemcpyAsync(host, out, sizeof(double) * nv, cudaMemcpyDeviceToHost, c->stream);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   if (e) return cuda_fail(c, e, "reduction readback");
+  if (!c->ev_readback &&
+      (e = cudaEventCreateWithFlags(&c->ev_readback, cudaEventDisableTiming)))
+    return cuda_fail(c, e, "readback event");
+  // the host waits for the readback only: work queued by before_wait runs on
+  if ((e = cudaEventRecord(c->ev_readback, c->stream))) return cuda_fail(c, e, "readback event");
+  if (int rc = before_wait()) return rc;
+  if ((e = cudaEventSynchronize(c->ev_readback))) return cuda_fail(c, e, "reduction readback");
   return GGEM_OK;
+}
+
+int finalize_to_host(ggem_ctx *c, int nq, int G, double *host, bool list_stats = false) {
+  return finalize_to_host_then(c, nq, G, host, list_stats, [] { return GGEM_OK; });
 }
 
 int sumsq_to_host(ggem_ctx *c, int nrhs, int64_t D, const double *v, double *host) {
@@ -344,8 +358,13 @@ constexpr int kRestartCheb = 1;
 // Only check points synchronise with the host.  On return *dm_is_my tells
 // whether c->w_out holds M y for every right-hand side (the last check ran
 // on the final y), which the Brownian displacement reuses.
+// spec_dw (optional, caller order): every error check also queues M dw into
+// it before the host waits for the check's readback; when the series ends at
+// a check, *spec_done says that spec_dw already holds M y.
 int cheb_slots(ggem_ctx *c, int nrhs, int N, double eig_min, double eig_max, double tol,
-               int check_every, const double *xi, ggem_cheb_report *rep, bool *dm_is_my) {
+               int check_every, const double *xi, ggem_cheb_report *rep, bool *dm_is_my,
+               double *spec_dw = nullptr, bool *spec_done = nullptr) {
+  if (spec_done) *spec_done = false;
   const int64_t D = 3 * c->n;
   const int sm = brownian_self_mode(c);
   const bool faithful = check_every == 1;
@@ -404,9 +423,13 @@ int cheb_slots(ggem_ctx *c, int nrhs, int N, double eig_min, double eig_max, dou
     if (int rc = matvec_slots(c, nrhs, dw, dm, sm)) return rc;
     k_dot_partials<<<dim3(G, nrhs), kVecThreads, 0, st>>>(D, dm, dm, p_dm);
     if (int rc = check_launch(c, "dm norm")) return rc;
-    // a deferred list build is checked in the same readback
+    // a deferred list build is checked in the same readback; the caller's
+    // M y is queued behind it in case this check ends the series
     const bool pending = c->list_unchecked;
-    if (int rc = finalize_to_host(c, 4 * nrhs, G, h, pending)) return rc;
+    if (int rc = finalize_to_host_then(c, 4 * nrhs, G, h, pending, [&]() -> int {
+          return spec_dw ? permute_from_slots(c, nrhs, dm, spec_dw) : GGEM_OK;
+        }))
+      return rc;
     if (pending) {
       const double *v = h + 4 * nrhs;
       bool rebuilt = false;
@@ -439,6 +462,7 @@ int cheb_slots(ggem_ctx *c, int nrhs, int N, double eig_min, double eig_max, dou
   if (faithful) {  // the estimators before the loop (:1064-1072)
     if (int rc = check_now(std::fabs(X[1]), false)) return rc;
     *dm_is_my = true;
+    if (spec_done) *spec_done = spec_dw != nullptr;
   }
   const double two_da = 2. * da, two_db = 2. * db;
   int first_check = -1;
@@ -475,9 +499,11 @@ int cheb_slots(ggem_ctx *c, int nrhs, int N, double eig_min, double eig_max, dou
         rep[r].n_terms = i + 1;
       }
     *dm_is_my = false;
+    if (spec_done) *spec_done = false;
     if (check) {
       if (int rc = check_now(std::fabs(X[i + 1]), true)) return rc;  // incl. kRestartCheb
       *dm_is_my = true;
+      if (spec_done) *spec_done = spec_dw != nullptr;
       if (first_check < 0) first_check = i + 1;
     }
     // x0 <- x1, x1 <- xm (:1152-1153) by rotating the buffers
@@ -589,10 +615,15 @@ extern "C" int ggem_brownian_displacement_dev(ggem_ctx *ctx, int nrhs, int N, do
   DeviceGuard dg(ctx->device);
   const size_t len = (size_t)ctx->n * 3 * nrhs;
   if (int rc = ensure_cheb_buffers(ctx, len)) return rc;
-  bool dm_is_my = false;
-  int rc = cheb_slots(ctx, nrhs, N, eig_min, eig_max, tol_cheb, check_every, d_xi, rep, &dm_is_my);
+  bool dm_is_my = false, spec_done = false;
+  // d_dw is the caller's output alone (unless it is xi itself), so every
+  // check may already queue M dw into it (overwritten if the series goes on)
+  double *spec = d_dw != d_xi ? d_dw : nullptr;
+  int rc = cheb_slots(ctx, nrhs, N, eig_min, eig_max, tol_cheb, check_every, d_xi, rep, &dm_is_my,
+                      spec, &spec_done);
   if (rc == kRestartCheb)  // the deferred list was rebuilt wider: run the series again
-    rc = cheb_slots(ctx, nrhs, N, eig_min, eig_max, tol_cheb, check_every, d_xi, rep, &dm_is_my);
+    rc = cheb_slots(ctx, nrhs, N, eig_min, eig_max, tol_cheb, check_every, d_xi, rep, &dm_is_my,
+                    spec, &spec_done);
   if (rc) return rc;
   bool all = true;
   for (int r = 0; r < nrhs; ++r) all = all && rep[r].converged;
@@ -600,7 +631,8 @@ extern "C" int ggem_brownian_displacement_dev(ggem_ctx *ctx, int nrhs, int N, do
     return ggem::fail(ctx, GGEM_ERR_CHEB_NOT_CONVERGED,
                       "Chebyshev polynomial fails to converge (brownian_system.C:1162-1163)");
   // hi_ewald: dw = M y (copss.C:1686); the last error check already
-  // computed M y when it ran on the final y
+  // computed M y when it ran on the final y (and queued it into d_dw)
+  if (spec_done) return GGEM_OK;
   if (!dm_is_my) {
     if (int rc = matvec_slots(ctx, nrhs, ctx->w_y.p, ctx->w_out.p, brownian_self_mode(ctx)))
       return rc;

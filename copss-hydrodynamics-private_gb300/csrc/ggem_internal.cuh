@@ -170,6 +170,7 @@ struct ggem_ctx {
   ggem::DevBuf<double> w_red;   // reduction partials
   ggem::DevBuf<double> lz_Q;    // Lanczos basis
   double *h_red = nullptr;      // pinned host mirror of reductions
+  cudaEvent_t ev_readback = nullptr;  // recorded behind the reductions' readback
   double *h_stage = nullptr;    // pinned host staging
   size_t h_stage_bytes = 0;
 
