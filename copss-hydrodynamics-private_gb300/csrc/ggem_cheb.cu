@@ -119,6 +119,9 @@ __global__ void __launch_bounds__(kVecThreads) k_cheb_init(int64_t D, double c0,
 
 // one term (brownian_system.C:1091-1108):
 //   ||dw|| -> q0 ; xm = (2db x1 + 2da xm) - x0 ; dw += c[r] xm ; ||xm|| -> q1
+// The norms feed only the error estimators: a term that no check follows
+// skips them (NORMS = false), a third of the term's FP64 work.
+template <bool NORMS>
 __global__ void __launch_bounds__(kVecThreads) k_cheb_term(int64_t D, double two_da,
                                                            double two_db, RhsCoef cf,
                                                            const double *__restrict__ x0,
@@ -134,18 +137,20 @@ __global__ void __launch_bounds__(kVecThreads) k_cheb_term(int64_t D, double two
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < D;
        k += (int64_t)gridDim.x * blockDim.x) {
     const double y = dw[off + k];
-    a4 += y * y;
+    if (NORMS) a4 += y * y;
     double v = two_db * x1[off + k] + two_da * xm[off + k];
     v -= x0[off + k];
     xm[off + k] = v;
     dw[off + k] = y + c * v;
-    a3 += v * v;
+    if (NORMS) a3 += v * v;
   }
-  const double s4 = block_sum(a4, sh);
-  const double s3 = block_sum(a3, sh);
-  if (threadIdx.x == 0) {
-    partial[(int64_t)(0 * nrhs + r) * gridDim.x + blockIdx.x] = s4;
-    partial[(int64_t)(1 * nrhs + r) * gridDim.x + blockIdx.x] = s3;
+  if (NORMS) {
+    const double s4 = block_sum(a4, sh);
+    const double s3 = block_sum(a3, sh);
+    if (threadIdx.x == 0) {
+      partial[(int64_t)(0 * nrhs + r) * gridDim.x + blockIdx.x] = s4;
+      partial[(int64_t)(1 * nrhs + r) * gridDim.x + blockIdx.x] = s3;
+    }
   }
 }
 
@@ -487,8 +492,12 @@ int cheb_slots(ggem_ctx *c, int nrhs, int N, double eig_min, double eig_max, dou
       RhsCoef cf;
       for (int r = 0; r < nrhs; ++r) cf.c[r] = active[r] ? X[i + 1] : 0.0;
       kt_start(c, kKChebTerm);
-      k_cheb_term<<<dim3(G, nrhs), kVecThreads, 0, st>>>(D, two_da, two_db, cf, x0, x1, xm, dw,
-                                                          p_term);
+      if (check)
+        k_cheb_term<true><<<dim3(G, nrhs), kVecThreads, 0, st>>>(D, two_da, two_db, cf, x0, x1,
+                                                                  xm, dw, p_term);
+      else
+        k_cheb_term<false><<<dim3(G, nrhs), kVecThreads, 0, st>>>(D, two_da, two_db, cf, x0, x1,
+                                                                   xm, dw, p_term);
       kt_stop(c, kKChebTerm);
       if (int rc = check_launch(c, "cheb term")) return rc;
       records_fresh = false;

@@ -218,3 +218,24 @@ extern "C" int ggem_get_launch_trace(ggem_ctx *ctx, int64_t max, double *t_ms,
   }
   return GGEM_OK;
 }
+
+namespace ggem {
+__global__ void k_convert_check(int64_t n, const double *__restrict__ in, float *__restrict__ out,
+                                float *__restrict__ ref) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  out[i] = d2f_bits(in[i]);
+  ref[i] = __double2float_rn(in[i]);
+}
+}  // namespace ggem
+
+extern "C" int ggem_diag_convert_f32(ggem_ctx *ctx, int64_t n, const double *d_in, float *d_out,
+                                     float *d_ref) {
+  if (!ctx || n < 0 || (n > 0 && (!d_in || !d_out || !d_ref))) return GGEM_ERR_BAD_ARG;
+  if (n == 0) return GGEM_OK;
+  k_convert_check<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(n, d_in, d_out, d_ref);
+  if (int rc = check_launch(ctx, "convert check")) return rc;
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  if (e) return cuda_fail(ctx, e, "convert check");
+  return GGEM_OK;
+}

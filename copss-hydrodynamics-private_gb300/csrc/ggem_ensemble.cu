@@ -169,7 +169,7 @@ __global__ void k_ens_pair(int64_t ntot, const int32_t *__restrict__ cnt, int W,
       v -= x0[k0 + c];
       u[k0 + c] = v;  // u is xm here
       dw[k0 + c] = dw[k0 + c] + cf * v;
-      out[c] = __double2float_rn(v);
+      out[c] = d2f_bits(v);
     }
     next[s * kR + r] = make_float4(out[0], out[1], out[2], 0.f);
   }

@@ -192,6 +192,29 @@ struct ggem_ctx {
 
 namespace ggem {
 
+#ifdef __CUDACC__
+// double -> float rounded to nearest even, from the IEEE 754 bit fields
+// with integer operations only (GB300 runs FP64 conversions at the FP64
+// rate, 1/64 of FP32); results below the float normal range (|x| < 2^-126)
+// take the hardware conversion.  Checked bit for bit against
+// __double2float_rn (ggem_diag_convert_f32).
+__device__ __forceinline__ float d2f_bits(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const uint32_t sign = (uint32_t)(b >> 32) & 0x80000000u;
+  const int ex = (int)((b >> 52) & 0x7ffu);
+  const unsigned long long m = b & 0xfffffffffffffull;
+  if (ex == 0x7ff) return __uint_as_float(sign | 0x7f800000u | (m ? 0x400000u : 0u));
+  const int e32 = ex - 1023 + 127;
+  if (e32 >= 255) return __uint_as_float(sign | 0x7f800000u);
+  if (e32 <= 0) return __double2float_rn(x);
+  unsigned long long keep = m >> 29;
+  const unsigned long long rem = m & 0x1fffffffull, half = 0x10000000ull;
+  keep += (rem > half || (rem == half && (keep & 1ull))) ? 1ull : 0ull;
+  // a carry out of the mantissa moves into the exponent (up to infinity)
+  return __uint_as_float(sign | (uint32_t)(((unsigned long long)e32 << 23) + keep));
+}
+#endif
+
 // kernel kinds of the timing hooks
 enum : int { kKPairF32 = 0, kKPairF64 = 1, kKChebTerm = 2, kKListBuild = 3, kKPairCheb = 4 };
 

@@ -261,7 +261,7 @@ __global__ void k_build_src(int64_t n, const float4 *__restrict__ pos32,
   if (s >= n) return;
   Rec32 r;
   r.a = pos32[s];
-  r.b = make_float4((float)f[3 * s], (float)f[3 * s + 1], (float)f[3 * s + 2], 0.f);
+  r.b = make_float4(d2f_bits(f[3 * s]), d2f_bits(f[3 * s + 1]), d2f_bits(f[3 * s + 2]), 0.f);
   src[s] = r;
 }
 
@@ -457,7 +457,7 @@ __global__ void __launch_bounds__(256, kComputedMinBlocks[V]) k_pair_first(
     const double x1k = db * xk + da * mk;
     x1[k] = x1k;
     dw[k] = c0 * xk + c1 * x1k;
-    nf[4 + sub] = __double2float_rn(x1k);
+    nf[4 + sub] = d2f_bits(x1k);
   } else {
     reinterpret_cast<float4 *>(nf)[0] = ri.a;
     nf[7] = 0.f;
@@ -494,7 +494,7 @@ __global__ void __launch_bounds__(256, kComputedMinBlocks[V]) k_pair_cheb(
     const double v = fma(two_da, f2d_bits(h) + f2d_bits(l), fma(c1, x1[k], -x0[k]));
     xm[k] = v;
     dw[k] = fma(coef, v, dw[k]);
-    nf[4 + sub] = __double2float_rn(v);
+    nf[4 + sub] = d2f_bits(v);
   } else {
     reinterpret_cast<float4 *>(nf)[0] = ri.a;  // the target's position record
     nf[7] = 0.f;
@@ -562,7 +562,7 @@ __global__ void __launch_bounds__(256) k_pair_tensor(
 __global__ void k_stage_f4(int64_t n, const double *__restrict__ f, float4 *__restrict__ f4) {
   const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (s >= n) return;
-  f4[s] = make_float4((float)f[3 * s], (float)f[3 * s + 1], (float)f[3 * s + 2], 0.f);
+  f4[s] = make_float4(d2f_bits(f[3 * s]), d2f_bits(f[3 * s + 1]), d2f_bits(f[3 * s + 2]), 0.f);
 }
 
 // float-float sum over the G lanes of a target's group
@@ -705,7 +705,7 @@ __global__ void __launch_bounds__(256) k_pair_cheb_tv(
     v -= x0[k];
     xm[k] = v;
     dw[k] = dw[k] + coef * v;
-    nf[sub] = __double2float_rn(v);
+    nf[sub] = d2f_bits(v);
   } else if (sub == 3) {
     nf[3] = 0.f;
   }
@@ -834,7 +834,7 @@ __global__ void __launch_bounds__(256) k_stage_b64(int64_t n, int nr, const doub
   const int ns = (int)(n - s0 < 32 ? n - s0 : 32);
   for (int k = threadIdx.x; k < kBatchR * 96; k += blockDim.x) {
     const int r = k / 96, q = k - r * 96;
-    t[r][q] = (r < nr && q < 3 * ns) ? (float)f[((int64_t)r * n + s0) * 3 + q] : 0.f;
+    t[r][q] = (r < nr && q < 3 * ns) ? d2f_bits(f[((int64_t)r * n + s0) * 3 + q]) : 0.f;
   }
   __syncthreads();
   float *out = fb + s0 * 3 * kBatchR;

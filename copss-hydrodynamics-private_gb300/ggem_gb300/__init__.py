@@ -123,6 +123,7 @@ def lib():
         "ggem_probe_fp32_peak": (i, [vp, P(d)]),
         "ggem_set_kernel_timing": (i, [vp, i]),
         "ggem_set_launch_trace": (i, [vp, i]),
+        "ggem_diag_convert_f32": (i, [vp, i64, vp, vp, vp]),
         "ggem_get_launch_trace": (i, [vp, i64, vp, vp, P(i64)]),
         "ggem_get_kernel_timing": (i, [vp, i, P(d), P(i64)]),
         "ggem_lanczos_bounds": (i, [vp, i, C.c_uint64, P(d), P(d)]),

@@ -25,6 +25,11 @@ extern "C" {
 int ggem_set_launch_trace(ggem_ctx *ctx, int enable);
 int ggem_get_launch_trace(ggem_ctx *ctx, int64_t max, double *t_ms, const char **names,
                           int64_t *count);
+/* the library's integer-only double -> float conversion (used where FP64
+ * conversion throughput matters) and the hardware __double2float_rn, both
+ * applied to d_in[n] on the device, for a bit-for-bit check */
+int ggem_diag_convert_f32(ggem_ctx *ctx, int64_t n, const double *d_in, float *d_out,
+                          float *d_ref);
 /* number of CUDA kernels this context has launched so far */
 int ggem_get_launch_count(const ggem_ctx *ctx, int64_t *count);
 /* ordered in-cutoff pairs of the current FP32 pair list (the work unit of

@@ -345,6 +345,34 @@ def test_non_finite_position_reported_by_the_build():
         assert ctx.pair_count() > 0
 
 
+def test_integer_double_to_float_conversion_matches_hardware():
+    """the library's bit-field double -> float rounding (used on the hot
+    paths) equals __double2float_rn bit for bit, ties and edges included"""
+    import torch
+    rng = np.random.default_rng(12)
+    vals = [rng.standard_normal(200000), rng.standard_normal(20000) * 1e30,
+            rng.standard_normal(20000) * 1e-30, np.exp(rng.uniform(-700, 700, 20000))]
+    # exact ties between two floats, both parities, and values next to them
+    f = rng.standard_normal(20000).astype(np.float32)
+    up = np.nextafter(f, np.float32(np.inf))
+    mid = (f.astype(np.float64) + up.astype(np.float64)) / 2.0
+    vals += [mid, np.nextafter(mid, np.inf), np.nextafter(mid, -np.inf)]
+    vals.append(np.array([0.0, -0.0, np.inf, -np.inf, np.nan, 3.4028235677973366e38,
+                          3.4028236e38, 1e39, -1e39, 1.1754943508222875e-38, 1e-45, 1e-320]))
+    x = np.concatenate(vals)
+    d = torch.from_numpy(x).cuda()
+    out = torch.empty(len(x), dtype=torch.float32, device="cuda")
+    ref = torch.empty_like(out)
+    with G.Context(box_hi=(30.0,) * 3) as ctx:
+        ctx._check(G.lib().ggem_diag_convert_f32(ctx.h, len(x), d.data_ptr(), out.data_ptr(),
+                                                 ref.data_ptr()))
+    a = out.cpu().numpy().view(np.uint32)
+    b = ref.cpu().numpy().view(np.uint32)
+    nan = np.isnan(x)
+    assert np.array_equal(a[~nan], b[~nan])
+    assert np.all(np.isnan(out.cpu().numpy()[nan]))
+
+
 def test_errors_are_reported_not_raised_on_device():
     with G.Context(box_hi=(20.0,) * 3, periodic=(0, 0, 0), precision=G.FP64) as ctx:
         ctx.set_particles(np.array([[1.0, 1.0, 1.0], [25.0, 1.0, 1.0]]))
