@@ -382,6 +382,9 @@ int cheb_slots(ggem_ctx *c, int nrhs, int N, double eig_min, double eig_max, dou
   const bool can_fuse = nrhs == 1 && c->prm.precision == GGEM_FP32 &&
                         c->prm.nb_mode == GGEM_NB_CUTOFF;
   const bool fused = can_fuse && !faithful && !c->pretensor_ok && c->n > 0;
+  // 16 .. 64 right-hand sides: an unchecked term is one batched kernel
+  const bool batch_fused = !faithful && c->n > 0 && batch_term_fusable(c, nrhs);
+  bool staged_fresh = false;
   const int G = vec_blocks(D);
   cudaStream_t st = c->stream;
   double *x0 = c->w_c.p, *x1 = c->w_d.p, *xm = c->w_e.p, *dw = c->w_y.p, *dm = c->w_out.p;
@@ -487,6 +490,12 @@ int cheb_slots(ggem_ctx *c, int nrhs, int N, double eig_min, double eig_max, dou
         k_term_norms<<<G, kVecThreads, 0, st>>>(D, X[i + 1], xm, dw, p_term);
         if (int rc = check_launch(c, "term norms")) return rc;
       }
+    } else if (batch_fused && !check) {
+      double cf[kMaxRhs];
+      for (int r = 0; r < nrhs; ++r) cf[r] = active[r] ? X[i + 1] : 0.0;
+      if (int rc = batch_cheb_term(c, nrhs, staged_fresh, x0, x1, xm, dw, two_da, two_db, cf, sm))
+        return rc;
+      staged_fresh = true;
     } else {
       if (int rc = matvec_slots(c, nrhs, x1, xm, sm)) return rc;
       RhsCoef cf;
@@ -501,6 +510,7 @@ int cheb_slots(ggem_ctx *c, int nrhs, int N, double eig_min, double eig_max, dou
       kt_stop(c, kKChebTerm);
       if (int rc = check_launch(c, "cheb term")) return rc;
       records_fresh = false;
+      staged_fresh = false;
     }
     for (int r = 0; r < nrhs; ++r)
       if (active[r]) {

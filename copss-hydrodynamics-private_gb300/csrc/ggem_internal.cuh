@@ -167,6 +167,7 @@ struct ggem_ctx {
   ggem::DevBuf<double> w_in, w_out, w_a, w_b, w_c, w_d, w_e, w_y;
   ggem::DevBuf<float4> w_f32;
   ggem::DevBuf<float> w_fb;     // batched forces [slot][3][64] FP32
+  ggem::DevBuf<float> w_fb2;    // the next term's staging in a fused batched series
   ggem::DevBuf<double> w_red;   // reduction partials
   ggem::DevBuf<double> lz_Q;    // Lanczos basis
   double *h_red = nullptr;      // pinned host mirror of reductions
@@ -266,6 +267,12 @@ int build_pair_tensors(ggem_ctx *c);
 int pair_cheb_term(ggem_ctx *c, bool records_fresh, const double *x0, const double *x1,
                    double *xm, double *dw, double two_da, double two_db, double coef,
                    int self_mode);
+// an unchecked Chebyshev term for this many right-hand sides can run as one
+// batched kernel (batch_cheb_term)
+bool batch_term_fusable(const ggem_ctx *c, int nrhs);
+int batch_cheb_term(ggem_ctx *c, int nrhs, bool staged_fresh, const double *x0, const double *x1,
+                    double *xm, double *dw, double two_da, double two_db, const double *coef,
+                    int self_mode);
 // blocks of the single-RHS pair kernels
 int pair_grid_blocks(const ggem_ctx *c);
 // u = M f, one right-hand side, caller order in and out (FP32 list with

@@ -880,12 +880,24 @@ __device__ __forceinline__ void b64_flush(float2 (&sum)[3], float2 (&cmp)[3], fl
   b0 = b1 = b2 = make_float2(0.f, 0.f);
 }
 
-template <int CD, bool POLY>
+// per right-hand side Chebyshev coefficient of a fused batched term (0 for
+// a right-hand side whose series has stopped)
+struct BatchCoef {
+  double c[kBatchR];
+};
+
+// With CHEB the kernel is one unchecked Chebyshev term for up to 64
+// right-hand sides (brownian_system.C:1091-1108, the order of k_cheb_term):
+// u is x_{k+1}: u = (2db x1 + 2da M x1) - x0, dw += c_r u, and fb_next
+// receives the FP32 staging of u for the next term.
+template <int CD, bool POLY, bool CHEB>
 __global__ void __launch_bounds__(32 * kBatchWarps, 3) k_pair_b64(
     int64_t n, int nr, const float4 *__restrict__ pos32, const float2 *__restrict__ fb,
     const int32_t *__restrict__ cnt, int W, const uint32_t *__restrict__ list, PolyAB P,
     const Rec32 *__restrict__ tab, float inv_ds, float hx, float hy, float hz, float self_hi,
-    float self_lo, double *__restrict__ u) {
+    float self_lo, double *__restrict__ u, double two_da, double two_db, BatchCoef cf,
+    const double *__restrict__ x0, const double *__restrict__ x1, double *__restrict__ dw,
+    float *__restrict__ fb_next) {
   // per entry, pre-duplicated for the packed arithmetic:
   // g0 = (dx, dx, dy, dy), g1 = (dz, dz, A, A), g2 = (B, B), source slot
   __shared__ float4 s_g0[kBatchWarps][32], s_g1[kBatchWarps][32];
@@ -982,7 +994,28 @@ __global__ void __launch_bounds__(32 * kBatchWarps, 3) k_pair_b64(
     const int t = q / 3, c = q - t * 3;
     if (t >= ns) continue;
     const float2 v = s_out[t][r][c];
-    u[((int64_t)r * n + s0) * 3 + q] = f2d_bits(v.x) + f2d_bits(v.y);
+    const int64_t idx = ((int64_t)r * n + s0) * 3 + q;
+    double m = f2d_bits(v.x) + f2d_bits(v.y);
+    if (CHEB) {
+      double x = two_db * x1[idx] + two_da * m;
+      x -= x0[idx];
+      const double y = dw[idx];
+      dw[idx] = y + cf.c[r] * x;
+      m = x;
+      // FP32 staging of x_{k+1}, transposed through shared memory below
+      reinterpret_cast<float *>(&s_out[t][r][c])[0] = d2f_bits(x);
+    }
+    u[idx] = m;
+  }
+  if (CHEB) {
+    __syncthreads();
+    // staging layout [slot][3][64], right-hand sides fastest
+    float *out = fb_next + s0 * 3 * kBatchR;
+    for (int k = threadIdx.x; k < ns * 3 * kBatchR; k += blockDim.x) {
+      const int sc = k / kBatchR, r = k - sc * kBatchR;
+      const int t = sc / 3, c = sc - t * 3;
+      out[k] = r < nr ? reinterpret_cast<const float *>(&s_out[t][r][c])[0] : 0.f;
+    }
   }
 }
 
@@ -1114,10 +1147,24 @@ template <int CD, bool POLY>
 void launch_b64_t(ggem_ctx *c, int nr, const double *f, double *u, double self_c) {
   const Grid &g = c->grid;
   const unsigned grid = (unsigned)((c->n + kBatchWarps - 1) / kBatchWarps);
-  k_pair_b64<CD, POLY><<<grid, 32 * kBatchWarps, 0, c->stream>>>(
+  k_pair_b64<CD, POLY, false><<<grid, 32 * kBatchWarps, 0, c->stream>>>(
       c->n, nr, c->pos32.p, reinterpret_cast<const float2 *>(c->w_fb.p), c->nb_cnt.p, c->nb_w,
       c->nb_list.p, poly_of(c), reinterpret_cast<const Rec32 *>(c->tab.p), c->tab_inv_ds,
-      g.h32[0], g.h32[1], g.h32[2], (float)self_c, (float)(self_c - (double)(float)self_c), u);
+      g.h32[0], g.h32[1], g.h32[2], (float)self_c, (float)(self_c - (double)(float)self_c), u,
+      0.0, 0.0, BatchCoef{}, nullptr, nullptr, nullptr, nullptr);
+}
+
+template <int CD, bool POLY>
+void launch_b64_cheb(ggem_ctx *c, int nr, const float *fb, float *fb_next, double self_c,
+                     double two_da, double two_db, const BatchCoef &cf, const double *x0,
+                     const double *x1, double *xm, double *dw) {
+  const Grid &g = c->grid;
+  const unsigned grid = (unsigned)((c->n + kBatchWarps - 1) / kBatchWarps);
+  k_pair_b64<CD, POLY, true><<<grid, 32 * kBatchWarps, 0, c->stream>>>(
+      c->n, nr, c->pos32.p, reinterpret_cast<const float2 *>(fb), c->nb_cnt.p, c->nb_w,
+      c->nb_list.p, poly_of(c), reinterpret_cast<const Rec32 *>(c->tab.p), c->tab_inv_ds,
+      g.h32[0], g.h32[1], g.h32[2], (float)self_c, (float)(self_c - (double)(float)self_c), xm,
+      two_da, two_db, cf, x0, x1, dw, fb_next);
 }
 
 // many right-hand sides: passes of 64 (k_stage_b64 + k_pair_b64)
@@ -1225,6 +1272,47 @@ int pair_cheb_term(ggem_ctx *c, bool records_fresh, const double *x0, const doub
   kt_stop(c, kKPairCheb);
   c->rec_cur ^= 1;
   return check_launch(c, "pair chebyshev term");
+}
+
+// (the batched kernels evaluate their tensors per pair whether or not the
+// single-RHS path stores them)
+bool batch_term_fusable(const ggem_ctx *c, int nrhs) {
+  return nrhs >= kBatchMinRhs && nrhs <= kBatchR && c->prm.precision == GGEM_FP32 &&
+         c->prm.nb_mode == GGEM_NB_CUTOFF;
+}
+
+// One unchecked Chebyshev term for 16 .. 64 right-hand sides in one kernel
+// (k_pair_b64 with the recurrence in its write-out).  staged_fresh:
+// c->w_fb holds the FP32 staging of x1 (the previous fused term wrote it);
+// otherwise it is staged here first.  coef[r] is 0 for a stopped series.
+int batch_cheb_term(ggem_ctx *c, int nrhs, bool staged_fresh, const double *x0, const double *x1,
+                    double *xm, double *dw, double two_da, double two_db, const double *coef,
+                    int self_mode) {
+  const int64_t n = c->n;
+  if (n == 0) return GGEM_OK;
+  cudaError_t e;
+  if ((e = c->w_fb.ensure((size_t)n * 3 * kBatchR)) || (e = c->w_fb2.ensure((size_t)n * 3 * kBatchR)))
+    return cuda_fail(c, e, "batched staging");
+  if (!staged_fresh) {
+    k_stage_b64<<<(unsigned)((n + 31) / 32), 256, 0, c->stream>>>(n, nrhs, x1, c->w_fb.p);
+    if (int rc = check_launch(c, "batched staging")) return rc;
+  }
+  BatchCoef cf{};
+  for (int r = 0; r < nrhs; ++r) cf.c[r] = coef[r];
+  const double self_c = self_coefficient(c, self_mode);
+  const bool cd2 = c->prm.cell_div == 2;
+  kt_start(c, kKPairCheb);
+  if (c->use_poly) {
+    if (cd2) launch_b64_cheb<2, true>(c, nrhs, c->w_fb.p, c->w_fb2.p, self_c, two_da, two_db, cf, x0, x1, xm, dw);
+    else launch_b64_cheb<1, true>(c, nrhs, c->w_fb.p, c->w_fb2.p, self_c, two_da, two_db, cf, x0, x1, xm, dw);
+  } else {
+    if (cd2) launch_b64_cheb<2, false>(c, nrhs, c->w_fb.p, c->w_fb2.p, self_c, two_da, two_db, cf, x0, x1, xm, dw);
+    else launch_b64_cheb<1, false>(c, nrhs, c->w_fb.p, c->w_fb2.p, self_c, two_da, two_db, cf, x0, x1, xm, dw);
+  }
+  kt_stop(c, kKPairCheb);
+  std::swap(c->w_fb.p, c->w_fb2.p);  // the staging of x_{k+1} is the next term's x1
+  std::swap(c->w_fb.count, c->w_fb2.count);
+  return check_launch(c, "pair chebyshev term (batched)");
 }
 
 int pair_grid_blocks(const ggem_ctx *c) {

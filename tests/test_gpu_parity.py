@@ -467,6 +467,32 @@ def test_fused_chebyshev_terms_match_unfused_path():
     assert 0.5 * rep_o.err1 <= r2[0]["err1"] <= 2.0 * rep_o.err1
 
 
+def test_fused_batched_chebyshev_terms_match_unfused_path():
+    """16 .. 64 right-hand sides: unchecked terms run as one batched kernel
+    (pair sum, recurrence and the next term's FP32 staging); the series
+    equals the one that checks every term (unfused) to rounding."""
+    xyz, L = G.make_chains(5, 60, 20, 2.0, 0.05)
+    n = len(xyz)
+    xi = np.random.default_rng(31).standard_normal((40, 3 * n))
+    N = 12
+    with G.Context(box_hi=(L,) * 3, rc=7.0, precision=G.FP32) as ctx:
+        ctx.set_pair_tensors(False)
+        ctx.set_particles(xyz)
+        ctx.build_cells()
+        lo, hi = ctx.lanczos_bounds(k=30, seed=3)
+        lo, hi = lo / 1.05, hi * 1.05
+        y1, r1 = ctx.cheb_inv_sqrt(xi, N, lo, hi, 0.0, check_every=1)
+        ctx.set_kernel_timing(True)
+        y2, r2 = ctx.cheb_inv_sqrt(xi, N, lo, hi, 0.0, check_every=N - 1)
+        fused_ms, fused_n = ctx.kernel_timing(G.KERNEL_PAIR_CHEB)
+        ctx.set_kernel_timing(False)
+    assert all(r["n_terms"] == N for r in r1 + r2)
+    assert fused_n == N - 2  # terms 1 .. N-2; the last term is checked
+    assert rel(y2, y1) <= 1e-12
+    for a, b in zip(r1, r2):
+        assert b["err1"] == pytest.approx(a["err1"], rel=1e-9)
+
+
 def test_batched_64_rhs_chains_matvec_and_chebyshev():
     """The polymer workload's shape at a small size: 20-bead chains, phi=0.05,
     64 noise right-hand sides through the batched pair kernel (lanes over
