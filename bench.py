@@ -694,6 +694,7 @@ def ensemble_leg(G, torch, dev, flush, sur, margins, reps=3):
     for _ in range(2):
         step()
     ts, terms, ok = [], [], True
+    torch.cuda.nvtx.range_push("ensemble_steps")  # selects these launches for a profiler
     for _ in range(reps):
         flush.zero_()
         torch.cuda.synchronize()
@@ -703,6 +704,7 @@ def ensemble_leg(G, torch, dev, flush, sur, margins, reps=3):
         ts.append(time.perf_counter() - t0)
         ok = ok and rc == 0
         terms.append(max(r["n_terms"] for rb in rp for r in rb))
+    torch.cuda.nvtx.range_pop()
     f = torch.randn(beads * ENS_NRHS * 3, dtype=torch.float64, device="cuda")
     u = torch.empty_like(f)
     ens.matvec_dev(ENS_NRHS, f.data_ptr(), u.data_ptr())

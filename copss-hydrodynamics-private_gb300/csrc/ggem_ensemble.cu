@@ -493,8 +493,8 @@ extern "C" int ggem_ensemble_brownian_dev(ggem_ensemble *e, int nrhs, int N,
     db[b] = -(eig_max[b] + eig_min[b]) / d;
     tda[b] = 2.0 * da[b];
     tdb[b] = 2.0 * db[b];
-    cheb_coeffs_host(N, da[b], db[b], GGEM_CHEB_GAUSS, coef.data() + (size_t)b * ldc);
   }
+  cheb_coeffs_host_many(N, K, da.data(), db.data(), GGEM_CHEB_GAUSS, coef.data(), ldc);
   std::vector<uint8_t> act((size_t)K * kR, 0);
   for (int b = 0; b < K; ++b)
     for (int r = 0; r < nrhs; ++r) act[b * kR + r] = 1;
@@ -630,13 +630,24 @@ extern "C" int ggem_ensemble_brownian_dev(ggem_ensemble *e, int nrhs, int N,
   if (int rc = elaunch(e, "ensemble permute")) return rc;
   if ((c = cudaStreamSynchronize(e->stream))) return ecuda(e, c, "ensemble brownian");
   // adaptive schedule: the next call checks from the degree this one needed
+  // (one degree less only when every series passed its first check with
+  // room for it: the error shrinks by about rho = (sqrt(k) - 1) / (sqrt(k) + 1)
+  // per degree, k = eig_max / eig_min of the suspension; otherwise a steady
+  // workload would fail a check, a matvec and a host round trip more, every
+  // other call)
   int worst = 0;
-  bool all = true;
-  for (int q = 0; q < K * nrhs; ++q) {
-    all = all && rep[q].converged;
-    worst = std::max(worst, rep[q].n_terms);
+  bool all = true, room = true;
+  for (int b = 0; b < K; ++b) {
+    const double kap = eig_min[b] > 0 ? eig_max[b] / eig_min[b] : 1e30;
+    const double rho = (std::sqrt(kap) - 1.0) / (std::sqrt(kap) + 1.0);
+    for (int r = 0; r < nrhs; ++r) {
+      const ggem_cheb_report &R = rep[b * nrhs + r];
+      all = all && R.converged;
+      worst = std::max(worst, R.n_terms);
+      room = room && R.err1 <= 0.8 * rho * tol;
+    }
   }
-  if (all) e->pred_terms = (worst == first_check) ? std::max(2, worst - 1) : worst;
+  if (all) e->pred_terms = (worst == first_check && room) ? std::max(2, worst - 1) : worst;
   return all ? GGEM_OK : efail(e, GGEM_ERR_CHEB_NOT_CONVERGED, "some series did not converge");
 }
 

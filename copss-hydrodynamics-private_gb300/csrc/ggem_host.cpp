@@ -275,7 +275,13 @@ void tridiag_extremes(int k, const double *a, const double *b, double *lmin, dou
 // Chebyshev::chebyshev_coefficients and its three quadratures
 // (chebyshev.C:44-190).  The expressions keep the reference's evaluation
 // order so that the coefficients agree bit for bit.
-void cheb_coeffs_host(int N, double da, double db, int method, double *coef) {
+// K intervals at once (the ensemble's suspensions): the quadrature nodes,
+// weights and cos(tmpt) depend only on N and the method, so they are formed
+// once; each coefficient keeps the reference's expression and summation
+// order (acc += w_j cos(tmpt) f_j over j), so the values are the same bits
+// as one interval at a time.  coef of interval b starts at coef + b * ldc.
+void cheb_coeffs_host_many(int N, int K, const double *da, const double *db, int method,
+                           double *coef, int ldc) {
   std::vector<double> x(N + 1), w(N + 1);
   const double PI = kPi;
   for (int i = 0; i <= N; ++i) {
@@ -298,20 +304,32 @@ void cheb_coeffs_host(int N, double da, double db, int method, double *coef) {
     w[0] = PI / (2. * (double)N + 1.);
   }
   const double RN = (double)N;
-  for (int k = 0; k <= N; ++k) {
-    double acc = 0.0;
+  std::vector<double> wc((size_t)(N + 1) * (N + 1));  // w_j cos(tmpt(k, j))
+  for (int k = 0; k <= N; ++k)
     for (int j = 0; j <= N; ++j) {
       double tmpt;
       if (method == GGEM_CHEB_GAUSS_LOBATTO) tmpt = PI * (double)((size_t)k * (size_t)j) / RN;
       else if (method == GGEM_CHEB_GAUSS_RADAU)
         tmpt = 2. * PI * (double)((size_t)k * (size_t)j) / (2. * RN + 1.);
       else tmpt = PI * (double)(2. * j + 1.) * (double)k / (2. * RN + 2.);
-      const double fj = 1.0 / std::sqrt((x[j] - db) / da);
-      acc += w[j] * std::cos(tmpt) * fj;
+      wc[(size_t)k * (N + 1) + j] = w[j] * std::cos(tmpt);
     }
-    const double ck = (k == 0) ? 2.0 : 1.0;
-    coef[k] = acc * (2. / (PI * ck));
+  std::vector<double> fj(N + 1);
+  for (int b = 0; b < K; ++b) {
+    for (int j = 0; j <= N; ++j) fj[j] = 1.0 / std::sqrt((x[j] - db[b]) / da[b]);
+    double *cb = coef + (size_t)b * ldc;
+    for (int k = 0; k <= N; ++k) {
+      const double *row = wc.data() + (size_t)k * (N + 1);
+      double acc = 0.0;
+      for (int j = 0; j <= N; ++j) acc += row[j] * fj[j];
+      const double ck = (k == 0) ? 2.0 : 1.0;
+      cb[k] = acc * (2. / (PI * ck));
+    }
   }
+}
+
+void cheb_coeffs_host(int N, double da, double db, int method, double *coef) {
+  cheb_coeffs_host_many(N, 1, &da, &db, method, coef, N + 1);
 }
 
 }  // namespace ggem

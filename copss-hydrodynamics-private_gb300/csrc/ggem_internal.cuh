@@ -238,6 +238,8 @@ int fit_tensor_poly(const ggem_constants &c, double s_max, float *a, float *b, f
 bool tensor_b_nonnegative(const ggem_constants &c, double s_max);
 void tridiag_extremes(int k, const double *a, const double *b, double *lmin, double *lmax);
 void cheb_coeffs_host(int N, double da, double db, int method, double *coef);
+void cheb_coeffs_host_many(int N, int K, const double *da, const double *db, int method,
+                           double *coef, int ldc);
 
 // cell build and pair list (ggem_cells.cu)
 // defer_flags: leave the device error word unread (build_pair_list reads it)
