@@ -113,14 +113,17 @@ __device__ __forceinline__ double f2d(float x) {
 // slot, lane r its r-th right-hand side.  TERM = false: u = M f (+ self term
 // from the FP64 f).  TERM = true: one Chebyshev term of every series,
 // xm = (2db x1 + 2da M x1) - x0, dw += c xm (c of the series' suspension,
-// zero once the series has stopped), and the FP32 forces of xm.
+// zero once the series has stopped), and the FP32 forces of xm.  With
+// c1 = 2db + 2da self_c (per suspension) the term is
+// xm = 2da (pair sum) + (c1 x1 - x0): four FP64 operations per element
+// (GB300 runs FP64 at 1/64 of the FP32 rate).
 template <bool TERM>
 __global__ void k_ens_pair(int64_t ntot, const int32_t *__restrict__ cnt, int W,
                            const uint32_t *__restrict__ list, const float4 *__restrict__ ten,
                            const float4 *__restrict__ f4, double self_c,
                            const double *__restrict__ f, double *__restrict__ u,
                            const int32_t *__restrict__ susp, const double *__restrict__ two_da,
-                           const double *__restrict__ two_db, const double *__restrict__ coef,
+                           const double *__restrict__ c1x, const double *__restrict__ coef,
                            int ldc, int term, const uint8_t *__restrict__ active,
                            const double *__restrict__ x0, double *__restrict__ dw,
                            float4 *__restrict__ next) {
@@ -159,16 +162,14 @@ __global__ void k_ens_pair(int64_t ntot, const int32_t *__restrict__ cnt, int W,
   } else {
     const int b = susp[s];
     const double cf = active[b * kR + r] ? coef[(int64_t)b * ldc + term] : 0.0;
-    const double tda = two_da[b], tdb = two_db[b];
+    const double tda = two_da[b], c1 = c1x[b];
     float out[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       const double xk = f[k0 + c];  // f is x1 here
-      const double mv = fma(self_c, xk, f2d(hs[c]) + f2d(ls[c]));
-      double v = tdb * xk + tda * mv;
-      v -= x0[k0 + c];
+      const double v = fma(tda, f2d(hs[c]) + f2d(ls[c]), fma(c1, xk, -x0[k0 + c]));
       u[k0 + c] = v;  // u is xm here
-      dw[k0 + c] = dw[k0 + c] + cf * v;
+      dw[k0 + c] = fma(cf, v, dw[k0 + c]);
       out[c] = d2f_bits(v);
     }
     next[s * kR + r] = make_float4(out[0], out[1], out[2], 0.f);
@@ -242,7 +243,7 @@ struct ggem_ensemble {
   // Chebyshev state: vectors [slot][8][3] and FP32 forces [slot][8]
   DevBuf<double> v[6];
   DevBuf<float4> f4[3];
-  DevBuf<double> coef, da, db, two_da, two_db, red;
+  DevBuf<double> coef, da, db, two_da, c1x, red;  // c1x: 2db + 2da self_c
   DevBuf<uint8_t> active;
   double *h_red = nullptr;
   int pred_terms = 0;
@@ -328,7 +329,7 @@ extern "C" int ggem_ensemble_create(const ggem_params *base, int k, const double
       (c = cudaMallocHost((void **)&e->h_red, sizeof(double) * 4 * kR * (size_t)k)) ||
       (c = e->d_off.ensure(k + 1)) || (c = e->views.ensure(k)) || (c = e->red.ensure(4 * kR * (size_t)k)) ||
       (c = e->active.ensure(kR * (size_t)k)) || (c = e->da.ensure(k)) || (c = e->db.ensure(k)) ||
-      (c = e->two_da.ensure(k)) || (c = e->two_db.ensure(k))) {
+      (c = e->two_da.ensure(k)) || (c = e->c1x.ensure(k))) {
     cudaGetLastError();
     ggem_ensemble_destroy(e);
     return c == cudaErrorMemoryAllocation ? GGEM_ERR_OOM : GGEM_ERR_CUDA;
@@ -461,7 +462,7 @@ int ens_term(ggem_ensemble *e, int term, int ldc, const double *x0, const double
              double *dw, const float4 *fcur, float4 *fnext) {
   k_ens_pair<true><<<eblocks(e->ntot * kR, e->block), e->block, 0, e->stream>>>(
       e->ntot, e->cnt.p, e->W, e->list.p, e->ten.p, fcur, e->self_c, x1, xm, e->susp.p,
-      e->two_da.p, e->two_db.p, e->coef.p, ldc, term, e->active.p, x0, dw, fnext);
+      e->two_da.p, e->c1x.p, e->coef.p, ldc, term, e->active.p, x0, dw, fnext);
   return elaunch(e, "ensemble chebyshev term");
 }
 
@@ -492,7 +493,7 @@ extern "C" int ggem_ensemble_brownian_dev(ggem_ensemble *e, int nrhs, int N,
     da[b] = 2.0 / d;
     db[b] = -(eig_max[b] + eig_min[b]) / d;
     tda[b] = 2.0 * da[b];
-    tdb[b] = 2.0 * db[b];
+    tdb[b] = 2.0 * db[b] + tda[b] * e->self_c;  // c1 of the fused term
   }
   cheb_coeffs_host_many(N, K, da.data(), db.data(), GGEM_CHEB_GAUSS, coef.data(), ldc);
   std::vector<uint8_t> act((size_t)K * kR, 0);
@@ -510,7 +511,7 @@ extern "C" int ggem_ensemble_brownian_dev(ggem_ensemble *e, int nrhs, int N,
                            e->stream)) ||
       (c = cudaMemcpyAsync(e->two_da.p, tda.data(), sizeof(double) * K, cudaMemcpyHostToDevice,
                            e->stream)) ||
-      (c = cudaMemcpyAsync(e->two_db.p, tdb.data(), sizeof(double) * K, cudaMemcpyHostToDevice,
+      (c = cudaMemcpyAsync(e->c1x.p, tdb.data(), sizeof(double) * K, cudaMemcpyHostToDevice,
                            e->stream)) ||
       (c = cudaMemcpyAsync(e->active.p, act.data(), K * kR, cudaMemcpyHostToDevice, e->stream)))
     return ecuda(e, c, "chebyshev tables");
@@ -699,7 +700,7 @@ extern "C" int ggem_ensemble_autotune(ggem_ensemble *e, int nrhs, int *block_thr
                            cudaMemcpyHostToDevice, e->stream)) ||
       (c = cudaMemcpyAsync(e->two_da.p, one.data(), sizeof(double) * e->K, cudaMemcpyHostToDevice,
                            e->stream)) ||
-      (c = cudaMemcpyAsync(e->two_db.p, one.data(), sizeof(double) * e->K, cudaMemcpyHostToDevice,
+      (c = cudaMemcpyAsync(e->c1x.p, one.data(), sizeof(double) * e->K, cudaMemcpyHostToDevice,
                            e->stream)) ||
       (c = cudaMemcpyAsync(e->active.p, act.data(), act.size(), cudaMemcpyHostToDevice,
                            e->stream)) ||
