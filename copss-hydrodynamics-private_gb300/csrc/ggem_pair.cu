@@ -997,10 +997,11 @@ __global__ void __launch_bounds__(32 * kBatchWarps, 3) k_pair_b64(
     const int64_t idx = ((int64_t)r * n + s0) * 3 + q;
     double m = f2d_bits(v.x) + f2d_bits(v.y);
     if (CHEB) {
-      double x = two_db * x1[idx] + two_da * m;
-      x -= x0[idx];
-      const double y = dw[idx];
-      dw[idx] = y + cf.c[r] * x;
+      // x_{k+1} = 2da M x_k + (2db x_k - x_{k-1}), dw += c x_{k+1}: four
+      // FP64 operations per element with the add above (FP64 issues at a
+      // small fraction of the FP32 rate on this GPU)
+      const double x = fma(two_da, m, fma(two_db, x1[idx], -x0[idx]));
+      dw[idx] = fma(cf.c[r], x, dw[idx]);
       m = x;
       // FP32 staging of x_{k+1}, transposed through shared memory below
       reinterpret_cast<float *>(&s_out[t][r][c])[0] = d2f_bits(x);
