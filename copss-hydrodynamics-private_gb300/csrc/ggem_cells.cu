@@ -152,6 +152,60 @@ int scan_impl(ggem_ctx *c, const T *in, T *out, int64_t n, int level) {
   return check_launch(c, "scan total");
 }
 
+// the cell list's exclusive scan in one block when the grid is small
+// enough: tiles of 1024 counts, all loaded (coalesced) before the first
+// tile is scanned, then one block-wide scan per tile with a running carry;
+// start[0..ncell].  The counts are zeroed as they are read, ready for the
+// next build's k_assign.
+constexpr int kScanTiles = 32;
+constexpr int64_t kScanCellsMax = 1024 * kScanTiles;
+
+__global__ void __launch_bounds__(1024) k_scan_cells(int32_t *__restrict__ count,
+                                                     int32_t *__restrict__ start, int64_t n) {
+  __shared__ int32_t warp_tot[2][32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int tiles = (int)((n + 1023) / 1024);
+  int32_t v[kScanTiles];
+#pragma unroll
+  for (int k = 0; k < kScanTiles; ++k) {
+    const int64_t i = (int64_t)k * 1024 + threadIdx.x;
+    v[k] = (k < tiles && i < n) ? count[i] : 0;
+  }
+#pragma unroll
+  for (int k = 0; k < kScanTiles; ++k) {
+    const int64_t i = (int64_t)k * 1024 + threadIdx.x;
+    if (k < tiles && i < n) count[i] = 0;
+  }
+  int32_t carry = 0;
+#pragma unroll
+  for (int k = 0; k < kScanTiles; ++k) {
+    if (k < tiles) {
+      int32_t x = v[k];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+      }
+      int32_t *wt = warp_tot[k & 1];  // alternate buffers: one barrier per tile
+      if (lane == 31) wt[warp] = x;
+      __syncthreads();
+      int32_t w = wt[lane];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int32_t y = __shfl_up_sync(0xffffffffu, w, o);
+        if (lane >= o) w += y;
+      }
+      // every warp scans the 32 warp totals itself (no second barrier)
+      const int32_t before = __shfl_sync(0xffffffffu, w, (warp + 31) & 31);
+      const int32_t total = __shfl_sync(0xffffffffu, w, 31);
+      const int64_t i = (int64_t)k * 1024 + threadIdx.x;
+      if (i < n) start[i] = carry + (warp ? before : 0) + x - v[k];
+      carry += total;
+    }
+  }
+  if (threadIdx.x == 0) start[n] = carry;
+}
+
 __global__ void k_scatter(int64_t n, const int32_t *__restrict__ cell_of,
                           const int32_t *__restrict__ start, int32_t *__restrict__ fill,
                           int32_t *__restrict__ order) {
@@ -165,11 +219,13 @@ __global__ void k_scatter(int64_t n, const int32_t *__restrict__ cell_of,
 // ascending particle id inside each cell (deterministic slot order, and the
 // order of build_elem_point_containing_list, point_mesh.C:585-631): cells of
 // up to 16 particles are sorted in registers by an odd-even transposition
-// network, larger ones by insertion in place
+// network, larger ones by insertion in place.  The cell's fill counter is
+// zeroed for the next build.
 __global__ void k_sort_cells(int64_t ncell, const int32_t *__restrict__ start,
-                             int32_t *__restrict__ order) {
+                             int32_t *__restrict__ order, int32_t *__restrict__ fill) {
   const int64_t cidx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (cidx >= ncell) return;
+  fill[cidx] = 0;  // scattered; ready for the next build
   const int32_t b = start[cidx], e = start[cidx + 1];
   const int32_t m = e - b;
   if (m <= 1) return;
@@ -400,8 +456,15 @@ int build_cells(ggem_ctx *c, bool defer_flags) {
       (e = c->pos64.ensure(n)) || (e = c->pos32.ensure(n)))
     return cuda_fail(c, e, "cell buffers");
   cudaStream_t st = c->stream;
-  if ((e = cudaMemsetAsync(c->cell_count.p, 0, sizeof(int32_t) * g.ncell, st)) ||
-      (e = cudaMemsetAsync(c->cell_fill.p, 0, sizeof(int32_t) * g.ncell, st)) ||
+  // the cell counters are left at zero by the previous build (the
+  // single-block scan zeroes the counts, k_sort_gather the fills); they are
+  // cleared here only after a reallocation, an interrupted build or on
+  // grids too large for the single-block scan
+  const bool small = g.ncell <= kScanCellsMax;
+  const bool clean = small && c->cell_counters_zero && c->cell_count.p == c->cell_counters_at;
+  c->cell_counters_zero = false;
+  if ((!clean && ((e = cudaMemsetAsync(c->cell_count.p, 0, sizeof(int32_t) * g.ncell, st)) ||
+                  (e = cudaMemsetAsync(c->cell_fill.p, 0, sizeof(int32_t) * g.ncell, st)))) ||
       (e = cudaMemsetAsync(c->err.p, 0, sizeof(int), st)))
     return cuda_fail(c, e, "cell memset");
   const int T = 256;
@@ -411,17 +474,27 @@ int build_cells(ggem_ctx *c, bool defer_flags) {
                                c->err.p);
     if (int rc = check_launch(c, "assign")) return rc;
   }
-  if (int rc = device_exclusive_scan_i32(c, c->cell_count.p, c->cell_start.p, g.ncell)) return rc;
+  if (small) {
+    k_scan_cells<<<1, 1024, 0, st>>>(c->cell_count.p, c->cell_start.p, g.ncell);
+    if (int rc = check_launch(c, "scan cells")) return rc;
+  } else if (int rc = device_exclusive_scan_i32(c, c->cell_count.p, c->cell_start.p, g.ncell)) {
+    return rc;
+  }
   if (n > 0) {
     k_scatter<<<bn, T, 0, st>>>(n, c->cell_of.p, c->cell_start.p, c->cell_fill.p, c->order.p);
     if (int rc = check_launch(c, "scatter")) return rc;
-    k_sort_cells<<<(unsigned)((g.ncell + T - 1) / T), T, 0, st>>>(g.ncell, c->cell_start.p,
-                                                                   c->order.p);
-    if (int rc = check_launch(c, "sort cells")) return rc;
+  }
+  // (for n = 0 only the fill counters are cleared)
+  k_sort_cells<<<(unsigned)((g.ncell + T - 1) / T), T, 0, st>>>(g.ncell, c->cell_start.p,
+                                                                 c->order.p, c->cell_fill.p);
+  if (int rc = check_launch(c, "sort cells")) return rc;
+  if (n > 0) {
     k_gather_sorted<<<bn, T, 0, st>>>(n, g, c->order.p, c->cell_of.p, c->wrapped.p, c->rank.p,
                                       c->pos64.p, c->pos32.p);
     if (int rc = check_launch(c, "gather sorted")) return rc;
   }
+  c->cell_counters_zero = small;
+  c->cell_counters_at = c->cell_count.p;
   c->cells_built = false;
   c->list_built = false;
   c->pretensor_ok = false;

@@ -112,6 +112,10 @@ struct ggem_ctx {
   bool cells_built = false;
   ggem::DevBuf<double> xyz_in;
   ggem::DevBuf<int32_t> cell_of, cell_count, cell_start, cell_fill, order, rank;
+  // the cell counters were left at zero by the last build (and still live
+  // at cell_counters_at)
+  bool cell_counters_zero = false;
+  const int32_t *cell_counters_at = nullptr;
   ggem::DevBuf<double4_32a> wrapped, pos64;
   ggem::DevBuf<float4> pos32;
   ggem::DevBuf<int> err;

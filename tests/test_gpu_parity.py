@@ -90,6 +90,32 @@ def test_cutoff_neighbor_lists_bit_exact(prec, cell_div):
         assert ctx.pair_count() == want.offsets[-1]
 
 
+@pytest.mark.parametrize("n", [1500, 5000])
+def test_crowded_cells_lists_bit_exact_over_rebuilds(n):
+    """Cells of ~55 particles (ranked in registers, two chunks) and of ~185
+    (the in-place path): the cell order, the neighbour lists and the matvec
+    are the oracle's, and stay so over rebuilds that reuse the zeroed cell
+    counters, across a particle-count change and back."""
+    rng = np.random.default_rng(n)
+    L = 21.0  # three cells of side 7 per axis
+    xyz = rng.uniform(0, L, (n, 3))
+    other = rng.uniform(0, L, (n // 3, 3))
+    box = O.make_box([0] * 3, [L] * 3, [1, 1, 1])
+    want = O.neighbors_cutoff(box, xyz, 7.0)
+    cells = np.minimum(np.floor(xyz / 7.0).astype(int), 2)
+    cell_want = cells[:, 0] + 3 * (cells[:, 1] + 3 * cells[:, 2])
+    for prec in (G.FP64, G.FP32):
+        with G.Context(box_hi=(L,) * 3, rc=7.0, precision=prec) as ctx:
+            for cfg in (xyz, xyz, other, xyz):
+                ctx.set_particles(cfg)
+                ctx.build_cells()
+                if cfg is other:
+                    continue
+                assert np.array_equal(ctx.cell_of_particles(), cell_want)
+                off, ids = ctx.neighbors()
+                assert np.array_equal(off, want.offsets) and np.array_equal(ids, want.ids)
+
+
 def test_cutoff_lists_with_boundary_pairs_bit_exact():
     """Pairs placed at |r| = rc within rounding: the FP32 filter must defer
     to the exact FP64 predicate."""
