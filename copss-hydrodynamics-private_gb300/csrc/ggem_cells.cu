@@ -156,13 +156,16 @@ int scan_impl(ggem_ctx *c, const T *in, T *out, int64_t n, int level) {
 // enough: tiles of 1024 counts, all loaded (coalesced) before the first
 // tile is scanned, then one block-wide scan per tile with a running carry;
 // start[0..ncell].  The counts are zeroed as they are read, ready for the
-// next build's k_assign.
+// next build's k_assign, and so are the pair-list statistics (stat, when
+// given) that the list build of the same configuration accumulates.
 constexpr int kScanTiles = 32;
 constexpr int64_t kScanCellsMax = 1024 * kScanTiles;
 
 __global__ void __launch_bounds__(1024) k_scan_cells(int32_t *__restrict__ count,
-                                                     int32_t *__restrict__ start, int64_t n) {
+                                                     int32_t *__restrict__ start, int64_t n,
+                                                     unsigned long long *__restrict__ stat) {
   __shared__ int32_t warp_tot[2][32];
+  if (stat && threadIdx.x < 2) stat[threadIdx.x] = 0ull;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int tiles = (int)((n + 1023) / 1024);
   int32_t v[kScanTiles];
@@ -314,8 +317,8 @@ __device__ __forceinline__ bool exact_within(const Grid &g, double4_32a a, doubl
 // Warp-per-cell pair list, one pass into fixed-width rows.  The candidates
 // of a target cell are the concatenation of its stencil cells (stencil
 // order, slot order inside a cell); lanes take 32 consecutive candidates
-// with coalesced loads, the cell's targets are broadcast one at a time by
-// shuffle, and a ballot prefix places each accepted candidate.  Entries
+// with coalesced loads, the cell's targets are broadcast one at a time from
+// shared memory, and a ballot prefix places each accepted candidate.  Entries
 // therefore come out in exactly the per-target order of a sequential sweep.
 // Row s holds entries [s*W, s*W + cnt[s]); a row longer than W is counted
 // but not stored: the kernel records the longest row and sets
@@ -332,6 +335,7 @@ __global__ void __launch_bounds__(32 * kListWarps) k_pair_list_warp(
   __shared__ int32_t s_base[kListWarps][kMaxStencil];
   __shared__ int32_t s_pre[kListWarps][kMaxStencil + 1];
   __shared__ int32_t s_code[kListWarps][kMaxStencil];
+  __shared__ float4 s_pi[kListWarps][32];  // the targets of the current chunk
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t C = blockIdx.x * (int64_t)kListWarps + w;
   if (C >= g.ncell) return;  // whole warp
@@ -376,7 +380,9 @@ __global__ void __launch_bounds__(32 * kListWarps) k_pair_list_warp(
     const int ntc = min(32, te - t0);
     const int32_t own = t0 + lane;
     const bool own_ok = lane < ntc;
-    const float4 po = own_ok ? pos32[own] : make_float4(0.f, 0.f, 0.f, 0.f);
+    __syncwarp();  // the previous chunk's targets are no longer read
+    s_pi[w][lane] = own_ok ? pos32[own] : make_float4(0.f, 0.f, 0.f, 0.f);
+    __syncwarp();
     int32_t own_cnt = 0;
     for (int32_t v0 = 0; v0 < V; v0 += 32) {
       const int32_t v = v0 + lane;
@@ -392,14 +398,15 @@ __global__ void __launch_bounds__(32 * kListWarps) k_pair_list_warp(
       const int code = s_code[w][lo];
       const float4 sh = shift[code];
       const float4 pj = valid ? pos32[t] : make_float4(0.f, 0.f, 0.f, 0.f);
+      // the candidate in the target cell's frame (the shift added once per
+      // candidate; the filter's band absorbs the different rounding)
+      const float qx = pj.x + sh.x, qy = pj.y + sh.y, qz = pj.z + sh.z;
       for (int i = 0; i < ntc; ++i) {
-        const float pix = __shfl_sync(0xffffffffu, po.x, i);
-        const float piy = __shfl_sync(0xffffffffu, po.y, i);
-        const float piz = __shfl_sync(0xffffffffu, po.z, i);
+        const float4 pi = s_pi[w][i];  // one broadcast read
         const int32_t ti = t0 + i;
-        const float dx = (pj.x - pix) + sh.x;
-        const float dy = (pj.y - piy) + sh.y;
-        const float dz = (pj.z - piz) + sh.z;
+        const float dx = qx - pi.x;
+        const float dy = qy - pi.y;
+        const float dz = qz - pi.z;
         const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
         // accepted below rc2_lo, rejected above rc2_hi; in between (FP32
         // rounding of |r| = rc) the exact FP64 test decides, behind a
@@ -474,9 +481,11 @@ int build_cells(ggem_ctx *c, bool defer_flags) {
                                c->err.p);
     if (int rc = check_launch(c, "assign")) return rc;
   }
+  c->list_stat_zero = false;
   if (small) {
-    k_scan_cells<<<1, 1024, 0, st>>>(c->cell_count.p, c->cell_start.p, g.ncell);
+    k_scan_cells<<<1, 1024, 0, st>>>(c->cell_count.p, c->cell_start.p, g.ncell, c->nb_stat.p);
     if (int rc = check_launch(c, "scan cells")) return rc;
+    c->list_stat_zero = c->nb_stat.p != nullptr;
   } else if (int rc = device_exclusive_scan_i32(c, c->cell_count.p, c->cell_start.p, g.ncell)) {
     return rc;
   }
@@ -548,8 +557,11 @@ int build_pair_list(ggem_ctx *c) {
     // keep the width of the previous build; a longer row is stored clipped
     // (counts never exceed W) and found when the statistics are read
     if ((e = c->nb_list.ensure((size_t)n * c->nb_w))) return cuda_fail(c, e, "pair list");
-    if ((e = cudaMemsetAsync(c->nb_stat.p, 0, 2 * sizeof(unsigned long long), st)))
+    // (the statistics were zeroed by this configuration's cell scan)
+    if (!c->list_stat_zero &&
+        (e = cudaMemsetAsync(c->nb_stat.p, 0, 2 * sizeof(unsigned long long), st)))
       return cuda_fail(c, e, "memset");
+    c->list_stat_zero = false;
     kt_start(c, kKListBuild);
     k_pair_list_warp<<<cb, 32 * kListWarps, 0, st>>>(
         c->grid, c->d_stencil.p, nst, c->d_shift.p, c->cell_start.p, c->pos32.p, c->pos64.p,
@@ -566,6 +578,7 @@ int build_pair_list(ggem_ctx *c) {
   // the list statistics in one host synchronisation.  A row longer than the
   // current width makes the host widen the rows and fill once more.
   unsigned long long *h = reinterpret_cast<unsigned long long *>(c->h_red);
+  c->list_stat_zero = false;
   for (int attempt = 0; attempt < 2; ++attempt) {
     const int W = c->nb_w;
     if ((e = c->nb_list.ensure((size_t)n * W))) return cuda_fail(c, e, "pair list");

@@ -128,6 +128,7 @@ struct ggem_ctx {
   bool defer_checks = false;
   bool list_checked_once = false;
   bool list_unchecked = false;
+  bool list_stat_zero = false;  // the cell scan of this configuration zeroed nb_stat
   int64_t n_pairs = 0;
   ggem::DevBuf<int32_t> nb_cnt;       // entries per target row
   ggem::DevBuf<unsigned long long> nb_stat;  // [0] total entries, [1] longest row
