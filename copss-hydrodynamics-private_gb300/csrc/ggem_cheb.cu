@@ -71,9 +71,19 @@ __global__ void __launch_bounds__(kVecThreads) k_finalize(int G, const double *_
                                                           const int *__restrict__ err) {
   __shared__ double sh[32];
   const int q = blockIdx.x;
-  double acc = 0.0;
-  for (int b = threadIdx.x; b < G; b += blockDim.x) acc += partial[(int64_t)q * G + b];
-  const double t = block_sum(acc, sh);
+  // four running sums per thread keep four loads in flight (fixed order)
+  const double *p = partial + (int64_t)q * G;
+  const int T = blockDim.x;
+  double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+  int b = threadIdx.x;
+  for (; b + 3 * T < G; b += 4 * T) {
+    a0 += p[b];
+    a1 += p[b + T];
+    a2 += p[b + 2 * T];
+    a3 += p[b + 3 * T];
+  }
+  for (; b < G; b += T) a0 += p[b];
+  const double t = block_sum((a0 + a1) + (a2 + a3), sh);
   if (threadIdx.x == 0) out[q] = t;
   if (stat && q == 0 && threadIdx.x == 0) {
     out[nq] = __longlong_as_double((long long)stat[0]);
@@ -151,29 +161,6 @@ __global__ void __launch_bounds__(kVecThreads) k_cheb_term(int64_t D, double two
       partial[(int64_t)(0 * nrhs + r) * gridDim.x + blockIdx.x] = s4;
       partial[(int64_t)(1 * nrhs + r) * gridDim.x + blockIdx.x] = s3;
     }
-  }
-}
-
-// the norms of a fused term (k_cheb_term's q0, q1 for one right-hand side):
-// |dw - coef xm|^2 (the dw before the term) and |xm|^2
-__global__ void __launch_bounds__(kVecThreads) k_term_norms(int64_t D, double coef,
-                                                            const double *__restrict__ xm,
-                                                            const double *__restrict__ dw,
-                                                            double *__restrict__ partial) {
-  __shared__ double sh[32];
-  double a4 = 0.0, a3 = 0.0;
-  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < D;
-       k += (int64_t)gridDim.x * blockDim.x) {
-    const double v = xm[k];
-    const double y = dw[k] - coef * v;
-    a4 += y * y;
-    a3 += v * v;
-  }
-  const double s4 = block_sum(a4, sh);
-  const double s3 = block_sum(a3, sh);
-  if (threadIdx.x == 0) {
-    partial[blockIdx.x] = s4;
-    partial[gridDim.x + blockIdx.x] = s3;
   }
 }
 
@@ -385,8 +372,15 @@ int cheb_slots(ggem_ctx *c, int nrhs, int N, double eig_min, double eig_max, dou
   // 16 .. 64 right-hand sides: an unchecked term is one batched kernel
   const bool batch_fused = !faithful && c->n > 0 && batch_term_fusable(c, nrhs);
   bool staged_fresh = false;
-  const int G = vec_blocks(D);
+  // partial sums per reduction: vector-kernel blocks, or in a fused series
+  // the pair kernels' blocks (the first step, the checked terms and the
+  // check matvec leave their estimator sums themselves)
+  const int G = fused ? (int)pair_partials(c) : vec_blocks(D);
   cudaStream_t st = c->stream;
+  if (fused) {
+    cudaError_t e = c->w_red.ensure((size_t)4 * G + 64);
+    if (e) return cuda_fail(c, e, "reduction partials");
+  }
   double *x0 = c->w_c.p, *x1 = c->w_d.p, *xm = c->w_e.p, *dw = c->w_y.p, *dm = c->w_out.p;
   // reduction regions: term norms [2 nrhs][G], |dm|^2 [nrhs][G], xi.M.xi
   // [nrhs][G], then the 4 nrhs finalized values
@@ -410,9 +404,8 @@ int cheb_slots(ggem_ctx *c, int nrhs, int N, double eig_min, double eig_max, dou
   bool records_fresh = false;
   if (fused) {
     // dm holds m = M x0 until the first check
-    if (int rc = cheb_start_fused(c, xi, x0, dm, x1, dw, da, db, X[0], X[1], sm)) return rc;
-    k_dot_partials<<<dim3(G, 1), kVecThreads, 0, st>>>(D, dm, x0, p_aux2);
-    if (int rc = check_launch(c, "aux2")) return rc;
+    if (int rc = cheb_start_fused(c, xi, x0, dm, x1, dw, da, db, X[0], X[1], sm, p_aux2))
+      return rc;
     records_fresh = true;
   } else {
     if (int rc = permute_to_slots(c, nrhs, xi, x0)) return rc;
@@ -428,9 +421,13 @@ int cheb_slots(ggem_ctx *c, int nrhs, int N, double eig_min, double eig_max, dou
 
   // evaluate err1 / err2 of the current dw for the active right-hand sides
   auto check_now = [&](double coef_abs, bool apply_rules) -> int {
-    if (int rc = matvec_slots(c, nrhs, dw, dm, sm)) return rc;
-    k_dot_partials<<<dim3(G, nrhs), kVecThreads, 0, st>>>(D, dm, dm, p_dm);
-    if (int rc = check_launch(c, "dm norm")) return rc;
+    if (fused) {  // dw's records come from the checked term
+      if (int rc = matvec_dw_records(c, dw, dm, sm, p_dm)) return rc;
+    } else {
+      if (int rc = matvec_slots(c, nrhs, dw, dm, sm)) return rc;
+      k_dot_partials<<<dim3(G, nrhs), kVecThreads, 0, st>>>(D, dm, dm, p_dm);
+      if (int rc = check_launch(c, "dm norm")) return rc;
+    }
     // a deferred list build is checked in the same readback; the caller's
     // M y is queued behind it in case this check ends the series
     const bool pending = c->list_unchecked;
@@ -483,13 +480,11 @@ int cheb_slots(ggem_ctx *c, int nrhs, int N, double eig_min, double eig_max, dou
     else if (check_every > 1) check = (i % check_every == 0) || (i == N - 1);
     else check = (i + 1 >= k_first) || (i == N - 1);
     if (can_fuse && (!check || fused)) {
-      if (int rc = pair_cheb_term(c, records_fresh, x0, x1, xm, dw, two_da, two_db, X[i + 1], sm))
+      // a checked fused term leaves its two norms and the records of dw
+      if (int rc = pair_cheb_term(c, records_fresh, x0, x1, xm, dw, two_da, two_db, X[i + 1], sm,
+                                  check ? p_term : nullptr))
         return rc;
       records_fresh = true;
-      if (check) {
-        k_term_norms<<<G, kVecThreads, 0, st>>>(D, X[i + 1], xm, dw, p_term);
-        if (int rc = check_launch(c, "term norms")) return rc;
-      }
     } else if (batch_fused && !check) {
       double cf[kMaxRhs];
       for (int r = 0; r < nrhs; ++r) cf[r] = active[r] ? X[i + 1] : 0.0;

@@ -273,21 +273,27 @@ double self_coefficient(const ggem_ctx *c, int self_mode);
 int build_pair_tensors(ggem_ctx *c);
 int pair_cheb_term(ggem_ctx *c, bool records_fresh, const double *x0, const double *x1,
                    double *xm, double *dw, double two_da, double two_db, double coef,
-                   int self_mode);
+                   int self_mode, double *norms = nullptr);
 // an unchecked Chebyshev term for this many right-hand sides can run as one
 // batched kernel (batch_cheb_term)
 bool batch_term_fusable(const ggem_ctx *c, int nrhs);
 int batch_cheb_term(ggem_ctx *c, int nrhs, bool staged_fresh, const double *x0, const double *x1,
                     double *xm, double *dw, double two_da, double two_db, const double *coef,
                     int self_mode);
-// blocks of the single-RHS pair kernels
+// blocks of the single-RHS pair kernels, and the partial sums a fused
+// series' estimator sums leave (one per block)
 int pair_grid_blocks(const ggem_ctx *c);
+int64_t pair_partials(const ggem_ctx *c);
+// u = M dw from the dw records a checked fused term left (norms given to
+// pair_cheb_term); |u|^2 as per-block partials into norm
+int matvec_dw_records(ggem_ctx *c, const double *dw, double *u, int self_mode, double *norm);
 // u = M f, one right-hand side, caller order in and out (FP32 list with
 // per-matvec tensors only); f_slot receives f in slot order
 int matvec_orig_fused(ggem_ctx *c, const double *f, double *u, double *f_slot, int self_mode);
 // the fused first step of a series (xi in caller order; m = M x0 is kept)
 int cheb_start_fused(ggem_ctx *c, const double *xi, double *x0, double *m, double *x1,
-                     double *dw, double da, double db, double c0, double c1, int self_mode);
+                     double *dw, double da, double db, double c0, double c1, int self_mode,
+                     double *aux2 = nullptr);
 int permute_to_slots(ggem_ctx *c, int nrhs, const double *d_orig, double *d_slot);
 int permute_from_slots(ggem_ctx *c, int nrhs, const double *d_slot, double *d_orig);
 

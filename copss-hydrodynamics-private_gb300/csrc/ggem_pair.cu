@@ -393,6 +393,68 @@ __device__ __forceinline__ PairSum pair_sum_r1(int64_t s, bool act, int sub, con
   return PairSum{sx, -cx, sy, -cy, sz, -cz};
 }
 
+// The fused series' estimator sums (x0 . M x0, |dw|^2, |x_{k+1}|^2, |M dw|^2)
+// without FP64 arithmetic, which issues at a small fraction of the FP32
+// rate: each double is split with integer operations into a truncated
+// float and the float of its remaining 29 mantissa bits (about 47 bits in
+// all), products are formed as float-float values with fused multiply-adds,
+// and the sums run as float-float values (TwoSum): a warp butterfly, then
+// the block's eight warps in order, one partial per block (256 threads).
+__device__ __forceinline__ void split_f64(double v, float &hi, float &lo) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  const uint32_t sign = (uint32_t)(b >> 32) & 0x80000000u;
+  const int e = (int)((b >> 52) & 0x7ffu) - 1023;
+  if (e < -126 || e > 127) {  // zero, tiny, huge or not finite: one float
+    hi = d2f_bits(v);
+    lo = 0.f;
+    return;
+  }
+  hi = __uint_as_float(sign | ((uint32_t)(e + 127) << 23) | (uint32_t)((b >> 29) & 0x7fffffu));
+  // the rest: (low 29 mantissa bits) x 2^(e - 52), zero below the float range
+  const float scale = e - 52 >= -126 ? __uint_as_float((uint32_t)(e - 52 + 127) << 23) : 0.f;
+  const float r = (float)(uint32_t)(b & 0x1fffffffu) * scale;
+  lo = sign ? -r : r;
+}
+
+// (ah + al)(bh + bl) as a float-float value (the al bl term is below it)
+__device__ __forceinline__ void ff_prod(float ah, float al, float bh, float bl, float &ph,
+                                        float &pl) {
+  ph = ah * bh;
+  pl = fmaf(ah, bl, fmaf(al, bh, fmaf(ah, bh, -ph)));
+}
+
+__device__ __forceinline__ void block_partial_ff(float hi, float lo, double *__restrict__ part) {
+  __shared__ float2 sh[8];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float h2 = __shfl_xor_sync(0xffffffffu, hi, o);
+    const float l2 = __shfl_xor_sync(0xffffffffu, lo, o);
+    ff_add(hi, lo, h2, l2);  // the same value in both lanes (TwoSum is exact)
+  }
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = make_float2(hi, lo);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float th = sh[0].x, tl = sh[0].y;
+#pragma unroll
+    for (int w = 1; w < 8; ++w) ff_add(th, tl, sh[w].x, sh[w].y);
+    part[blockIdx.x] = f2d_bits(th) + f2d_bits(tl);
+  }
+}
+
+// a . b for doubles, as a float-float value
+__device__ __forceinline__ void dot_ff(double a, double b, float &ph, float &pl) {
+  float ah, al, bh, bl;
+  split_f64(a, ah, al);
+  split_f64(b, bh, bl);
+  ff_prod(ah, al, bh, bl, ph, pl);
+}
+
+__device__ __forceinline__ void sq_ff(double a, float &ph, float &pl) {
+  float ah, al;
+  split_f64(a, ah, al);
+  ff_prod(ah, al, ah, al, ph, pl);
+}
+
 // the per-matvec-tensor kernel shapes the autotuner chooses from: blocks of
 // 256 threads per SM that the register cap allows (6 at 40 registers, with a
 // few spilled epilogue values in some kernels; 5 at 48 without)
@@ -406,7 +468,7 @@ __global__ void __launch_bounds__(256, kComputedMinBlocks[V]) k_pair_r1(
     int64_t n, const Rec32 *__restrict__ src, const int32_t *__restrict__ cnt, int W,
     const uint32_t *__restrict__ list, PolyAB P, const Rec32 *__restrict__ tab, float inv_ds,
     const float4 *__restrict__ shift, double self_c, const double *__restrict__ f,
-    double *__restrict__ u, const int32_t *__restrict__ order) {
+    double *__restrict__ u, const int32_t *__restrict__ order, double *__restrict__ part) {
   __shared__ float4 sh[kMaxCode];
   stage_shifts(sh, shift);
   const int64_t gid = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / kGroup;
@@ -417,11 +479,15 @@ __global__ void __launch_bounds__(256, kComputedMinBlocks[V]) k_pair_r1(
   const PairSum r = pair_sum_r1<POLY>(s, act, sub, ri, src, cnt, W, list, P, tab, inv_ds, sh);
   float h, l;
   group_scatter3(sub, r, h, l);
-  if (!act || sub >= 3) return;
-  const int64_t k = 3 * s + sub;
-  const double v = fma(self_c, f[k], f2d_bits(h) + f2d_bits(l));
-  if (ORIG) u[3 * (int64_t)order[s] + sub] = v;
-  else u[k] = v;
+  float qh = 0.f, ql = 0.f;
+  if (act && sub < 3) {
+    const int64_t k = 3 * s + sub;
+    const double v = fma(self_c, f[k], f2d_bits(h) + f2d_bits(l));
+    if (ORIG) u[3 * (int64_t)order[s] + sub] = v;
+    else u[k] = v;
+    if (part) sq_ff(v, qh, ql);
+  }
+  if (part) block_partial_ff(qh, ql, part);  // |u|^2 (uniform branch)
 }
 
 // The first Chebyshev step in one pass (brownian_system.C:1036-1056 for one
@@ -436,7 +502,7 @@ __global__ void __launch_bounds__(256, kComputedMinBlocks[V]) k_pair_first(
     const uint32_t *__restrict__ list, PolyAB P, const Rec32 *__restrict__ tab, float inv_ds,
     const float4 *__restrict__ shift, double self_c, double da, double db, double c0, double c1,
     const double *__restrict__ x0, double *__restrict__ m, double *__restrict__ x1,
-    double *__restrict__ dw, Rec32 *__restrict__ next) {
+    double *__restrict__ dw, Rec32 *__restrict__ next, double *__restrict__ part) {
   __shared__ float4 sh[kMaxCode];
   stage_shifts(sh, shift);
   const int64_t gid = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / kGroup;
@@ -447,21 +513,25 @@ __global__ void __launch_bounds__(256, kComputedMinBlocks[V]) k_pair_first(
   const PairSum r = pair_sum_r1<POLY>(s, act, sub, ri, src, cnt, W, list, P, tab, inv_ds, sh);
   float h, l;
   group_scatter3(sub, r, h, l);
-  if (!act) return;
-  float *nf = reinterpret_cast<float *>(next + s);
-  if (sub < 3) {
-    const int64_t k = 3 * s + sub;
-    const double xk = x0[k];
-    const double mk = fma(self_c, xk, f2d_bits(h) + f2d_bits(l));
-    m[k] = mk;
-    const double x1k = db * xk + da * mk;
-    x1[k] = x1k;
-    dw[k] = c0 * xk + c1 * x1k;
-    nf[4 + sub] = d2f_bits(x1k);
-  } else {
-    reinterpret_cast<float4 *>(nf)[0] = ri.a;
-    nf[7] = 0.f;
+  float qh = 0.f, ql = 0.f;
+  if (act) {
+    float *nf = reinterpret_cast<float *>(next + s);
+    if (sub < 3) {
+      const int64_t k = 3 * s + sub;
+      const double xk = x0[k];
+      const double mk = fma(self_c, xk, f2d_bits(h) + f2d_bits(l));
+      m[k] = mk;
+      const double x1k = db * xk + da * mk;
+      x1[k] = x1k;
+      dw[k] = c0 * xk + c1 * x1k;
+      nf[4 + sub] = d2f_bits(x1k);
+      if (part) dot_ff(xk, mk, qh, ql);
+    } else {
+      reinterpret_cast<float4 *>(nf)[0] = ri.a;
+      nf[7] = 0.f;
+    }
   }
+  if (part) block_partial_ff(qh, ql, part);  // x0 . M x0 (aux2; uniform branch)
 }
 
 // One Chebyshev term with the pair sum (brownian_system.C:1091-1108 for one
@@ -470,13 +540,14 @@ __global__ void __launch_bounds__(256, kComputedMinBlocks[V]) k_pair_first(
 //   dw += coef xm,  and the 32-byte records of xm for the next term.
 // With c1 = 2db + 2da self_c this is xm = 2da (pair sum) + (c1 x1 - x0).
 // src holds the records of x1; next must be a different buffer.
-template <bool POLY, int V>
+template <bool POLY, int V, bool NORMS>
 __global__ void __launch_bounds__(256, kComputedMinBlocks[V]) k_pair_cheb(
     int64_t n, const Rec32 *__restrict__ src, const int32_t *__restrict__ cnt, int W,
     const uint32_t *__restrict__ list, PolyAB P, const Rec32 *__restrict__ tab, float inv_ds,
     const float4 *__restrict__ shift, double two_da, double c1, double coef,
     const double *__restrict__ x0, const double *__restrict__ x1, double *__restrict__ xm,
-    double *__restrict__ dw, Rec32 *__restrict__ next) {
+    double *__restrict__ dw, Rec32 *__restrict__ next, double *__restrict__ part,
+    int64_t nw, Rec32 *__restrict__ dw_next) {
   __shared__ float4 sh[kMaxCode];
   stage_shifts(sh, shift);
   const int64_t gid = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / kGroup;
@@ -487,17 +558,36 @@ __global__ void __launch_bounds__(256, kComputedMinBlocks[V]) k_pair_cheb(
   const PairSum r = pair_sum_r1<POLY>(s, act, sub, ri, src, cnt, W, list, P, tab, inv_ds, sh);
   float h, l;
   group_scatter3(sub, r, h, l);
-  if (!act) return;
-  float *nf = reinterpret_cast<float *>(next + s);
-  if (sub < 3) {
-    const int64_t k = 3 * s + sub;
-    const double v = fma(two_da, f2d_bits(h) + f2d_bits(l), fma(c1, x1[k], -x0[k]));
-    xm[k] = v;
-    dw[k] = fma(coef, v, dw[k]);
-    nf[4 + sub] = d2f_bits(v);
-  } else {
-    reinterpret_cast<float4 *>(nf)[0] = ri.a;  // the target's position record
-    nf[7] = 0.f;
+  float q0h = 0.f, q0l = 0.f, q1h = 0.f, q1l = 0.f;
+  if (act) {
+    float *nf = reinterpret_cast<float *>(next + s);
+    float *df = reinterpret_cast<float *>(dw_next + s);
+    if (sub < 3) {
+      const int64_t k = 3 * s + sub;
+      const double v = fma(two_da, f2d_bits(h) + f2d_bits(l), fma(c1, x1[k], -x0[k]));
+      xm[k] = v;
+      const double y = dw[k];
+      const double yn = fma(coef, v, y);
+      dw[k] = yn;
+      nf[4 + sub] = d2f_bits(v);
+      if (NORMS) {
+        sq_ff(y, q0h, q0l);  // |dw|^2 before the term
+        sq_ff(v, q1h, q1l);  // |x_{k+1}|^2
+        df[4 + sub] = d2f_bits(yn);
+      }
+    } else {
+      reinterpret_cast<float4 *>(nf)[0] = ri.a;  // the target's position record
+      nf[7] = 0.f;
+      if (NORMS) {
+        reinterpret_cast<float4 *>(df)[0] = ri.a;
+        df[7] = 0.f;
+      }
+    }
+  }
+  if (NORMS) {  // the estimators' two norms (the records of dw are written)
+    block_partial_ff(q0h, q0l, part);
+    __syncthreads();  // the shared partials are reused
+    block_partial_ff(q1h, q1l, part + nw);
   }
 }
 
@@ -1080,17 +1170,19 @@ PolyAB poly_of(const ggem_ctx *c) {
 }
 
 template <bool POLY, int V, bool ORIG>
-void launch_r1(ggem_ctx *c, const Rec32 *src, const double *f, double *u, double self_c) {
+void launch_r1(ggem_ctx *c, const Rec32 *src, const double *f, double *u, double self_c,
+               double *part) {
   k_pair_r1<POLY, V, ORIG><<<(unsigned)pair_grid_blocks(c), 256, 0, c->stream>>>(
       c->n, src, c->nb_cnt.p, c->nb_w, c->nb_list.p, poly_of(c),
       reinterpret_cast<const Rec32 *>(c->tab.p), c->tab_inv_ds, c->d_shift.p, self_c, f, u,
-      c->order.p);
+      c->order.p, part);
 }
 
 template <bool POLY, bool ORIG = false>
-void dispatch_r1(ggem_ctx *c, const Rec32 *src, const double *f, double *u, double self_c) {
-  if (c->computed_variant == 1) launch_r1<POLY, 1, ORIG>(c, src, f, u, self_c);
-  else launch_r1<POLY, 0, ORIG>(c, src, f, u, self_c);
+void dispatch_r1(ggem_ctx *c, const Rec32 *src, const double *f, double *u, double self_c,
+                 double *part = nullptr) {
+  if (c->computed_variant == 1) launch_r1<POLY, 1, ORIG>(c, src, f, u, self_c, part);
+  else launch_r1<POLY, 0, ORIG>(c, src, f, u, self_c, part);
 }
 
 // single right-hand side: records from FP64 slot-order f, then the pair sum
@@ -1118,30 +1210,40 @@ int launch_f32_r1(ggem_ctx *c, const double *f, double *u, double self_c) {
 }
 
 // c1 = 2db + 2da self_c folds the self term into the x1 coefficient
-template <bool POLY, int V>
+template <bool POLY, int V, bool NORMS>
 void launch_cheb(ggem_ctx *c, const Rec32 *src, Rec32 *next, double two_da, double c1,
-                 double coef, const double *x0, const double *x1, double *xm, double *dw) {
-  k_pair_cheb<POLY, V><<<(unsigned)pair_grid_blocks(c), 256, 0, c->stream>>>(
+                 double coef, const double *x0, const double *x1, double *xm, double *dw,
+                 double *part, Rec32 *dw_next) {
+  k_pair_cheb<POLY, V, NORMS><<<(unsigned)pair_grid_blocks(c), 256, 0, c->stream>>>(
       c->n, src, c->nb_cnt.p, c->nb_w, c->nb_list.p, poly_of(c),
       reinterpret_cast<const Rec32 *>(c->tab.p), c->tab_inv_ds, c->d_shift.p, two_da, c1, coef,
-      x0, x1, xm, dw, next);
+      x0, x1, xm, dw, next, part, pair_partials(c), dw_next);
 }
 
+// with part (and dw_next) the term also leaves the estimators' two norms as
+// per-block partials and the records of the new dw
 template <bool POLY>
 void dispatch_cheb(ggem_ctx *c, const Rec32 *src, Rec32 *next, double two_da, double c1,
-                   double coef, const double *x0, const double *x1, double *xm, double *dw) {
-  if (c->computed_variant == 1) launch_cheb<POLY, 1>(c, src, next, two_da, c1, coef, x0, x1, xm, dw);
-  else launch_cheb<POLY, 0>(c, src, next, two_da, c1, coef, x0, x1, xm, dw);
+                   double coef, const double *x0, const double *x1, double *xm, double *dw,
+                   double *part, Rec32 *dw_next) {
+  const bool v1 = c->computed_variant == 1;
+  if (part) {
+    if (v1) launch_cheb<POLY, 1, true>(c, src, next, two_da, c1, coef, x0, x1, xm, dw, part, dw_next);
+    else launch_cheb<POLY, 0, true>(c, src, next, two_da, c1, coef, x0, x1, xm, dw, part, dw_next);
+  } else {
+    if (v1) launch_cheb<POLY, 1, false>(c, src, next, two_da, c1, coef, x0, x1, xm, dw, part, dw_next);
+    else launch_cheb<POLY, 0, false>(c, src, next, two_da, c1, coef, x0, x1, xm, dw, part, dw_next);
+  }
 }
 
 template <bool POLY, int V>
 void launch_first(ggem_ctx *c, const Rec32 *src, Rec32 *next, double self_c, double da,
                   double db, double c0, double c1, const double *x0, double *m, double *x1,
-                  double *dw) {
+                  double *dw, double *part) {
   k_pair_first<POLY, V><<<(unsigned)pair_grid_blocks(c), 256, 0, c->stream>>>(
       c->n, src, c->nb_cnt.p, c->nb_w, c->nb_list.p, poly_of(c),
       reinterpret_cast<const Rec32 *>(c->tab.p), c->tab_inv_ds, c->d_shift.p, self_c, da, db, c0,
-      c1, x0, m, x1, dw, next);
+      c1, x0, m, x1, dw, next, part);
 }
 
 template <int CD, bool POLY>
@@ -1239,12 +1341,13 @@ int permute_from_slots(ggem_ctx *c, int nrhs, const double *d_slot, double *d_or
 // previous fused term wrote them); otherwise they are built here first.
 int pair_cheb_term(ggem_ctx *c, bool records_fresh, const double *x0, const double *x1,
                    double *xm, double *dw, double two_da, double two_db, double coef,
-                   int self_mode) {
+                   int self_mode, double *norms) {
   const int64_t n = c->n;
   if (n == 0) return GGEM_OK;
   cudaError_t e;
   const double self_c0 = self_coefficient(c, self_mode);
   if (c->pretensor_ok) {
+    if (norms) return fail(c, GGEM_ERR_BAD_ARG, "fused norms need per-matvec pair tensors");
     if ((e = c->w_f4[0].ensure((size_t)n)) || (e = c->w_f4[1].ensure((size_t)n)))
       return cuda_fail(c, e, "chebyshev forces");
     float4 *cur = c->w_f4[c->rec_cur].p, *nxt = c->w_f4[c->rec_cur ^ 1].p;
@@ -1267,9 +1370,16 @@ int pair_cheb_term(ggem_ctx *c, bool records_fresh, const double *x0, const doub
     if (int rc = check_launch(c, "chebyshev records")) return rc;
   }
   const double c1 = two_db + two_da * self_c0;
+  // a checked term leaves the records of the new dw in w_src for the check
+  // matvec (matvec_dw_records)
+  Rec32 *dwr = nullptr;
+  if (norms) {
+    if ((e = c->w_src.ensure(2 * (size_t)n))) return cuda_fail(c, e, "pair records");
+    dwr = reinterpret_cast<Rec32 *>(c->w_src.p);
+  }
   kt_start(c, kKPairCheb);
-  if (c->use_poly) dispatch_cheb<true>(c, cur, nxt, two_da, c1, coef, x0, x1, xm, dw);
-  else dispatch_cheb<false>(c, cur, nxt, two_da, c1, coef, x0, x1, xm, dw);
+  if (c->use_poly) dispatch_cheb<true>(c, cur, nxt, two_da, c1, coef, x0, x1, xm, dw, norms, dwr);
+  else dispatch_cheb<false>(c, cur, nxt, two_da, c1, coef, x0, x1, xm, dw, norms, dwr);
   kt_stop(c, kKPairCheb);
   c->rec_cur ^= 1;
   return check_launch(c, "pair chebyshev term");
@@ -1320,11 +1430,14 @@ int pair_grid_blocks(const ggem_ctx *c) {
   return (int)std::max<int64_t>(1, (c->n * kGroup + 255) / 256);
 }
 
+int64_t pair_partials(const ggem_ctx *c) { return pair_grid_blocks(c); }
+
 // The first step of a fused series: xi (caller order) into slot order (x0)
 // with its records, then k_pair_first (m = M x0, x1, dw and the records of
 // x1 for the first term).
 int cheb_start_fused(ggem_ctx *c, const double *xi, double *x0, double *m, double *x1,
-                     double *dw, double da, double db, double c0, double c1, int self_mode) {
+                     double *dw, double da, double db, double c0, double c1, int self_mode,
+                     double *aux2) {
   const int64_t n = c->n;
   if (n == 0) return GGEM_OK;
   if (c->pretensor_ok) return fail(c, GGEM_ERR_BAD_ARG, "fused start needs per-matvec pair tensors");
@@ -1340,15 +1453,29 @@ int cheb_start_fused(ggem_ctx *c, const double *xi, double *x0, double *m, doubl
   kt_start(c, kKPairF32);
   const bool v1 = c->computed_variant == 1;
   if (c->use_poly) {
-    if (v1) launch_first<true, 1>(c, cur, nxt, self_c, da, db, c0, c1, x0, m, x1, dw);
-    else launch_first<true, 0>(c, cur, nxt, self_c, da, db, c0, c1, x0, m, x1, dw);
+    if (v1) launch_first<true, 1>(c, cur, nxt, self_c, da, db, c0, c1, x0, m, x1, dw, aux2);
+    else launch_first<true, 0>(c, cur, nxt, self_c, da, db, c0, c1, x0, m, x1, dw, aux2);
   } else {
-    if (v1) launch_first<false, 1>(c, cur, nxt, self_c, da, db, c0, c1, x0, m, x1, dw);
-    else launch_first<false, 0>(c, cur, nxt, self_c, da, db, c0, c1, x0, m, x1, dw);
+    if (v1) launch_first<false, 1>(c, cur, nxt, self_c, da, db, c0, c1, x0, m, x1, dw, aux2);
+    else launch_first<false, 0>(c, cur, nxt, self_c, da, db, c0, c1, x0, m, x1, dw, aux2);
   }
   kt_stop(c, kKPairF32);
   c->rec_cur ^= 1;
   return check_launch(c, "pair first step");
+}
+
+// u = M dw after a checked fused term: the term left the records of dw in
+// w_src, so the check matvec is one launch, and |u|^2 leaves as per-block
+// partials (norm)
+int matvec_dw_records(ggem_ctx *c, const double *dw, double *u, int self_mode, double *norm) {
+  if (c->n == 0) return GGEM_OK;
+  const Rec32 *src = reinterpret_cast<const Rec32 *>(c->w_src.p);
+  const double self_c = self_coefficient(c, self_mode);
+  kt_start(c, kKPairF32);
+  if (c->use_poly) dispatch_r1<true>(c, src, dw, u, self_c, norm);
+  else dispatch_r1<false>(c, src, dw, u, self_c, norm);
+  kt_stop(c, kKPairF32);
+  return check_launch(c, "pair f32 r1");
 }
 
 // u = M f for one right-hand side with f and u in the caller's particle
