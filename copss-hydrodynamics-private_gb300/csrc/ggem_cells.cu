@@ -153,13 +153,14 @@ int scan_impl(ggem_ctx *c, const T *in, T *out, int64_t n, int level) {
 }
 
 // the cell list's exclusive scan in one block when the grid is small
-// enough: tiles of 1024 counts, all loaded (coalesced) before the first
-// tile is scanned, then one block-wide scan per tile with a running carry;
-// start[0..ncell].  The counts are zeroed as they are read, ready for the
-// next build's k_assign, and so are the pair-list statistics (stat, when
-// given) that the list build of the same configuration accumulates.
-constexpr int kScanTiles = 32;
-constexpr int64_t kScanCellsMax = 1024 * kScanTiles;
+// enough: tiles of 4096 counts (four consecutive counts per thread), all
+// loaded before the first tile is scanned, then one block-wide scan of the
+// threads' sums per tile with a running carry; start[0..ncell].  The counts
+// are zeroed as they are read, ready for the next build's k_assign, and so
+// are the pair-list statistics (stat, when given) that the list build of
+// the same configuration accumulates.
+constexpr int kScanTiles = 8;
+constexpr int64_t kScanCellsMax = 4096 * kScanTiles;
 
 __global__ void __launch_bounds__(1024) k_scan_cells(int32_t *__restrict__ count,
                                                      int32_t *__restrict__ start, int64_t n,
@@ -167,23 +168,28 @@ __global__ void __launch_bounds__(1024) k_scan_cells(int32_t *__restrict__ count
   __shared__ int32_t warp_tot[2][32];
   if (stat && threadIdx.x < 2) stat[threadIdx.x] = 0ull;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int tiles = (int)((n + 1023) / 1024);
-  int32_t v[kScanTiles];
+  const int tiles = (int)((n + 4095) / 4096);
+  int32_t v[kScanTiles][4];
 #pragma unroll
-  for (int k = 0; k < kScanTiles; ++k) {
-    const int64_t i = (int64_t)k * 1024 + threadIdx.x;
-    v[k] = (k < tiles && i < n) ? count[i] : 0;
-  }
+  for (int k = 0; k < kScanTiles; ++k)
 #pragma unroll
-  for (int k = 0; k < kScanTiles; ++k) {
-    const int64_t i = (int64_t)k * 1024 + threadIdx.x;
-    if (k < tiles && i < n) count[i] = 0;
-  }
+    for (int j = 0; j < 4; ++j) {
+      const int64_t i = (int64_t)k * 4096 + 4 * threadIdx.x + j;
+      v[k][j] = (k < tiles && i < n) ? count[i] : 0;
+    }
+#pragma unroll
+  for (int k = 0; k < kScanTiles; ++k)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int64_t i = (int64_t)k * 4096 + 4 * threadIdx.x + j;
+      if (k < tiles && i < n) count[i] = 0;
+    }
   int32_t carry = 0;
 #pragma unroll
   for (int k = 0; k < kScanTiles; ++k) {
     if (k < tiles) {
-      int32_t x = v[k];
+      const int32_t tsum = (v[k][0] + v[k][1]) + (v[k][2] + v[k][3]);
+      int32_t x = tsum;
 #pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
         const int32_t y = __shfl_up_sync(0xffffffffu, x, o);
@@ -201,8 +207,13 @@ __global__ void __launch_bounds__(1024) k_scan_cells(int32_t *__restrict__ count
       // every warp scans the 32 warp totals itself (no second barrier)
       const int32_t before = __shfl_sync(0xffffffffu, w, (warp + 31) & 31);
       const int32_t total = __shfl_sync(0xffffffffu, w, 31);
-      const int64_t i = (int64_t)k * 1024 + threadIdx.x;
-      if (i < n) start[i] = carry + (warp ? before : 0) + x - v[k];
+      int32_t run = carry + (warp ? before : 0) + x - tsum;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int64_t i = (int64_t)k * 4096 + 4 * threadIdx.x + j;
+        if (i < n) start[i] = run;
+        run += v[k][j];
+      }
       carry += total;
     }
   }
