@@ -493,6 +493,42 @@ def test_fused_chebyshev_terms_match_unfused_path():
     assert 0.5 * rep_o.err1 <= r2[0]["err1"] <= 2.0 * rep_o.err1
 
 
+def test_fused_series_estimators_match_unfused_path():
+    """Per-matvec pair tensors: the whole series is fused, and the
+    estimator sums (xi.M.xi, the checked term's norms, |M dw|^2) come from
+    the pair kernels as float-float partials without FP64 arithmetic; err1,
+    err2 and y agree with the path that checks every term in FP64 vector
+    kernels, and the adaptive series stops at the same degree."""
+    xyz, L = suspension(4000, 0.1, 57)
+    xi = np.random.default_rng(23).standard_normal(3 * len(xyz))
+    # err1 = sqrt(|y.M.M.y - xi.M.xi| / xi.M.xi): at 8 terms err1 ~ 1e-3, so
+    # the sums' ~1e-14 relative error moves err1 by ~1e-8 relative (deeper
+    # series cancel more: at err1 ~ 2e-5 it is ~1e-5)
+    N = 8
+    with G.Context(box_hi=(L,) * 3, rc=7.0, precision=G.FP32) as ctx:
+        ctx.set_pair_tensors(False)
+        ctx.set_particles(xyz)
+        ctx.build_cells()
+        lo, hi = ctx.lanczos_bounds(k=30, seed=3)
+        lo, hi = lo / 1.05, hi * 1.05
+        y1, r1 = ctx.cheb_inv_sqrt(xi, N, lo, hi, 0.0, check_every=1)
+        y2, r2 = ctx.cheb_inv_sqrt(xi, N, lo, hi, 0.0, check_every=N - 1)
+        rc, dw_a, ra = ctx.brownian_displacement(xi, 50, lo, hi, 1e-3, check_every=1)
+        rc2, dw_b, rb = ctx.brownian_displacement(xi, 50, lo, hi, 1e-3, check_every=0)
+        rc3, dw_c, rc_ = ctx.brownian_displacement(xi, 50, lo, hi, 1e-3, check_every=0)
+    assert rel(y2, y1) <= 1e-12
+    assert r2[0]["err1"] == pytest.approx(r1[0]["err1"], rel=1e-6)
+    assert r2[0]["err2"] == pytest.approx(r1[0]["err2"], rel=1e-9)
+    assert rc == rc2 == rc3 == 0
+    # the adaptive (fused) series converges at the degree the every-term
+    # check finds, with the same err1
+    assert rb[0]["n_terms"] == ra[0]["n_terms"] or rc_[0]["n_terms"] == ra[0]["n_terms"]
+    same = rc_ if rc_[0]["n_terms"] == ra[0]["n_terms"] else rb
+    dw_s = dw_c if same is rc_ else dw_b
+    assert same[0]["err1"] == pytest.approx(ra[0]["err1"], rel=1e-6)
+    assert rel(dw_s, dw_a) <= 1e-12
+
+
 def test_fused_batched_chebyshev_terms_match_unfused_path():
     """16 .. 64 right-hand sides: unchecked terms run as one batched kernel
     (pair sum, recurrence and the next term's FP32 staging); the series
