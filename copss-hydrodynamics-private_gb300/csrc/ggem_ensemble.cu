@@ -191,28 +191,51 @@ __global__ void k_ens_start(int64_t ntot, const int32_t *__restrict__ susp,
 }
 
 // out[b][r] = sum over the slots of suspension b of a . b (per right-hand
-// side), one block of kDotThreads per suspension, fixed order.  Element k of
-// a vector belongs to right-hand side (k % 24) / 3; the block's stride (a
-// multiple of 24) keeps every thread on one right-hand side.
+// side), fixed order.  Element k of a vector belongs to right-hand side
+// (k % 24) / 3; a block's stride (a multiple of 24) keeps every thread on one
+// right-hand side.
 constexpr int kDotThreads = 192;
 
-__global__ void __launch_bounds__(kDotThreads) k_ens_dot(const int64_t *__restrict__ off,
-                                                         const double *__restrict__ a,
-                                                         const double *__restrict__ bv,
-                                                         double *__restrict__ out) {
+// The sums are split into chunks of at most kDotSlots slots (one block per
+// whole suspension made the largest suspension's block the critical path):
+// one block per chunk, four running sums per thread, then the chunks of each
+// suspension added in order (k_ens_dot_fin).  part[c][r] per chunk c and
+// right-hand side r.
+constexpr int kDotSlots = 256;
+
+__global__ void __launch_bounds__(kDotThreads) k_ens_dot_part(const int64_t *__restrict__ cs,
+                                                              const double *__restrict__ a,
+                                                              const double *__restrict__ bv,
+                                                              double *__restrict__ part) {
   __shared__ double sh[kDotThreads];
-  const int b = blockIdx.x;
-  const int64_t k0 = off[b] * kE, k1 = off[b + 1] * kE;
-  double v = 0.0;
-  for (int64_t k = k0 + threadIdx.x; k < k1; k += kDotThreads) v += a[k] * bv[k];
-  sh[threadIdx.x] = v;
+  const int64_t c = blockIdx.x;
+  const int64_t k0 = cs[c] * kE, k1 = cs[c + 1] * kE;
+  double v0 = 0.0, v1 = 0.0, v2 = 0.0, v3 = 0.0;
+  int64_t k = k0 + threadIdx.x;
+  for (; k + 3 * kDotThreads < k1; k += 4 * kDotThreads) {
+    v0 = fma(a[k], bv[k], v0);
+    v1 = fma(a[k + kDotThreads], bv[k + kDotThreads], v1);
+    v2 = fma(a[k + 2 * kDotThreads], bv[k + 2 * kDotThreads], v2);
+    v3 = fma(a[k + 3 * kDotThreads], bv[k + 3 * kDotThreads], v3);
+  }
+  for (; k < k1; k += kDotThreads) v0 = fma(a[k], bv[k], v0);
+  sh[threadIdx.x] = (v0 + v1) + (v2 + v3);
   __syncthreads();
   if (threadIdx.x < kR) {
     double t = 0.0;
     for (int i = 0; i < kDotThreads; ++i)
       if ((i % kE) / 3 == (int)threadIdx.x) t += sh[i];
-    out[b * kR + threadIdx.x] = t;
+    part[c * kR + threadIdx.x] = t;
   }
+}
+
+__global__ void k_ens_dot_fin(const int32_t *__restrict__ coff, const double *__restrict__ part,
+                              double *__restrict__ out) {
+  const int b = blockIdx.x, r = threadIdx.x;
+  if (r >= kR) return;
+  double t = 0.0;
+  for (int c = coff[b]; c < coff[b + 1]; ++c) t += part[(int64_t)c * kR + r];
+  out[b * kR + r] = t;
 }
 
 }  // namespace ens
@@ -239,6 +262,12 @@ struct ggem_ensemble {
   DevBuf<uint32_t> list;
   DevBuf<float4> ten;
   DevBuf<int64_t> d_off;
+  // dot chunks: slot starts [nchunk + 1], first chunk of every suspension
+  // [K + 1], partial sums [nchunk][8]
+  DevBuf<int64_t> chunk_s;
+  DevBuf<int32_t> chunk_off;
+  DevBuf<double> chunk_part;
+  int nchunk = 0;
   DevBuf<SubView> views;
   // Chebyshev state: vectors [slot][8][3] and FP32 forces [slot][8]
   DevBuf<double> v[6];
@@ -419,6 +448,23 @@ extern "C" int ggem_ensemble_set_particles_dev(ggem_ensemble *e, const int64_t *
       (c = cudaMemcpyAsync(e->d_off.p, e->off.data(), sizeof(int64_t) * (e->K + 1),
                            cudaMemcpyHostToDevice, e->stream)))
     return ecuda(e, c, "ensemble tables");
+  // the dot chunks (each within one suspension)
+  std::vector<int64_t> cs;
+  std::vector<int32_t> coff(e->K + 1, 0);
+  for (int b = 0; b < e->K; ++b) {
+    coff[b] = (int32_t)cs.size();
+    for (int64_t s0 = e->off[b]; s0 < e->off[b + 1]; s0 += kDotSlots) cs.push_back(s0);
+  }
+  coff[e->K] = (int32_t)cs.size();
+  e->nchunk = (int)cs.size();
+  cs.push_back(e->ntot);  // a chunk ends where the next one (or the next suspension) begins
+  if ((c = e->chunk_s.ensure(cs.size())) || (c = e->chunk_off.ensure(coff.size())) ||
+      (c = e->chunk_part.ensure((size_t)e->nchunk * kR)) ||
+      (c = cudaMemcpyAsync(e->chunk_s.p, cs.data(), sizeof(int64_t) * cs.size(),
+                           cudaMemcpyHostToDevice, e->stream)) ||
+      (c = cudaMemcpyAsync(e->chunk_off.p, coff.data(), sizeof(int32_t) * coff.size(),
+                           cudaMemcpyHostToDevice, e->stream)))
+    return ecuda(e, c, "ensemble dot chunks");
   int64_t nmax = 0;
   for (int b = 0; b < e->K; ++b) nmax = std::max(nmax, n[b]);
   dim3 grid(eblocks(nmax, 256), e->K);
@@ -467,8 +513,10 @@ int ens_term(ggem_ensemble *e, int term, int ldc, const double *x0, const double
 }
 
 int ens_dot(ggem_ensemble *e, const double *a, const double *b, double *out) {
-  k_ens_dot<<<e->K, kDotThreads, 0, e->stream>>>(e->d_off.p, a, b, out);
-  return elaunch(e, "ensemble dot");
+  k_ens_dot_part<<<e->nchunk, kDotThreads, 0, e->stream>>>(e->chunk_s.p, a, b, e->chunk_part.p);
+  if (int rc = elaunch(e, "ensemble dot")) return rc;
+  k_ens_dot_fin<<<e->K, 32, 0, e->stream>>>(e->chunk_off.p, e->chunk_part.p, out);
+  return elaunch(e, "ensemble dot sum");
 }
 
 }  // namespace
