@@ -17,6 +17,8 @@ ggem_ctx::~ggem_ctx() {
   for (cudaEvent_t e : ev_pool) cudaEventDestroy(e);
   for (auto &t : trace_ev) cudaEventDestroy(t.second);
   if (ev_readback) cudaEventDestroy(ev_readback);
+  if (ev_copy) cudaEventDestroy(ev_copy);
+  if (copy_stream) cudaStreamDestroy(copy_stream);
   for (auto *b : scan_scratch) delete b;
   if (h_red) cudaFreeHost(h_red);
   if (h_stage) cudaFreeHost(h_stage);

@@ -608,11 +608,25 @@ extern "C" int ggem_brownian_displacement(ggem_ctx *ctx, int nrhs, int N, double
   DeviceGuard dg(ctx->device);
   const size_t len = (size_t)ctx->n * 3 * nrhs;
   cudaError_t e;
-  if ((e = ctx->w_a.ensure(len)) || (e = ctx->w_b.ensure(len))) return cuda_fail(ctx, e, "bd io");
-  if (len && (e = cudaMemcpyAsync(ctx->w_a.p, xi, 8 * len, cudaMemcpyHostToDevice, ctx->stream)))
-    return cuda_fail(ctx, e, "bd h2d");
+  if ((e = ctx->w_hin.ensure(len)) || (e = ctx->w_b.ensure(len)))
+    return cuda_fail(ctx, e, "bd io");
+  if (len) {
+    // xi travels on a copy stream into a buffer only this call uses, so the
+    // copy overlaps the work already queued (a deferred cell and list
+    // build); the series waits for it
+    if (!ctx->copy_stream &&
+        (e = cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking)))
+      return cuda_fail(ctx, e, "copy stream");
+    if (!ctx->ev_copy && (e = cudaEventCreateWithFlags(&ctx->ev_copy, cudaEventDisableTiming)))
+      return cuda_fail(ctx, e, "copy event");
+    if ((e = cudaMemcpyAsync(ctx->w_hin.p, xi, 8 * len, cudaMemcpyHostToDevice,
+                             ctx->copy_stream)) ||
+        (e = cudaEventRecord(ctx->ev_copy, ctx->copy_stream)) ||
+        (e = cudaStreamWaitEvent(ctx->stream, ctx->ev_copy, 0)))
+      return cuda_fail(ctx, e, "bd h2d");
+  }
   int rc = ggem_brownian_displacement_dev(ctx, nrhs, N, eig_min, eig_max, tol_cheb, check_every,
-                                          ctx->w_a.p, ctx->w_b.p, rep);
+                                          ctx->w_hin.p, ctx->w_b.p, rep);
   if (rc) return rc;
   if (len && (e = cudaMemcpyAsync(dw, ctx->w_b.p, 8 * len, cudaMemcpyDeviceToHost, ctx->stream)))
     return cuda_fail(ctx, e, "bd d2h");

@@ -177,6 +177,11 @@ struct ggem_ctx {
   ggem::DevBuf<double> lz_Q;    // Lanczos basis
   double *h_red = nullptr;      // pinned host mirror of reductions
   cudaEvent_t ev_readback = nullptr;  // recorded behind the reductions' readback
+  // host inputs of ggem_brownian_displacement: copied on their own stream
+  // into a buffer no other call uses
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t ev_copy = nullptr;
+  ggem::DevBuf<double> w_hin;
   double *h_stage = nullptr;    // pinned host staging
   size_t h_stage_bytes = 0;
 
