@@ -13,6 +13,7 @@
 #include <cmath>
 #include <vector>
 
+#include "ggem_ff.cuh"
 #include "ggem_internal.cuh"
 
 namespace ggem {
@@ -61,6 +62,26 @@ __global__ void __launch_bounds__(kVecThreads) k_dot_partials(int64_t D, const d
   if (threadIdx.x == 0) partial[(int64_t)r * gridDim.x + blockIdx.x] = t;
 }
 
+// k_dot_partials with float-float products and sums (no FP64 arithmetic):
+// the estimator sums of the FP32 multi-RHS series, whose matvecs carry
+// ~1e-7 relative error, so that their ~1e-14 serves as well as FP64
+__global__ void __launch_bounds__(kVecThreads) k_dot_ff(int64_t D, const double *__restrict__ a,
+                                                        const double *__restrict__ b,
+                                                        double *__restrict__ partial) {
+  __shared__ float2 sh[32];
+  const int r = blockIdx.y;
+  const double *pa = a + (int64_t)r * D, *pb = b + (int64_t)r * D;
+  float h = 0.f, l = 0.f;
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < D;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    float ph, pl;
+    dot_ff(pa[k], pb[k], ph, pl);
+    ff_add(h, l, ph, pl);
+  }
+  const double t = block_ff_sum(h, l, sh);
+  if (threadIdx.x == 0) partial[(int64_t)r * gridDim.x + blockIdx.x] = t;
+}
+
 // out[q] = sum_b partial[q][b], fixed order (deterministic).  With stat and
 // err given, out[nq .. nq+2] also receive the pair-list statistics (total
 // and longest row, as bit patterns) and the error word of a deferred build,
@@ -92,38 +113,40 @@ __global__ void __launch_bounds__(kVecThreads) k_finalize(int G, const double *_
   }
 }
 
-// x1 = db * x0 + da * x1   (VecAXPBY(x1, db, da, x0), brownian_system.C:1041)
-__global__ void k_cheb_first(int64_t D, int nrhs, double da, double db,
-                             const double *__restrict__ x0, double *__restrict__ x1) {
-  const int64_t tot = D * nrhs;
-  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < tot;
-       k += (int64_t)gridDim.x * blockDim.x)
-    x1[k] = db * x0[k] + da * x1[k];
-}
-
-// dw = c0 x0 (norm -> q0), dw += c1 x1, ||x1|| -> q1  (brownian_system.C:1050-1056)
-__global__ void __launch_bounds__(kVecThreads) k_cheb_init(int64_t D, double c0, double c1,
-                                                           const double *__restrict__ x0,
-                                                           const double *__restrict__ x1,
-                                                           double *__restrict__ dw,
-                                                           double *__restrict__ partial) {
+// the series' first step in one pass (brownian_system.C:1041, 1050-1056):
+// x1 = db x0 + da x1 (VecAXPBY; x1 holds M x0), dw = c0 x0 + c1 x1, with
+// the norms |c0 x0| -> q0 and |x1| -> q1 only where a check precedes the
+// first term (the reference-faithful mode)
+template <bool NORMS>
+__global__ void __launch_bounds__(kVecThreads) k_cheb_start(int64_t D, double da, double db,
+                                                            double c0, double c1,
+                                                            const double *__restrict__ x0,
+                                                            double *__restrict__ x1,
+                                                            double *__restrict__ dw,
+                                                            double *__restrict__ partial) {
   __shared__ double sh[32];
   const int r = blockIdx.y, nrhs = gridDim.y;
   const int64_t off = (int64_t)r * D;
   double a4 = 0.0, a3 = 0.0;
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < D;
        k += (int64_t)gridDim.x * blockDim.x) {
-    const double t = c0 * x0[off + k];
-    a4 += t * t;
-    const double v = x1[off + k];
+    const double x = x0[off + k];
+    const double v = db * x + da * x1[off + k];
+    x1[off + k] = v;
+    const double t = c0 * x;
     dw[off + k] = t + c1 * v;
-    a3 += v * v;
+    if (NORMS) {
+      a4 += t * t;
+      a3 += v * v;
+    }
   }
-  const double s4 = block_sum(a4, sh);
-  const double s3 = block_sum(a3, sh);
-  if (threadIdx.x == 0) {
-    partial[(int64_t)(0 * nrhs + r) * gridDim.x + blockIdx.x] = s4;
-    partial[(int64_t)(1 * nrhs + r) * gridDim.x + blockIdx.x] = s3;
+  if (NORMS) {
+    const double s4 = block_sum(a4, sh);
+    const double s3 = block_sum(a3, sh);
+    if (threadIdx.x == 0) {
+      partial[(int64_t)(0 * nrhs + r) * gridDim.x + blockIdx.x] = s4;
+      partial[(int64_t)(1 * nrhs + r) * gridDim.x + blockIdx.x] = s3;
+    }
   }
 }
 
@@ -131,7 +154,9 @@ __global__ void __launch_bounds__(kVecThreads) k_cheb_init(int64_t D, double c0,
 //   ||dw|| -> q0 ; xm = (2db x1 + 2da xm) - x0 ; dw += c[r] xm ; ||xm|| -> q1
 // The norms feed only the error estimators: a term that no check follows
 // skips them (NORMS = false), a third of the term's FP64 work.
-template <bool NORMS>
+// With FF the norms are float-float sums (no FP64 arithmetic; the FP32
+// series) instead of FP64 ones.
+template <bool NORMS, bool FF = false>
 __global__ void __launch_bounds__(kVecThreads) k_cheb_term(int64_t D, double two_da,
                                                            double two_db, RhsCoef cf,
                                                            const double *__restrict__ x0,
@@ -140,23 +165,33 @@ __global__ void __launch_bounds__(kVecThreads) k_cheb_term(int64_t D, double two
                                                            double *__restrict__ dw,
                                                            double *__restrict__ partial) {
   __shared__ double sh[32];
+  __shared__ float2 shf[32];
   const int r = blockIdx.y, nrhs = gridDim.y;
   const int64_t off = (int64_t)r * D;
   const double c = cf.c[r];
   double a4 = 0.0, a3 = 0.0;
+  float h4 = 0.f, l4 = 0.f, h3 = 0.f, l3 = 0.f;
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < D;
        k += (int64_t)gridDim.x * blockDim.x) {
     const double y = dw[off + k];
-    if (NORMS) a4 += y * y;
     double v = two_db * x1[off + k] + two_da * xm[off + k];
     v -= x0[off + k];
     xm[off + k] = v;
     dw[off + k] = y + c * v;
-    if (NORMS) a3 += v * v;
+    if (NORMS && FF) {
+      float ph, pl;
+      sq_ff(y, ph, pl);
+      ff_add(h4, l4, ph, pl);
+      sq_ff(v, ph, pl);
+      ff_add(h3, l3, ph, pl);
+    } else if (NORMS) {
+      a4 += y * y;
+      a3 += v * v;
+    }
   }
   if (NORMS) {
-    const double s4 = block_sum(a4, sh);
-    const double s3 = block_sum(a3, sh);
+    const double s4 = FF ? block_ff_sum(h4, l4, shf) : block_sum(a4, sh);
+    const double s3 = FF ? block_ff_sum(h3, l3, shf) : block_sum(a3, sh);
     if (threadIdx.x == 0) {
       partial[(int64_t)(0 * nrhs + r) * gridDim.x + blockIdx.x] = s4;
       partial[(int64_t)(1 * nrhs + r) * gridDim.x + blockIdx.x] = s3;
@@ -360,6 +395,9 @@ int cheb_slots(ggem_ctx *c, int nrhs, int N, double eig_min, double eig_max, dou
   const int64_t D = 3 * c->n;
   const int sm = brownian_self_mode(c);
   const bool faithful = check_every == 1;
+  // the FP32 series' estimator sums run as float-float sums (the FP64
+  // precision and the reference-faithful mode keep FP64 dots)
+  const bool ff_sums = c->prm.precision == GGEM_FP32 && !faithful;
   // Terms that no error check follows need neither norm: on the FP32
   // single-RHS path they run as one fused pair-sum + recurrence kernel that
   // also writes the FP32 records of the next x1 (records_fresh).  With
@@ -410,12 +448,17 @@ int cheb_slots(ggem_ctx *c, int nrhs, int N, double eig_min, double eig_max, dou
   } else {
     if (int rc = permute_to_slots(c, nrhs, xi, x0)) return rc;
     if (int rc = matvec_slots(c, nrhs, x0, x1, sm)) return rc;
-    k_dot_partials<<<dim3(G, nrhs), kVecThreads, 0, st>>>(D, x1, x0, p_aux2);
+    if (ff_sums) k_dot_ff<<<dim3(G, nrhs), kVecThreads, 0, st>>>(D, x1, x0, p_aux2);
+    else k_dot_partials<<<dim3(G, nrhs), kVecThreads, 0, st>>>(D, x1, x0, p_aux2);
     if (int rc = check_launch(c, "aux2")) return rc;
-    k_cheb_first<<<grid1(D * nrhs), 256, 0, st>>>(D, nrhs, da, db, x0, x1);
-    if (int rc = check_launch(c, "cheb first")) return rc;
-    k_cheb_init<<<dim3(G, nrhs), kVecThreads, 0, st>>>(D, X[0], X[1], x0, x1, dw, p_term);
-    if (int rc = check_launch(c, "cheb init")) return rc;
+    // the start's norms feed only a check before the first term
+    if (faithful)
+      k_cheb_start<true><<<dim3(G, nrhs), kVecThreads, 0, st>>>(D, da, db, X[0], X[1], x0, x1,
+                                                                dw, p_term);
+    else
+      k_cheb_start<false><<<dim3(G, nrhs), kVecThreads, 0, st>>>(D, da, db, X[0], X[1], x0, x1,
+                                                                 dw, p_term);
+    if (int rc = check_launch(c, "cheb start")) return rc;
   }
   for (int r = 0; r < nrhs; ++r) rep[r].n_matvecs = 1;
 
@@ -425,7 +468,8 @@ int cheb_slots(ggem_ctx *c, int nrhs, int N, double eig_min, double eig_max, dou
       if (int rc = matvec_dw_records(c, dw, dm, sm, p_dm)) return rc;
     } else {
       if (int rc = matvec_slots(c, nrhs, dw, dm, sm)) return rc;
-      k_dot_partials<<<dim3(G, nrhs), kVecThreads, 0, st>>>(D, dm, dm, p_dm);
+      if (ff_sums) k_dot_ff<<<dim3(G, nrhs), kVecThreads, 0, st>>>(D, dm, dm, p_dm);
+      else k_dot_partials<<<dim3(G, nrhs), kVecThreads, 0, st>>>(D, dm, dm, p_dm);
       if (int rc = check_launch(c, "dm norm")) return rc;
     }
     // a deferred list build is checked in the same readback; the caller's
@@ -496,7 +540,10 @@ int cheb_slots(ggem_ctx *c, int nrhs, int N, double eig_min, double eig_max, dou
       RhsCoef cf;
       for (int r = 0; r < nrhs; ++r) cf.c[r] = active[r] ? X[i + 1] : 0.0;
       kt_start(c, kKChebTerm);
-      if (check)
+      if (check && ff_sums)
+        k_cheb_term<true, true><<<dim3(G, nrhs), kVecThreads, 0, st>>>(D, two_da, two_db, cf,
+                                                                        x0, x1, xm, dw, p_term);
+      else if (check)
         k_cheb_term<true><<<dim3(G, nrhs), kVecThreads, 0, st>>>(D, two_da, two_db, cf, x0, x1,
                                                                   xm, dw, p_term);
       else

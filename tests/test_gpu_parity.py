@@ -551,8 +551,10 @@ def test_fused_batched_chebyshev_terms_match_unfused_path():
     assert all(r["n_terms"] == N for r in r1 + r2)
     assert fused_n == N - 2  # terms 1 .. N-2; the last term is checked
     assert rel(y2, y1) <= 1e-12
+    # the FP32 series' estimator sums are float-float (~1e-15 relative here);
+    # err1 = sqrt(|a1 - a2| / a2) divides that by err1^2 ~ 7.6e-7
     for a, b in zip(r1, r2):
-        assert b["err1"] == pytest.approx(a["err1"], rel=1e-9)
+        assert b["err1"] == pytest.approx(a["err1"], rel=1e-7)
 
 
 def test_batched_64_rhs_chains_matvec_and_chebyshev():
