@@ -446,8 +446,14 @@ int cheb_slots(ggem_ctx *c, int nrhs, int N, double eig_min, double eig_max, dou
       return rc;
     records_fresh = true;
   } else {
-    if (int rc = permute_to_slots(c, nrhs, xi, x0)) return rc;
-    if (int rc = matvec_slots(c, nrhs, x0, x1, sm)) return rc;
+    int prc = GGEM_OK;
+    if (batch_fused && to_slots_staged(c, nrhs, xi, x0, &prc)) {
+      if (prc) return prc;
+      if (int rc = matvec_slots_prestaged(c, nrhs, x0, x1, sm)) return rc;
+    } else {
+      if (int rc = permute_to_slots(c, nrhs, xi, x0)) return rc;
+      if (int rc = matvec_slots(c, nrhs, x0, x1, sm)) return rc;
+    }
     if (ff_sums) k_dot_ff<<<dim3(G, nrhs), kVecThreads, 0, st>>>(D, x1, x0, p_aux2);
     else k_dot_partials<<<dim3(G, nrhs), kVecThreads, 0, st>>>(D, x1, x0, p_aux2);
     if (int rc = check_launch(c, "aux2")) return rc;
@@ -536,7 +542,10 @@ int cheb_slots(ggem_ctx *c, int nrhs, int N, double eig_min, double eig_max, dou
         return rc;
       staged_fresh = true;
     } else {
-      if (int rc = matvec_slots(c, nrhs, x1, xm, sm)) return rc;
+      // (a fused batched term before this one left x1's staging)
+      if (int rc = batch_fused && staged_fresh ? matvec_slots_prestaged(c, nrhs, x1, xm, sm)
+                                               : matvec_slots(c, nrhs, x1, xm, sm))
+        return rc;
       RhsCoef cf;
       for (int r = 0; r < nrhs; ++r) cf.c[r] = active[r] ? X[i + 1] : 0.0;
       kt_start(c, kKChebTerm);

@@ -274,6 +274,13 @@ int matvec_slots(ggem_ctx *c, int nrhs, const double *d_f_slot, double *d_u_slot
                  int self_mode);
 int matvec_f32_staged(ggem_ctx *c, int nrhs, const double *d_f_slot, double *d_u_slot,
                       int self_mode);
+// xi (caller order) into slot order x0 with its batched FP32 staging in w_fb
+// (16 .. 64 right-hand sides; returns false and does nothing otherwise)
+bool to_slots_staged(ggem_ctx *c, int nrhs, const double *xi, double *x0, int *rc);
+// u = M f for 16 .. 64 right-hand sides whose batched FP32 staging a fused
+// batched term left in w_fb (other counts: matvec_slots)
+int matvec_slots_prestaged(ggem_ctx *c, int nrhs, const double *d_f_slot, double *d_u_slot,
+                           int self_mode);
 double self_coefficient(const ggem_ctx *c, int self_mode);
 int build_pair_tensors(ggem_ctx *c);
 int pair_cheb_term(ggem_ctx *c, bool records_fresh, const double *x0, const double *x1,

@@ -853,6 +853,35 @@ __global__ void __launch_bounds__(256) k_stage_b64(int64_t n, int nr, const doub
   }
 }
 
+// xi (caller order, [r][i][3]) into slot order (x0) and its batched FP32
+// staging in one pass: k_to_slots followed by k_stage_b64
+__global__ void __launch_bounds__(256) k_to_slots_b64(int64_t n, int nr,
+                                                      const int32_t *__restrict__ order,
+                                                      const double *__restrict__ xi,
+                                                      double *__restrict__ x0,
+                                                      float *__restrict__ fb) {
+  __shared__ float t[kBatchR][97];
+  const int64_t s0 = blockIdx.x * 32LL;
+  const int ns = (int)(n - s0 < 32 ? n - s0 : 32);
+  for (int k = threadIdx.x; k < kBatchR * 96; k += blockDim.x) {
+    const int r = k / 96, q = k - r * 96;
+    float v = 0.f;
+    if (r < nr && q < 3 * ns) {
+      const int sl = q / 3, c = q - 3 * sl;
+      const double x = xi[((int64_t)r * n + order[s0 + sl]) * 3 + c];
+      x0[((int64_t)r * n + s0) * 3 + q] = x;
+      v = d2f_bits(x);
+    }
+    t[r][q] = v;
+  }
+  __syncthreads();
+  float *out = fb + s0 * 3 * kBatchR;
+  for (int k = threadIdx.x; k < ns * 3 * kBatchR; k += blockDim.x) {
+    const int sc = k / kBatchR, r = k - sc * kBatchR;
+    out[k] = t[r][sc];
+  }
+}
+
 // forces of row entry q (clamped to the last one) for the two right-hand
 // sides of this lane: fw = fb + lane, jw = the warp's source slots
 __device__ __forceinline__ void b64_fetch(const float2 *__restrict__ fw, const uint32_t *jw, int q,
@@ -1190,7 +1219,9 @@ void launch_b64_cheb(ggem_ctx *c, int nr, const float *fb, float *fb_next, doubl
 }
 
 // many right-hand sides: passes of 64 (k_stage_b64 + k_pair_b64)
-int matvec_b64(ggem_ctx *c, int nrhs, const double *f, double *u, double self_c) {
+// (staged: w_fb already holds the FP32 staging of f, one pass of at most 64)
+int matvec_b64(ggem_ctx *c, int nrhs, const double *f, double *u, double self_c,
+               bool staged = false) {
   const int64_t n = c->n;
   cudaError_t e = c->w_fb.ensure((size_t)n * 3 * kBatchR);
   if (e) return cuda_fail(c, e, "batched staging");
@@ -1199,8 +1230,10 @@ int matvec_b64(ggem_ctx *c, int nrhs, const double *f, double *u, double self_c)
     const int nr = std::min(kBatchR, nrhs - r0);
     const double *fr = f + (int64_t)r0 * n * 3;
     double *ur = u + (int64_t)r0 * n * 3;
-    k_stage_b64<<<(unsigned)((n + 31) / 32), 256, 0, c->stream>>>(n, nr, fr, c->w_fb.p);
-    if (int rc = check_launch(c, "batched staging")) return rc;
+    if (!staged) {
+      k_stage_b64<<<(unsigned)((n + 31) / 32), 256, 0, c->stream>>>(n, nr, fr, c->w_fb.p);
+      if (int rc = check_launch(c, "batched staging")) return rc;
+    }
     kt_start(c, kKPairF32);
     if (c->use_poly) cd2 ? launch_b64_t<2, true>(c, nr, fr, ur, self_c)
                          : launch_b64_t<1, true>(c, nr, fr, ur, self_c);
@@ -1496,6 +1529,31 @@ int matvec_slots(ggem_ctx *c, int nrhs, const double *f, double *u, int self_mod
                                                                        c->w_f32.p);
   if (int rc = check_launch(c, "to f32")) return rc;
   return matvec_f32_staged(c, nrhs, f, u, self_mode);
+}
+
+// xi (caller order) into slot order x0 and, for a batched series, x0's
+// staging in w_fb (then matvec_slots_prestaged); false: nothing done
+bool to_slots_staged(ggem_ctx *c, int nrhs, const double *xi, double *x0, int *rc) {
+  *rc = GGEM_OK;
+  if (c->n == 0 || !batch_term_fusable(c, nrhs)) return false;
+  const int64_t n = c->n;
+  cudaError_t e = c->w_fb.ensure((size_t)n * 3 * kBatchR);
+  if (e) {
+    *rc = cuda_fail(c, e, "batched staging");
+    return true;
+  }
+  k_to_slots_b64<<<(unsigned)((n + 31) / 32), 256, 0, c->stream>>>(n, nrhs, c->order.p, xi, x0,
+                                                                  c->w_fb.p);
+  *rc = check_launch(c, "to slots + staging");
+  return true;
+}
+
+// u = M f when the batched staging of f is already in w_fb (the last fused
+// batched term wrote it): the batched kernel without the staging pass
+int matvec_slots_prestaged(ggem_ctx *c, int nrhs, const double *f, double *u, int self_mode) {
+  if (c->n == 0) return GGEM_OK;
+  if (!batch_term_fusable(c, nrhs)) return matvec_slots(c, nrhs, f, u, self_mode);
+  return matvec_b64(c, nrhs, f, u, self_coefficient(c, self_mode), true);
 }
 
 // FP32 pair sum from the already staged c->w_f32 ([r][n] float4); f is the
