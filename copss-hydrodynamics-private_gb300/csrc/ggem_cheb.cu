@@ -458,13 +458,17 @@ int cheb_slots(ggem_ctx *c, int nrhs, int N, double eig_min, double eig_max, dou
     else k_dot_partials<<<dim3(G, nrhs), kVecThreads, 0, st>>>(D, x1, x0, p_aux2);
     if (int rc = check_launch(c, "aux2")) return rc;
     // the start's norms feed only a check before the first term
-    if (faithful)
+    if (batch_fused) {  // (not faithful) x1's staging for the first fused term
+      if (int rc = cheb_start_staged(c, nrhs, da, db, X[0], X[1], x0, x1, dw)) return rc;
+      staged_fresh = true;
+    } else if (faithful)
       k_cheb_start<true><<<dim3(G, nrhs), kVecThreads, 0, st>>>(D, da, db, X[0], X[1], x0, x1,
                                                                 dw, p_term);
     else
       k_cheb_start<false><<<dim3(G, nrhs), kVecThreads, 0, st>>>(D, da, db, X[0], X[1], x0, x1,
                                                                  dw, p_term);
-    if (int rc = check_launch(c, "cheb start")) return rc;
+    if (!batch_fused)
+      if (int rc = check_launch(c, "cheb start")) return rc;
   }
   for (int r = 0; r < nrhs; ++r) rep[r].n_matvecs = 1;
 

@@ -274,6 +274,10 @@ int matvec_slots(ggem_ctx *c, int nrhs, const double *d_f_slot, double *d_u_slot
                  int self_mode);
 int matvec_f32_staged(ggem_ctx *c, int nrhs, const double *d_f_slot, double *d_u_slot,
                       int self_mode);
+// the batched series' first step (x1 = db x0 + da x1, dw = c0 x0 + c1 x1)
+// with x1's FP32 staging left in w_fb (16 .. 64 right-hand sides)
+int cheb_start_staged(ggem_ctx *c, int nrhs, double da, double db, double c0, double c1,
+                      const double *x0, double *x1, double *dw);
 // xi (caller order) into slot order x0 with its batched FP32 staging in w_fb
 // (16 .. 64 right-hand sides; returns false and does nothing otherwise)
 bool to_slots_staged(ggem_ctx *c, int nrhs, const double *xi, double *x0, int *rc);

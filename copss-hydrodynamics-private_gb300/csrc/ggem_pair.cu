@@ -882,6 +882,40 @@ __global__ void __launch_bounds__(256) k_to_slots_b64(int64_t n, int nr,
   }
 }
 
+// The first step of a batched series in one pass (brownian_system.C:1041,
+// 1050-1056): x1 = db x0 + da x1 (x1 holds M x0 on entry), dw = c0 x0 +
+// c1 x1, and the batched FP32 staging of x1 for the first fused term
+__global__ void __launch_bounds__(256) k_cheb_start_b64(int64_t n, int nr, double da, double db,
+                                                        double c0, double c1,
+                                                        const double *__restrict__ x0,
+                                                        double *__restrict__ x1,
+                                                        double *__restrict__ dw,
+                                                        float *__restrict__ fb) {
+  __shared__ float t[kBatchR][97];
+  const int64_t s0 = blockIdx.x * 32LL;
+  const int ns = (int)(n - s0 < 32 ? n - s0 : 32);
+  for (int k = threadIdx.x; k < kBatchR * 96; k += blockDim.x) {
+    const int r = k / 96, q = k - r * 96;
+    float v = 0.f;
+    if (r < nr && q < 3 * ns) {
+      const int64_t idx = ((int64_t)r * n + s0) * 3 + q;
+      const double x = x0[idx];
+      const double y = db * x + da * x1[idx];
+      x1[idx] = y;
+      const double c0x = c0 * x;
+      dw[idx] = c0x + c1 * y;
+      v = d2f_bits(y);
+    }
+    t[r][q] = v;
+  }
+  __syncthreads();
+  float *out = fb + s0 * 3 * kBatchR;
+  for (int k = threadIdx.x; k < ns * 3 * kBatchR; k += blockDim.x) {
+    const int sc = k / kBatchR, r = k - sc * kBatchR;
+    out[k] = t[r][sc];
+  }
+}
+
 // forces of row entry q (clamped to the last one) for the two right-hand
 // sides of this lane: fw = fb + lane, jw = the warp's source slots
 __device__ __forceinline__ void b64_fetch(const float2 *__restrict__ fw, const uint32_t *jw, int q,
@@ -1546,6 +1580,19 @@ bool to_slots_staged(ggem_ctx *c, int nrhs, const double *xi, double *x0, int *r
                                                                   c->w_fb.p);
   *rc = check_launch(c, "to slots + staging");
   return true;
+}
+
+// the batched series' first step with x1's staging left in w_fb (see
+// k_cheb_start_b64; 16 .. 64 right-hand sides)
+int cheb_start_staged(ggem_ctx *c, int nrhs, double da, double db, double c0, double c1,
+                      const double *x0, double *x1, double *dw) {
+  const int64_t n = c->n;
+  if (n == 0) return GGEM_OK;
+  cudaError_t e = c->w_fb.ensure((size_t)n * 3 * kBatchR);
+  if (e) return cuda_fail(c, e, "batched staging");
+  k_cheb_start_b64<<<(unsigned)((n + 31) / 32), 256, 0, c->stream>>>(n, nrhs, da, db, c0, c1, x0,
+                                                                    x1, dw, c->w_fb.p);
+  return check_launch(c, "cheb start + staging");
 }
 
 // u = M f when the batched staging of f is already in w_fb (the last fused
