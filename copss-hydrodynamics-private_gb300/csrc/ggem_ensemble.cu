@@ -543,6 +543,17 @@ extern "C" int ggem_ensemble_brownian_dev(ggem_ensemble *e, int nrhs, int N,
     tda[b] = 2.0 * da[b];
     tdb[b] = 2.0 * db[b] + tda[b] * e->self_c;  // c1 of the fused term
   }
+  double *x0 = e->v[0].p, *x1 = e->v[1].p, *xm = e->v[2].p, *dw = e->v[3].p, *dm = e->v[4].p;
+  float4 *fa = e->f4[0].p, *fb = e->f4[1].p, *fc = e->f4[2].p;
+  double *aux2 = e->red.p, *q0 = aux2 + K * kR, *q1 = q0 + K * kR, *q2 = q1 + K * kR;
+  const unsigned gv = eblocks(e->ntot * kE, 256);
+  // x0 = xi; x1 = M x0; aux2 = x1 . x0; x1 = db x0 + da x1; dw = c0 x0 + c1 x1
+  k_ens_to_slots<<<gv, 256, 0, e->stream>>>(e->ntot, nrhs, e->order_g.p, d_xi, x0);
+  if (int rc = elaunch(e, "ensemble permute")) return rc;
+  if (int rc = ens_matvec_slots(e, x0, x1, fa, e->self_c)) return rc;
+  if (int rc = ens_dot(e, x1, x0, aux2)) return rc;
+  // the coefficients and tables are prepared on the host while the device
+  // runs the first matvec (nothing before k_ens_start reads them)
   cheb_coeffs_host_many(N, K, da.data(), db.data(), GGEM_CHEB_GAUSS, coef.data(), ldc);
   std::vector<uint8_t> act((size_t)K * kR, 0);
   for (int b = 0; b < K; ++b)
@@ -563,15 +574,6 @@ extern "C" int ggem_ensemble_brownian_dev(ggem_ensemble *e, int nrhs, int N,
                            e->stream)) ||
       (c = cudaMemcpyAsync(e->active.p, act.data(), K * kR, cudaMemcpyHostToDevice, e->stream)))
     return ecuda(e, c, "chebyshev tables");
-  double *x0 = e->v[0].p, *x1 = e->v[1].p, *xm = e->v[2].p, *dw = e->v[3].p, *dm = e->v[4].p;
-  float4 *fa = e->f4[0].p, *fb = e->f4[1].p, *fc = e->f4[2].p;
-  double *aux2 = e->red.p, *q0 = aux2 + K * kR, *q1 = q0 + K * kR, *q2 = q1 + K * kR;
-  const unsigned gv = eblocks(e->ntot * kE, 256);
-  // x0 = xi; x1 = M x0; aux2 = x1 . x0; x1 = db x0 + da x1; dw = c0 x0 + c1 x1
-  k_ens_to_slots<<<gv, 256, 0, e->stream>>>(e->ntot, nrhs, e->order_g.p, d_xi, x0);
-  if (int rc = elaunch(e, "ensemble permute")) return rc;
-  if (int rc = ens_matvec_slots(e, x0, x1, fa, e->self_c)) return rc;
-  if (int rc = ens_dot(e, x1, x0, aux2)) return rc;
   k_ens_start<<<gv, 256, 0, e->stream>>>(e->ntot, e->susp.p, e->da.p, e->db.p, e->coef.p, ldc,
                                         x0, x1, dw);
   if (int rc = elaunch(e, "ensemble start")) return rc;
