@@ -280,10 +280,60 @@ void tridiag_extremes(int k, const double *a, const double *b, double *lmin, dou
 // once; each coefficient keeps the reference's expression and summation
 // order (acc += w_j cos(tmpt) f_j over j), so the values are the same bits
 // as one interval at a time.  coef of interval b starts at coef + b * ldc.
+// c_k of every interval from the nodes x_j and the table w_j cos(tmpt(k, j))
+static void cheb_coeffs_from_table(int N, int K, const double *__restrict__ da,
+                                   const double *__restrict__ db, const double *__restrict__ x,
+                                   const double *__restrict__ wc, double *__restrict__ coef,
+                                   int ldc) {
+  const double PI = kPi;
+  std::vector<double> fjv(N + 1);
+  double *__restrict__ fj = fjv.data();
+  for (int b = 0; b < K; ++b) {
+    for (int j = 0; j <= N; ++j) fj[j] = 1.0 / std::sqrt((x[j] - db[b]) / da[b]);
+    double *cb = coef + (size_t)b * ldc;
+    // four coefficients at a time: four independent sums, each in j order
+    int k = 0;
+    for (; k + 3 <= N; k += 4) {
+      const double *r0 = wc + (size_t)k * (N + 1), *r1 = r0 + (N + 1), *r2 = r1 + (N + 1),
+                   *r3 = r2 + (N + 1);
+      double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+      for (int j = 0; j <= N; ++j) {
+        const double f = fj[j];
+        a0 += r0[j] * f;
+        a1 += r1[j] * f;
+        a2 += r2[j] * f;
+        a3 += r3[j] * f;
+      }
+      cb[k] = a0 * (2. / (PI * (k == 0 ? 2.0 : 1.0)));
+      cb[k + 1] = a1 * (2. / PI);
+      cb[k + 2] = a2 * (2. / PI);
+      cb[k + 3] = a3 * (2. / PI);
+    }
+    for (; k <= N; ++k) {
+      const double *row = wc + (size_t)k * (N + 1);
+      double acc = 0.0;
+      for (int j = 0; j <= N; ++j) acc += row[j] * fj[j];
+      const double ck = (k == 0) ? 2.0 : 1.0;
+      cb[k] = acc * (2. / (PI * ck));
+    }
+  }
+}
+
 void cheb_coeffs_host_many(int N, int K, const double *da, const double *db, int method,
                            double *coef, int ldc) {
-  std::vector<double> x(N + 1), w(N + 1);
+  // the nodes and the w_j cos(tmpt(k, j)) table depend on (N, method) only:
+  // kept per thread for the next call
+  struct Table {
+    int N = -1, method = -1;
+    std::vector<double> x, wc;
+  };
+  thread_local Table T;
   const double PI = kPi;
+  if (T.N == N && T.method == method) {
+    cheb_coeffs_from_table(N, K, da, db, T.x.data(), T.wc.data(), coef, ldc);
+    return;
+  }
+  std::vector<double> x(N + 1), w(N + 1);
   for (int i = 0; i <= N; ++i) {
     const double j = (double)i;
     if (method == GGEM_CHEB_GAUSS_LOBATTO) {
@@ -314,18 +364,11 @@ void cheb_coeffs_host_many(int N, int K, const double *da, const double *db, int
       else tmpt = PI * (double)(2. * j + 1.) * (double)k / (2. * RN + 2.);
       wc[(size_t)k * (N + 1) + j] = w[j] * std::cos(tmpt);
     }
-  std::vector<double> fj(N + 1);
-  for (int b = 0; b < K; ++b) {
-    for (int j = 0; j <= N; ++j) fj[j] = 1.0 / std::sqrt((x[j] - db[b]) / da[b]);
-    double *cb = coef + (size_t)b * ldc;
-    for (int k = 0; k <= N; ++k) {
-      const double *row = wc.data() + (size_t)k * (N + 1);
-      double acc = 0.0;
-      for (int j = 0; j <= N; ++j) acc += row[j] * fj[j];
-      const double ck = (k == 0) ? 2.0 : 1.0;
-      cb[k] = acc * (2. / (PI * ck));
-    }
-  }
+  cheb_coeffs_from_table(N, K, da, db, x.data(), wc.data(), coef, ldc);
+  T.x = std::move(x);
+  T.wc = std::move(wc);
+  T.N = N;
+  T.method = method;
 }
 
 void cheb_coeffs_host(int N, double da, double db, int method, double *coef) {
