@@ -100,3 +100,39 @@ def test_deferred_out_of_domain_reported_by_the_chebyshev_call():
         ctx.build_cells()  # deferred: returns without the verdict
         rc, _, _ = ctx.brownian_displacement(xi, 50, lo / 1.05, hi * 1.05, 1e-3, check_every=0)
         assert rc == G.ERR_OUT_OF_DOMAIN
+
+
+def test_host_buffer_step_matches_device_step_exactly():
+    """ggem_brownian_displacement copies xi on its own stream while the
+    deferred cell and list build runs; the series waits for the copy.  With
+    a different xi every call, the host-buffer step equals the
+    device-pointer step bit for bit (a series that read the previous call's
+    xi would not)."""
+    import torch
+    xyz, L = G.make_suspension(93, 20000, 0.1)
+    n = len(xyz)
+    xis = [np.random.default_rng(50 + k).standard_normal(3 * n) for k in range(4)]
+    with G.Context(box_hi=(L,) * 3, rc=7.0, precision=G.FP32) as ctx:
+        ctx.set_pair_tensors(False)
+        ctx.set_particles(xyz)
+        ctx.build_cells()
+        lo, hi = ctx.lanczos_bounds(k=24, seed=3)
+        lo, hi = lo / 1.05, hi * 1.05
+        ctx.set_deferred_checks(True)
+        host = []
+        for xi in xis:
+            ctx.set_particles(xyz)
+            ctx.build_cells()  # queued, not waited for
+            rc, dw, rep = ctx.brownian_displacement(xi, 50, lo, hi, 1e-3, check_every=0)
+            assert rc == 0, rep
+            host.append(dw.copy())
+        d_xyz = torch.from_numpy(xyz.reshape(-1).copy()).cuda()
+        for xi, want in zip(xis, host):
+            ctx.set_particles_dev(d_xyz.data_ptr(), n)
+            ctx.build_cells()
+            d_xi = torch.from_numpy(xi).cuda()
+            d_dw = torch.empty_like(d_xi)
+            rc, rep = ctx.brownian_displacement_dev(d_xi.data_ptr(), d_dw.data_ptr(), 1, 50, lo,
+                                                    hi, 1e-3, 0)
+            assert rc == 0, rep
+            assert np.array_equal(d_dw.cpu().numpy(), want)
