@@ -337,7 +337,7 @@ __device__ __forceinline__ bool exact_within(const Grid &g, double4_32a a, doubl
 constexpr int kListWarps = 8;     // warps per CTA
 constexpr int kMaxStencil = 128;  // stencil cells per target cell
 
-__global__ void __launch_bounds__(32 * kListWarps) k_pair_list_warp(
+__global__ void __launch_bounds__(32 * kListWarps, 6) k_pair_list_warp(
     Grid g, const int4 *__restrict__ stencil, int nst, const float4 *__restrict__ shift,
     const int32_t *__restrict__ start, const float4 *__restrict__ pos32,
     const double4_32a *__restrict__ pos64, float rc2_lo, float rc2_hi, double rc2, int W,
