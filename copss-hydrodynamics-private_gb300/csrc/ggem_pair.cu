@@ -963,7 +963,7 @@ struct BatchCoef {
 // u is x_{k+1}: u = (2db x1 + 2da M x1) - x0, dw += c_r u, and fb_next
 // receives the FP32 staging of u for the next term.
 template <int CD, bool POLY, bool CHEB>
-__global__ void __launch_bounds__(32 * kBatchWarps, 3) k_pair_b64(
+__global__ void __launch_bounds__(32 * kBatchWarps, 4) k_pair_b64(
     int64_t n, int nr, const float4 *__restrict__ pos32, const float2 *__restrict__ fb,
     const int32_t *__restrict__ cnt, int W, const uint32_t *__restrict__ list, PolyAB P,
     const Rec32 *__restrict__ tab, float inv_ds, float hx, float hy, float hz, float self_hi,
