@@ -51,9 +51,9 @@ CHEB_MAX = 50
 CHEB_TOL = 1e-3
 SEED = 20261203
 # DRAM bytes (read + write) per launch of the dominant pair kernel from one
-# ncu capture of this bench's workload (profiles/k_pair_cheb_N200k.md; ncu
-# flushes the caches before the launch, so this is the cold-cache figure)
-PAIR_TRAFFIC = {"k_pair_cheb": 72.76e6}
+# ncu capture of this bench's workload (ncu flushes the caches before the
+# launch, so this is the cold-cache figure)
+PAIR_TRAFFIC = {"k_pair_cheb": 73.01e6}
 
 
 def measured_peaks():
