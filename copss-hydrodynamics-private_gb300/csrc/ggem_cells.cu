@@ -475,7 +475,7 @@ int build_cells(ggem_ctx *c, bool defer_flags) {
     return cuda_fail(c, e, "cell buffers");
   cudaStream_t st = c->stream;
   // the cell counters are left at zero by the previous build (the
-  // single-block scan zeroes the counts, k_sort_gather the fills); they are
+  // single-block scan zeroes the counts, k_sort_cells the fills); they are
   // cleared here only after a reallocation, an interrupted build or on
   // grids too large for the single-block scan
   const bool small = g.ncell <= kScanCellsMax;
