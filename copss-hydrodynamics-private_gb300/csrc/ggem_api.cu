@@ -253,6 +253,16 @@ int validate_and_setup(ggem_ctx *c) {
   for (int d = 0; d < 3; ++d) {
     g.h32[d] = (float)g.h[d];
     g.inv_h[d] = 1.0 / g.h[d];
+    // FP32 cell index (k_assign): xf - lo32 is within 2^-24 (|x| + |lo| +
+    // |t|) <= 2^-23 (|lo| + |hi|) of x - lo; the margins are four times the
+    // worst case, and the cell band adds the rounding of t / h up to nc
+    const double eps = std::ldexp(1.0, -24);
+    const double mag = std::fabs(g.lo[d]) + std::fabs(g.lo[d] + g.L[d]);
+    g.lo32[d] = (float)g.lo[d];
+    g.L32[d] = (float)g.L[d];
+    g.inv_h32[d] = (float)g.inv_h[d];
+    g.margin32[d] = (float)(8.0 * eps * mag + 1e-30);
+    g.band32[d] = (float)(8.0 * eps * mag / g.h[d] + 8.0 * eps * (g.nc[d] + 2));
   }
   return upload_stencil(c);
 }

@@ -39,6 +39,22 @@ __global__ void k_assign(int64_t n, const double *__restrict__ xyz, Grid g,
   bool bad = false, nonfinite = false;
   for (int d = 0; d < 3; ++d) {
     double x = xyz[3 * i + d];
+    // common case without FP64 arithmetic (GB300 issues FP64 at a small
+    // fraction of the FP32 rate): inside the box away from its faces and
+    // away from the cell faces, the FP32 index is the FP64 one
+    {
+      const float t = d2f_bits(x) - g.lo32[d];  // NaN and infinities fail below
+      if (t > g.margin32[d] && t < g.L32[d] - g.margin32[d]) {
+        const float q = t * g.inv_h32[d];
+        const float fq = floorf(q);
+        if (q - fq > g.band32[d] && (fq + 1.f) - q > g.band32[d]) {
+          const int k = (int)fq;
+          p[d] = x;
+          c[d] = k < 0 ? 0 : (k >= g.nc[d] ? g.nc[d] - 1 : k);
+          continue;
+        }
+      }
+    }
     if (!isfinite(x)) {  // reported as a bad argument; the cell index stays in range
       nonfinite = true;
       x = g.lo[d];
@@ -47,12 +63,14 @@ __global__ void k_assign(int64_t n, const double *__restrict__ xyz, Grid g,
     // (FP64 runs at a small fraction of the FP32 rate: fmod and the division
     // are taken only where they can change the result)
     if (g.periodic[d]) {
-      if (!(t >= 0.0 && t < g.L[d])) {  // inside, fmod(t, L) == t
+      // inside, fmod(t, L) == t; a bead inside the box whose x - lo rounded
+      // up to L keeps t = L and so the last cell (the element search's
+      // closed upper face, point_mesh.C) instead of wrapping to cell 0
+      if (!(t >= 0.0 && t < g.L[d]) && !(x >= g.lo[d] && x < g.lo[d] + g.L[d])) {
         t = fmod(t, g.L[d]);
         if (t < 0) t += g.L[d];
         if (t >= g.L[d]) t = 0.0;
-        // keep the caller's value when it already lies in the box
-        if (!(x >= g.lo[d] && x < g.lo[d] + g.L[d])) x = g.lo[d] + t;
+        x = g.lo[d] + t;  // a caller's value inside the box is kept as it is
       }
     } else if (!(t >= 0.0 && t <= g.L[d])) {
       bad = true;

@@ -57,6 +57,10 @@ struct Grid {
   double lo[3], L[3], h[3];
   double inv_h[3];  // 1 / h, for the fast path of the cell index
   float h32[3];
+  // the cell index in FP32 away from the box faces and the cell faces:
+  // lo, L and 1/h as floats, and the margins (box, in length; cell, in
+  // units of h) beyond which FP32 rounding cannot change the FP64 result
+  float lo32[3], L32[3], inv_h32[3], margin32[3], band32[3];
   int nc[3];
   int periodic[3];
   int64_t ncell;

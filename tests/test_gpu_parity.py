@@ -157,6 +157,45 @@ def test_reference_mode_lists_bit_exact():
         assert np.array_equal(ctx.cell_of_particles(), eop)
 
 
+def _face_points(lo, L, nm, seed):
+    """Beads on every element face of every axis and 1 and 3 ulps either
+    side of it, plus uniform beads, all inside [lo, lo + L)."""
+    rng = np.random.default_rng(seed)
+    lo, L = np.asarray(lo, float), np.asarray(L, float)
+    h = L / nm
+    pts = []
+    for k in range(nm + 1):
+        for d in range(3):
+            for s in (-3, -1, 0, 1, 3):
+                p = lo + rng.uniform(0.05, 0.95, 3) * L
+                x = lo[d] + k * h[d]
+                for _ in range(abs(s)):
+                    x = np.nextafter(x, np.inf if s > 0 else -np.inf)
+                p[d] = x
+                pts.append(p)
+    pts = np.array(pts)
+    pts = pts[np.all((pts >= lo) & (pts < lo + L), axis=1)]
+    return np.concatenate([pts, lo + rng.uniform(0, 1, (2000, 3)) * L])
+
+
+@pytest.mark.parametrize("lo", [(0.0, 0.0, 0.0), (-10.3, 1000.0, 0.1), (-7.0, 3.3, -1e4)])
+def test_element_index_at_element_faces_matches_oracle(lo):
+    """The cell index takes an FP32 shortcut away from the box and element
+    faces; beads on the faces and a few ulps off them, in boxes away from the
+    origin, must still land in the oracle's element."""
+    nm, L = 16, 21.0
+    xyz = _face_points(lo, (L,) * 3, nm, 7)
+    hi = tuple(x + L for x in lo)
+    box = O.make_box(lo, hi, [1, 1, 1])
+    sre = 0.5 * L / nm + 4.0 / 0.5 + 1e-3
+    _, eop = O.elem_lists(box, O.make_mesh(nm, nm, nm, sre), xyz)
+    with G.Context(box_lo=lo, box_hi=hi, nb_mode=G.NB_REFERENCE, n_mesh=(nm,) * 3,
+                   search_radius_e=sre, precision=G.FP64) as ctx:
+        ctx.set_particles(xyz)
+        ctx.build_cells()
+        assert np.array_equal(ctx.cell_of_particles(), eop)
+
+
 @pytest.mark.parametrize("self_mode", [G.SELF_NONE, G.SELF_BEAD, G.SELF_LAGRANGIAN])
 @pytest.mark.parametrize("nrhs", [1, 3])
 def test_fp64_matvec_cutoff(self_mode, nrhs):
