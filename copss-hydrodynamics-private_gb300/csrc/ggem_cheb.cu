@@ -687,7 +687,14 @@ extern "C" int ggem_brownian_displacement(ggem_ctx *ctx, int nrhs, int N, double
   }
   int rc = ggem_brownian_displacement_dev(ctx, nrhs, N, eig_min, eig_max, tol_cheb, check_every,
                                           ctx->w_hin.p, ctx->w_b.p, rep);
-  if (rc) return rc;
+  if (rc) {
+    // the next call's copy stream is ordered only before its own series:
+    // let the kernels this call queued before failing finish reading w_hin
+    // (a successful call synchronises below)
+    cudaStreamSynchronize(ctx->stream);
+    cudaGetLastError();
+    return rc;
+  }
   if (len && (e = cudaMemcpyAsync(dw, ctx->w_b.p, 8 * len, cudaMemcpyDeviceToHost, ctx->stream)))
     return cuda_fail(ctx, e, "bd d2h");
   if ((e = cudaStreamSynchronize(ctx->stream))) return cuda_fail(ctx, e, "bd sync");

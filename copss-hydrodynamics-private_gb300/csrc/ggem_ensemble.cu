@@ -277,11 +277,45 @@ struct ggem_ensemble {
   double *h_red = nullptr;
   int pred_terms = 0;
   int64_t vec_cap = 0;
-  // captured stretches of unchecked terms: (first term, last term) -> graph
+  // captured stretches of unchecked terms: (last term, coefficient stride) -> graph
   std::map<std::pair<int, int>, cudaGraphExec_t> graphs;
+  // what the captured launches hold by value: the bead count, the row width,
+  // the launch shape and the operator's and tables' device pointers.  A
+  // reconfiguration can change any of them (a row overflow widens W, a new
+  // bead count moves ntot, ensure() reallocates a grown buffer), so the
+  // graphs are dropped whenever the signature differs from the captured one.
+  struct GraphSig {
+    int64_t ntot = -1;
+    int W = -1, block = -1;
+    const void *p[14] = {nullptr};
+    bool operator==(const GraphSig &o) const {
+      if (ntot != o.ntot || W != o.W || block != o.block) return false;
+      for (int k = 0; k < 14; ++k)
+        if (p[k] != o.p[k]) return false;
+      return true;
+    }
+  } graph_sig;
+  GraphSig signature() const {
+    GraphSig g;
+    g.ntot = ntot;
+    g.W = W;
+    g.block = block;
+    const void *q[14] = {cnt.p,    list.p, ten.p,  susp.p, coef.p, two_da.p, c1x.p,
+                         active.p, v[0].p, v[1].p, v[2].p, v[3].p, f4[0].p, f4[1].p};
+    for (int k = 0; k < 14; ++k) g.p[k] = q[k];
+    return g;
+  }
   void drop_graphs() {
     for (auto &g : graphs) cudaGraphExecDestroy(g.second);
     graphs.clear();
+  }
+  // drops the captured graphs if anything they hold by value has changed
+  void check_graphs() {
+    const GraphSig now = signature();
+    if (!(now == graph_sig)) {
+      drop_graphs();
+      graph_sig = now;
+    }
   }
 };
 
@@ -591,6 +625,7 @@ extern "C" int ggem_ensemble_brownian_dev(ggem_ensemble *e, int nrhs, int N,
   // terms 1 .. k_first-2 carry no check: one captured graph per stretch
   const int last_unchecked = std::min(k_first - 2, N - 2);
   if (last_unchecked >= 1) {
+    e->check_graphs();
     const auto key = std::make_pair(last_unchecked, ldc);
     auto it = e->graphs.find(key);
     if (it == e->graphs.end()) {

@@ -84,26 +84,38 @@ __global__ void k_na_clear(int64_t ncell, NaBufs b, int *err) {
   if (k == 0) *err = 0;
 }
 
-// cell of each particle (periodic axes wrapped, floor((x - lo) / h))
+// cell of each particle, floor((x - lo) / h) with the context path's rules:
+// a coordinate outside [lo, lo + L) on a periodic axis is wrapped, one
+// inside keeps its value (a bead whose x - lo rounds up to L stays in the
+// last cell, the element search's closed upper face); a NaN or infinite
+// coordinate sets the non-finite status bit and takes cell 0 on that axis
 __global__ void k_na_assign(int64_t n, const double *__restrict__ xyz, Grid g, NaBufs b,
                             int *err) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
   int c[3];
-  bool bad = false;
+  bool bad = false, nonfinite = false;
   for (int d = 0; d < 3; ++d) {
-    double t = xyz[3 * i + d] - g.lo[d];
+    double x = xyz[3 * i + d];
+    if (!isfinite(x)) {
+      nonfinite = true;
+      x = g.lo[d];
+    }
+    double t = x - g.lo[d];
     if (g.periodic[d]) {
-      t = fmod(t, g.L[d]);
-      if (t < 0) t += g.L[d];
-      if (t >= g.L[d]) t = 0.0;
+      if (!(t >= 0.0 && t < g.L[d]) && !(x >= g.lo[d] && x < g.lo[d] + g.L[d])) {
+        t = fmod(t, g.L[d]);
+        if (t < 0) t += g.L[d];
+        if (t >= g.L[d]) t = 0.0;
+      }
     } else if (!(t >= 0.0 && t <= g.L[d])) {
       bad = true;
     }
     const int k = (int)floor(t / g.h[d]);
     c[d] = k < 0 ? 0 : (k >= g.nc[d] ? g.nc[d] - 1 : k);
   }
-  if (bad) atomicOr(err, kErrOutOfDomain);
+  if (bad) atomicOr(err, GGEM_NOALLOC_STATUS_OUT_OF_BOX);
+  if (nonfinite) atomicOr(err, GGEM_NOALLOC_STATUS_NON_FINITE);
   const int32_t id = c[0] + g.nc[0] * (c[1] + g.nc[1] * c[2]);
   b.cell_of[i] = id;
   atomicAdd(&b.count[id], 1);

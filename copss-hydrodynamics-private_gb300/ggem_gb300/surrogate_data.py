@@ -55,6 +55,13 @@ def sample_configs(count, seed, n_range=(1000, 50000), phi_range=(0.02, 0.2)):
     return out
 
 
+def range_kwargs(summary):
+    """the bead-count and volume-fraction ranges of a training run (the
+    summary of save()), as keyword arguments of sample_configs"""
+    return {"n_range": tuple(summary.get("n_range", (1000, 50000))),
+            "phi_range": tuple(summary.get("phi_range", (0.02, 0.2)))}
+
+
 def positions(cfg):
     return make_mixture(cfg["seed"], cfg["n_chains"], BEADS_PER_CHAIN, cfg["n_free"], 2.0,
                         cfg["phi"])

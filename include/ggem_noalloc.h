@@ -42,13 +42,17 @@ extern "C" {
 #define GGEM_NOALLOC_MAX_CELLS 32768
 #define GGEM_NOALLOC_SCRATCH_BYTES 2621696
 
+/* bits of *d_status */
+#define GGEM_NOALLOC_STATUS_OUT_OF_BOX 1 /* a particle outside the box on a non-periodic axis */
+#define GGEM_NOALLOC_STATUS_NON_FINITE 2 /* a coordinate is NaN or infinite */
+
 /* p: constants, box and rc (nb_mode must be GGEM_NB_CUTOFF; precision and
  * device are ignored: FP64 on the current device).  d_xyz[3n], d_f[3n] and
  * d_u[3n] are device arrays in the reference's particle order; d_status is a
- * device int the call sets to 0, or to 1 when a particle lies outside the
- * box on a non-periodic axis.  Work is enqueued on `stream` (a
- * cudaStream_t, NULL for the legacy default stream); the call returns
- * without synchronising. */
+ * device int the call sets to 0, or to the OR of the status bits above (the
+ * context path's GGEM_ERR_OUT_OF_DOMAIN and GGEM_ERR_BAD_ARG); u is then
+ * not meaningful.  Work is enqueued on `stream` (a cudaStream_t, NULL for
+ * the legacy default stream); the call returns without synchronising. */
 int ggem_local_matvec_noalloc(const ggem_params *p, int64_t n, const double *d_xyz,
                               const double *d_f, double *d_u, int self_mode, int *d_status,
                               void *stream);

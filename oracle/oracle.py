@@ -18,7 +18,10 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 LIB_PATH = HERE / "_build" / "libggem_oracle.so"
 REF_LIB_PATH = HERE / "_ref" / "libref_chebyshev.so"
-REF_SRC = Path(os.environ.get("GGEM_REFERENCE_SRC", "/root/reference/src"))
+# the reference tree: GGEM_REFERENCE_SRC, else a checkout named "reference"
+# beside this repository (absent on machines that only run the tests)
+REF_SRC = Path(os.environ.get("GGEM_REFERENCE_SRC",
+                              str(HERE.parent.parent / "reference" / "src")))
 
 POLYMER_BEAD, POINT_PARTICLE, LAGRANGIAN_POINT = 0, 1, 2
 SELF_NONE, SELF_BEAD, SELF_LAGRANGIAN = 0, 1, 2

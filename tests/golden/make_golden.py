@@ -1,7 +1,7 @@
 """Regenerate the committed golden fixtures in tests/golden/.
 
-Run on a machine that has the reference tree (default /root/reference, or
-GGEM_REFERENCE_ROOT).  Two fixtures come out:
+Run on a machine that has the reference tree: GGEM_REFERENCE_ROOT, else a
+checkout named "reference" beside this repository.  Two fixtures come out:
 
 * ggem_profile_3P.json -- the reference's PointParticle_Stokes_GGEM golden
   velocity profiles (tests/integration_tests/resources/PointParticle_Stokes_GGEM/
@@ -33,7 +33,7 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 ROOT = HERE.parent.parent
-REF_ROOT = Path(os.environ.get("GGEM_REFERENCE_ROOT", "/root/reference"))
+REF_ROOT = Path(os.environ.get("GGEM_REFERENCE_ROOT", str(ROOT.parent / "reference")))
 PROFILE_DIR = (REF_ROOT / "tests" / "integration_tests" / "resources"
                / "PointParticle_Stokes_GGEM")
 

@@ -135,3 +135,54 @@ def test_ensemble_intervals_from_the_network():
         assert len(failed) <= 2
         assert all(r["converged"] for rb in reps for r in rb)
     sur.close()
+
+
+def _in_box(seed, L, phi):
+    """a non-overlapping suspension at volume fraction ~phi inside [0, L)^3
+    (generated in the largest box L2 <= L that make_suspension gives for an
+    integer bead count: its minimum-image separations only grow in L)"""
+    n = int(np.floor(phi * L ** 3 * 3.0 / (4.0 * np.pi)))
+    xyz, L2 = G.make_suspension(seed, n, phi)
+    assert L2 <= L + 1e-12
+    return xyz
+
+
+def test_ensemble_reconfiguration_drops_captured_terms():
+    """A Brownian step captures its unchecked terms as a graph that holds the
+    bead count, the row width and the operator's buffers.  After
+    set_particles on denser suspensions (more beads, wider rows, reallocated
+    lists) the next step must not replay the old graph: it gives exactly
+    what a fresh ensemble gives on the same configuration."""
+    import torch
+    boxes = [30.0, 34.0, 38.0]
+    R, N, tol = 8, 4, 1e-14  # 4 terms, nothing converges: the same schedule every call
+    sparse = [_in_box(10 + b, L, 0.03) for b, L in enumerate(boxes)]
+    dense = [_in_box(20 + b, L, 0.2) for b, L in enumerate(boxes)]
+    rng = np.random.default_rng(3)
+    xi_s = _device(rng.standard_normal((sum(len(x) for x in sparse), R, 3)))
+    xi_d = _device(rng.standard_normal((sum(len(x) for x in dense), R, 3)))
+    lo, hi = np.full(3, 0.05), np.full(3, 2.5)
+    with G.Ensemble(boxes) as fresh:
+        fresh.set_particles_dev([len(x) for x in dense], _device(np.concatenate(dense)).data_ptr())
+        d_want = torch.empty_like(xi_d)
+        rc, rep_want = fresh.brownian_dev(R, N, lo, hi, tol, xi_d.data_ptr(), d_want.data_ptr())
+        assert rc == G.ERR_CHEB_NOT_CONVERGED
+        want = d_want.cpu().numpy()
+        w_dense = fresh.sizes()
+    with G.Ensemble(boxes) as ens:
+        d_s = _device(np.concatenate(sparse))
+        ens.set_particles_dev([len(x) for x in sparse], d_s.data_ptr())
+        d_dw = torch.empty_like(xi_s)
+        for _ in range(2):  # captures the graph, then replays it
+            ens.brownian_dev(R, N, lo, hi, tol, xi_s.data_ptr(), d_dw.data_ptr())
+        d_d = _device(np.concatenate(dense))
+        ens.set_particles_dev([len(x) for x in dense], d_d.data_ptr())
+        assert ens.sizes() == w_dense
+        d_dw = torch.empty_like(xi_d)
+        for _ in range(2):
+            rc, reps = ens.brownian_dev(R, N, lo, hi, tol, xi_d.data_ptr(), d_dw.data_ptr())
+            assert rc == G.ERR_CHEB_NOT_CONVERGED
+            got = d_dw.cpu().numpy()
+            assert np.array_equal(got, want)
+            assert [[r["n_terms"] for r in rb] for rb in reps] == \
+                [[r["n_terms"] for r in rb] for rb in rep_want]
