@@ -413,27 +413,46 @@ def run_gb300(args, rank, world):
 
     # ---- plain FP64 GPU path (the comparison baseline) ------------------
     fp64 = None
+    fp64_list = None
     if not args.skip_fp64:
-        st64 = {"reports": []}
+        def fp64_run(c64, path, steps):
+            st64 = {"reports": []}
 
-        def fp64_step(step_id):
-            ctx64.set_particles_dev(d_xyz.data_ptr(), N_BEADS)
-            ctx64.build_cells()
-            ctx64.philox_normals_dev(SEED, step_id, 3 * N_BEADS, d_xi.data_ptr())
-            lo, hi = ctx64.lanczos_bounds(k=24, seed=7)  # every step
-            rc, rep = ctx64.brownian_displacement_dev(d_xi.data_ptr(), d_dw.data_ptr(), 1,
-                                                      CHEB_MAX, lo / 1.05, hi * 1.05, CHEB_TOL,
-                                                      check_every=1)
-            st64["reports"].append(rep[0])
+            def fp64_step(step_id):
+                c64.set_particles_dev(d_xyz.data_ptr(), N_BEADS)
+                c64.build_cells()
+                c64.philox_normals_dev(SEED, step_id, 3 * N_BEADS, d_xi.data_ptr())
+                lo, hi = c64.lanczos_bounds(k=24, seed=7)  # every step
+                rc, rep = c64.brownian_displacement_dev(d_xi.data_ptr(), d_dw.data_ptr(), 1,
+                                                        CHEB_MAX, lo / 1.05, hi * 1.05,
+                                                        CHEB_TOL, check_every=1)
+                st64["reports"].append(rep[0])
 
-        ctx64.set_stream(stream.cuda_stream)
-        ts64 = timed(fp64_step, args.fp64_steps, 1)
-        ctx64.set_stream(0)
-        fp64 = {"steps_per_s": 1e3 / float(np.mean(ts64)) * world,
-                "ms_per_step": float(np.mean(ts64)), "steps": args.fp64_steps,
-                "cheb_terms": [r["n_terms"] for r in st64["reports"][-args.fp64_steps:]],
-                "path": "FP64 cell-stencil pair sweep, Lanczos(24) every step, err1 check "
-                        "every term, one RHS, no graphs"}
+            c64.set_stream(stream.cuda_stream)
+            c64.set_kernel_timing(True)
+            ts64 = timed(fp64_step, steps, 1)
+            k_ms, k_n = c64.kernel_timing(G.KERNEL_PAIR_FP64)
+            c64.set_kernel_timing(False)
+            c64.set_stream(0)
+            return {"steps_per_s": 1e3 / float(np.mean(ts64)) * world,
+                    "ms_per_step": float(np.mean(ts64)), "steps": steps,
+                    "cheb_terms": [r["n_terms"] for r in st64["reports"][-steps:]],
+                    "pair_kernel_ms_avg": k_ms / max(k_n, 1), "pair_kernel_launches": k_n,
+                    "path": path}
+
+        fp64 = fp64_run(ctx64, "B1: FP64 cell-stencil pair sweep (27 cells per bead), "
+                        "Lanczos(24) every step, err1 check every term, one RHS, no graphs",
+                        args.fp64_steps)
+        ctx64l = make_ctx(G.FP64)
+        ctx64l.set_fp64_pair_list(True)
+        fp64_list = fp64_run(ctx64l, "B1 with the FP64 pair kernel over the exact pair list "
+                             "(in-cutoff pairs only, k_pair_list_f64), Lanczos(24) every step, "
+                             "err1 check every term, one RHS, no graphs", max(args.fp64_steps, 3))
+        # the FP64 list kernel against the FP64 pipe: flops per pair with the
+        # FP64 special functions counted as the survey does (erf, exp = 1)
+        fp64_list["pair_kernel_tflops"] = (n_pairs * 47 / (fp64_list["pair_kernel_ms_avg"] * 1e-3)
+                                           / 1e12)
+        ctx64l.close()
     ctx64.close()
 
     # ---- eigen bounds refreshed every step: network vs Lanczos ----------
@@ -474,6 +493,8 @@ def run_gb300(args, rank, world):
     # ---- polymer suspension, 64 batched noise right-hand sides ----------
     poly = None if args.skip_polymer else polymer_leg(G, torch, dev, flush, peak_fn=None)
     ens_res = None if args.skip_ensemble else ensemble_leg(G, torch, dev, flush, sur, sur_margins)
+    spread = None if args.skip_spread else spread_leg(G, torch, dev, flush, xyz, L,
+                                                     ctx.probe_fp32_peak())
 
     # ---- roofline of the dominant kernel --------------------------------
     # the dominant kernel of the timed steps: the fused pair-sum + Chebyshev
@@ -542,6 +563,9 @@ def run_gb300(args, rank, world):
         "matvecs_per_s": matvecs_per_s, "matvec_ms": float(np.mean(mv_ts)),
         "plain_fp64_gpu": fp64,
         "speedup_vs_plain_fp64": (steps_per_s / fp64["steps_per_s"]) if fp64 else None,
+        "plain_fp64_gpu_pair_list": fp64_list,
+        "speedup_vs_plain_fp64_pair_list": (steps_per_s / fp64_list["steps_per_s"])
+        if fp64_list else None,
         "velocity_rel_err_fp32_vs_fp64": rel_err, "velocity_max_component_err": comp_err,
         "cheb": {"terms": [r["n_terms"] for r in reps], "err1_max": max(r["err1"] for r in reps),
                  "converged": all(r["converged"] for r in reps),
@@ -555,6 +579,7 @@ def run_gb300(args, rank, world):
         "clocks": clk.summary(), "wall_s_timed": t_wall,
         "polymer_64rhs": poly,
         "ensemble_512x8": ens_res,
+        "spread": spread,
     }
     if rank == 0 and not args.no_cpu_baseline and world == 1:
         result["cpu_baseline"] = cpu_baseline(xyz, L, state["bounds"], args)
@@ -639,6 +664,115 @@ def polymer_leg(G, torch, dev, flush, peak_fn=None, reps=5):
             "kernel_avg_launch_ms": avg, "kernel_tflops": tf, "fp32_peak_tflops": peak,
             "kernel_frac_of_fp32_peak": tf / peak if peak else None,
             "flops_per_launch": flops}
+
+
+# --------------------------------------------------------------------------
+# Gaussian spread onto the quadrature points of the HEX20 mesh
+# --------------------------------------------------------------------------
+SPREAD_H_MAX = 1.414  # h <= 1/(sqrt(2) alpha), the reference tutorial's mesh rule
+SPREAD_NQ = 8         # QGauss SECOND on the HEX20 velocity element (assemble_stokes.C:397)
+
+
+def spread_leg(G, torch, dev, flush, xyz, L, peak, reps=5, old_fraction=16):
+    """rho at the 8 Gauss points of every element of the box's HEX20 mesh
+    (h = L / ceil(L / 1.414), 144^3 elements at L = 203.1), element
+    neighbour lists of search_radius_e = 0.5 h + 4/alpha, for the N = 200k
+    suspension: the brick kernel in FP32 and FP64, and the per-point FP64
+    kernel on a 1/old_fraction slab of the elements (its per-point work is
+    the same everywhere in a periodic box).  Device resident, L2 flushed
+    before each timed call, CUDA events on the context's stream."""
+    n = len(xyz)
+    nm = int(np.ceil(L / SPREAD_H_MAX))
+    h = L / nm
+    sre = 0.5 * h + 4.0 / ALPHA
+    ctx = G.Context(alpha=ALPHA, box_hi=(L,) * 3, nb_mode=G.NB_REFERENCE, n_mesh=(nm,) * 3,
+                    search_radius_e=sre, precision=G.FP64, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    ctx.set_stream(stream.cuda_stream)
+    d_xyz = torch.from_numpy(xyz.reshape(-1)).cuda()
+    torch.cuda.synchronize()
+    ctx.set_particles_dev(d_xyz.data_ptr(), n)
+    ctx.build_cells()
+    ne = nm ** 3
+    g = [0.5 - 0.5 / np.sqrt(3.0), 0.5 + 0.5 / np.sqrt(3.0)]
+    loc = torch.tensor([[g[a], g[b], g[c]] for c in range(2) for b in range(2) for a in range(2)],
+                       dtype=torch.float64, device="cuda")
+    ar = torch.arange(nm, dtype=torch.float64, device="cuda")
+    ez, ey, ex = torch.meshgrid(ar, ar, ar, indexing="ij")
+    base = torch.stack([ex.reshape(-1), ey.reshape(-1), ez.reshape(-1)], dim=1)
+    q = ((base[:, None, :] + loc[None, :, :]) * h).reshape(-1).contiguous()
+    del base, ex, ey, ez
+    nqt = ne * SPREAD_NQ
+    torch.cuda.synchronize()
+    ctx.set_quadrature_dev(q.data_ptr(), SPREAD_NQ, nqt)
+    f = torch.from_numpy(G.make_normals(SEED + 21, 3 * n)).cuda()
+    rho32 = torch.empty(3 * nqt, dtype=torch.float64, device="cuda")
+    rho64 = torch.empty_like(rho32)
+    torch.cuda.synchronize()
+    pairs = ctx.spread_elements_dev(f.data_ptr(), rho64.data_ptr(), G.FP64, count_pairs=True)
+
+    def time_call(fn, k):
+        ts = []
+        for _ in range(k):
+            flush.zero_()
+            torch.cuda.synchronize()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            b.synchronize()
+            ts.append(a.elapsed_time(b))
+        return float(np.mean(ts)), ts
+
+    for _ in range(2):
+        ctx.spread_elements_dev(f.data_ptr(), rho32.data_ptr(), G.FP32)
+    t32, ts32 = time_call(lambda: ctx.spread_elements_dev(f.data_ptr(), rho32.data_ptr(), G.FP32),
+                          reps)
+    t64, _ = time_call(lambda: ctx.spread_elements_dev(f.data_ptr(), rho64.data_ptr(), G.FP64), 2)
+    # the per-point FP64 kernel (one thread per point, every stencil element
+    # visited) on the first 1/old_fraction of the elements
+    ne_old = ne // old_fraction
+    nq_old = ne_old * SPREAD_NQ
+    qe = torch.arange(ne_old, dtype=torch.int32, device="cuda").repeat_interleave(SPREAD_NQ)
+    rho_old = torch.empty(3 * nq_old, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    ctx.spread_qp_dev(nq_old, q.data_ptr(), qe.data_ptr(), f.data_ptr(), rho_old.data_ptr())
+    t_old, _ = time_call(lambda: ctx.spread_qp_dev(nq_old, q.data_ptr(), qe.data_ptr(),
+                                                   f.data_ptr(), rho_old.data_ptr()), 1)
+    same_old = float(torch.linalg.norm(rho_old - rho64[:3 * nq_old]) /
+                     torch.linalg.norm(rho64[:3 * nq_old]))
+    d = (rho32 - rho64).abs()
+    err = float(torch.linalg.norm(rho32 - rho64) / torch.linalg.norm(rho64))
+    comp = float(d.max() / rho64.abs().max())
+    per = (d / rho64.abs().clamp_min(1e-300))[::7].cpu().numpy()  # a 1/7 sample
+    ctx.close()
+    flops = pairs * 21
+    tf32 = flops / (t32 * 1e-3) / 1e12
+    t_old_full = t_old * old_fraction
+    # algorithmic bytes: per point its FP32 element-relative position (16 B)
+    # and its FP64 rho (24 B); per particle its record (32 B) and force (24 B)
+    byts = nqt * 40 + n * 56
+    return {"workload": f"HEX20 mesh {nm}^3 = {ne} elements (h = {h:.4f}) x {SPREAD_NQ} Gauss "
+                        f"points = {nqt} points, element lists of search_radius_e = "
+                        f"{sre:.4f}, N = {n} beads (phi = {PHI})",
+            "pairs": pairs, "pairs_per_point": pairs / nqt,
+            "fp32_ms": t32, "fp32_ms_all": ts32, "fp64_ms": t64,
+            "pairs_per_s_fp32": pairs / (t32 * 1e-3), "pairs_per_s_fp64": pairs / (t64 * 1e-3),
+            "per_point_fp64_ms_scaled": t_old_full,
+            "per_point_fp64_sample": f"first {ne_old} elements ({nq_old} points), "
+                                    f"{t_old:.2f} ms x {old_fraction}",
+            "per_point_vs_brick_fp64_rel_diff": same_old,
+            "speedup_fp32_vs_per_point_fp64": t_old_full / t32,
+            "speedup_fp32_vs_brick_fp64": t64 / t32,
+            "fp32_vs_fp64_rel_err": err, "fp32_max_component_err": comp,
+            "fp32_per_component_rel_median": float(np.median(per)),
+            "fp32_per_component_rel_p99": float(np.percentile(per, 99)),
+            "roofline": {"bound": "fp32", "kernel": "k_spread_brick<FP32>", "achieved": tf32,
+                         "peak": peak, "unit": "TFLOP/s", "frac": tf32 / peak if peak else None,
+                         "flops_per_launch": flops, "work": "20 flops + 1 exp per (point, "
+                         "listed particle)", "bytes_per_launch": byts,
+                         "hbm_gbs": byts / (t32 * 1e-3) / 1e9}}
 
 
 # --------------------------------------------------------------------------
@@ -823,6 +957,7 @@ def main():
     ap.add_argument("--skip-polymer", action="store_true")
     ap.add_argument("--no-surrogate", action="store_true")
     ap.add_argument("--skip-ensemble", action="store_true")
+    ap.add_argument("--skip-spread", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
 

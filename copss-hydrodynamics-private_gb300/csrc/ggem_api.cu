@@ -424,11 +424,13 @@ extern "C" int ggem_build_cells(ggem_ctx *ctx) {
   if (int rc = settle_list(ctx)) return rc;
   // the FP32 path builds its pair list right after the cells; both error
   // checks then share the list's single host readback
-  const bool with_list = ctx->prm.precision == GGEM_FP32 && ctx->prm.nb_mode == GGEM_NB_CUTOFF;
+  const bool cutoff = ctx->prm.nb_mode == GGEM_NB_CUTOFF;
+  const bool fp32 = ctx->prm.precision == GGEM_FP32;
+  const bool with_list = cutoff && (fp32 || ctx->f64_list);
   if (int rc = build_cells(ctx, with_list)) return rc;
   if (with_list) {
     if (int rc = build_pair_list(ctx)) return rc;
-    return build_pair_tensors(ctx);
+    return fp32 ? build_pair_tensors(ctx) : GGEM_OK;
   }
   return GGEM_OK;
 }
@@ -437,7 +439,7 @@ static int require_built(ggem_ctx *ctx) {
   if (int rc = settle_list(ctx)) return rc;
   if (!ctx->cells_built)
     return fail(ctx, GGEM_ERR_BAD_ARG, "call ggem_build_cells after setting particles");
-  if (ctx->prm.precision == GGEM_FP32 && !ctx->list_built)
+  if ((ctx->prm.precision == GGEM_FP32 || ctx->f64_list) && !ctx->list_built)
     return fail(ctx, GGEM_ERR_BAD_ARG, "pair list not built");
   return GGEM_OK;
 }

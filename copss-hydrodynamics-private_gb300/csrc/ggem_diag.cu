@@ -128,6 +128,16 @@ extern "C" int ggem_get_pair_storage(const ggem_ctx *ctx, int *row_width, int *t
   return GGEM_OK;
 }
 
+extern "C" int ggem_set_fp64_pair_list(ggem_ctx *ctx, int enable) {
+  if (!ctx) return GGEM_ERR_BAD_ARG;
+  if (ctx->prm.precision != GGEM_FP64 || ctx->prm.nb_mode != GGEM_NB_CUTOFF)
+    return ggem::fail(ctx, GGEM_ERR_BAD_ARG, "the FP64 pair list needs a GGEM_FP64 cutoff context");
+  ctx->f64_list = enable != 0;
+  ctx->cells_built = false;  // the next ggem_build_cells builds (or drops) the list
+  ctx->list_built = false;
+  return GGEM_OK;
+}
+
 extern "C" int ggem_set_pair_tensors(ggem_ctx *ctx, int enable) {
   if (!ctx) return GGEM_ERR_BAD_ARG;
   ctx->allow_pretensor = enable != 0;

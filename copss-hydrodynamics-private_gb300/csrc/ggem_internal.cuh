@@ -124,8 +124,10 @@ struct ggem_ctx {
   ggem::DevBuf<float4> pos32;
   ggem::DevBuf<int> err;
 
-  // FP32 pair list
+  // FP32 pair list (built for GGEM_FP64 contexts too when f64_list is set:
+  // the FP64 pair kernel then walks the exact list instead of sweeping cells)
   bool list_built = false;
+  bool f64_list = false;
   // deferred checks (ggem_set_deferred_checks): a build after the first one
   // keeps the row width and leaves its statistics and error word on the
   // device; the next synchronising call reads them (list_unchecked)
@@ -168,6 +170,15 @@ struct ggem_ctx {
   int64_t bond_n = -1;                 // particle count the bonds were set for
   ggem::DevBuf<int64_t> bond_off;      // [n+1]
   ggem::DevBuf<int32_t> bond_nbr;      // [2m]
+
+  // element-major quadrature points of the mesh (ggem_set_quadrature,
+  // reference mode): FP64 as given and FP32 relative to the element centre;
+  // the spread's element-offset bitmap and its pair counter
+  int q_per_elem = 0;
+  ggem::DevBuf<double> q_xyz;
+  ggem::DevBuf<float4> q_rel;
+  ggem::DevBuf<uint32_t> sp_bits;
+  ggem::DevBuf<unsigned long long> sp_pairs;
 
   // scan scratch (one per recursion level)
   std::vector<ggem::DevBuf<int64_t> *> scan_scratch;

@@ -145,6 +145,82 @@ __global__ void __launch_bounds__(128) k_matvec_f64(int64_t n, Grid g, DevConsts
   (void)nrhs_total;
 }
 
+// FP64 pair sum over the exact pair list: only the in-cutoff pairs (the
+// list is the oracle's), the oracle's arithmetic per pair (minimum image of
+// the wrapped FP64 positions, pm_periodic_boundary.C:350-374, and
+// green_tensor_local_regularized with erf and exp in FP64,
+// ggem_stokes.C:304-357); the tensor's two coefficients are formed once per
+// pair and applied to NR right-hand sides.  kGroup lanes per target take
+// every kGroup-th entry of its row and add their sums by shuffles.
+template <int NR>
+__global__ void __launch_bounds__(256) k_pair_list_f64(int64_t n, Grid g, DevConsts K,
+                                                       const int32_t *__restrict__ cnt, int W,
+                                                       const uint32_t *__restrict__ list,
+                                                       const double4_32a *__restrict__ pos64,
+                                                       const double *__restrict__ f,
+                                                       double *__restrict__ u, int self_mode,
+                                                       int r0) {
+  const int64_t gid = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / kGroup;
+  const int sub = (int)(threadIdx.x % kGroup);
+  const bool act = gid < n;
+  const int64_t s = act ? gid : n - 1;
+  const double4_32a pi = pos64[s];
+  const int64_t vstride = 3 * n;
+  double acc[NR][3];
+#pragma unroll
+  for (int q = 0; q < NR; ++q) acc[q][0] = acc[q][1] = acc[q][2] = 0.0;
+  const int m = act ? cnt[s] : 0;
+  const uint32_t *row = list + s * (int64_t)W;
+  for (int k = sub; k < m; k += kGroup) {
+    const int64_t t = (int64_t)(__ldg(row + k) >> kCodeBits);
+    const double4_32a pj = pos64[t];
+    double x[3] = {pj.x - pi.x, pj.y - pi.y, pj.z - pi.z};
+    min_image(g, x);
+    const double r2 = x[0] * x[0] + x[1] * x[1] + x[2] * x[2];
+    const double r = sqrt(r2);
+    if (r < K.r_eps) {
+#pragma unroll
+      for (int q = 0; q < NR; ++q) {
+        const double *fj = f + (int64_t)(r0 + q) * vstride + 3 * t;
+        acc[q][0] += K.coeff_2 * fj[0];
+        acc[q][1] += K.coeff_2 * fj[1];
+        acc[q][2] += K.coeff_2 * fj[2];
+      }
+      continue;
+    }
+    const double kr = K.ksi * r, ar = K.alpha * r;
+    const double c1 = (erf(kr) - erf(ar)) / r;
+    const double c2 = K.two_ksi_sqrt_pi * exp(-kr * kr) - K.two_alpha_sqrt_pi * exp(-ar * ar);
+    const double p = (c1 + c2) * K.one_eight_pi_mu, mc = (c1 - c2) * K.one_eight_pi_mu / r2;
+#pragma unroll
+    for (int q = 0; q < NR; ++q) {
+      const double *fj = f + (int64_t)(r0 + q) * vstride + 3 * t;
+      const double f0 = fj[0], f1 = fj[1], f2 = fj[2];
+      const double xf = (x[0] * f0 + x[1] * f1 + x[2] * f2) * mc;
+      acc[q][0] += p * f0 + xf * x[0];
+      acc[q][1] += p * f1 + xf * x[1];
+      acc[q][2] += p * f2 + xf * x[2];
+    }
+  }
+#pragma unroll
+  for (int o = 1; o < kGroup; o <<= 1)
+#pragma unroll
+    for (int q = 0; q < NR; ++q)
+#pragma unroll
+      for (int a = 0; a < 3; ++a) acc[q][a] += __shfl_xor_sync(0xffffffffu, acc[q][a], o);
+  if (!act || sub != 0) return;
+#pragma unroll
+  for (int q = 0; q < NR; ++q) {
+    const double *fi = f + (int64_t)(r0 + q) * vstride + 3 * s;
+    const double fv[3] = {fi[0], fi[1], fi[2]};
+    self_term(K, self_mode, fv, acc[q]);
+    double *ui = u + (int64_t)(r0 + q) * vstride + 3 * s;
+    ui[0] = acc[q][0];
+    ui[1] = acc[q][1];
+    ui[2] = acc[q][2];
+  }
+}
+
 __device__ __forceinline__ void kahan_add(float &sum, float &comp, float v) {
   const float y = v - comp;
   const float t = sum + y;
@@ -1129,6 +1205,15 @@ __global__ void k_from_slots(int64_t n, int nrhs, const int32_t *__restrict__ ra
 
 template <int NR>
 int launch_f64(ggem_ctx *c, const double *f, double *u, int self_mode, int r0) {
+  if (c->f64_list && c->list_built) {
+    const int64_t threads = c->n * kGroup;
+    kt_start(c, kKPairF64);
+    k_pair_list_f64<NR><<<(unsigned)((threads + 255) / 256), 256, 0, c->stream>>>(
+        c->n, c->grid, c->dc, c->nb_cnt.p, c->nb_w, c->nb_list.p, c->pos64.p, f, u, self_mode,
+        r0);
+    kt_stop(c, kKPairF64);
+    return check_launch(c, "matvec f64 list");
+  }
   const int T = 128;
   const unsigned bn = (unsigned)((c->n + T - 1) / T);
   const bool ref = c->prm.nb_mode == GGEM_NB_REFERENCE;

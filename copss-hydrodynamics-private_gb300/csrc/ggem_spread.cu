@@ -382,6 +382,27 @@ extern "C" int ggem_spread_qp(ggem_ctx *ctx, int64_t nq, const double *qxyz, con
   return GGEM_OK;
 }
 
+extern "C" int ggem_spread_qp_dev(ggem_ctx *ctx, int64_t nq, const double *d_qxyz,
+                                  const int32_t *d_qp_elem, const double *d_f, double spread_rc,
+                                  double *d_rho) {
+  if (!ctx || nq < 0 || (nq > 0 && (!d_qxyz || !d_rho)) || (ctx->n > 0 && !d_f))
+    return GGEM_ERR_BAD_ARG;
+  if (int rc = ggem::settle_list(ctx)) return rc;
+  if (!ctx->cells_built) return ggem::fail(ctx, GGEM_ERR_BAD_ARG, "call ggem_build_cells first");
+  const bool ref = ctx->prm.nb_mode == GGEM_NB_REFERENCE;
+  if (ref && !d_qp_elem && nq > 0)
+    return ggem::fail(ctx, GGEM_ERR_BAD_ARG, "reference mode needs the element of each point");
+  DeviceGuard dg(ctx->device);
+  const size_t n3 = (size_t)ctx->n * 3;
+  cudaError_t e = ctx->w_in.ensure(std::max<size_t>(n3, 1));
+  if (e) return cuda_fail(ctx, e, "spread buffers");
+  if (n3) {
+    if (int rc = permute_to_slots(ctx, 1, d_f, ctx->w_in.p)) return rc;
+  }
+  return field_sums(ctx, 1, nq, d_qxyz, ref ? d_qp_elem : nullptr, spread_radius(ctx, spread_rc),
+                    ctx->w_in.p, d_rho);
+}
+
 extern "C" int ggem_element_rhs(ggem_ctx *ctx, int64_t n_elem, int nq_per_elem, int n_u,
                                 const double *qxyz, const double *int_force, const double *f,
                                 double spread_rc, double *Fe) {

@@ -109,6 +109,11 @@ def lib():
         "ggem_local_field": (i, [vp, i64, vp, vp, vp]),
         "ggem_spread_qp": (i, [vp, i64, vp, vp, vp, d, vp]),
         "ggem_element_rhs": (i, [vp, i64, i, i, vp, vp, vp, d, vp]),
+        "ggem_spread_qp_dev": (i, [vp, i64, vp, vp, vp, d, vp]),
+        "ggem_set_quadrature": (i, [vp, i, vp]),
+        "ggem_set_quadrature_dev": (i, [vp, i, vp]),
+        "ggem_spread_elements": (i, [vp, i, vp, vp]),
+        "ggem_spread_elements_dev": (i, [vp, i, vp, vp, P(i64)]),
         "ggem_cheb_coeffs": (i, [i, d, d, i, vp]),
         "ggem_cheb_inv_sqrt": (i, [vp, i, i, d, d, d, i, vp, P(ChebReport)]),
         "ggem_cheb_inv_sqrt_dev": (i, [vp, i, i, d, d, d, i, vp, P(ChebReport)]),
@@ -118,6 +123,7 @@ def lib():
         "ggem_get_pair_count": (i, [vp, P(i64)]),
         "ggem_get_pair_storage": (i, [vp, P(i), P(i)]),
         "ggem_set_pair_tensors": (i, [vp, i]),
+        "ggem_set_fp64_pair_list": (i, [vp, i]),
         "ggem_autotune_pair_storage": (i, [vp, i, d, P(i), P(d), P(d), P(i)]),
         "ggem_set_pair_variant": (i, [vp, i, i]),
         "ggem_probe_fp32_peak": (i, [vp, P(d)]),
@@ -481,6 +487,39 @@ class Context:
                                            _p(f), float(spread_rc), _p(Fe)))
         return Fe
 
+    def spread_qp_dev(self, nq, d_qxyz, d_qp_elem, d_f, d_rho, spread_rc=0.0):
+        self._check(lib().ggem_spread_qp_dev(self.h, int(nq), C.c_void_p(d_qxyz),
+                                             C.c_void_p(d_qp_elem), C.c_void_p(d_f),
+                                             float(spread_rc), C.c_void_p(d_rho)))
+
+    def set_quadrature(self, qxyz, nq_per_elem):
+        """element-major quadrature points [n_elem * nq][3] (reference mode)"""
+        q = _f64(qxyz).reshape(-1, 3)
+        self._check(lib().ggem_set_quadrature(self.h, int(nq_per_elem), _p(q)))
+        self.nq_per_elem = int(nq_per_elem)
+        self.n_qp = len(q)
+
+    def set_quadrature_dev(self, d_qxyz, nq_per_elem, n_qp):
+        self._check(lib().ggem_set_quadrature_dev(self.h, int(nq_per_elem), C.c_void_p(d_qxyz)))
+        self.nq_per_elem = int(nq_per_elem)
+        self.n_qp = int(n_qp)
+
+    def spread_elements(self, f, precision=FP64):
+        """rho [n_elem * nq][3] at every quadrature point of every element"""
+        f = _f64(f)
+        rho = np.zeros((self.n_qp, 3))
+        self._check(lib().ggem_spread_elements(self.h, int(precision), _p(f), _p(rho)))
+        return rho
+
+    def spread_elements_dev(self, d_f, d_rho, precision=FP64, count_pairs=False):
+        """the device-pointer form; returns the (point, particle) pair count
+        when count_pairs (one host synchronisation)"""
+        pairs = C.c_int64(0)
+        self._check(lib().ggem_spread_elements_dev(self.h, int(precision), C.c_void_p(d_f),
+                                                   C.c_void_p(d_rho),
+                                                   C.byref(pairs) if count_pairs else None))
+        return pairs.value if count_pairs else None
+
     def cheb_inv_sqrt(self, xi, N, eig_min, eig_max, tol, check_every=1):
         xi = _f64(xi).copy()
         nrhs = xi.size // (3 * self.n)
@@ -533,6 +572,10 @@ class Context:
         self._check(lib().ggem_get_launch_trace(self.h, max_events, _p(t), names, C.byref(n)))
         m = min(n.value, max_events)
         return [(float(t[k]), names[k].decode()) for k in range(m)]
+
+    def set_fp64_pair_list(self, enable: bool):
+        """FP64 cutoff contexts: walk the exact pair list instead of the cells"""
+        self._check(lib().ggem_set_fp64_pair_list(self.h, 1 if enable else 0))
 
     def set_pair_tensors(self, enable: bool):
         self._check(lib().ggem_set_pair_tensors(self.h, 1 if enable else 0))

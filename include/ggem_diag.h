@@ -42,6 +42,11 @@ int ggem_get_pair_storage(const ggem_ctx *ctx, int *row_width, int *tensors_stor
 /* allow (1, the default when B(s) >= 0 on [0, rc^2]) or forbid (0) stored
  * pair tensors; takes effect at the next ggem_build_cells */
 int ggem_set_pair_tensors(ggem_ctx *ctx, int enable);
+/* GGEM_FP64 cutoff contexts: 1 = build the exact pair list with the cells
+ * and walk it in the FP64 pair kernel (only in-cutoff pairs, the
+ * reference's FP64 arithmetic per pair); 0 (default) = sweep the 27 cells
+ * around every bead.  Takes effect at the next ggem_build_cells. */
+int ggem_set_fp64_pair_list(ggem_ctx *ctx, int enable);
 /* autotune the pair storage on the current configuration (cells and list
  * built, FP32): times `reps` single-RHS matvecs with tensors evaluated per
  * pair and with stored tensors (plus the one tensor pass per build,
@@ -65,7 +70,7 @@ int ggem_probe_fp32_peak(ggem_ctx *ctx, double *tflops);
  * every launch of the kernels below; totals are read back (with a stream
  * synchronisation) by ggem_get_kernel_timing.  Enabling resets the totals. */
 #define GGEM_KERNEL_PAIR_FP32 0  /* FP32 pair-list sum                        */
-#define GGEM_KERNEL_PAIR_FP64 1  /* FP64 cell-stencil sum                     */
+#define GGEM_KERNEL_PAIR_FP64 1  /* FP64 pair sum (cell sweep or pair list)   */
 #define GGEM_KERNEL_CHEB_TERM 2  /* fused Chebyshev term                       */
 #define GGEM_KERNEL_LIST_BUILD 3 /* pair-list count + fill                     */
 #define GGEM_KERNEL_PAIR_CHEB 4  /* FP32 pair sum with the Chebyshev term fused */

@@ -180,12 +180,37 @@ int ggem_local_field(ggem_ctx *ctx, int64_t nt, const double *targets, const dou
  * 0.5*hmax + 4/alpha) are used and qp_elem may be NULL. */
 int ggem_spread_qp(ggem_ctx *ctx, int64_t nq, const double *qxyz, const int32_t *qp_elem,
                    const double *f, double spread_rc, double *rho);
+/* the same with device arrays (f in the caller's particle order) */
+int ggem_spread_qp_dev(ggem_ctx *ctx, int64_t nq, const double *d_qxyz, const int32_t *d_qp_elem,
+                       const double *d_f, double spread_rc, double *d_rho);
 /* fused element right-hand side, assemble_stokes.C:645-671 with the cached
  * JxW*phi of assemble_int_force (:733-757): for each element e,
  * Fe[e][j*n_u + l] = sum_q int_force[e][l*nq + q] * rho_j(q_e,q) */
 int ggem_element_rhs(ggem_ctx *ctx, int64_t n_elem, int nq_per_elem, int n_u,
                      const double *qxyz, const double *int_force, const double *f,
                      double spread_rc, double *Fe);
+
+/* ---- Gaussian spreading onto every element's quadrature points --------- */
+/* The quadrature points of the mesh, element-major: qxyz[(e * nq + q) * 3 + d]
+ * for the n_mesh[0] * n_mesh[1] * n_mesh[2] elements in the reference's
+ * build_cube order (x fastest), nq_per_elem in [1, 32] each (8 for the
+ * QGauss SECOND rule of the HEX20 velocity element, assemble_stokes.C:397).
+ * Reference mode only.  The points are kept on the device (the mesh is fixed
+ * for a run; the reference takes them from fe->get_xyz() per element,
+ * assemble_stokes.C:404). */
+int ggem_set_quadrature(ggem_ctx *ctx, int nq_per_elem, const double *qxyz);
+int ggem_set_quadrature_dev(ggem_ctx *ctx, int nq_per_elem, const double *d_qxyz);
+/* rho at every quadrature point of every element: the loop of
+ * AssembleStokes::compute_element_rhs over the element neighbour list
+ * (assemble_stokes.C:645-662) with GGEMStokes::smoothed_force_exp
+ * (ggem_stokes.C:117-128) for all elements at once.  f[3n] in the caller's
+ * particle order; rho[(e * nq + q) * 3 + d].  precision GGEM_FP64 (the
+ * reference's arithmetic) or GGEM_FP32 (element-relative coordinates, error
+ * stated against FP64).  pairs (may be NULL) receives the number of
+ * (quadrature point, listed particle) pairs summed. */
+int ggem_spread_elements(ggem_ctx *ctx, int precision, const double *f, double *rho);
+int ggem_spread_elements_dev(ggem_ctx *ctx, int precision, const double *d_f, double *d_rho,
+                             int64_t *pairs);
 
 /* ---- Chebyshev and spectral bounds ------------------------------------ */
 /* Chebyshev::chebyshev_coefficients (chebyshev.C:57-107), N+1 values */

@@ -116,10 +116,10 @@ def _cfg1_mode(mode):
     return xyz, L, box, nb, kw, want_off, want_ids
 
 
-@pytest.mark.parametrize("mode", ["cutoff", "reference"])
+@pytest.mark.parametrize("mode", ["cutoff", "reference", "cutoff-list"])
 def test_cfg1_lists_matvec_and_faithful_series(mode):
     t0 = time.perf_counter()
-    xyz, L, box, nb, kw, want_off, want_ids = _cfg1_mode(mode)
+    xyz, L, box, nb, kw, want_off, want_ids = _cfg1_mode(mode.split("-")[0])
     c = O.constants(alpha=ALPHA)
     n = len(xyz)
     f = np.random.default_rng(5).standard_normal((n, 3))
@@ -129,6 +129,8 @@ def test_cfg1_lists_matvec_and_faithful_series(mode):
     # the reference's noise stream (random_generator.C:43-67)
     xi = O.std_normal_vector(123456789, 3 * n)
     with G.Context(alpha=ALPHA, box_hi=(L,) * 3, precision=G.FP64, **kw) as ctx:
+        if mode == "cutoff-list":  # the FP64 pair kernel over the exact list
+            ctx.set_fp64_pair_list(True)
         ctx.set_particles(xyz)
         ctx.build_cells()
         off, ids = ctx.neighbors()
@@ -204,8 +206,11 @@ def test_cfg2_N200k_lists_fp64_and_fp32_matvecs():
     f = np.random.default_rng(17).standard_normal((len(xyz), 3))
     u_o = O.local_matvec(c, box, xyz, nb, f, O.SELF_BEAD, nthreads=THREADS)
     _timed("cfg2 oracle", t0)
-    for prec in (G.FP64, G.FP32):
+    # FP64 with the cell sweep, FP64 over the exact pair list, FP32
+    for prec, f64_list in ((G.FP64, False), (G.FP64, True), (G.FP32, False)):
         with G.Context(alpha=ALPHA, box_hi=(L,) * 3, rc=RC, precision=prec) as ctx:
+            if f64_list:
+                ctx.set_fp64_pair_list(True)
             ctx.set_particles(xyz)
             ctx.build_cells()
             off, ids = ctx.neighbors()
@@ -215,7 +220,8 @@ def test_cfg2_N200k_lists_fp64_and_fp32_matvecs():
         err = rel(u, u_o)
         comp = np.abs(u - u_o).max() / np.abs(u_o).max()
         per = np.abs(u - u_o) / np.maximum(np.abs(u_o), 1e-300)
-        print(f"cfg2 precision {prec}: pairs {nb.offsets[-1]}, norm-wise {err:.2e}, "
+        print(f"cfg2 precision {prec} (pair list {f64_list or prec == G.FP32}): "
+              f"pairs {nb.offsets[-1]}, norm-wise {err:.2e}, "
               f"max component {comp:.2e} of the largest, median per-component relative "
               f"{np.median(per):.2e}, 99.9th percentile {np.percentile(per, 99.9):.2e}")
         assert err <= (FP64_TOL if prec == G.FP64 else FP32_TOL)
