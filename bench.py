@@ -262,7 +262,8 @@ def run_gb300(args, rank, world):
     p_xyz, p_xi, p_dw = (C.c_void_p(t.data_ptr()) for t in (d_xyz, d_xi, d_dw))
     rep_buf = (G.ChebReport * 1)()
 
-    def device_step(step_id):
+    def device_step(step_id, check_every=None):
+        ce = args.check_every if check_every is None else check_every
         rc = L_lib.ggem_set_particles_dev(ctx.h, N_BEADS, p_xyz)
         rc |= L_lib.ggem_build_cells(ctx.h)
         rc |= L_lib.ggem_philox_normals_dev(ctx.h, SEED, step_id, 3 * N_BEADS, p_xi)
@@ -273,7 +274,7 @@ def run_gb300(args, rank, world):
         for attempt in range(2):
             lo, hi = state["bounds"]
             rc = L_lib.ggem_brownian_displacement_dev(ctx.h, 1, CHEB_MAX, lo, hi, CHEB_TOL,
-                                                      args.check_every, p_xi, p_dw, rep_buf)
+                                                      ce, p_xi, p_dw, rep_buf)
             if rc == 0:
                 state["reports"].append(bytes(rep_buf))  # parsed after the timing
                 return
@@ -325,6 +326,24 @@ def run_gb300(args, rank, world):
     ms_step, steps_per_s = replica_throughput(float(np.mean(ts)), world)
     n_pairs = ctx.pair_count()
     reps = [G.ChebReport.from_buffer_copy(b).as_dict() for b in state["reports"][-args.steps:]]
+
+    # ---- the reference's schedule: the err1 check after every term --------
+    # (brownian_system.C:1089-1155: two matvecs per term), the same work per
+    # step as the reference arm, which runs that schedule on the host
+    faithful = None
+    if args.check_every != 1:
+        n_rep0 = len(state["reports"])
+        ts_f = timed(lambda s_: device_step(s_, check_every=1), args.steps, 3)
+        f_reps = [G.ChebReport.from_buffer_copy(b).as_dict() for b in state["reports"][n_rep0:]]
+        f_reps = f_reps[-args.steps:]
+        faithful = {"steps_per_s": 1e3 / float(np.mean(ts_f)) * world,
+                    "ms_per_step": float(np.mean(ts_f)), "check_every": 1,
+                    "cheb_terms": sorted({r["n_terms"] for r in f_reps}),
+                    # the series' operator applications (the final dw = M y is
+                    # the last check's M dw, so no further matvec)
+                    "series_matvecs_per_step": float(np.mean([r["n_matvecs"] for r in f_reps])),
+                    "adaptive_series_matvecs_per_step": float(np.mean([r["n_matvecs"]
+                                                                       for r in reps]))}
 
     # ---- e2e through the host-pointer ABI --------------------------------
     h_xyz = torch.from_numpy(xyz.reshape(-1).copy()).pin_memory()
@@ -573,6 +592,7 @@ def run_gb300(args, rank, world):
                  "surrogate_calls": state["surrogate_calls"],
                  "lanczos_calls": state["lanczos_calls"]},
         "bounds_every_step": per_step,
+        "check_every_term": faithful,
         "roofline": roof,
         "kernel_ms_in_timed_region": {k: v[0] for k, v in kt.items()},
         "gpu_launches": int(lc1 - lc0),
@@ -953,7 +973,7 @@ def main():
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-steps", type=int, default=3)
-    ap.add_argument("--reference-max-steps", type=int, default=6)
+    ap.add_argument("--reference-max-steps", type=int, default=30)
     ap.add_argument("--skip-polymer", action="store_true")
     ap.add_argument("--no-surrogate", action="store_true")
     ap.add_argument("--skip-ensemble", action="store_true")

@@ -238,6 +238,277 @@ __global__ void k_ens_dot_fin(const int32_t *__restrict__ coff, const double *__
   out[b * kR + r] = t;
 }
 
+// ---- the whole Brownian series of every suspension in one launch ----------
+// A persistent cooperative kernel walks a fixed list of passes:
+//   START       m = M x0, x0 . m per series, x1 = db x0 + da m,
+//               dw = c0 x0 + c1 x1, FP32 forces of x1
+//   TERM        x_{k+1} = 2da M x_k + (c1 x_k - x_{k-1}), dw += c_{k+1} x_{k+1}
+//               (brownian_system.C:1091-1108)
+//   TERM_CHECK  the same, plus |dw|^2 before the term, |x_{k+1}|^2 and the
+//               FP32 forces of the new dw
+//   CHECK       M dw, |M dw|^2; the stopping decision of every series of the
+//               suspension (brownian_system.C:1117-1155): err1 <= tol
+//               converged, err2 <= 1e-9 stopped
+// Each pass is cut into tiles of S slots of one suspension.  A tile of
+// pass p waits until its suspension has completed pass p - 1 (a per-
+// suspension counter that the suspension's last tile of a pass advances,
+// after the decision when the pass is a CHECK); nothing waits on other
+// suspensions, so suspensions of different sizes and states overlap.  Block
+// c takes tiles c, c + G, c + 2G, ... in order: a tile only waits on tiles
+// of smaller index, all of which are held by running blocks (the launch is
+// cooperative, every block resident), so the smallest unfinished tile can
+// always proceed.  Every wait is bounded: a block that gives up sets the
+// error word and all blocks leave.  Data written inside the launch is read
+// through L2 (ld.global.cg): another block's writes are never served from a
+// stale L1 line.  The estimator sums are per tile and then per suspension
+// in tile order (deterministic).
+enum : int { kPassStart = 0, kPassTerm = 1, kPassTermCheck = 2, kPassCheck = 3 };
+constexpr int kSeriesThreads = 256;
+constexpr int kPartKinds = 4;  // aux2 (x0 . M x0), |dw|^2, |x_{k+1}|^2, |M dw|^2
+
+struct SeriesArgs {
+  int64_t ntot;
+  int W, K, S, T, npass, ldc;
+  double tol, self_c;
+  const int32_t *cnt;
+  const uint32_t *list;
+  const float4 *ten;
+  const int32_t *susp;
+  const int32_t *tile_b;      // [T] suspension of every tile of a pass
+  const int64_t *tile_s0;     // [T] first slot of every tile
+  const int32_t *susp_tile0;  // [K + 1] first tile of every suspension
+  const int64_t *off;         // [K + 1] first slot of every suspension
+  const int32_t *pass_type;   // [npass]
+  const int32_t *pass_term;   // [npass] term index t (x_{t+1} is formed)
+  double *X0, *X1, *X2, *dw, *dm;
+  float4 *F0, *F1, *Fdw;
+  const double *da, *db, *two_da, *c1x, *coef;
+  uint8_t *active;            // [K * 8]
+  ggem_cheb_report *rep;      // [K * 8]
+  double *part;               // [T][kPartKinds][8]
+  double *aux2;               // [K * 8]
+  unsigned int *arrive, *done;  // [K] tiles finished / passes completed
+  int *n_active, *all_done, *err;
+  uint32_t polls;
+  int never_ready;            // test hook: every wait runs out
+};
+
+__device__ __forceinline__ double series_x(const SeriesArgs &a, int q, int64_t k) {
+  const double *X = q == 0 ? a.X0 : (q == 1 ? a.X1 : a.X2);
+  return __ldcg(X + k);
+}
+__device__ __forceinline__ double *series_xp(const SeriesArgs &a, int q) {
+  return q == 0 ? a.X0 : (q == 1 ? a.X1 : a.X2);
+}
+
+// sum over r-lanes of a per-thread value: lane % 8 is the right-hand side;
+// sums of the 8 right-hand sides land in sh[w][r], then in out[r] (warps in
+// order; fixed tree, deterministic)
+__device__ __forceinline__ void tile_rsum(double v, double (*sh)[kR], double *out) {
+  v += __shfl_xor_sync(0xffffffffu, v, 8);
+  v += __shfl_xor_sync(0xffffffffu, v, 16);
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane < kR) sh[w][lane] = v;
+  __syncthreads();
+  if (threadIdx.x < kR) {
+    double t = 0.0;
+    for (int q = 0; q < kSeriesThreads / 32; ++q) t += sh[q][threadIdx.x];
+    out[threadIdx.x] = t;
+  }
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(kSeriesThreads) k_ens_series(SeriesArgs a) {
+  __shared__ double sh[kSeriesThreads / 32][kR];
+  __shared__ double dsum[kPartKinds][kR];
+  __shared__ int s_go, s_last;
+  const int tid = threadIdx.x;
+  const int64_t total = (int64_t)a.T * a.npass;
+  for (int64_t g = blockIdx.x; g < total; g += gridDim.x) {
+    const int p = (int)(g / a.T);
+    const int tl = (int)(g - (int64_t)p * a.T);
+    const int b = a.tile_b[tl];
+    const int type = a.pass_type[p], t = a.pass_term[p];
+    // ---- wait until this suspension has completed pass p - 1 ----
+    if (tid == 0) {
+      int go = 1;
+      const unsigned need = (unsigned)p + (a.never_ready ? 0x40000000u : 0u);
+      uint32_t n = 0;
+      while (true) {
+        if (*(volatile int *)a.err || *(volatile int *)a.all_done) {
+          go = 0;
+          break;
+        }
+        if (*(volatile unsigned *)(a.done + b) >= need) break;
+        if (++n > a.polls) {
+          atomicOr(a.err, kErrTimeout);
+          go = 0;
+          break;
+        }
+        __nanosleep(128);
+      }
+      __threadfence();
+      s_go = go;
+    }
+    __syncthreads();
+    if (!s_go) return;  // an error, or every series has stopped
+    const int64_t s_begin = a.tile_s0[tl];
+    const int64_t s_end = min(s_begin + a.S, a.off[b + 1]);
+    const double tda = a.two_da[b], c1 = a.c1x[b];
+    const int q0 = (t + 2) % 3, q1 = t % 3, qm = (t + 1) % 3;  // x_{t-1}, x_t, x_{t+1}
+    const float4 *Fsrc = type == kPassStart ? a.F1
+                                            : (type == kPassCheck ? a.Fdw
+                                                                  : ((t - 1) % 2 ? a.F1 : a.F0));
+    float4 *Fout = type == kPassStart ? a.F0 : (t % 2 ? a.F1 : a.F0);
+    double v0 = 0.0, v1 = 0.0;  // this thread's estimator terms
+    for (int64_t i = tid; i < (int64_t)a.S * kR; i += kSeriesThreads) {
+      const int64_t s = s_begin + i / kR;
+      const int r = (int)(i % kR);
+      if (s >= s_end) continue;
+      const uint8_t act = *(volatile const uint8_t *)(a.active + b * kR + r);
+      // pair sum over the stored tensors (entries and tensors are read-only)
+      const int64_t e0 = s * (int64_t)a.W, e1 = e0 + __ldg(a.cnt + s);
+      float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
+      float bx = 0.f, by = 0.f, bz = 0.f;
+      int blk = 0;
+      for (int64_t m = e0; m < e1; ++m) {
+        const uint32_t en = __ldg(a.list + m);
+        const float4 tt = __ldg(a.ten + m);
+        const float4 fj = __ldcg(Fsrc + (int64_t)(en >> kCodeBits) * kR + r);
+        const float d = fmaf(tt.w, fj.z, fmaf(tt.z, fj.y, tt.y * fj.x));
+        bx += fmaf(tt.x, fj.x, d * tt.y);
+        by += fmaf(tt.x, fj.y, d * tt.z);
+        bz += fmaf(tt.x, fj.z, d * tt.w);
+        if (++blk == 8) {
+          kahan(sx, cx, bx);
+          kahan(sy, cy, by);
+          kahan(sz, cz, bz);
+          bx = by = bz = 0.f;
+          blk = 0;
+        }
+      }
+      kahan(sx, cx, bx);
+      kahan(sy, cy, by);
+      kahan(sz, cz, bz);
+      const float hs[3] = {sx, sy, sz}, ls[3] = {-cx, -cy, -cz};
+      const int64_t k0 = (s * kR + r) * 3;
+      float out[3];
+      if (type == kPassStart) {
+        const double cc0 = __ldg(a.coef + (int64_t)b * a.ldc),
+                     cc1 = __ldg(a.coef + (int64_t)b * a.ldc + 1);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          const double x0 = __ldcg(a.X0 + k0 + c);
+          const double m = fma(a.self_c, x0, f2d(hs[c]) + f2d(ls[c]));
+          v0 = fma(x0, m, v0);
+          const double x1 = a.db[b] * x0 + a.da[b] * m;
+          a.X1[k0 + c] = x1;
+          a.dw[k0 + c] = cc0 * x0 + cc1 * x1;
+          out[c] = d2f_bits(x1);
+        }
+        Fout[s * kR + r] = make_float4(out[0], out[1], out[2], 0.f);
+      } else if (type == kPassCheck) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          const double m = fma(a.self_c, __ldcg(a.dw + k0 + c), f2d(hs[c]) + f2d(ls[c]));
+          v0 = fma(m, m, v0);
+          if (act) a.dm[k0 + c] = m;  // a stopped series keeps its final M y
+        }
+      } else {
+        const double cf = act ? __ldg(a.coef + (int64_t)b * a.ldc + t + 1) : 0.0;
+        double *XM = series_xp(a, qm);
+        float o2[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          const double xk = series_x(a, q1, k0 + c);
+          const double v = fma(tda, f2d(hs[c]) + f2d(ls[c]), fma(c1, xk, -series_x(a, q0, k0 + c)));
+          XM[k0 + c] = v;
+          const double y = __ldcg(a.dw + k0 + c);
+          const double yn = fma(cf, v, y);
+          a.dw[k0 + c] = yn;
+          out[c] = d2f_bits(v);
+          o2[c] = d2f_bits(yn);
+          if (type == kPassTermCheck) {
+            v0 = fma(y, y, v0);
+            v1 = fma(v, v, v1);
+          }
+        }
+        Fout[s * kR + r] = make_float4(out[0], out[1], out[2], 0.f);
+        if (type == kPassTermCheck) a.Fdw[s * kR + r] = make_float4(o2[0], o2[1], o2[2], 0.f);
+      }
+    }
+    // ---- this tile's estimator sums ----
+    double *pt = a.part + (int64_t)tl * kPartKinds * kR;
+    if (type == kPassStart) tile_rsum(v0, sh, pt + 0 * kR);
+    if (type == kPassTermCheck) {
+      tile_rsum(v0, sh, pt + 1 * kR);
+      tile_rsum(v1, sh, pt + 2 * kR);
+    }
+    if (type == kPassCheck) tile_rsum(v0, sh, pt + 3 * kR);
+    // ---- finish the tile; the suspension's last tile of the pass completes it ----
+    __syncthreads();
+    const int nt = a.susp_tile0[b + 1] - a.susp_tile0[b];
+    if (tid == 0) {
+      __threadfence();
+      const unsigned old = atomicAdd(a.arrive + b, 1u);
+      s_last = old == (unsigned)(p + 1) * (unsigned)nt - 1u;
+      if (s_last) __threadfence();
+    }
+    __syncthreads();
+    if (!s_last) continue;
+    if (type == kPassStart || type == kPassCheck) {
+      // the suspension's sums in tile order (fixed assignment and tree)
+      const int kind = type == kPassStart ? 0 : 3;
+      const int nk = type == kPassStart ? 1 : 3;
+      for (int q = 0; q < nk; ++q) {
+        const int kd = type == kPassStart ? 0 : q + 1;
+        double acc = 0.0;
+        const int r = tid % kR;
+        for (int j = tid / kR; j < nt; j += kSeriesThreads / kR)
+          acc += __ldcg(a.part + ((int64_t)(a.susp_tile0[b] + j) * kPartKinds + kd) * kR + r);
+        tile_rsum(acc, sh, dsum[kd]);
+      }
+      (void)kind;
+      if (tid < kR) {
+        // (state written by other blocks is read through L2: volatile / .cg)
+        const int r = tid, sr = b * kR + r;
+        if (type == kPassStart) {
+          a.aux2[sr] = dsum[0][r];
+        } else if (*(volatile const uint8_t *)(a.active + sr)) {
+          volatile ggem_cheb_report *R = a.rep + sr;
+          R->n_terms = t + 1;
+          const double a2 = __ldcg(a.aux2 + sr);
+          const double aux4 = sqrt(dsum[1][r]);
+          const double aux3 = sqrt(dsum[2][r]) * fabs(__ldg(a.coef + (int64_t)b * a.ldc + t + 1));
+          double e1 = R->err1, e2 = R->err2;
+          if (a2 != 0.0) e1 = sqrt(fabs(dsum[3][r] - a2) / a2);
+          if (aux4 != 0.0) e2 = aux3 / aux4;
+          R->err1 = e1;
+          R->err2 = e2;
+          bool stop = false;
+          if (e1 <= a.tol) {  // brownian_system.C:1138-1147
+            R->converged = 1;
+            stop = true;
+          } else if (e2 <= 1e-9) {  // :1150
+            stop = true;
+          }
+          if (stop) {
+            a.active[sr] = 0;
+            if (atomicSub(a.n_active, 1) == 1) atomicExch(a.all_done, 1);
+          }
+        }
+      }
+    } else if (tid < kR && *(volatile const uint8_t *)(a.active + b * kR + tid)) {
+      ((volatile ggem_cheb_report *)a.rep)[b * kR + tid].n_terms = t + 1;
+    }
+    __syncthreads();
+    if (tid == 0) {
+      __threadfence();
+      atomicExch(a.done + b, (unsigned)(p + 1));
+    }
+  }
+}
+
 }  // namespace ens
 }  // namespace ggem
 
@@ -277,6 +548,20 @@ struct ggem_ensemble {
   double *h_red = nullptr;
   int pred_terms = 0;
   int64_t vec_cap = 0;
+  // the persistent series launch (k_ens_series): tiles of S slots of one
+  // suspension, their per-pass estimator partials, counters and reports
+  bool persistent = true;
+  int S = 64;                  // slots per tile (autotuned)
+  int T = 0;                   // tiles per pass
+  int tiles_for_S = 0;         // S the tile tables were built for
+  int64_t tiles_for_ntot = -1;
+  DevBuf<int32_t> tile_b, susp_tile0, pass_type, pass_term;
+  DevBuf<int64_t> tile_s0;
+  DevBuf<double> part, aux2;
+  DevBuf<unsigned int> sync;   // arrive[K], done[K], n_active, all_done, err
+  DevBuf<ggem_cheb_report> d_rep;
+  uint32_t series_polls = 1u << 26;  // bounded waits of the persistent launch
+  int never_ready = 0;               // test hook: every wait runs out
   // captured stretches of unchecked terms: (last term, coefficient stride) -> graph
   std::map<std::pair<int, int>, cudaGraphExec_t> graphs;
   // what the captured launches hold by value: the bead count, the row width,
@@ -555,6 +840,228 @@ int ens_dot(ggem_ensemble *e, const double *a, const double *b, double *out) {
 
 }  // namespace
 
+namespace {
+
+// tile tables of the persistent launch for the current bead counts and S
+int ensure_tiles(ggem_ensemble *e) {
+  if (e->tiles_for_S == e->S && e->tiles_for_ntot == e->ntot && e->T > 0) return GGEM_OK;
+  std::vector<int32_t> tb, st0(e->K + 1, 0);
+  std::vector<int64_t> ts;
+  for (int b = 0; b < e->K; ++b) {
+    st0[b] = (int32_t)tb.size();
+    for (int64_t s0 = e->off[b]; s0 < e->off[b + 1]; s0 += e->S) {
+      tb.push_back(b);
+      ts.push_back(s0);
+    }
+  }
+  st0[e->K] = (int32_t)tb.size();
+  e->T = (int)tb.size();
+  cudaError_t c;
+  if ((c = e->tile_b.ensure(tb.size())) || (c = e->tile_s0.ensure(ts.size())) ||
+      (c = e->susp_tile0.ensure(st0.size())) ||
+      (c = e->part.ensure((size_t)e->T * kPartKinds * kR)) ||
+      (c = e->aux2.ensure((size_t)e->K * kR)) ||
+      (c = cudaMemcpyAsync(e->tile_b.p, tb.data(), sizeof(int32_t) * tb.size(),
+                           cudaMemcpyHostToDevice, e->stream)) ||
+      (c = cudaMemcpyAsync(e->tile_s0.p, ts.data(), sizeof(int64_t) * ts.size(),
+                           cudaMemcpyHostToDevice, e->stream)) ||
+      (c = cudaMemcpyAsync(e->susp_tile0.p, st0.data(), sizeof(int32_t) * st0.size(),
+                           cudaMemcpyHostToDevice, e->stream)) ||
+      (c = cudaStreamSynchronize(e->stream)))
+    return ecuda(e, c, "series tiles");
+  e->tiles_for_S = e->S;
+  e->tiles_for_ntot = e->ntot;
+  return GGEM_OK;
+}
+
+// blocks of the persistent launch: every block resident (cooperative)
+int series_grid(ggem_ensemble *e, int *grid) {
+  int sms = 0, per = 0, coop = 0;
+  cudaError_t c;
+  if ((c = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, e->device)) ||
+      (c = cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, e->device)) ||
+      (c = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_ens_series, kSeriesThreads, 0)))
+    return ecuda(e, c, "series occupancy");
+  if (!coop || per < 1) return efail(e, GGEM_ERR_CUDA, "cooperative launch unavailable");
+  *grid = sms * per;
+  return GGEM_OK;
+}
+
+// the whole step of every series in one persistent launch (k_ens_series):
+// permute xi in, stage x0's forces, the series, permute dw out
+int brownian_persistent(ggem_ensemble *e, int nrhs, int N, const double *eig_min,
+                        const double *eig_max, double tol, const double *d_xi, double *d_dw,
+                        ggem_cheb_report *rep) {
+  const int K = e->K, ldc = N + 1;
+  std::vector<double> coef((size_t)K * ldc), da(K), db(K), tda(K), tdb(K);
+  for (int b = 0; b < K; ++b) {
+    if (!(eig_min[b] >= 0) || !(eig_min[b] < eig_max[b]))
+      return efail(e, GGEM_ERR_INVALID_RANGE, "invalid eigenvalue range of suspension " +
+                                                  std::to_string(b));
+    const double d = eig_max[b] - eig_min[b];
+    da[b] = 2.0 / d;
+    db[b] = -(eig_max[b] + eig_min[b]) / d;
+    tda[b] = 2.0 * da[b];
+    tdb[b] = 2.0 * db[b] + tda[b] * e->self_c;
+  }
+  if (int rc = ensure_tiles(e)) return rc;
+  double *x0 = e->v[0].p;
+  const unsigned gv = eblocks(e->ntot * kE, 256);
+  k_ens_to_slots<<<gv, 256, 0, e->stream>>>(e->ntot, nrhs, e->order_g.p, d_xi, x0);
+  if (int rc = elaunch(e, "ensemble permute")) return rc;
+  k_ens_stage<<<eblocks(e->ntot * kR, 256), 256, 0, e->stream>>>(e->ntot, x0, e->f4[1].p);
+  if (int rc = elaunch(e, "ensemble stage")) return rc;
+  // coefficients of all suspensions (chebyshev.C:44-151) while x0 is staged
+  cheb_coeffs_host_many(N, K, da.data(), db.data(), GGEM_CHEB_GAUSS, coef.data(), ldc);
+  // the pass list: the start, the unchecked stretch up to the predicted
+  // degree, then a checked term and its check per term
+  const int k_first = std::max(2, e->pred_terms > 0 ? e->pred_terms : 8);
+  const int last_unchecked = std::min(k_first - 2, N - 2);
+  std::vector<int32_t> ptype{kPassStart}, pterm{0};
+  for (int t = 1; t <= last_unchecked; ++t) {
+    ptype.push_back(kPassTerm);
+    pterm.push_back(t);
+  }
+  for (int t = std::max(1, last_unchecked + 1); t < N; ++t) {
+    ptype.push_back(kPassTermCheck);
+    pterm.push_back(t);
+    ptype.push_back(kPassCheck);
+    pterm.push_back(t);
+  }
+  const int npass = (int)ptype.size();
+  std::vector<uint8_t> act((size_t)K * kR, 0);
+  std::vector<ggem_cheb_report> r0((size_t)K * kR, ggem_cheb_report{0, 1, 1, 0.0, 0.0});
+  for (int b = 0; b < K; ++b)
+    for (int r = 0; r < nrhs; ++r) act[b * kR + r] = 1;
+  std::vector<unsigned int> sync0(2 * (size_t)K + 3, 0u);
+  sync0[2 * K] = (unsigned)(K * nrhs);  // series still running
+  cudaError_t c;
+  if ((c = e->coef.ensure((size_t)K * ldc)) || (c = e->pass_type.ensure(npass)) ||
+      (c = e->pass_term.ensure(npass)) || (c = e->sync.ensure(sync0.size())) ||
+      (c = e->d_rep.ensure((size_t)K * kR)))
+    return ecuda(e, c, "series tables");
+  if ((c = cudaMemcpyAsync(e->coef.p, coef.data(), sizeof(double) * K * ldc,
+                           cudaMemcpyHostToDevice, e->stream)) ||
+      (c = cudaMemcpyAsync(e->da.p, da.data(), sizeof(double) * K, cudaMemcpyHostToDevice,
+                           e->stream)) ||
+      (c = cudaMemcpyAsync(e->db.p, db.data(), sizeof(double) * K, cudaMemcpyHostToDevice,
+                           e->stream)) ||
+      (c = cudaMemcpyAsync(e->two_da.p, tda.data(), sizeof(double) * K, cudaMemcpyHostToDevice,
+                           e->stream)) ||
+      (c = cudaMemcpyAsync(e->c1x.p, tdb.data(), sizeof(double) * K, cudaMemcpyHostToDevice,
+                           e->stream)) ||
+      (c = cudaMemcpyAsync(e->active.p, act.data(), K * kR, cudaMemcpyHostToDevice, e->stream)) ||
+      (c = cudaMemcpyAsync(e->pass_type.p, ptype.data(), sizeof(int32_t) * npass,
+                           cudaMemcpyHostToDevice, e->stream)) ||
+      (c = cudaMemcpyAsync(e->pass_term.p, pterm.data(), sizeof(int32_t) * npass,
+                           cudaMemcpyHostToDevice, e->stream)) ||
+      (c = cudaMemcpyAsync(e->sync.p, sync0.data(), sizeof(unsigned int) * sync0.size(),
+                           cudaMemcpyHostToDevice, e->stream)) ||
+      (c = cudaMemcpyAsync(e->d_rep.p, r0.data(), sizeof(ggem_cheb_report) * r0.size(),
+                           cudaMemcpyHostToDevice, e->stream)))
+    return ecuda(e, c, "series tables");
+  SeriesArgs a;
+  a.ntot = e->ntot;
+  a.W = e->W;
+  a.K = K;
+  a.S = e->S;
+  a.T = e->T;
+  a.npass = npass;
+  a.ldc = ldc;
+  a.tol = tol;
+  a.self_c = e->self_c;
+  a.cnt = e->cnt.p;
+  a.list = e->list.p;
+  a.ten = e->ten.p;
+  a.susp = e->susp.p;
+  a.tile_b = e->tile_b.p;
+  a.tile_s0 = e->tile_s0.p;
+  a.susp_tile0 = e->susp_tile0.p;
+  a.off = e->d_off.p;
+  a.pass_type = e->pass_type.p;
+  a.pass_term = e->pass_term.p;
+  a.X0 = e->v[0].p;
+  a.X1 = e->v[1].p;
+  a.X2 = e->v[2].p;
+  a.dw = e->v[3].p;
+  a.dm = e->v[4].p;
+  a.F0 = e->f4[0].p;
+  a.F1 = e->f4[1].p;
+  a.Fdw = e->f4[2].p;
+  a.da = e->da.p;
+  a.db = e->db.p;
+  a.two_da = e->two_da.p;
+  a.c1x = e->c1x.p;
+  a.coef = e->coef.p;
+  a.active = e->active.p;
+  a.rep = e->d_rep.p;
+  a.part = e->part.p;
+  a.aux2 = e->aux2.p;
+  a.arrive = e->sync.p;
+  a.done = e->sync.p + K;
+  a.n_active = reinterpret_cast<int *>(e->sync.p + 2 * K);
+  a.all_done = reinterpret_cast<int *>(e->sync.p + 2 * K + 1);
+  a.err = reinterpret_cast<int *>(e->sync.p + 2 * K + 2);
+  a.polls = e->series_polls;
+  a.never_ready = e->never_ready;
+  int grid = 0;
+  if (int rc = series_grid(e, &grid)) return rc;
+  grid = (int)std::min<int64_t>(grid, (int64_t)e->T * npass);
+  void *args[] = {&a};
+  if ((c = cudaLaunchCooperativeKernel((const void *)k_ens_series, dim3(grid),
+                                       dim3(kSeriesThreads), args, 0, e->stream)))
+    return ecuda(e, c, "series launch");
+  if (int rc = elaunch(e, "series")) return rc;
+  k_ens_from_slots<<<gv, 256, 0, e->stream>>>(e->ntot, nrhs, e->order_g.p, e->v[4].p, d_dw);
+  if (int rc = elaunch(e, "ensemble permute")) return rc;
+  std::vector<ggem_cheb_report> rr((size_t)K * kR);
+  unsigned int flags[3] = {0u, 0u, 0u};
+  if ((c = cudaMemcpyAsync(rr.data(), e->d_rep.p, sizeof(ggem_cheb_report) * rr.size(),
+                           cudaMemcpyDeviceToHost, e->stream)) ||
+      (c = cudaMemcpyAsync(flags, e->sync.p + 2 * K, sizeof(flags), cudaMemcpyDeviceToHost,
+                           e->stream)) ||
+      (c = cudaStreamSynchronize(e->stream)))
+    return ecuda(e, c, "series reports");
+  if (flags[2] & kErrTimeout)
+    return efail(e, GGEM_ERR_TIMEOUT, "a wait of the persistent series ran out");
+  // reports; operator applications: the start, one per unchecked term, two
+  // per checked term (brownian_system.C:1093, :1117)
+  bool all = true;
+  int worst = 0;
+  const int first_check = last_unchecked + 2;
+  bool room = true;
+  for (int b = 0; b < K; ++b) {
+    const double kap = eig_min[b] > 0 ? eig_max[b] / eig_min[b] : 1e30;
+    const double rho = (std::sqrt(kap) - 1.0) / (std::sqrt(kap) + 1.0);
+    for (int r = 0; r < nrhs; ++r) {
+      ggem_cheb_report R = rr[b * kR + r];
+      const int T = R.n_terms;
+      const int unchecked = std::min(T - 1, last_unchecked);
+      R.n_matvecs = 1 + unchecked + 2 * std::max(0, T - 1 - unchecked);
+      rep[b * nrhs + r] = R;
+      all = all && R.converged;
+      worst = std::max(worst, T);
+      room = room && R.err1 <= 0.8 * rho * tol;
+    }
+  }
+  // adaptive schedule, as the launch-per-term path
+  if (all) e->pred_terms = (worst == first_check && room) ? std::max(2, worst - 1) : worst;
+  return all ? GGEM_OK : efail(e, GGEM_ERR_CHEB_NOT_CONVERGED, "some series did not converge");
+}
+
+}  // namespace
+
+extern "C" int ggem_ensemble_set_series_mode(ggem_ensemble *e, int persistent, int slots_per_tile,
+                                             uint32_t wait_polls, int never_ready) {
+  if (!e || (slots_per_tile != 0 && (slots_per_tile < 8 || slots_per_tile > 1024)))
+    return GGEM_ERR_BAD_ARG;
+  e->persistent = persistent != 0;
+  if (slots_per_tile) e->S = slots_per_tile;
+  e->series_polls = wait_polls ? wait_polls : (1u << 26);
+  e->never_ready = never_ready != 0;
+  return GGEM_OK;
+}
+
 extern "C" int ggem_ensemble_brownian_dev(ggem_ensemble *e, int nrhs, int N,
                                           const double *eig_min, const double *eig_max,
                                           double tol, const double *d_xi, double *d_dw,
@@ -564,6 +1071,9 @@ extern "C" int ggem_ensemble_brownian_dev(ggem_ensemble *e, int nrhs, int N,
     return GGEM_ERR_BAD_ARG;
   if (!e->built) return efail(e, GGEM_ERR_BAD_ARG, "set the ensemble's particles first");
   EnsGuard g(e->device);
+  if (e->persistent)
+    return brownian_persistent(e, nrhs, N, eig_min, eig_max, tol, d_xi, d_dw, rep);
+
   const int K = e->K, ldc = N + 1;
   // per suspension: interval (copss.C:1609-1615), coefficients (chebyshev.C:44-151)
   std::vector<double> coef((size_t)K * ldc), da(K), db(K), tda(K), tdb(K);

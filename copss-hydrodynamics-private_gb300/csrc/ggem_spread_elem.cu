@@ -48,17 +48,20 @@ namespace {
 
 constexpr int kSpThreads = 256;
 constexpr int kSpWarps = kSpThreads / 32;
-constexpr int kSpCap32 = 1024;   // staged particles per pass (FP32 records, 32 B)
-constexpr int kSpCap64 = 512;    // staged particles per pass (FP64 records, 64 B)
+constexpr int kSpCap32 = 512;    // staged particles per pass (FP32 records, 32 B)
+constexpr int kSpCap64 = 256;    // staged particles per pass (FP64 records, 64 B)
 constexpr int kSpMaxSeg = 2048;  // contiguous slot ranges of one dilated brick
 constexpr int kSpMaxExt = 32;    // dilated brick extent per axis (5-bit coordinates)
-constexpr size_t kSpRecBytes = 32768;
-constexpr size_t kSpShared = kSpRecBytes + kSpWarps * kSpCap32 * sizeof(uint16_t) +
-                             2 * (kSpMaxSeg + 1) * sizeof(int32_t);
+constexpr size_t kSpRecBytes = 16384;
+constexpr int kSpMaxWords = 1024;  // stencil bitmap words (32768 element offsets)
+constexpr size_t kSpShared = kSpRecBytes + kSpWarps * kSpCap32 * sizeof(uint32_t) +
+                             2 * (kSpMaxSeg + 1) * sizeof(int32_t) +
+                             kSpMaxWords * sizeof(uint32_t);
 
 struct SpreadGeo {
   Grid g;
   int lo[3], hi[3], dim[3];  // element-offset range of the stencil bitmap
+  int nwords;                // 32-bit words of the bitmap
   int B;                     // brick edge in elements
   int nb[3];                 // bricks per axis
   int nq;                    // quadrature points per element (<= 32)
@@ -138,11 +141,18 @@ __global__ void __launch_bounds__(kSpThreads) k_spread_brick(
   constexpr int CAP = F32 ? kSpCap32 : kSpCap64;
   float4 *rec32 = reinterpret_cast<float4 *>(sp_smem);        // [CAP][2]
   double4_32a *rec64 = reinterpret_cast<double4_32a *>(sp_smem);  // [CAP][2]
-  uint16_t *members = reinterpret_cast<uint16_t *>(sp_smem + kSpRecBytes);
+  uint32_t *members = reinterpret_cast<uint32_t *>(sp_smem + kSpRecBytes);
   int32_t *seg_begin = reinterpret_cast<int32_t *>(members + kSpWarps * kSpCap32);
   int32_t *seg_pre = seg_begin + kSpMaxSeg + 1;
-  __shared__ int s_nseg;
+  uint32_t *s_bits = reinterpret_cast<uint32_t *>(seg_pre + kSpMaxSeg + 1);
+  // the element-offset shifts and the stencil bitmap in shared memory: lanes
+  // index them with different offsets (divergent constant-bank reads would
+  // serialise)
+  __shared__ float s_shift[3][kSpMaxExt];
   __shared__ int s_total;
+  for (int k = threadIdx.x; k < 3 * kSpMaxExt; k += kSpThreads)
+    s_shift[k / kSpMaxExt][k % kSpMaxExt] = sg.shift[k / kSpMaxExt][k % kSpMaxExt];
+  for (int k = threadIdx.x; k < sg.nwords; k += kSpThreads) s_bits[k] = bits[k];
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int B = sg.B;
@@ -209,10 +219,7 @@ __global__ void __launch_bounds__(kSpThreads) k_spread_brick(
     if (threadIdx.x == kSpThreads - 1) seg_pre[min(s0 + kSpThreads, nseg)] = before + incl;
     __syncthreads();
   }
-  if (threadIdx.x == 0) {
-    s_nseg = nseg;
-    s_total = seg_pre[nseg];
-  }
+  if (threadIdx.x == 0) s_total = seg_pre[nseg];
   __syncthreads();
   const int total = s_total;
   // elements of this brick, one warp at a time
@@ -221,7 +228,9 @@ __global__ void __launch_bounds__(kSpThreads) k_spread_brick(
   const int nq = sg.nq, lq = sg.lq;
   const int qi = lane / lq, sub = lane - qi * lq;
   unsigned long long my_pairs = 0;
-  uint16_t *mlist = members + warp * kSpCap32;
+  // member entry: staged index (10 bits; < kSpCap32) and the element offset minus the
+  // stencil's lower corner (5 bits per axis)
+  uint32_t *mlist = members + warp * kSpCap32;
   for (int c0 = 0; c0 < total; c0 += CAP) {
     const int cn = min(CAP, total - c0);
     // stage particles [c0, c0 + cn): segment by binary search
@@ -268,21 +277,22 @@ __global__ void __launch_bounds__(kSpThreads) k_spread_brick(
       for (int k0 = 0; k0 < cn; k0 += 32) {
         const int k = k0 + lane;
         bool in = false;
+        uint32_t entry = 0;
         if (k < cn) {
           const uint32_t u = F32 ? __float_as_uint(rec32[2 * k].w)
                                  : (uint32_t)__double_as_longlong(rec64[2 * k].w);
-          const int ox = axis_offset(sg, 0, (int)(u & 31u), uex, fr[0].full);
-          const int oy = axis_offset(sg, 1, (int)((u >> 5) & 31u), uey, fr[1].full);
-          const int oz = axis_offset(sg, 2, (int)(u >> 10), uez, fr[2].full);
-          if (ox >= sg.lo[0] && ox <= sg.hi[0] && oy >= sg.lo[1] && oy <= sg.hi[1] &&
-              oz >= sg.lo[2] && oz <= sg.hi[2]) {
-            const int idx = ((oz - sg.lo[2]) * sg.dim[1] + (oy - sg.lo[1])) * sg.dim[0] +
-                            (ox - sg.lo[0]);
-            in = (__ldg(bits + (idx >> 5)) >> (idx & 31)) & 1u;
+          const int ix = axis_offset(sg, 0, (int)(u & 31u), uex, fr[0].full) - sg.lo[0];
+          const int iy = axis_offset(sg, 1, (int)((u >> 5) & 31u), uey, fr[1].full) - sg.lo[1];
+          const int iz = axis_offset(sg, 2, (int)(u >> 10), uez, fr[2].full) - sg.lo[2];
+          if ((unsigned)ix < (unsigned)sg.dim[0] && (unsigned)iy < (unsigned)sg.dim[1] &&
+              (unsigned)iz < (unsigned)sg.dim[2]) {
+            const int idx = (iz * sg.dim[1] + iy) * sg.dim[0] + ix;
+            in = (s_bits[idx >> 5] >> (idx & 31)) & 1u;
+            entry = (uint32_t)k | ((uint32_t)ix << 10) | ((uint32_t)iy << 15) | ((uint32_t)iz << 20);
           }
         }
         const unsigned bal = __ballot_sync(0xffffffffu, in);
-        if (in) mlist[M + __popc(bal & ((1u << lane) - 1u))] = (uint16_t)k;
+        if (in) mlist[M + __popc(bal & ((1u << lane) - 1u))] = entry;
         M += __popc(bal);
       }
       __syncwarp();
@@ -296,15 +306,12 @@ __global__ void __launch_bounds__(kSpThreads) k_spread_brick(
         float bx_ = 0.f, by_ = 0.f, bz_ = 0.f;
         int blk = 0;
         for (int m = sub; m < M && qok; m += lq) {
-          const int k = mlist[m];
+          const uint32_t en = mlist[m];
+          const int k = (int)(en & 1023u);
           const float4 a = rec32[2 * k], fb = rec32[2 * k + 1];
-          const uint32_t u = __float_as_uint(a.w);
-          const int ox = axis_offset(sg, 0, (int)(u & 31u), uex, fr[0].full);
-          const int oy = axis_offset(sg, 1, (int)((u >> 5) & 31u), uey, fr[1].full);
-          const int oz = axis_offset(sg, 2, (int)(u >> 10), uez, fr[2].full);
-          float dx = (a.x + sg.shift[0][ox - sg.lo[0]]) - qr.x;
-          float dy = (a.y + sg.shift[1][oy - sg.lo[1]]) - qr.y;
-          float dz = (a.z + sg.shift[2][oz - sg.lo[2]]) - qr.z;
+          float dx = (a.x + s_shift[0][(en >> 10) & 31u]) - qr.x;
+          float dy = (a.y + s_shift[1][(en >> 15) & 31u]) - qr.y;
+          float dz = (a.z + s_shift[2][en >> 20]) - qr.z;
           // minimum image (pm_periodic_boundary.C:350-374); only an axis
           // whose frame is the whole box can produce |d| > L/2
           if (fr[0].full) {
@@ -354,7 +361,7 @@ __global__ void __launch_bounds__(kSpThreads) k_spread_brick(
         const double q0 = q_xyz[3 * qg], q1 = q_xyz[3 * qg + 1], q2 = q_xyz[3 * qg + 2];
         double ax = 0.0, ay = 0.0, az = 0.0;
         for (int m = sub; m < M && qok; m += lq) {
-          const int k = mlist[m];
+          const int k = (int)(mlist[m] & 1023u);
           const double4_32a a = rec64[2 * k], fb = rec64[2 * k + 1];
           // point_vector(q, x_j) with the minimum image (pm_periodic_boundary.C:350-374)
           double x[3] = {a.x - q0, a.y - q1, a.z - q2};
@@ -401,7 +408,6 @@ __global__ void __launch_bounds__(kSpThreads) k_spread_brick(
   if (pairs) {
     if (lane == 0 && my_pairs) atomicAdd(pairs, my_pairs * (unsigned long long)nq);
   }
-  (void)s_nseg;
 }
 
 // quadrature points relative to their element centre (FP64 difference,
@@ -471,7 +477,10 @@ int spread_geometry(ggem_ctx *c, SpreadGeo *sg) {
     sg->L32[d] = (float)g.L[d];
   }
   const int nbits = sg->dim[0] * sg->dim[1] * sg->dim[2];
-  std::vector<uint32_t> bits((nbits + 31) / 32, 0u);
+  sg->nwords = (nbits + 31) / 32;
+  if (sg->nwords > kSpMaxWords)
+    return fail(c, GGEM_ERR_BAD_ARG, "element stencil bitmap too large for the brick spread");
+  std::vector<uint32_t> bits(sg->nwords, 0u);
   auto set = [&](int x, int y, int z) {
     const int idx = ((z - sg->lo[2]) * sg->dim[1] + (y - sg->lo[1])) * sg->dim[0] + (x - sg->lo[0]);
     bits[idx >> 5] |= 1u << (idx & 31);

@@ -60,7 +60,7 @@ constexpr int kKChunk = 64;
 __global__ void __launch_bounds__(128) k_gemm_bf16(const bf16 *__restrict__ A, int lda,
                                                    const bf16 *__restrict__ Bt, int ldb,
                                                    float *__restrict__ C, int ldc, int N, int K,
-                                                   int *__restrict__ err) {
+                                                   uint32_t polls, int *__restrict__ err) {
   // K-major core-matrix tiles: offset(row, k) = ((row/8)*8 + k/8)*128 +
   // (row%8)*16 + (k%8)*2, so core matrices adjacent along K are 128 B apart
   // (leading byte offset) and 8-row groups 1024 B apart (stride byte offset)
@@ -109,7 +109,8 @@ __global__ void __launch_bounds__(128) k_gemm_bf16(const bf16 *__restrict__ A, i
       tc::mma_commit(&bar);
     }
     // the tiles are reused only after the MMAs that read them completed
-    const bool done = tc::mbar_wait_bounded(&bar, phase, kMaxPolls);
+    // (polls bounds this wait; the drain below keeps the full window)
+    const bool done = tc::mbar_wait_bounded(&bar, phase, polls);
     phase ^= 1u;
     ok = __syncthreads_and(done) != 0;
   }
@@ -133,6 +134,166 @@ __global__ void __launch_bounds__(128) k_gemm_bf16(const bf16 *__restrict__ A, i
   if (warp == 0) {
     tc::fence_after_sync();
     tc::tmem_dealloc(tmem, ncols);
+  }
+}
+
+// ---- the whole forward pass in one kernel (inference) ----------------------
+// One CTA of 4 warps per 128 rows.  All four BF16 weight matrices W^T stay in
+// shared memory (K-major core-matrix tiles) for the CTA's lifetime; the
+// activations of a layer are written back into one shared tile that the
+// next product reads, so nothing but the raw features and the two outputs
+// touches global memory.  Per layer: one thread issues the 128 x N x 16 MMA
+// steps into a TMEM accumulator of 128 columns, commits to an mbarrier, all
+// threads wait (bounded) and thread t reads TMEM lane t (its row), adds the
+// bias, applies SiLU and stores the BF16 row into the activation tile.  The
+// arithmetic is the layer-by-layer path's (same products in the same K
+// order, same bias, SiLU and BF16 rounding), so the outputs agree bit for bit.
+// Tile of R rows x KP 16-byte pieces: offset(row, piece) =
+// ((row / 8) * KP + piece) * 128 + (row % 8) * 16; LBO 128 B, SBO KP * 128 B.
+constexpr int kOutN = 16;  // N of the last product (outputs 0, 1 used)
+constexpr size_t kMlpActBytes = (size_t)kRowBlock * kHid * 2;
+constexpr size_t kMlpW0 = kMlpActBytes;
+constexpr size_t kMlpW1 = kMlpW0 + (size_t)kHid * kInPad * 2;
+constexpr size_t kMlpW2 = kMlpW1 + (size_t)kHid * kHid * 2;
+constexpr size_t kMlpW3 = kMlpW2 + (size_t)kHid * kHid * 2;
+constexpr size_t kMlpSmem = kMlpW3 + (size_t)kOutN * kHid * 2;
+
+// offset of layer l's bias in the flat parameter vector (W1^T [128 x 48],
+// b1, then [128 x 128] weights and 128 biases per layer)
+__host__ __device__ constexpr int bias_off_d(int l) {
+  return l == 0 ? kHid * kInPad
+                : kHid * kInPad + kHid + (l - 1) * (kHid * kHid + kHid) + kHid * kHid;
+}
+
+__device__ __forceinline__ uint32_t tile_off(int row, int piece, int kp) {
+  return (uint32_t)(((row >> 3) * kp + piece) * 128 + (row & 7) * 16);
+}
+
+// W^T [rows x K] into its tile with 16-byte asynchronous copies (cp.async:
+// every copy of the thread in flight at once; completed by cp_async_wait)
+__device__ __forceinline__ void stage_wt(uint8_t *dst, const bf16 *__restrict__ W, int rows,
+                                         int K) {
+  const int kp = K >> 3;
+  for (int c = threadIdx.x; c < rows * kp; c += blockDim.x) {
+    const int row = c / kp, kb = c - row * kp;
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(
+                     tc::smem_u32(dst + tile_off(row, kb, kp))),
+                 "l"(W + (int64_t)row * K + kb * 8)
+                 : "memory");
+  }
+}
+
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
+}
+
+__device__ __forceinline__ float silu_f(float z) { return z * (1.f / (1.f + expf(-z))); }
+
+constexpr int kMlpThreads = 256;  // 8 warps: warp w reads TMEM lanes 32 (w % 4) .. + 31,
+                                  // columns 64 (w / 4) .. + 63
+
+__global__ void __launch_bounds__(kMlpThreads) k_mlp_forward(
+    const float *__restrict__ x, int n, const float *__restrict__ mean,
+    const float *__restrict__ inv_std, const bf16 *__restrict__ w0, const bf16 *__restrict__ w1,
+    const bf16 *__restrict__ w2, const bf16 *__restrict__ w3, const float *__restrict__ params,
+    float *__restrict__ Y, uint32_t polls, int *__restrict__ err) {
+  extern __shared__ __align__(1024) uint8_t mlp_smem[];
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ uint32_t tslot;
+  uint8_t *sA = mlp_smem;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int quarter = warp & 3, half = warp >> 2;
+  const int row = quarter * 32 + lane;  // this thread's row = its TMEM lane
+  const int64_t row_g = (int64_t)blockIdx.x * kRowBlock + row;
+  if (warp == 0) tc::tmem_alloc(&tslot, (uint32_t)kHid);
+  if (tid == 0) {
+    tc::mbar_init(&bar, 1);
+    tc::mbar_fence_init();
+  }
+  // weights (asynchronous copies), and meanwhile the standardised input
+  // rows (48 BF16, zero padded; the first half of the block)
+  stage_wt(mlp_smem + kMlpW0, w0, kHid, kInPad);
+  stage_wt(mlp_smem + kMlpW1, w1, kHid, kHid);
+  stage_wt(mlp_smem + kMlpW2, w2, kHid, kHid);
+  stage_wt(mlp_smem + kMlpW3, w3, kOutN, kHid);
+  if (half == 0) {
+#pragma unroll
+    for (int kb = 0; kb < kInPad / 8; ++kb) {
+      __align__(16) bf16 h[8];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const int c = kb * 8 + i;
+        const float v =
+            (row_g < n && c < kIn) ? (x[row_g * kIn + c] - mean[c]) * inv_std[c] : 0.f;
+        h[i] = __float2bfloat16_rn(v);
+      }
+      *reinterpret_cast<uint4 *>(sA + tile_off(row, kb, kInPad / 8)) =
+          *reinterpret_cast<const uint4 *>(h);
+    }
+  }
+  cp_async_wait();
+  tc::fence_proxy_async_smem();
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = tslot;
+  const uint32_t lane_base = tmem + ((uint32_t)(quarter * 32) << 16);
+  const size_t woff[kLayers] = {kMlpW0, kMlpW1, kMlpW2, kMlpW3};
+  bool ok = true;
+  uint32_t phase = 0;
+  for (int l = 0; l < kLayers && ok; ++l) {
+    const int K = l == 0 ? kInPad : kHid, N = l == kLayers - 1 ? kOutN : kHid;
+    if (tid == 0) {
+      const uint32_t a0 = tc::smem_u32(sA), b0 = tc::smem_u32(mlp_smem + woff[l]);
+      const uint32_t idesc = tc::idesc_bf16_f32(kRowBlock, N);
+      for (int s = 0; s < K / 16; ++s) {
+        const uint64_t ad = tc::smem_desc(a0 + s * 256, 128, (uint32_t)(K / 8) * 128);
+        const uint64_t bd = tc::smem_desc(b0 + s * 256, 128, (uint32_t)(K / 8) * 128);
+        tc::mma_bf16(tmem, ad, bd, idesc, s > 0 ? 1u : 0u);
+      }
+      tc::mma_commit(&bar);
+    }
+    const bool done = tc::mbar_wait_bounded(&bar, phase, polls);
+    phase ^= 1u;
+    ok = __syncthreads_and(done) != 0;
+    if (!ok) break;
+    tc::fence_after_sync();
+    const float *bias = params + bias_off_d(l);
+    if (l < kLayers - 1) {
+      // H = silu(Z + b) into the activation tile (the product that read it
+      // has completed)
+      for (int c0 = half * (kHid / 2); c0 < (half + 1) * (kHid / 2); c0 += 8) {
+        float v[8];
+        tc::tmem_ld8(lane_base + (uint32_t)c0, v);
+        __align__(16) bf16 h[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) h[i] = __float2bfloat16_rn(silu_f(v[i] + bias[c0 + i]));
+        *reinterpret_cast<uint4 *>(sA + tile_off(row, c0 >> 3, kHid / 8)) =
+            *reinterpret_cast<const uint4 *>(h);
+      }
+      tc::fence_proxy_async_smem();
+      tc::fence_before_sync();
+      __syncthreads();
+      tc::fence_after_sync();
+    } else if (half == 0) {
+      float v[8];
+      tc::tmem_ld8(lane_base, v);
+      if (row_g < n) {
+        Y[row_g * kOut] = v[0] + bias[0];
+        Y[row_g * kOut + 1] = v[1] + bias[1];
+      }
+    }
+  }
+  if (!ok) {
+    if (tid == 0) atomicOr(err, kErrTimeout);
+    // the product still in flight completes before TMEM is freed
+    tc::mbar_wait_bounded(&bar, phase ^ 1u, kMaxPolls);
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) {
+    tc::fence_after_sync();
+    tc::tmem_dealloc(tmem, (uint32_t)kHid);
   }
 }
 
@@ -323,6 +484,11 @@ constexpr int kWOff[kLayers] = {0, 128 * 48 + 128, 128 * 48 + 128 + 128 * 128 + 
                                 128 * 48 + 128 + 2 * (128 * 128 + 128)};
 constexpr int kInDim[kLayers] = {kInPad, kHid, kHid, kHid};
 inline int bias_off(int l) { return kWOff[l] + kHid * kInDim[l]; }
+static_assert(bias_off_d(0) == kWOff[0] + kHid * kInDim[0] &&
+                  bias_off_d(1) == kWOff[1] + kHid * kInDim[1] &&
+                  bias_off_d(2) == kWOff[2] + kHid * kInDim[2] &&
+                  bias_off_d(3) == kWOff[3] + kHid * kInDim[3],
+              "bias offsets");
 
 // seeded host generator (SplitMix64) for initialisation and shuffles
 struct Rng {
@@ -357,7 +523,9 @@ struct ggem_surrogate {
   DevBuf<float> xin, yin;
   DevBuf<int32_t> idx;
   DevBuf<int> flag;
+  DevBuf<float> yout;                     // fused forward outputs [n x 2]
   int64_t adam_t = 0;
+  uint32_t polls = kMaxPolls;             // first-wait poll budget of the products
 };
 
 namespace {
@@ -409,8 +577,22 @@ int gemm(ggem_surrogate *s, const bf16 *A, int lda, const bf16 *Bt, int ldb, flo
          int M, int N, int K) {
   if (M % kRowBlock || N % 16 || N < 16 || N > kHid || K % 16 || K <= 0 || lda % 8 || ldb % 8)
     return sfail(s, GGEM_ERR_BAD_ARG, "surrogate product shape");
-  k_gemm_bf16<<<M / kRowBlock, 128, 0, s->stream>>>(A, lda, Bt, ldb, C, ldc, N, K, s->flag.p);
+  k_gemm_bf16<<<M / kRowBlock, 128, 0, s->stream>>>(A, lda, Bt, ldb, C, ldc, N, K, s->polls,
+                                                    s->flag.p);
   return slaunch(s, "tensor-core product");
+}
+
+// raw device features d_x [n x 35] through the fused forward kernel into
+// d_y [n x 2] (standardised outputs)
+int forward_fused(ggem_surrogate *s, const float *d_x, int64_t n, float *d_y) {
+  cudaError_t e = cudaFuncSetAttribute(k_mlp_forward, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)kMlpSmem);
+  if (e) return scuda(s, e, "network attributes");
+  k_mlp_forward<<<(unsigned)((n + kRowBlock - 1) / kRowBlock), kMlpThreads, kMlpSmem,
+                  s->stream>>>(
+      d_x, (int)n, s->d_mean.p, s->d_inv_std.p, s->wt[0].p, s->wt[1].p, s->wt[2].p, s->wt[3].p,
+      s->p.p, d_y, s->polls, s->flag.p);
+  return slaunch(s, "network forward");
 }
 
 unsigned blocks(int64_t n, int t = 256) { return (unsigned)((n + t - 1) / t); }
@@ -596,6 +778,7 @@ extern "C" void ggem_surrogate_destroy(ggem_surrogate *s) {
     s->yin.release();
     s->idx.release();
     s->flag.release();
+    s->yout.release();
     s->d_mean.release();
     s->d_inv_std.release();
     if (s->stream) cudaStreamDestroy(s->stream);
@@ -744,6 +927,29 @@ extern "C" int ggem_surrogate_train(ggem_surrogate *s, const float *X, const flo
 extern "C" int ggem_surrogate_predict(ggem_surrogate *s, const float *X, int64_t n, float *Y) {
   if (!s || !X || !Y || n <= 0 || n > (int64_t)1 << 30) return GGEM_ERR_BAD_ARG;
   SurDeviceGuard dg(s->device);
+  if (int rc = upload_data(s, X, nullptr, n)) return rc;
+  cudaError_t e;
+  if ((e = s->yout.ensure((size_t)n * kOut)) ||
+      (e = cudaMemsetAsync(s->flag.p, 0, sizeof(int), s->stream)))
+    return scuda(s, e, "predict");
+  // one launch: all layers, weights resident in shared memory
+  if (int rc = forward_fused(s, s->xin.p, n, s->yout.p)) return rc;
+  std::vector<float> out((size_t)n * kOut);
+  if ((e = cudaMemcpyAsync(out.data(), s->yout.p, sizeof(float) * n * kOut,
+                           cudaMemcpyDeviceToHost, s->stream)) ||
+      (e = cudaStreamSynchronize(s->stream)))
+    return scuda(s, e, "predict readback");
+  if (int rc = check_flag(s)) return rc;
+  for (int64_t r = 0; r < n; ++r)
+    for (int c = 0; c < kOut; ++c)
+      Y[r * kOut + c] = out[r * kOut + c] * s->norm[2 * kIn + kOut + c] + s->norm[2 * kIn + c];
+  return GGEM_OK;
+}
+
+extern "C" int ggem_surrogate_predict_layers(ggem_surrogate *s, const float *X, int64_t n,
+                                             float *Y) {
+  if (!s || !X || !Y || n <= 0 || n > (int64_t)1 << 30) return GGEM_ERR_BAD_ARG;
+  SurDeviceGuard dg(s->device);
   const int cap = std::max(s->cap, std::min(round_rows(n), 4096));
   if (int rc = ensure_cap(s, cap)) return rc;
   if (int rc = upload_data(s, X, nullptr, n)) return rc;
@@ -764,6 +970,38 @@ extern "C" int ggem_surrogate_predict(ggem_surrogate *s, const float *X, int64_t
         Y[(r0 + r) * kOut + c] =
             out[r * kOut + c] * s->norm[2 * kIn + kOut + c] + s->norm[2 * kIn + c];
   }
+  return check_flag(s);
+}
+
+extern "C" int ggem_surrogate_set_poll_budget(ggem_surrogate *s, uint32_t polls) {
+  if (!s) return GGEM_ERR_BAD_ARG;
+  s->polls = polls;
+  return GGEM_OK;
+}
+
+extern "C" int ggem_surrogate_time_forward(ggem_surrogate *s, int64_t n, int reps, double *ms) {
+  if (!s || n <= 0 || n > (int64_t)1 << 20 || reps < 1 || !ms) return GGEM_ERR_BAD_ARG;
+  SurDeviceGuard dg(s->device);
+  cudaError_t e;
+  if ((e = s->xin.ensure((size_t)n * kIn)) || (e = s->yout.ensure((size_t)n * kOut)) ||
+      (e = cudaMemsetAsync(s->xin.p, 0, sizeof(float) * n * kIn, s->stream)) ||
+      (e = cudaMemsetAsync(s->flag.p, 0, sizeof(int), s->stream)))
+    return scuda(s, e, "forward timing");
+  if (int rc = forward_fused(s, s->xin.p, n, s->yout.p)) return rc;  // warm-up
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  cudaEventRecord(a, s->stream);
+  int rc = GGEM_OK;
+  for (int r = 0; r < reps && !rc; ++r) rc = forward_fused(s, s->xin.p, n, s->yout.p);
+  cudaEventRecord(b, s->stream);
+  cudaEventSynchronize(b);
+  float t = 0.f;
+  cudaEventElapsedTime(&t, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  if (rc) return rc;
+  *ms = t / reps;
   return check_flag(s);
 }
 

@@ -149,6 +149,9 @@ def lib():
         "ggem_surrogate_get_params": (i, [vp, vp]),
         "ggem_surrogate_train": (i, [vp, vp, vp, i64, i, i, C.c_float, C.c_uint64, vp]),
         "ggem_surrogate_predict": (i, [vp, vp, i64, vp]),
+        "ggem_surrogate_predict_layers": (i, [vp, vp, i64, vp]),
+        "ggem_surrogate_set_poll_budget": (i, [vp, C.c_uint32]),
+        "ggem_surrogate_time_forward": (i, [vp, i64, i, P(d)]),
         "ggem_surrogate_gradient": (i, [vp, vp, vp, i64, P(C.c_float), vp]),
         "ggem_surrogate_features": (i, [vp, d, vp]),
         "ggem_surrogate_interval": (i, [vp, vp, d, d, d, P(d), P(d)]),
@@ -179,6 +182,7 @@ def lib():
         "ggem_ensemble_intervals": (i, [vp, vp, vp, d, d, vp, vp]),
         "ggem_ensemble_lanczos": (i, [vp, i, i, C.c_uint64, P(d), P(d)]),
         "ggem_ensemble_autotune": (i, [vp, i, P(i), P(d)]),
+        "ggem_ensemble_set_series_mode": (i, [vp, i, i, C.c_uint32, i]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -311,6 +315,23 @@ class Surrogate:
         Y = np.zeros((len(X), SUR_OUTPUTS), dtype=np.float32)
         self._check(lib().ggem_surrogate_predict(self.h, _p(X), len(X), _p(Y)))
         return Y
+
+    def predict_layers(self, X) -> np.ndarray:
+        """the layer-by-layer path of training (one product per layer)"""
+        X = np.ascontiguousarray(np.atleast_2d(X), dtype=np.float32)
+        Y = np.zeros((len(X), SUR_OUTPUTS), dtype=np.float32)
+        self._check(lib().ggem_surrogate_predict_layers(self.h, _p(X), len(X), _p(Y)))
+        return Y
+
+    def set_poll_budget(self, polls):
+        """test hook: polls of the first mbarrier wait of every product"""
+        self._check(lib().ggem_surrogate_set_poll_budget(self.h, int(polls)))
+
+    def time_forward(self, n, reps=50):
+        """mean ms of the one-kernel forward pass over n rows"""
+        ms = C.c_double()
+        self._check(lib().ggem_surrogate_time_forward(self.h, int(n), int(reps), C.byref(ms)))
+        return ms.value
 
     def gradient(self, X, Y):
         X = np.ascontiguousarray(X, dtype=np.float32)
@@ -779,6 +800,17 @@ class Ensemble:
         if rc and rc != ERR_CHEB_NOT_CONVERGED:
             self._check(rc)
         return rc, [[reps[b * nrhs + r].as_dict() for r in range(nrhs)] for b in range(self.K)]
+
+    def set_series_mode(self, persistent=True, slots_per_tile=0, wait_polls=0,
+                        never_ready=False):
+        """persistent: the whole Brownian step in one cooperative launch (the
+        default) or one launch per term with host-side checks; slots per
+        tile of the persistent launch (0 keeps the current); the polls of its
+        bounded waits (0 = default); never_ready (test hook) makes every wait
+        run out"""
+        self._check(lib().ggem_ensemble_set_series_mode(self.h, 1 if persistent else 0,
+                                                        int(slots_per_tile), int(wait_polls),
+                                                        1 if never_ready else 0))
 
     def intervals(self, sur, chain_fraction=None, margin_lo=0.0, margin_hi=0.0):
         cf = np.zeros(self.K) if chain_fraction is None else \

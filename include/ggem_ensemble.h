@@ -74,6 +74,17 @@ int ggem_ensemble_lanczos(ggem_ensemble *e, int b, int k, uint64_t seed, double 
  * (candidates 128, 256, 512 threads; CUDA-event timing of the fused term);
  * the choice is kept and reported */
 int ggem_ensemble_autotune(ggem_ensemble *e, int nrhs, int *block_threads, double *ms_per_term);
+/* How ggem_ensemble_brownian_dev runs the series.  persistent = 1 (the
+ * default): one cooperative launch walks the whole step (start, terms,
+ * error checks and every series' stopping decision, brownian_system.C:
+ * 1036-1155) with tiles of slots_per_tile slots of one suspension; a tile
+ * waits only for its own suspension's previous pass, and every wait is
+ * bounded by wait_polls polls (0 = the default, ~8 s) after which the call
+ * returns GGEM_ERR_TIMEOUT.  persistent = 0: one launch per term with the
+ * checks read back on the host.  slots_per_tile 0 keeps the current value;
+ * never_ready = 1 is a test hook that makes every wait run out. */
+int ggem_ensemble_set_series_mode(ggem_ensemble *e, int persistent, int slots_per_tile,
+                                  uint32_t wait_polls, int never_ready);
 
 #ifdef __cplusplus
 }

@@ -64,6 +64,18 @@ int ggem_surrogate_train(ggem_surrogate *s, const float *X, const float *Y, int6
                          int epochs, int batch, float lr, uint64_t seed, float *loss);
 /* predictions Y [n x 2] (log lambda) for raw features X [n x 35] */
 int ggem_surrogate_predict(ggem_surrogate *s, const float *X, int64_t n, float *Y);
+/* the same predictions through the layer-by-layer path of training (one
+ * tensor-core product and one bias/activation kernel per layer; the default
+ * ggem_surrogate_predict runs all layers in one kernel with the weights
+ * resident in shared memory) */
+int ggem_surrogate_predict_layers(ggem_surrogate *s, const float *X, int64_t n, float *Y);
+/* measurement and test hooks: the mean time of the one-kernel forward pass
+ * over n rows (CUDA events, reps launches); and the number of polls the
+ * first mbarrier wait of every product makes before the kernel gives up and
+ * reports GGEM_ERR_TIMEOUT (default 4194304; the wait that drains a product
+ * before its TMEM is freed keeps the full budget) */
+int ggem_surrogate_time_forward(ggem_surrogate *s, int64_t n, int reps, double *ms);
+int ggem_surrogate_set_poll_budget(ggem_surrogate *s, uint32_t polls);
 /* one forward + backward pass over X, Y (n <= 4096 rows) without an update:
  * the loss and the gradient with respect to every parameter (GGEM_SUR_PARAMS
  * floats, same layout as the parameters) */

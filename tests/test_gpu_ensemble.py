@@ -186,3 +186,79 @@ def test_ensemble_reconfiguration_drops_captured_terms():
             assert np.array_equal(got, want)
             assert [[r["n_terms"] for r in rb] for rb in reps] == \
                 [[r["n_terms"] for r in rb] for rb in rep_want]
+
+
+def test_persistent_series_equals_launch_per_term():
+    """The whole step in one persistent launch (device-side checks and
+    stopping decisions) gives the launch-per-term path's displacements and
+    reports, for every tile size, on a first call and on a second call that
+    starts its checks at the learned degree (fresh ensembles, so both paths
+    run the same check schedule)."""
+    import torch
+    sus = _ensemble(7, 21)
+    R = 8
+    xi = np.random.default_rng(9).standard_normal((sum(len(x) for x, _ in sus), R, 3))
+    d_xyz = _device(np.concatenate([x for x, _ in sus]))
+    d_xi = _device(xi)
+
+    def run(persistent, S=0):
+        out = []
+        with G.Ensemble([L for _, L in sus]) as ens:
+            ens.set_particles_dev([len(x) for x, _ in sus], d_xyz.data_ptr())
+            ens.set_series_mode(persistent=persistent, slots_per_tile=S)
+            bounds = [ens.lanczos(b, k=40, seed=1) for b in range(len(sus))]
+            lo = np.array([x[0] for x in bounds]) / 1.05
+            hi = np.array([x[1] for x in bounds]) * 1.05
+            for _ in range(2):
+                d_dw = torch.zeros_like(d_xi)
+                rc, rep = ens.brownian_dev(R, 50, lo, hi, 1e-3, d_xi.data_ptr(), d_dw.data_ptr())
+                assert rc == 0
+                out.append((d_dw.cpu().numpy(), rep))
+        return out
+
+    want = run(False)
+    for S in (16, 64, 256):
+        got = run(True, S)
+        for call, ((g, rep), (w, wrep)) in enumerate(zip(got, want)):
+            assert rel(g, w) <= 1e-12, (S, call)
+            for b in range(len(sus)):
+                for r in range(R):
+                    a, x = rep[b][r], wrep[b][r]
+                    assert a["converged"] == x["converged"] and a["n_terms"] == x["n_terms"]
+                    assert a["n_matvecs"] == x["n_matvecs"]
+                    # err1^2 is a difference of two nearly equal FP64 sums
+                    # (summed per tile here, per chunk there): ~1e-15 absolute
+                    assert abs(a["err1"] - x["err1"]) <= max(1e-9 * x["err1"],
+                                                             1e-13 / x["err1"])
+
+
+def test_persistent_series_wait_timeout_is_reported():
+    """A wait of the persistent launch that runs out (test hook: no pass is
+    ever marked complete) sets the error word; every block leaves, the call
+    returns GGEM_ERR_TIMEOUT and the ensemble stays usable: the next call
+    gives the launch-per-term path's displacements."""
+    import torch
+    sus = _ensemble(3, 33)
+    R = 8
+    d_xyz = _device(np.concatenate([x for x, _ in sus]))
+    xi = _device(np.random.default_rng(2).standard_normal((sum(len(x) for x, _ in sus), R, 3)))
+    out = []
+    for persistent in (True, False):
+        with G.Ensemble([L for _, L in sus]) as ens:
+            ens.set_particles_dev([len(x) for x, _ in sus], d_xyz.data_ptr())
+            bounds = [ens.lanczos(b, k=40, seed=1) for b in range(len(sus))]
+            lo = np.array([x[0] for x in bounds]) / 1.05
+            hi = np.array([x[1] for x in bounds]) * 1.05
+            dw = torch.empty_like(xi)
+            if persistent:
+                ens.set_series_mode(persistent=True, wait_polls=2000, never_ready=True)
+                with pytest.raises(G.GGEMError) as e:
+                    ens.brownian_dev(R, 50, lo, hi, 1e-3, xi.data_ptr(), dw.data_ptr())
+                assert e.value.code == G.ERR_TIMEOUT
+                ens.set_series_mode(persistent=True)
+            else:
+                ens.set_series_mode(persistent=False)
+            rc, reps = ens.brownian_dev(R, 50, lo, hi, 1e-3, xi.data_ptr(), dw.data_ptr())
+            assert rc == 0 and all(r["converged"] for rb in reps for r in rb)
+            out.append(dw.cpu().numpy())
+    assert rel(out[0], out[1]) <= 1e-12

@@ -102,7 +102,7 @@ def test_spread_open_axis_offset_box():
 
 def test_spread_dense_staging_in_several_passes():
     """more particles in a brick's dilated region than one shared-memory
-    pass holds (1024 FP32 / 512 FP64 records): the passes add up"""
+    pass holds (512 FP32 / 256 FP64 records): the passes add up"""
     rng = np.random.default_rng(4)
     L = 40.0
     xyz = rng.uniform(0, L, (6400, 3))

@@ -159,3 +159,38 @@ def test_features_on_a_known_lattice():
     for b in range(32):
         has = np.any((shells >= edges[b]) & (shells < edges[b + 1]))
         assert (hist[b] > 0) == has, b
+
+
+@pytest.mark.parametrize("n", [1, 100, 700])
+def test_fused_forward_equals_layer_path(n):
+    """the one-kernel forward pass (weights resident in shared memory) gives
+    the layer-by-layer path's outputs: same products in the same K order,
+    same bias, SiLU and BF16 rounding"""
+    sur, X, _ = _random_net(4, n)
+    a = sur.predict(X)
+    b = sur.predict_layers(X)
+    assert np.array_equal(a, b), np.abs(a - b).max()
+    ms = sur.time_forward(1, 100)
+    print(f"one interval prediction (1 row): {ms * 1e3:.1f} us per forward launch")
+    sur.close()
+
+
+def test_tensor_core_wait_timeout_is_reported_and_recovers():
+    """A poll budget of zero makes the first mbarrier wait of a product give
+    up at once: the kernel drains the product still in flight with its full
+    window, frees TMEM and reports GGEM_ERR_TIMEOUT; the network stays
+    usable and the next products are exact.  (No wait is left unbounded and
+    nothing faults: the products complete within microseconds.)"""
+    sur, X, Y = _random_net(5, 300)
+    want = M.predict(sur.params, sur.norm, X)
+    for fn in (sur.predict, sur.predict_layers):
+        sur.set_poll_budget(0)
+        with pytest.raises(G.GGEMError) as e:
+            fn(X)
+        assert e.value.code == G.ERR_TIMEOUT
+        sur.set_poll_budget(1 << 22)
+        assert rel(fn(X), want) <= 2e-3
+    loss, g = sur.gradient(X, Y)
+    loss_o, _ = M.loss_and_grad(sur.params, sur.norm, X, Y)
+    assert loss == pytest.approx(loss_o, rel=1e-4)
+    sur.close()
