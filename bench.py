@@ -865,6 +865,23 @@ def ensemble_leg(G, torch, dev, flush, sur, margins, reps=3):
         ok = ok and rc == 0
         terms.append(max(r["n_terms"] for rb in rp for r in rb))
     torch.cuda.nvtx.range_pop()
+    # both forms of the step: one persistent launch (device-side checks and
+    # stopping decisions) and one launch per term (host-side checks)
+    modes = {}
+    for name, pers in (("persistent_launch", True), ("launch_per_term", False)):
+        ens.set_series_mode(persistent=pers)
+        for _ in range(2):
+            step()
+        mts = []
+        for _ in range(reps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            rc_m, _ = step()
+            torch.cuda.synchronize()
+            mts.append((time.perf_counter() - t0) * 1e3)
+        modes[name] = {"brownian_step_ms": float(np.mean(mts)), "converged": rc_m == 0}
+    ens.set_series_mode(persistent=True)
     f = torch.randn(beads * ENS_NRHS * 3, dtype=torch.float64, device="cuda")
     u = torch.empty_like(f)
     ens.matvec_dev(ENS_NRHS, f.data_ptr(), u.data_ptr())
@@ -895,6 +912,7 @@ def ensemble_leg(G, torch, dev, flush, sur, margins, reps=3):
             "brownian_step_ms": step_s * 1e3,
             "series_steps_per_s": ENS_K * ENS_NRHS / step_s,
             "cheb_terms_max": terms, "converged": ok,
+            "step_forms": modes,
             "matvec_8rhs_ms": float(np.mean(mv)),
             "term_kernel": {"kernel": "k_ens_pair<true> (stored tensors, 8 lanes per slot)",
                             "bytes": term_bytes, "ms": ms_term,

@@ -20,6 +20,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdio>
 #include <cmath>
 #include <map>
 #include <string>
@@ -253,17 +254,17 @@ __global__ void k_ens_dot_fin(const int32_t *__restrict__ coff, const double *__
 // pass p waits until its suspension has completed pass p - 1 (a per-
 // suspension counter that the suspension's last tile of a pass advances,
 // after the decision when the pass is a CHECK); nothing waits on other
-// suspensions, so suspensions of different sizes and states overlap.  Block
-// c takes tiles c, c + G, c + 2G, ... in order: a tile only waits on tiles
-// of smaller index, all of which are held by running blocks (the launch is
-// cooperative, every block resident), so the smallest unfinished tile can
-// always proceed.  Every wait is bounded: a block that gives up sets the
-// error word and all blocks leave.  Data written inside the launch is read
-// through L2 (ld.global.cg): another block's writes are never served from a
-// stale L1 line.  The estimator sums are per tile and then per suspension
-// in tile order (deterministic).
+// suspensions, so suspensions of different sizes and states overlap.  A
+// free block takes the next tile in index order from one counter: a tile
+// only waits on tiles of smaller index, all of which have been taken by
+// running blocks (the launch is cooperative, every block resident), so the
+// smallest unfinished tile can always proceed.  Every wait is bounded: a block that gives up sets the
+// error word and all blocks leave.  A tile's reads of data other blocks
+// wrote in earlier passes follow the wait's acquire fence and a block
+// barrier; the per-series state and the partial sums are read through L2
+// (volatile / ld.global.cg).  The estimator sums are per tile and then per
+// suspension in tile order (deterministic).
 enum : int { kPassStart = 0, kPassTerm = 1, kPassTermCheck = 2, kPassCheck = 3 };
-constexpr int kSeriesThreads = 256;
 constexpr int kPartKinds = 4;  // aux2 (x0 . M x0), |dw|^2, |x_{k+1}|^2, |M dw|^2
 
 struct SeriesArgs {
@@ -289,6 +290,7 @@ struct SeriesArgs {
   double *aux2;               // [K * 8]
   unsigned int *arrive, *done;  // [K] tiles finished / passes completed
   int *n_active, *all_done, *err;
+  unsigned long long *claim;  // next tile to take (tiles are taken in order)
   uint32_t polls;
   int never_ready;            // test hook: every wait runs out
 };
@@ -304,6 +306,7 @@ __device__ __forceinline__ double *series_xp(const SeriesArgs &a, int q) {
 // sum over r-lanes of a per-thread value: lane % 8 is the right-hand side;
 // sums of the 8 right-hand sides land in sh[w][r], then in out[r] (warps in
 // order; fixed tree, deterministic)
+template <int NT>
 __device__ __forceinline__ void tile_rsum(double v, double (*sh)[kR], double *out) {
   v += __shfl_xor_sync(0xffffffffu, v, 8);
   v += __shfl_xor_sync(0xffffffffu, v, 16);
@@ -312,19 +315,33 @@ __device__ __forceinline__ void tile_rsum(double v, double (*sh)[kR], double *ou
   __syncthreads();
   if (threadIdx.x < kR) {
     double t = 0.0;
-    for (int q = 0; q < kSeriesThreads / 32; ++q) t += sh[q][threadIdx.x];
+    for (int q = 0; q < NT / 32; ++q) t += sh[q][threadIdx.x];
     out[threadIdx.x] = t;
   }
   __syncthreads();
 }
 
-__global__ void __launch_bounds__(kSeriesThreads) k_ens_series(SeriesArgs a) {
-  __shared__ double sh[kSeriesThreads / 32][kR];
+// launch shapes of the persistent kernel (threads, blocks per SM that the
+// register cap must allow); the autotuner picks one with the tile size
+constexpr int kSeriesShapes = 3;
+constexpr int kSeriesShapeThreads[kSeriesShapes] = {256, 256, 128};
+constexpr int kSeriesShapeMinBlocks[kSeriesShapes] = {4, 6, 12};
+
+template <int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) k_ens_series(SeriesArgs a) {
+  __shared__ double sh[NT / 32][kR];
   __shared__ double dsum[kPartKinds][kR];
   __shared__ int s_go, s_last;
+  __shared__ long long s_g;
   const int tid = threadIdx.x;
   const int64_t total = (int64_t)a.T * a.npass;
-  for (int64_t g = blockIdx.x; g < total; g += gridDim.x) {
+  for (;;) {
+    // the next tile in pass-major order: a block that is free takes it, so
+    // cheap and expensive tiles balance over the blocks
+    if (tid == 0) s_g = (long long)atomicAdd(a.claim, 1ull);
+    __syncthreads();
+    const int64_t g = s_g;
+    if (g >= total) return;
     const int p = (int)(g / a.T);
     const int tl = (int)(g - (int64_t)p * a.T);
     const int b = a.tile_b[tl];
@@ -348,10 +365,20 @@ __global__ void __launch_bounds__(kSeriesThreads) k_ens_series(SeriesArgs a) {
         __nanosleep(128);
       }
       __threadfence();
+      // a suspension whose series have all stopped skips the work of its
+      // later passes (its tiles still arrive, so that its passes complete);
+      // the flags are read after the wait, when every earlier decision of
+      // this suspension is visible
+      if (go && type != kPassStart) {
+        int any = 0;
+        for (int r = 0; r < kR; ++r) any |= *(volatile const uint8_t *)(a.active + b * kR + r);
+        if (!any) go = 2;
+      }
       s_go = go;
     }
     __syncthreads();
     if (!s_go) return;  // an error, or every series has stopped
+    const bool work = s_go == 1;
     const int64_t s_begin = a.tile_s0[tl];
     const int64_t s_end = min(s_begin + a.S, a.off[b + 1]);
     const double tda = a.two_da[b], c1 = a.c1x[b];
@@ -361,7 +388,7 @@ __global__ void __launch_bounds__(kSeriesThreads) k_ens_series(SeriesArgs a) {
                                                                   : ((t - 1) % 2 ? a.F1 : a.F0));
     float4 *Fout = type == kPassStart ? a.F0 : (t % 2 ? a.F1 : a.F0);
     double v0 = 0.0, v1 = 0.0;  // this thread's estimator terms
-    for (int64_t i = tid; i < (int64_t)a.S * kR; i += kSeriesThreads) {
+    for (int64_t i = tid; work && i < (int64_t)a.S * kR; i += NT) {
       const int64_t s = s_begin + i / kR;
       const int r = (int)(i % kR);
       if (s >= s_end) continue;
@@ -374,7 +401,12 @@ __global__ void __launch_bounds__(kSeriesThreads) k_ens_series(SeriesArgs a) {
       for (int64_t m = e0; m < e1; ++m) {
         const uint32_t en = __ldg(a.list + m);
         const float4 tt = __ldg(a.ten + m);
-        const float4 fj = __ldcg(Fsrc + (int64_t)(en >> kCodeBits) * kR + r);
+        // a plain (L1-cacheable) load: the wait above ended with an acquire
+        // fence at gpu scope and a block barrier, which orders these reads
+        // after every write another block released for the previous pass
+        // (PTX memory model, message passing); L1 keeps the sources that
+        // neighbouring targets share
+        const float4 fj = Fsrc[(int64_t)(en >> kCodeBits) * kR + r];
         const float d = fmaf(tt.w, fj.z, fmaf(tt.z, fj.y, tt.y * fj.x));
         bx += fmaf(tt.x, fj.x, d * tt.y);
         by += fmaf(tt.x, fj.y, d * tt.z);
@@ -439,12 +471,12 @@ __global__ void __launch_bounds__(kSeriesThreads) k_ens_series(SeriesArgs a) {
     }
     // ---- this tile's estimator sums ----
     double *pt = a.part + (int64_t)tl * kPartKinds * kR;
-    if (type == kPassStart) tile_rsum(v0, sh, pt + 0 * kR);
+    if (type == kPassStart) tile_rsum<NT>(v0, sh, pt + 0 * kR);
     if (type == kPassTermCheck) {
-      tile_rsum(v0, sh, pt + 1 * kR);
-      tile_rsum(v1, sh, pt + 2 * kR);
+      tile_rsum<NT>(v0, sh, pt + 1 * kR);
+      tile_rsum<NT>(v1, sh, pt + 2 * kR);
     }
-    if (type == kPassCheck) tile_rsum(v0, sh, pt + 3 * kR);
+    if (type == kPassCheck) tile_rsum<NT>(v0, sh, pt + 3 * kR);
     // ---- finish the tile; the suspension's last tile of the pass completes it ----
     __syncthreads();
     const int nt = a.susp_tile0[b + 1] - a.susp_tile0[b];
@@ -464,9 +496,9 @@ __global__ void __launch_bounds__(kSeriesThreads) k_ens_series(SeriesArgs a) {
         const int kd = type == kPassStart ? 0 : q + 1;
         double acc = 0.0;
         const int r = tid % kR;
-        for (int j = tid / kR; j < nt; j += kSeriesThreads / kR)
+        for (int j = tid / kR; j < nt; j += NT / kR)
           acc += __ldcg(a.part + ((int64_t)(a.susp_tile0[b] + j) * kPartKinds + kd) * kR + r);
-        tile_rsum(acc, sh, dsum[kd]);
+        tile_rsum<NT>(acc, sh, dsum[kd]);
       }
       (void)kind;
       if (tid < kR) {
@@ -551,7 +583,8 @@ struct ggem_ensemble {
   // the persistent series launch (k_ens_series): tiles of S slots of one
   // suspension, their per-pass estimator partials, counters and reports
   bool persistent = true;
-  int S = 64;                  // slots per tile (autotuned)
+  int S = 128;                 // slots per tile (autotuned)
+  int series_shape = 1;        // launch shape of k_ens_series (autotuned)
   int T = 0;                   // tiles per pass
   int tiles_for_S = 0;         // S the tile tables were built for
   int64_t tiles_for_ntot = -1;
@@ -559,6 +592,7 @@ struct ggem_ensemble {
   DevBuf<int64_t> tile_s0;
   DevBuf<double> part, aux2;
   DevBuf<unsigned int> sync;   // arrive[K], done[K], n_active, all_done, err
+  DevBuf<unsigned long long> claim;
   DevBuf<ggem_cheb_report> d_rep;
   uint32_t series_polls = 1u << 26;  // bounded waits of the persistent launch
   int never_ready = 0;               // test hook: every wait runs out
@@ -874,13 +908,22 @@ int ensure_tiles(ggem_ensemble *e) {
   return GGEM_OK;
 }
 
+const void *series_kernel(int shape) {
+  switch (shape) {
+    case 0: return (const void *)k_ens_series<kSeriesShapeThreads[0], kSeriesShapeMinBlocks[0]>;
+    case 1: return (const void *)k_ens_series<kSeriesShapeThreads[1], kSeriesShapeMinBlocks[1]>;
+    default: return (const void *)k_ens_series<kSeriesShapeThreads[2], kSeriesShapeMinBlocks[2]>;
+  }
+}
+
 // blocks of the persistent launch: every block resident (cooperative)
-int series_grid(ggem_ensemble *e, int *grid) {
+int series_grid(ggem_ensemble *e, int shape, int *grid) {
   int sms = 0, per = 0, coop = 0;
   cudaError_t c;
   if ((c = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, e->device)) ||
       (c = cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, e->device)) ||
-      (c = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_ens_series, kSeriesThreads, 0)))
+      (c = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, series_kernel(shape),
+                                                          kSeriesShapeThreads[shape], 0)))
     return ecuda(e, c, "series occupancy");
   if (!coop || per < 1) return efail(e, GGEM_ERR_CUDA, "cooperative launch unavailable");
   *grid = sms * per;
@@ -938,7 +981,7 @@ int brownian_persistent(ggem_ensemble *e, int nrhs, int N, const double *eig_min
   cudaError_t c;
   if ((c = e->coef.ensure((size_t)K * ldc)) || (c = e->pass_type.ensure(npass)) ||
       (c = e->pass_term.ensure(npass)) || (c = e->sync.ensure(sync0.size())) ||
-      (c = e->d_rep.ensure((size_t)K * kR)))
+      (c = e->claim.ensure(1)) || (c = e->d_rep.ensure((size_t)K * kR)))
     return ecuda(e, c, "series tables");
   if ((c = cudaMemcpyAsync(e->coef.p, coef.data(), sizeof(double) * K * ldc,
                            cudaMemcpyHostToDevice, e->stream)) ||
@@ -958,7 +1001,8 @@ int brownian_persistent(ggem_ensemble *e, int nrhs, int N, const double *eig_min
       (c = cudaMemcpyAsync(e->sync.p, sync0.data(), sizeof(unsigned int) * sync0.size(),
                            cudaMemcpyHostToDevice, e->stream)) ||
       (c = cudaMemcpyAsync(e->d_rep.p, r0.data(), sizeof(ggem_cheb_report) * r0.size(),
-                           cudaMemcpyHostToDevice, e->stream)))
+                           cudaMemcpyHostToDevice, e->stream)) ||
+      (c = cudaMemsetAsync(e->claim.p, 0, sizeof(unsigned long long), e->stream)))
     return ecuda(e, c, "series tables");
   SeriesArgs a;
   a.ntot = e->ntot;
@@ -1002,14 +1046,16 @@ int brownian_persistent(ggem_ensemble *e, int nrhs, int N, const double *eig_min
   a.n_active = reinterpret_cast<int *>(e->sync.p + 2 * K);
   a.all_done = reinterpret_cast<int *>(e->sync.p + 2 * K + 1);
   a.err = reinterpret_cast<int *>(e->sync.p + 2 * K + 2);
+  a.claim = e->claim.p;
   a.polls = e->series_polls;
   a.never_ready = e->never_ready;
   int grid = 0;
-  if (int rc = series_grid(e, &grid)) return rc;
+  const int shape = e->series_shape;
+  if (int rc = series_grid(e, shape, &grid)) return rc;
   grid = (int)std::min<int64_t>(grid, (int64_t)e->T * npass);
   void *args[] = {&a};
-  if ((c = cudaLaunchCooperativeKernel((const void *)k_ens_series, dim3(grid),
-                                       dim3(kSeriesThreads), args, 0, e->stream)))
+  if ((c = cudaLaunchCooperativeKernel(series_kernel(shape), dim3(grid),
+                                       dim3(kSeriesShapeThreads[shape]), args, 0, e->stream)))
     return ecuda(e, c, "series launch");
   if (int rc = elaunch(e, "series")) return rc;
   k_ens_from_slots<<<gv, 256, 0, e->stream>>>(e->ntot, nrhs, e->order_g.p, e->v[4].p, d_dw);
@@ -1059,6 +1105,102 @@ extern "C" int ggem_ensemble_set_series_mode(ggem_ensemble *e, int persistent, i
   if (slots_per_tile) e->S = slots_per_tile;
   e->series_polls = wait_polls ? wait_polls : (1u << 26);
   e->never_ready = never_ready != 0;
+  return GGEM_OK;
+}
+
+extern "C" int ggem_ensemble_autotune_series(ggem_ensemble *e, int nrhs, int N,
+                                             const double *eig_min, const double *eig_max,
+                                             double tol, const double *d_xi, double *d_dw,
+                                             const char *cache_path, int *shape,
+                                             int *slots_per_tile, double *ms_per_step) {
+  if (!e || nrhs < 1 || nrhs > kR || N < 2 || !eig_min || !eig_max || !d_xi || !d_dw || !shape ||
+      !slots_per_tile || !ms_per_step)
+    return GGEM_ERR_BAD_ARG;
+  if (!e->built) return efail(e, GGEM_ERR_BAD_ARG, "set the ensemble's particles first");
+  EnsGuard g(e->device);
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, e->device) != cudaSuccess) {
+    cudaGetLastError();
+    return efail(e, GGEM_ERR_CUDA, "device properties");
+  }
+  // the cache key: the device, the ensemble's sizes and the right-hand sides
+  std::string key = std::string(prop.name) + "|K=" + std::to_string(e->K) +
+                    "|beads=" + std::to_string(e->ntot) + "|pairs=" + std::to_string(e->pairs) +
+                    "|W=" + std::to_string(e->W) + "|rhs=" + std::to_string(nrhs);
+  for (char &ch : key)
+    if (ch == ' ') ch = '_';
+  if (cache_path) {
+    if (FILE *fp = std::fopen(cache_path, "r")) {
+      char k[512];
+      int sh = 0, S = 0;
+      double ms = 0.0;
+      bool hit = false;
+      while (std::fscanf(fp, "%511s %d %d %lf", k, &sh, &S, &ms) == 4)
+        if (key == k && sh >= 0 && sh < kSeriesShapes && S >= 8 && S <= 1024) {
+          e->series_shape = sh;
+          e->S = S;
+          *shape = sh;
+          *slots_per_tile = S;
+          *ms_per_step = ms;
+          hit = true;
+        }
+      std::fclose(fp);
+      if (hit) {
+        e->persistent = true;
+        return GGEM_OK;
+      }
+    }
+  }
+  // time one Brownian step of every series for each launch shape and tile
+  // size (tol = 0: every series runs the same N - 1 terms)
+  const int tiles[3] = {64, 128, 256};
+  const bool keep_pers = e->persistent;
+  const int keep_pred = e->pred_terms;
+  e->persistent = true;
+  double best = 1e30;
+  int best_sh = e->series_shape, best_S = e->S;
+  std::vector<ggem_cheb_report> rep((size_t)e->K * nrhs);
+  cudaEvent_t t0, t1;
+  cudaEventCreate(&t0);
+  cudaEventCreate(&t1);
+  int rc = GGEM_OK;
+  for (int sh = 0; sh < kSeriesShapes && (rc == GGEM_OK || rc == GGEM_ERR_CHEB_NOT_CONVERGED); ++sh)
+    for (int S : tiles) {
+      e->series_shape = sh;
+      e->S = S;
+      e->pred_terms = N;
+      rc = brownian_persistent(e, nrhs, N, eig_min, eig_max, 0.0, d_xi, d_dw, rep.data());
+      if (rc != GGEM_OK && rc != GGEM_ERR_CHEB_NOT_CONVERGED) break;
+      cudaEventRecord(t0, e->stream);
+      e->pred_terms = N;
+      rc = brownian_persistent(e, nrhs, N, eig_min, eig_max, 0.0, d_xi, d_dw, rep.data());
+      cudaEventRecord(t1, e->stream);
+      cudaEventSynchronize(t1);
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, t0, t1);
+      if (rc != GGEM_OK && rc != GGEM_ERR_CHEB_NOT_CONVERGED) break;
+      if (ms < best) {
+        best = ms;
+        best_sh = sh;
+        best_S = S;
+      }
+    }
+  cudaEventDestroy(t0);
+  cudaEventDestroy(t1);
+  e->persistent = keep_pers;
+  e->pred_terms = keep_pred;
+  if (rc != GGEM_OK && rc != GGEM_ERR_CHEB_NOT_CONVERGED) return rc;
+  e->series_shape = best_sh;
+  e->S = best_S;
+  *shape = best_sh;
+  *slots_per_tile = best_S;
+  *ms_per_step = best;
+  if (cache_path) {
+    if (FILE *fp = std::fopen(cache_path, "a")) {
+      std::fprintf(fp, "%s %d %d %.6f\n", key.c_str(), best_sh, best_S, best);
+      std::fclose(fp);
+    }
+  }
   return GGEM_OK;
 }
 

@@ -183,6 +183,8 @@ def lib():
         "ggem_ensemble_lanczos": (i, [vp, i, i, C.c_uint64, P(d), P(d)]),
         "ggem_ensemble_autotune": (i, [vp, i, P(i), P(d)]),
         "ggem_ensemble_set_series_mode": (i, [vp, i, i, C.c_uint32, i]),
+        "ggem_ensemble_autotune_series": (i, [vp, i, i, vp, vp, d, vp, vp, C.c_char_p, P(i),
+                                              P(i), P(d)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -811,6 +813,17 @@ class Ensemble:
         self._check(lib().ggem_ensemble_set_series_mode(self.h, 1 if persistent else 0,
                                                         int(slots_per_tile), int(wait_polls),
                                                         1 if never_ready else 0))
+
+    def autotune_series(self, nrhs, N, eig_min, eig_max, d_xi, d_dw, cache_path=None):
+        """(shape, slots per tile, ms per step) of the fastest persistent
+        launch; cache_path keeps the choice across runs"""
+        lo = np.ascontiguousarray(eig_min, dtype=np.float64)
+        hi = np.ascontiguousarray(eig_max, dtype=np.float64)
+        sh, S, ms = C.c_int(), C.c_int(), C.c_double()
+        self._check(lib().ggem_ensemble_autotune_series(
+            self.h, int(nrhs), int(N), _p(lo), _p(hi), 0.0, C.c_void_p(d_xi), C.c_void_p(d_dw),
+            cache_path.encode() if cache_path else None, C.byref(sh), C.byref(S), C.byref(ms)))
+        return sh.value, S.value, ms.value
 
     def intervals(self, sur, chain_fraction=None, margin_lo=0.0, margin_hi=0.0):
         cf = np.zeros(self.K) if chain_fraction is None else \

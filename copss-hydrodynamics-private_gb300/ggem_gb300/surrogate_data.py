@@ -1,7 +1,9 @@
 """Training set and training run of the eigen-interval network.
 
 Configurations follow the learned-surrogate workload: N log-uniform in
-[1000, 50000] beads of radius 1, volume fraction uniform in [0.02, 0.2],
+[1000, 50000] beads of radius 1 (the shipped network: [1000, 200000], so
+that the benchmark's 200k-bead suspension lies inside the training range),
+volume fraction uniform in [0.02, 0.2],
 a chain fraction from {0, 1/4, 1/2, 3/4, 1} of the beads in 20-bead chains
 (bond 2a, self-avoiding growth) and the rest free (random sequential
 addition), periodic cube, alpha = 0.5, rc = 7.  Each configuration gives
@@ -18,7 +20,7 @@ Command line (writes an .npz with the parameters, the normalisation, the
 margins and the held-out statistics):
 
     python -m ggem_gb300.surrogate_data --configs 22000 --holdout 2000 \
-        --out eigen_surrogate.npz
+        --n-max 200000 --out eigen_surrogate.npz
 """
 from __future__ import annotations
 
@@ -147,6 +149,8 @@ def main():
     ap.add_argument("--holdout", type=int, default=2000)
     ap.add_argument("--seed", type=int, default=20261203)
     ap.add_argument("--lanczos-k", type=int, default=60)
+    ap.add_argument("--n-min", type=int, default=1000)
+    ap.add_argument("--n-max", type=int, default=50000)
     ap.add_argument("--epochs", type=int, default=300)
     ap.add_argument("--batch", type=int, default=256)
     ap.add_argument("--lr", type=float, default=2e-3)
@@ -155,7 +159,8 @@ def main():
     a = ap.parse_args()
     from .build import build
     build()
-    cfgs = sample_configs(a.configs, a.seed)
+    n_range = (a.n_min, a.n_max)
+    cfgs = sample_configs(a.configs, a.seed, n_range=n_range)
     t0 = time.perf_counter()
     X, Y = label(cfgs, k=a.lanczos_k, log=lambda m: print(m, flush=True))
     t_label = time.perf_counter() - t0
@@ -163,7 +168,7 @@ def main():
     sur, summary, loss = train(X[:ntr], Y[:ntr], X[ntr:], Y[ntr:], epochs=a.epochs,
                                batch=a.batch, lr=a.lr, seed=a.seed)
     summary.update({"label_seconds": t_label, "lanczos_k": a.lanczos_k, "configs": a.configs,
-                    "seed": a.seed})
+                    "seed": a.seed, "n_range": list(n_range), "phi_range": [0.02, 0.2]})
     save(a.out, sur, summary, loss)
     if a.data_out:
         np.savez(a.data_out, X=X, Y=Y)

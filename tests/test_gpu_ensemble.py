@@ -262,3 +262,45 @@ def test_persistent_series_wait_timeout_is_reported():
             assert rc == 0 and all(r["converged"] for rb in reps for r in rb)
             out.append(dw.cpu().numpy())
     assert rel(out[0], out[1]) <= 1e-12
+
+
+def test_series_autotuner_and_its_cache(tmp_path):
+    """The autotuner times every launch shape and tile size of the persistent
+    launch, keeps the fastest and appends it to the cache file; a second
+    ensemble of the same sizes reads the choice back without timing; the
+    tuned launch gives the launch-per-term path's displacements."""
+    import torch
+    sus = _ensemble(4, 44)
+    R = 8
+    d_xyz = _device(np.concatenate([x for x, _ in sus]))
+    xi = _device(np.random.default_rng(4).standard_normal((sum(len(x) for x, _ in sus), R, 3)))
+    cache = tmp_path / "series_tune.txt"
+    out = []
+    for run in range(2):
+        with G.Ensemble([L for _, L in sus]) as ens:
+            ens.set_particles_dev([len(x) for x, _ in sus], d_xyz.data_ptr())
+            bounds = [ens.lanczos(b, k=40, seed=1) for b in range(len(sus))]
+            lo = np.array([x[0] for x in bounds]) / 1.05
+            hi = np.array([x[1] for x in bounds]) * 1.05
+            dw = torch.empty_like(xi)
+            t0 = __import__("time").perf_counter()
+            sh, S, ms = ens.autotune_series(R, 14, lo, hi, xi.data_ptr(), dw.data_ptr(),
+                                            str(cache))
+            dt = __import__("time").perf_counter() - t0
+            assert 0 <= sh < 3 and S in (64, 128, 256) and ms > 0
+            lines = cache.read_text().splitlines()
+            assert len(lines) == 1  # the second run reads the line, it does not add one
+            out.append((sh, S, ms, dt))
+            rc, _ = ens.brownian_dev(R, 50, lo, hi, 1e-3, xi.data_ptr(), dw.data_ptr())
+            assert rc == 0
+            got = dw.cpu().numpy()
+    assert out[0][:3] == out[1][:3]
+    with G.Ensemble([L for _, L in sus]) as ens:
+        ens.set_particles_dev([len(x) for x, _ in sus], d_xyz.data_ptr())
+        ens.set_series_mode(persistent=False)
+        dw = torch.empty_like(xi)
+        rc, _ = ens.brownian_dev(R, 50, lo, hi, 1e-3, xi.data_ptr(), dw.data_ptr())
+        assert rc == 0
+        assert rel(got, dw.cpu().numpy()) <= 1e-12
+    print(f"series autotune: shape {out[0][0]}, {out[0][1]} slots per tile, "
+          f"{out[0][2]:.3f} ms per 14-term step; tuning {out[0][3]:.2f} s, cache hit {out[1][3]:.3f} s")
