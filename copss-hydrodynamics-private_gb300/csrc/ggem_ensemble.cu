@@ -277,7 +277,8 @@ struct SeriesArgs {
   const int32_t *susp;
   const int32_t *tile_b;      // [T] suspension of every tile of a pass
   const int64_t *tile_s0;     // [T] first slot of every tile
-  const int32_t *susp_tile0;  // [K + 1] first tile of every suspension
+  const int32_t *susp_tile0;  // [K] first tile of every suspension
+  const int32_t *susp_ntile;  // [K] its number of tiles
   const int64_t *off;         // [K + 1] first slot of every suspension
   const int32_t *pass_type;   // [npass]
   const int32_t *pass_term;   // [npass] term index t (x_{t+1} is formed)
@@ -479,7 +480,7 @@ __global__ void __launch_bounds__(NT, MINB) k_ens_series(SeriesArgs a) {
     if (type == kPassCheck) tile_rsum<NT>(v0, sh, pt + 3 * kR);
     // ---- finish the tile; the suspension's last tile of the pass completes it ----
     __syncthreads();
-    const int nt = a.susp_tile0[b + 1] - a.susp_tile0[b];
+    const int nt = a.susp_ntile[b];
     if (tid == 0) {
       __threadfence();
       const unsigned old = atomicAdd(a.arrive + b, 1u);
@@ -588,7 +589,7 @@ struct ggem_ensemble {
   int T = 0;                   // tiles per pass
   int tiles_for_S = 0;         // S the tile tables were built for
   int64_t tiles_for_ntot = -1;
-  DevBuf<int32_t> tile_b, susp_tile0, pass_type, pass_term;
+  DevBuf<int32_t> tile_b, susp_tile0, susp_ntile, pass_type, pass_term;
   DevBuf<int64_t> tile_s0;
   DevBuf<double> part, aux2;
   DevBuf<unsigned int> sync;   // arrive[K], done[K], n_active, all_done, err
@@ -876,23 +877,34 @@ int ens_dot(ggem_ensemble *e, const double *a, const double *b, double *out) {
 
 namespace {
 
-// tile tables of the persistent launch for the current bead counts and S
+// tile tables of the persistent launch for the current bead counts and S.
+// Within a pass the suspensions' tiles follow in order of decreasing size:
+// the many tiles of the large suspensions are taken first, so their pass is
+// complete by the time the next pass reaches them, and the tiles taken last
+// (whose next-pass tiles wait longest) are the small suspensions' few
+static_assert(sizeof(int32_t) == 4, "tile tables");
 int ensure_tiles(ggem_ensemble *e) {
   if (e->tiles_for_S == e->S && e->tiles_for_ntot == e->ntot && e->T > 0) return GGEM_OK;
-  std::vector<int32_t> tb, st0(e->K + 1, 0);
+  std::vector<int> by_size(e->K);
+  for (int b = 0; b < e->K; ++b) by_size[b] = b;
+  std::stable_sort(by_size.begin(), by_size.end(),
+                   [&](int x, int y) { return e->n[x] > e->n[y]; });
+  std::vector<int32_t> tb, st0(e->K, 0), ntl(e->K, 0);
   std::vector<int64_t> ts;
-  for (int b = 0; b < e->K; ++b) {
+  for (int b : by_size) {
     st0[b] = (int32_t)tb.size();
     for (int64_t s0 = e->off[b]; s0 < e->off[b + 1]; s0 += e->S) {
       tb.push_back(b);
       ts.push_back(s0);
     }
+    ntl[b] = (int32_t)tb.size() - st0[b];
   }
-  st0[e->K] = (int32_t)tb.size();
   e->T = (int)tb.size();
   cudaError_t c;
   if ((c = e->tile_b.ensure(tb.size())) || (c = e->tile_s0.ensure(ts.size())) ||
-      (c = e->susp_tile0.ensure(st0.size())) ||
+      (c = e->susp_tile0.ensure(st0.size())) || (c = e->susp_ntile.ensure(ntl.size())) ||
+      (c = cudaMemcpyAsync(e->susp_ntile.p, ntl.data(), sizeof(int32_t) * ntl.size(),
+                           cudaMemcpyHostToDevice, e->stream)) ||
       (c = e->part.ensure((size_t)e->T * kPartKinds * kR)) ||
       (c = e->aux2.ensure((size_t)e->K * kR)) ||
       (c = cudaMemcpyAsync(e->tile_b.p, tb.data(), sizeof(int32_t) * tb.size(),
@@ -1021,6 +1033,7 @@ int brownian_persistent(ggem_ensemble *e, int nrhs, int N, const double *eig_min
   a.tile_b = e->tile_b.p;
   a.tile_s0 = e->tile_s0.p;
   a.susp_tile0 = e->susp_tile0.p;
+  a.susp_ntile = e->susp_ntile.p;
   a.off = e->d_off.p;
   a.pass_type = e->pass_type.p;
   a.pass_term = e->pass_term.p;

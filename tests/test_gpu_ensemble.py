@@ -294,7 +294,7 @@ def test_series_autotuner_and_its_cache(tmp_path):
             rc, _ = ens.brownian_dev(R, 50, lo, hi, 1e-3, xi.data_ptr(), dw.data_ptr())
             assert rc == 0
             got = dw.cpu().numpy()
-    assert out[0][:3] == out[1][:3]
+    assert out[0][:2] == out[1][:2] and out[1][2] == pytest.approx(out[0][2], rel=1e-5)
     with G.Ensemble([L for _, L in sus]) as ens:
         ens.set_particles_dev([len(x) for x, _ in sus], d_xyz.data_ptr())
         ens.set_series_mode(persistent=False)
