@@ -360,7 +360,8 @@ __global__ void __launch_bounds__(32 * kListWarps, 6) k_pair_list_warp(
     const int32_t *__restrict__ start, const float4 *__restrict__ pos32,
     const double4_32a *__restrict__ pos64, float rc2_lo, float rc2_hi, double rc2, int W,
     int32_t *__restrict__ count, uint32_t *__restrict__ list,
-    unsigned long long *__restrict__ stat, int *__restrict__ err) {
+    unsigned long long *__restrict__ stat, int *__restrict__ err,
+    int32_t *__restrict__ count_h, uint32_t *__restrict__ list_h) {
   __shared__ int32_t s_base[kListWarps][kMaxStencil];
   __shared__ int32_t s_pre[kListWarps][kMaxStencil + 1];
   __shared__ int32_t s_code[kListWarps][kMaxStencil];
@@ -412,7 +413,7 @@ __global__ void __launch_bounds__(32 * kListWarps, 6) k_pair_list_warp(
     __syncwarp();  // the previous chunk's targets are no longer read
     s_pi[w][lane] = own_ok ? pos32[own] : make_float4(0.f, 0.f, 0.f, 0.f);
     __syncwarp();
-    int32_t own_cnt = 0;
+    int32_t own_cnt = 0, own_cnt_h = 0;
     for (int32_t v0 = 0; v0 < V; v0 += 32) {
       const int32_t v = v0 + lane;
       const bool valid = v < V;
@@ -452,9 +453,22 @@ __global__ void __launch_bounds__(32 * kListWarps, 6) k_pair_list_warp(
           if (k < W) list[(int64_t)ti * W + k] = ((uint32_t)t << kCodeBits) | (uint32_t)code;
         }
         if (lane == i) own_cnt += __popc(bal);
+        if (list_h) {
+          // the half list: each unordered pair once, in the row of its
+          // smaller slot (the full list is symmetric, its predicate exact)
+          const bool in_h = in && t > ti;
+          const unsigned bal_h = __ballot_sync(0xffffffffu, in_h);
+          const int32_t at_h = __shfl_sync(0xffffffffu, own_cnt_h, i);
+          if (in_h) {
+            const int32_t k = at_h + __popc(bal_h & lt_mask);
+            if (k < W) list_h[(int64_t)ti * W + k] = ((uint32_t)t << kCodeBits) | (uint32_t)code;
+          }
+          if (lane == i) own_cnt_h += __popc(bal_h);
+        }
       }
     }
     if (own_ok) {
+      if (count_h) count_h[own] = min(own_cnt_h, W);
       count[own] = min(own_cnt, W);  // the stored entries; the full length goes to stat
       cell_total += (unsigned long long)own_cnt;
       cell_max = max(cell_max, own_cnt);
@@ -592,9 +606,13 @@ int build_pair_list(ggem_ctx *c) {
       return cuda_fail(c, e, "memset");
     c->list_stat_zero = false;
     kt_start(c, kKListBuild);
+    if (c->sym_pairs && ((e = c->nb_list_h.ensure((size_t)n * c->nb_w)) ||
+                         (e = c->nb_cnt_h.ensure(n))))
+      return cuda_fail(c, e, "half pair list");
     k_pair_list_warp<<<cb, 32 * kListWarps, 0, st>>>(
         c->grid, c->d_stencil.p, nst, c->d_shift.p, c->cell_start.p, c->pos32.p, c->pos64.p,
-        c->rc2_lo, c->rc2_hi, c->rc2, c->nb_w, c->nb_cnt.p, c->nb_list.p, c->nb_stat.p, c->err.p);
+        c->rc2_lo, c->rc2_hi, c->rc2, c->nb_w, c->nb_cnt.p, c->nb_list.p, c->nb_stat.p, c->err.p,
+        c->sym_pairs ? c->nb_cnt_h.p : nullptr, c->sym_pairs ? c->nb_list_h.p : nullptr);
     kt_stop(c, kKListBuild);
     if (int rc = check_launch(c, "pair list")) return rc;
     c->cells_built = true;
@@ -613,10 +631,13 @@ int build_pair_list(ggem_ctx *c) {
     if ((e = c->nb_list.ensure((size_t)n * W))) return cuda_fail(c, e, "pair list");
     if ((e = cudaMemsetAsync(c->nb_stat.p, 0, 2 * sizeof(unsigned long long), st)))
       return cuda_fail(c, e, "memset");
+    if (c->sym_pairs && ((e = c->nb_list_h.ensure((size_t)n * W)) || (e = c->nb_cnt_h.ensure(n))))
+      return cuda_fail(c, e, "half pair list");
     if (attempt == 0) kt_start(c, kKListBuild);
     k_pair_list_warp<<<cb, 32 * kListWarps, 0, st>>>(
         c->grid, c->d_stencil.p, nst, c->d_shift.p, c->cell_start.p, c->pos32.p, c->pos64.p,
-        c->rc2_lo, c->rc2_hi, c->rc2, W, c->nb_cnt.p, c->nb_list.p, c->nb_stat.p, c->err.p);
+        c->rc2_lo, c->rc2_hi, c->rc2, W, c->nb_cnt.p, c->nb_list.p, c->nb_stat.p, c->err.p,
+        c->sym_pairs ? c->nb_cnt_h.p : nullptr, c->sym_pairs ? c->nb_list_h.p : nullptr);
     if (attempt == 0) kt_stop(c, kKListBuild);  // a widened refill is left out
     if (int rc = check_launch(c, "pair list")) return rc;
     h[2] = 0;

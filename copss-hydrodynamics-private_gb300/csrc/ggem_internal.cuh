@@ -128,6 +128,15 @@ struct ggem_ctx {
   // the FP64 pair kernel then walks the exact list instead of sweeping cells)
   bool list_built = false;
   bool f64_list = false;
+  // symmetric pair sums (ggem_set_symmetric_pairs): the list build also
+  // writes the half list (each unordered pair once, in the row of its smaller
+  // slot, same row width) and single-RHS FP32 matvecs evaluate each tensor
+  // once, scattering the source side into sym_acc (FP32, zero between uses)
+  bool sym_pairs = false;
+  ggem::DevBuf<int32_t> nb_cnt_h;
+  ggem::DevBuf<uint32_t> nb_list_h;
+  ggem::DevBuf<float4> sym_acc;
+  ggem::DevBuf<double> sym_part;
   // deferred checks (ggem_set_deferred_checks): a build after the first one
   // keeps the row width and leaves its statistics and error word on the
   // device; the next synchronising call reads them (list_unchecked)

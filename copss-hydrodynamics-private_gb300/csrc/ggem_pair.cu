@@ -450,6 +450,127 @@ __device__ __forceinline__ void block_partial_ff(float hi, float lo, double *__r
   if (threadIdx.x == 0) part[blockIdx.x] = v;
 }
 
+// ---- symmetric pair sums --------------------------------------------------
+// The tensor of a pair is symmetric (G(x) = G(-x)), so each unordered pair is
+// evaluated once, from the half list (the row of the smaller slot): the
+// target side A f_j + B (x.f_j) x is summed in registers as in pair_sum_r1,
+// the source side A f_i + B (x.f_i) x goes to the source's accumulator with
+// one 16-byte vector atomic (red.global.add.v4.f32).  The order in which a
+// source's contributions arrive varies from run to run, so the FP32 result
+// is not bit-reproducible (the FP64 paths and the full-row kernels are).
+__device__ __forceinline__ void red_add_v4(float4 *p, float x, float y, float z) {
+  asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(p), "f"(x), "f"(y),
+               "f"(z), "f"(0.f)
+               : "memory");
+}
+
+template <bool POLY>
+__device__ __forceinline__ PairSum pair_sum_sym(int64_t s, bool act, int sub, const Rec32 &ri,
+                                                const Rec32 *__restrict__ src,
+                                                const int32_t *__restrict__ cnt, int W,
+                                                const uint32_t *__restrict__ list,
+                                                const PolyAB &P, const Rec32 *__restrict__ tab,
+                                                float inv_ds, const float4 *sh,
+                                                float4 *__restrict__ acc) {
+  const uint32_t *lp = list + s * (int64_t)W + sub;
+  int left = (act ? cnt[s] : 0) - sub;
+  float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
+  float2 bxy = make_float2(0.f, 0.f);
+  float bz = 0.f;
+  int blk = 0;
+  const float2 fixy = make_float2(ri.b.x, ri.b.y);
+  uint32_t nxt = left > 0 ? __ldg(lp) : 0u;
+  while (left > 0) {
+    const uint32_t en = nxt;
+    left -= kGroup;
+    lp += kGroup;
+    if (left > 0) nxt = __ldg(lp);
+    const uint32_t j = en >> kCodeBits;
+    const Rec32 rj = ld_rec32(src + j);
+    const float4 o = sh[en & (kMaxCode - 1)];
+    const float dx = (rj.a.x - ri.a.x) + o.x;
+    const float dy = (rj.a.y - ri.a.y) + o.y;
+    const float dz = (rj.a.z - ri.a.z) + o.z;
+    const float s2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+    float A, B;
+    if (POLY) {
+      const float x = fmaf(s2, P.x1, P.x0);
+      const float2 xx = make_float2(x, x);
+      float2 ab = P.ab[kPolyDeg];
+#pragma unroll
+      for (int q = kPolyDeg - 1; q >= 0; --q) ab = __ffma2_rn(ab, xx, P.ab[q]);
+      const float p = s2 * P.e_hi;
+      const float r = fmaf(s2, P.e_lo, fmaf(s2, P.e_hi, -p));
+      const float E0 = ex2_sfu(p);
+      const float E = fmaf(E0, r * 0.6931471805599453f, E0);
+      ab = __fmul2_rn(ab, make_float2(E, E));
+      A = ab.x;
+      B = ab.y;
+    } else {
+      tensor_ab32<false>(s2, P, tab, inv_ds, A, B);
+    }
+    const float2 dxy = make_float2(dx, dy);
+    // target side: G f_j
+    const float2 fxy = make_float2(rj.b.x, rj.b.y);
+    const float2 pxy = __fmul2_rn(dxy, fxy);
+    const float bxf = B * fmaf(dz, rj.b.z, pxy.x + pxy.y);
+    bxy = __fadd2_rn(bxy, __ffma2_rn(make_float2(A, A), fxy,
+                                     __fmul2_rn(make_float2(bxf, bxf), dxy)));
+    bz += fmaf(A, rj.b.z, bxf * dz);
+    // source side: G f_i into the source's accumulator
+    const float2 qxy = __fmul2_rn(dxy, fixy);
+    const float bxi = B * fmaf(dz, ri.b.z, qxy.x + qxy.y);
+    const float2 vxy = __ffma2_rn(make_float2(A, A), fixy, __fmul2_rn(make_float2(bxi, bxi), dxy));
+    red_add_v4(acc + j, vxy.x, vxy.y, fmaf(A, ri.b.z, bxi * dz));
+    if (++blk == 8) {
+      kahan_add(sx, cx, bxy.x);
+      kahan_add(sy, cy, bxy.y);
+      kahan_add(sz, cz, bz);
+      bxy = make_float2(0.f, 0.f);
+      bz = 0.f;
+      blk = 0;
+    }
+  }
+  kahan_add(sx, cx, bxy.x);
+  kahan_add(sy, cy, bxy.y);
+  kahan_add(sz, cz, bz);
+  return PairSum{sx, -cx, sy, -cy, sz, -cz};
+}
+
+// the target sides of the half rows: part[3 s + c] (FP64 of the group's
+// float-float sum); the source sides accumulate in acc
+template <bool POLY>
+__global__ void __launch_bounds__(256, 6) k_pair_sym(
+    int64_t n, const Rec32 *__restrict__ src, const int32_t *__restrict__ cnt, int W,
+    const uint32_t *__restrict__ list, PolyAB P, const Rec32 *__restrict__ tab, float inv_ds,
+    const float4 *__restrict__ shift, float4 *__restrict__ acc, double *__restrict__ part) {
+  __shared__ float4 sh[kMaxCode];
+  stage_shifts(sh, shift);
+  const int64_t gid = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / kGroup;
+  const int sub = (int)(threadIdx.x % kGroup);
+  const bool act = gid < n;
+  const int64_t s = act ? gid : n - 1;
+  const Rec32 ri = src[s];
+  const PairSum r = pair_sum_sym<POLY>(s, act, sub, ri, src, cnt, W, list, P, tab, inv_ds, sh,
+                                       acc);
+  float h, l;
+  group_scatter3(sub, r, h, l);
+  if (act && sub < 3) part[3 * s + sub] = f2d_bits(h) + f2d_bits(l);
+}
+
+// u = part + acc + self term; acc is cleared for the next use
+__global__ void k_sym_finish(int64_t n, const double *__restrict__ part, float4 *__restrict__ acc,
+                             double self_c, const double *__restrict__ f, double *__restrict__ u) {
+  const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const float4 a = acc[s];
+  acc[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+  const float v[3] = {a.x, a.y, a.z};
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+    u[3 * s + c] = fma(self_c, f[3 * s + c], part[3 * s + c] + f2d_bits(v[c]));
+}
+
 // the per-matvec-tensor kernel shapes the autotuner chooses from: blocks of
 // 256 threads per SM that the register cap allows (6 at 40 registers, with a
 // few spilled epilogue values in some kernels; 5 at 48 without)
@@ -1253,6 +1374,36 @@ void dispatch_r1(ggem_ctx *c, const Rec32 *src, const double *f, double *u, doub
 }
 
 // single right-hand side: records from FP64 slot-order f, then the pair sum
+// u = M f for one right-hand side from the half list (k_pair_sym +
+// k_sym_finish); src holds the records of f
+int launch_sym_r1(ggem_ctx *c, const Rec32 *src, const double *f, double *u, double self_c) {
+  const int64_t n = c->n;
+  cudaError_t e;
+  if (c->sym_acc.count < (size_t)n) {
+    if ((e = c->sym_acc.ensure((size_t)n)) ||
+        (e = cudaMemsetAsync(c->sym_acc.p, 0, sizeof(float4) * c->sym_acc.count, c->stream)))
+      return cuda_fail(c, e, "symmetric accumulators");
+  }
+  if ((e = c->sym_part.ensure(3 * (size_t)n))) return cuda_fail(c, e, "symmetric sums");
+  const unsigned nb = (unsigned)((n * kGroup + 255) / 256);
+  kt_start(c, kKPairF32);
+  if (c->use_poly)
+    k_pair_sym<true><<<nb, 256, 0, c->stream>>>(
+        n, src, c->nb_cnt_h.p, c->nb_w, c->nb_list_h.p, poly_of(c),
+        reinterpret_cast<const Rec32 *>(c->tab.p), c->tab_inv_ds, c->d_shift.p, c->sym_acc.p,
+        c->sym_part.p);
+  else
+    k_pair_sym<false><<<nb, 256, 0, c->stream>>>(
+        n, src, c->nb_cnt_h.p, c->nb_w, c->nb_list_h.p, poly_of(c),
+        reinterpret_cast<const Rec32 *>(c->tab.p), c->tab_inv_ds, c->d_shift.p, c->sym_acc.p,
+        c->sym_part.p);
+  if (int rc = check_launch(c, "pair f32 symmetric")) return rc;
+  k_sym_finish<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(n, c->sym_part.p, c->sym_acc.p,
+                                                                  self_c, f, u);
+  kt_stop(c, kKPairF32);
+  return check_launch(c, "pair f32 symmetric finish");
+}
+
 int launch_f32_r1(ggem_ctx *c, const double *f, double *u, double self_c) {
   const int64_t n = c->n;
   cudaError_t e;
@@ -1269,6 +1420,7 @@ int launch_f32_r1(ggem_ctx *c, const double *f, double *u, double self_c) {
   Rec32 *src = reinterpret_cast<Rec32 *>(c->w_src.p);
   k_build_src<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(n, c->pos32.p, f, src);
   if (int rc = check_launch(c, "pair records")) return rc;
+  if (c->sym_pairs && c->nb_list_h.p) return launch_sym_r1(c, src, f, u, self_c);
   kt_start(c, kKPairF32);
   if (c->use_poly) dispatch_r1<true>(c, src, f, u, self_c);
   else dispatch_r1<false>(c, src, f, u, self_c);
@@ -1709,6 +1861,16 @@ int matvec_f32_staged(ggem_ctx *c, int nrhs, const double *f, double *u, int sel
 
 
 using namespace ggem;
+
+extern "C" int ggem_set_symmetric_pairs(ggem_ctx *ctx, int enable) {
+  if (!ctx) return GGEM_ERR_BAD_ARG;
+  if (ctx->prm.precision != GGEM_FP32 || ctx->prm.nb_mode != GGEM_NB_CUTOFF)
+    return ggem::fail(ctx, GGEM_ERR_BAD_ARG, "symmetric pair sums need a GGEM_FP32 cutoff context");
+  ctx->sym_pairs = enable != 0;
+  ctx->cells_built = false;  // the next ggem_build_cells writes (or drops) the half list
+  ctx->list_built = false;
+  return GGEM_OK;
+}
 
 extern "C" int ggem_set_pair_variant(ggem_ctx *ctx, int computed, int stored) {
   if (!ctx || computed < 0 || computed >= kNumComputedVariants || stored < 0 ||

@@ -124,6 +124,7 @@ def lib():
         "ggem_get_pair_storage": (i, [vp, P(i), P(i)]),
         "ggem_set_pair_tensors": (i, [vp, i]),
         "ggem_set_fp64_pair_list": (i, [vp, i]),
+        "ggem_set_symmetric_pairs": (i, [vp, i]),
         "ggem_autotune_pair_storage": (i, [vp, i, d, P(i), P(d), P(d), P(i)]),
         "ggem_set_pair_variant": (i, [vp, i, i]),
         "ggem_probe_fp32_peak": (i, [vp, P(d)]),
@@ -599,6 +600,10 @@ class Context:
     def set_fp64_pair_list(self, enable: bool):
         """FP64 cutoff contexts: walk the exact pair list instead of the cells"""
         self._check(lib().ggem_set_fp64_pair_list(self.h, 1 if enable else 0))
+
+    def set_symmetric_pairs(self, enable: bool):
+        """FP32 cutoff contexts: evaluate each unordered pair once (half list)"""
+        self._check(lib().ggem_set_symmetric_pairs(self.h, 1 if enable else 0))
 
     def set_pair_tensors(self, enable: bool):
         self._check(lib().ggem_set_pair_tensors(self.h, 1 if enable else 0))

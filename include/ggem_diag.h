@@ -47,6 +47,13 @@ int ggem_set_pair_tensors(ggem_ctx *ctx, int enable);
  * reference's FP64 arithmetic per pair); 0 (default) = sweep the 27 cells
  * around every bead.  Takes effect at the next ggem_build_cells. */
 int ggem_set_fp64_pair_list(ggem_ctx *ctx, int enable);
+/* GGEM_FP32 cutoff contexts: 1 = single-RHS matvecs with tensors evaluated
+ * per pair use the symmetry G_ij = G_ji: the list build also writes the
+ * half list, each unordered pair is evaluated once and its source side added
+ * to the source with a vector atomic (results within the FP32 tolerance,
+ * not bit-reproducible from run to run); 0 (default) = full rows.  Takes
+ * effect at the next ggem_build_cells. */
+int ggem_set_symmetric_pairs(ggem_ctx *ctx, int enable);
 /* autotune the pair storage on the current configuration (cells and list
  * built, FP32): times `reps` single-RHS matvecs with tensors evaluated per
  * pair and with stored tensors (plus the one tensor pass per build,

@@ -252,6 +252,33 @@ def test_fp32_matvec_error(nrhs, cell_div):
     assert comp <= 10 * FP32_TOL
 
 
+@pytest.mark.parametrize("cell_div", [1, 2])
+def test_fp32_matvec_symmetric_pairs(cell_div):
+    """Each unordered pair evaluated once from the half list, its source side
+    scattered by vector atomics: the oracle's velocities within the FP32
+    tolerance on consecutive matvecs (the accumulators are cleared between
+    uses) and across a rebuild."""
+    xyz, L = suspension(5000, 0.1, 31)
+    box = O.make_box([0] * 3, [L] * 3, [1, 1, 1])
+    c = O.constants(alpha=0.5)
+    nb = O.neighbors_cutoff(box, xyz, 7.0)
+    rng = np.random.default_rng(3)
+    with G.Context(box_hi=(L,) * 3, rc=7.0, precision=G.FP32, cell_div=cell_div) as ctx:
+        ctx.set_pair_tensors(False)
+        ctx.set_symmetric_pairs(True)
+        for rebuild in range(2):
+            ctx.set_particles(xyz)
+            ctx.build_cells()
+            for _ in range(2):
+                f = rng.standard_normal((len(xyz), 3))
+                want = O.local_matvec(c, box, xyz, nb, f, O.SELF_BEAD, nthreads=8)
+                got = ctx.local_matvec(f, G.SELF_BEAD)
+                err = rel(got, want)
+                comp = np.abs(got - want).max() / np.abs(want).max()
+                print(f"symmetric FP32 div={cell_div}: norm-wise {err:.2e}, max component {comp:.2e}")
+                assert err <= FP32_TOL and comp <= 10 * FP32_TOL
+
+
 def test_fp32_matvec_chains_short_bonds():
     xyz, L = G.make_chains(4, 150, 20, 2.0, 0.05)
     box = O.make_box([0] * 3, [L] * 3, [1, 1, 1])
