@@ -579,7 +579,7 @@ extern "C" int ggem_local_matvec_dev(ggem_ctx *ctx, int nrhs, const double *d_f,
   if (e == cudaSuccess) e = ctx->w_out.ensure(len);
   if (e) return cuda_fail(ctx, e, "matvec workspace");
   if (nrhs == 1 && ctx->prm.precision == GGEM_FP32 && ctx->prm.nb_mode == GGEM_NB_CUTOFF &&
-      !ctx->pretensor_ok && d_f != d_u)
+      !ctx->pretensor_ok && !ctx->sym_pairs && d_f != d_u)
     return matvec_orig_fused(ctx, d_f, d_u, ctx->w_in.p, self_mode);
   if (int rc = permute_to_slots(ctx, nrhs, d_f, ctx->w_in.p)) return rc;
   if (int rc = matvec_slots(ctx, nrhs, ctx->w_in.p, ctx->w_out.p, self_mode)) return rc;

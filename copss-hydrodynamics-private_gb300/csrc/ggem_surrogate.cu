@@ -187,7 +187,11 @@ __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
 }
 
-__device__ __forceinline__ float silu_f(float z) { return z * (1.f / (1.f + expf(-z))); }
+// the logistic function on the special-function unit (ex2 and a correctly
+// rounded reciprocal): a few ulp from 1 / (1 + e^-z), far below the BF16
+// rounding of the activations; every kernel of the network uses this one
+__device__ __forceinline__ float sigmoid_sfu(float z) { return __frcp_rn(1.f + __expf(-z)); }
+__device__ __forceinline__ float silu_f(float z) { return z * sigmoid_sfu(z); }
 
 constexpr int kMlpThreads = 256;  // 8 warps: warp w reads TMEM lanes 32 (w % 4) .. + 31,
                                   // columns 64 (w / 4) .. + 63
@@ -298,7 +302,7 @@ __global__ void __launch_bounds__(kMlpThreads) k_mlp_forward(
 }
 
 // ---- elementwise pieces ---------------------------------------------------
-__device__ __forceinline__ float sigmoidf(float z) { return 1.f / (1.f + expf(-z)); }
+__device__ __forceinline__ float sigmoidf(float z) { return sigmoid_sfu(z); }
 
 // standardised, zero-padded inputs: X [B x 48] and X^T [48 x B] (BF16);
 // rows >= n (batch padding) are zero
@@ -330,7 +334,7 @@ __global__ void k_bias_act(float *__restrict__ Z, const float *__restrict__ bias
   const float z = Z[k] + bias[c];
   Z[k] = z;
   if (hidden) {
-    const bf16 h = __float2bfloat16_rn(z * sigmoidf(z));
+    const bf16 h = __float2bfloat16_rn(silu_f(z));
     H[k] = h;
     Ht[(int64_t)c * B + r] = h;
   } else if (c < kOut) {

@@ -19,7 +19,7 @@ PKG = Path(__file__).resolve().parent
 LIB_PATH = PKG / "_lib" / "libggem_gb300.so"
 
 GGEM_OK = 0
-POLYMER_BEAD, POINT_PARTICLE, LAGRANGIAN_POINT = 0, 1, 2
+POLYMER_BEAD, LAGRANGIAN_POINT, POINT_PARTICLE = 0, 1, 2  # point_particle.h:36-41
 SELF_NONE, SELF_BEAD, SELF_LAGRANGIAN = 0, 1, 2
 NB_REFERENCE, NB_CUTOFF = 0, 1
 FP64, FP32 = 0, 1

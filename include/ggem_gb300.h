@@ -49,8 +49,8 @@ extern "C" {
 /* ---- enumerations ------------------------------------------------------ */
 /* PointType, point_particle.h:36-41 */
 #define GGEM_POLYMER_BEAD 0
-#define GGEM_POINT_PARTICLE 1
-#define GGEM_LAGRANGIAN_POINT 2
+#define GGEM_LAGRANGIAN_POINT 1
+#define GGEM_POINT_PARTICLE 2
 
 /* self term of the local mobility */
 #define GGEM_SELF_NONE 0       /* local_solution_bead as is (ggem_stokes.C:427-503)         */

@@ -23,7 +23,8 @@ extern "C" {
 #endif
 
 /* point types, point_particle.h:36-41 */
-enum { ORC_POLYMER_BEAD = 0, ORC_POINT_PARTICLE = 1, ORC_LAGRANGIAN_POINT = 2 };
+/* PointType, point_particle.h:36-41 */
+enum { ORC_POLYMER_BEAD = 0, ORC_LAGRANGIAN_POINT = 1, ORC_POINT_PARTICLE = 2 };
 
 /* self-term handling of the local mobility */
 enum {

@@ -3,8 +3,9 @@
 Only tests/, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
 ``bench.py`` import this module: it is the checker, never the product path.
 ``build_oracle()`` compiles ``oracle/ggem_oracle.c`` with the committed
-Makefile; the reference's own ``chebyshev.C`` is compiled into
-``oracle/_ref`` when the reference tree is present on this machine.
+Makefile; the reference's own ``chebyshev.C`` and ``ggem_stokes.C`` are
+compiled into ``oracle/_ref`` when the reference tree is present on this
+machine.
 """
 from __future__ import annotations
 
@@ -18,12 +19,13 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 LIB_PATH = HERE / "_build" / "libggem_oracle.so"
 REF_LIB_PATH = HERE / "_ref" / "libref_chebyshev.so"
+REF_GGEM_PATH = HERE / "_ref" / "libref_ggem.so"
 # the reference tree: GGEM_REFERENCE_SRC, else a checkout named "reference"
 # beside this repository (absent on machines that only run the tests)
 REF_SRC = Path(os.environ.get("GGEM_REFERENCE_SRC",
                               str(HERE.parent.parent / "reference" / "src")))
 
-POLYMER_BEAD, POINT_PARTICLE, LAGRANGIAN_POINT = 0, 1, 2
+POLYMER_BEAD, LAGRANGIAN_POINT, POINT_PARTICLE = 0, 1, 2  # point_particle.h:36-41
 SELF_NONE, SELF_BEAD, SELF_LAGRANGIAN = 0, 1, 2
 
 
@@ -66,10 +68,12 @@ OP_FN = C.CFUNCTYPE(None, C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_doubl
 
 _lib = None
 _ref = None
+_ref_ggem = None
 
 
 def build_oracle(with_ref: bool = True) -> None:
-    """Compile the oracle (and the reference chebyshev.C when available)."""
+    """Compile the oracle (and the reference chebyshev.C / ggem_stokes.C when
+    the reference tree is available)."""
     subprocess.run(["make", "-s", "-C", str(HERE), "all"], check=True)
     if with_ref and (REF_SRC / "chebyshev.C").exists():
         subprocess.run(["make", "-s", "-C", str(HERE), "ref",
@@ -138,6 +142,85 @@ def ref_lib():
         R.ref_chebyshev_coefficients.restype = C.c_int
         _ref = R
     return _ref
+
+
+def ref_ggem_lib():
+    """The reference's own GGEMStokes (ggem_stokes.C) behind the C entry
+    points of oracle/ref_ggem_entry.cpp (None when it was not built here)."""
+    global _ref_ggem
+    if _ref_ggem is None and REF_GGEM_PATH.exists():
+        R = C.CDLL(str(REF_GGEM_PATH))
+        d, i64, vp = C.c_double, C.c_int64, C.c_void_p
+        head = [d, d, d, C.c_int, d, d]
+        R.ref_ggem_green_local.argtypes = head + [vp, vp]
+        R.ref_ggem_local_bead.argtypes = head + [vp, vp, vp, i64, vp, vp, vp, vp, vp, vp]
+        R.ref_ggem_local_field.argtypes = head + [vp, vp, vp, i64, vp, vp, i64, vp, vp, i64,
+                                                  vp, vp, vp]
+        for fn in (R.ref_ggem_green_local, R.ref_ggem_local_bead, R.ref_ggem_local_field):
+            fn.restype = C.c_int
+        _ref_ggem = R
+    return _ref_ggem
+
+
+def _ref_head(c: "Consts", point_type: int, ibm_beta: float, hmin: float):
+    return (c.mu, c.alpha, c.br0, int(point_type), float(hmin), float(ibm_beta))
+
+
+def ref_green_local(c, x, point_type=POLYMER_BEAD, ibm_beta=0.75, hmin=1.0):
+    """green_tensor_local_regularized of the reference's own GGEMStokes"""
+    x = _f64(x)
+    G = np.zeros(9)
+    rc = ref_ggem_lib().ref_ggem_green_local(*_ref_head(c, point_type, ibm_beta, hmin),
+                                             _p(x), _p(G))
+    if rc:
+        raise ValueError("bad point type")
+    return G.reshape(3, 3)
+
+
+def _box_arrays(box: "Box"):
+    lo = np.array([box.lo[d] for d in range(3)])
+    hi = np.array([box.hi[d] for d in range(3)])
+    per = np.array([box.periodic[d] for d in range(3)], np.int32)
+    return lo, hi, per
+
+
+def ref_local_bead(c, box, xyz, f, nbrs: "Neighbors", point_type=POLYMER_BEAD,
+                   ibm_beta=0.75, hmin=1.0):
+    """(local_solution_bead, global_self_exclusion) of every bead, from the
+    reference's own GGEMStokes over the given neighbour lists"""
+    xyz, f = _f64(xyz), _f64(f)
+    n = len(xyz)
+    off, ids = nbrs.offsets, nbrs.ids
+    off = np.ascontiguousarray(off, np.int64)
+    ids = np.ascontiguousarray(ids, np.int32)
+    lo, hi, per = _box_arrays(box)
+    ul, us = np.zeros((n, 3)), np.zeros((n, 3))
+    rc = ref_ggem_lib().ref_ggem_local_bead(*_ref_head(c, point_type, ibm_beta, hmin),
+                                            _p(lo), _p(hi), _p(per), n, _p(xyz), _p(f),
+                                            _p(off), _p(ids), _p(ul), _p(us))
+    if rc:
+        raise ValueError(f"reference local_solution_bead failed ({rc})")
+    return ul, us
+
+
+def ref_local_field(c, box, elem_nb: "Neighbors", xyz, f, targets, target_elem,
+                    point_type=POLYMER_BEAD, ibm_beta=0.75, hmin=1.0):
+    """local_solution_field of the reference's own GGEMStokes at targets
+    (each given with the element that holds it)"""
+    xyz, f, targets = _f64(xyz), _f64(f), _f64(targets)
+    off, ids = elem_nb.offsets, elem_nb.ids
+    off = np.ascontiguousarray(off, np.int64)
+    ids = np.ascontiguousarray(ids, np.int32)
+    te = np.ascontiguousarray(target_elem, np.int32)
+    lo, hi, per = _box_arrays(box)
+    u = np.zeros((len(targets), 3))
+    rc = ref_ggem_lib().ref_ggem_local_field(*_ref_head(c, point_type, ibm_beta, hmin),
+                                             _p(lo), _p(hi), _p(per), len(xyz), _p(xyz),
+                                             _p(f), len(off) - 1, _p(off), _p(ids),
+                                             len(targets), _p(targets), _p(te), _p(u))
+    if rc:
+        raise ValueError(f"reference local_solution_field failed ({rc})")
+    return u
 
 
 def _p(a: np.ndarray):

@@ -726,3 +726,33 @@ def test_spring_forces_match_oracle(kind):
         ctx.set_bonds(bonds)
         got = ctx.spring_forces(kind, *params)
     assert rel(got, want) <= 1e-12
+
+
+def test_fp64_and_fp32_bead_velocity_vs_reference_ggem_stokes_outputs():
+    """The CUDA matvec against outputs of the reference's own GGEMStokes
+    (src/ggem_stokes.C compiled into oracle/_ref, stored in
+    tests/golden/ref_ggem_local.json): local_solution_bead - self exclusion
+    + f for beads (pm_system_stokes.C:446-455), local_solution_bead with
+    G(0) f for Lagrangian points (ggem_stokes.C:485-499).  FP64 within
+    1e-12, FP32 within 1e-6 (norm-wise)."""
+    d = json.loads((GOLD / "ref_ggem_local.json").read_text())
+
+    def unhex(a):
+        return np.array([float.fromhex(x) for x in a]).reshape(-1, 3)
+
+    for b in d["beads"]:
+        kw = {k: b[k] for k in ("ibm_beta", "hmin") if k in b}
+        lag = b["point_type"] == G.LAGRANGIAN_POINT
+        xyz, f = unhex(b["xyz"]), unhex(b["f"])
+        ul, us = unhex(b["u_local"]), unhex(b["u_self"])
+        want = ul if lag else ul - us + f
+        mode = G.SELF_LAGRANGIAN if lag else G.SELF_BEAD
+        for prec, tol in ((G.FP64, FP64_TOL), (G.FP32, FP32_TOL)):
+            with G.Context(alpha=b["alpha"], point_type=b["point_type"], box_hi=(b["L"],) * 3,
+                           periodic=b["periodic"], rc=b["rc"], precision=prec, **kw) as ctx:
+                ctx.set_particles(xyz)
+                ctx.build_cells()
+                got = ctx.local_matvec(f, mode)
+            err = rel(got, want)
+            print(f"{b['case']} precision={prec}: {err:.2e}")
+            assert err <= tol, (b["case"], prec)

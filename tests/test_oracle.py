@@ -339,3 +339,97 @@ def test_fem_point_values_oracle_reproduces_quadratic_fields():
     assert outside == 0
     want = np.stack([quadratic(pts, v) for v in range(3)], axis=1)
     assert np.abs(u - want).max() <= 1e-12 * np.abs(want).max()
+
+
+# ---------------------------------------------------------------------------
+# the reference's own GGEMStokes (src/ggem_stokes.C through oracle/_ref)
+# ---------------------------------------------------------------------------
+def _unhex(a, shape=None):
+    v = np.array([float.fromhex(x) for x in a])
+    return v.reshape(shape) if shape is not None else v
+
+
+def _ggem_gold():
+    return json.loads((GOLD / "ref_ggem_local.json").read_text())
+
+
+def test_green_tensor_bit_exact_vs_reference_ggem_stokes():
+    """green_tensor_local_regularized (ggem_stokes.C:304-352) for bead,
+    Lagrangian and point-particle constants, r = 0, r < r_eps and generic r"""
+    d = _ggem_gold()
+    vecs = _unhex(d["vectors"], (-1, 3))
+    for g in d["green"]:
+        kw = {k: g[k] for k in ("ibm_beta", "hmin") if k in g}
+        c = O.constants(alpha=g["alpha"], point_type=g["point_type"], **kw)
+        want = _unhex(g["G"], (-1, 3, 3))
+        got = np.stack([O.green_local(c, x) for x in vecs])
+        assert np.array_equal(got, want), g["type"]
+
+
+def _bead_case(b):
+    kw = {k: b[k] for k in ("ibm_beta", "hmin") if k in b}
+    c = O.constants(alpha=b["alpha"], point_type=b["point_type"], **kw)
+    L = b["L"]
+    box = O.make_box((0, 0, 0), (L, L, L), b["periodic"])
+    xyz = _unhex(b["xyz"], (-1, 3))
+    f = _unhex(b["f"], (-1, 3))
+    return c, box, xyz, f, kw
+
+
+def test_bead_local_sums_bit_exact_vs_reference_ggem_stokes():
+    """local_solution_bead (ggem_stokes.C:426-503) with global_self_exclusion
+    (:506-521) and the bead velocity of pm_system_stokes.C:446-455:
+    the oracle's SELF_NONE / SELF_BEAD / SELF_LAGRANGIAN sums equal the
+    reference's own outputs bit for bit, over the same cut-off lists"""
+    for b in _ggem_gold()["beads"]:
+        c, box, xyz, f, _ = _bead_case(b)
+        nb = O.neighbors_cutoff(box, xyz, b["rc"])
+        assert np.array_equal(nb.offsets, b["offsets"]) and np.array_equal(nb.ids, b["ids"])
+        ul = _unhex(b["u_local"], (-1, 3))
+        us = _unhex(b["u_self"], (-1, 3))
+        if b["point_type"] == O.LAGRANGIAN_POINT:
+            # the reference adds G(0) f inside local_solution_bead (:485-499)
+            got = O.local_matvec(c, box, xyz, nb, f, O.SELF_LAGRANGIAN)
+            assert np.array_equal(got, ul), b["case"]
+        else:
+            assert np.array_equal(O.local_matvec(c, box, xyz, nb, f, O.SELF_NONE), ul), b["case"]
+            got = O.local_matvec(c, box, xyz, nb, f, O.SELF_BEAD)
+            assert np.array_equal(got, ul - us + f), b["case"]
+        assert np.array_equal(us, c.coeff_1 * f)
+
+
+def test_field_local_sums_bit_exact_vs_reference_ggem_stokes():
+    """local_solution_field (ggem_stokes.C:358-423) over the element
+    point-neighbour lists, at targets inside the elements"""
+    fd = _ggem_gold()["field"]
+    L, nm = fd["L"], fd["n_mesh"]
+    c = O.constants(alpha=fd["alpha"])
+    box = O.make_box((0, 0, 0), (L, L, L), fd["periodic"])
+    mesh = O.make_mesh(nm, nm, nm, fd["search_radius_e"])
+    xyz = _unhex(fd["xyz"], (-1, 3))
+    f = _unhex(fd["f"], (-1, 3))
+    enb, _ = O.elem_lists(box, mesh, xyz)
+    targets = _unhex(fd["targets"], (-1, 3))
+    got = O.local_field_reference(c, box, mesh, enb, xyz, f, targets)
+    assert np.array_equal(got, _unhex(fd["u"], (-1, 3)))
+
+
+def test_live_reference_ggem_stokes_build():
+    """fresh cases through the reference's GGEMStokes compiled here"""
+    if O.ref_ggem_lib() is None:
+        pytest.skip("reference source tree not present on this machine")
+    rng = np.random.default_rng(11)
+    for pt, kw in ((O.POLYMER_BEAD, {}), (O.LAGRANGIAN_POINT, {"ibm_beta": 0.6, "hmin": 1.5})):
+        c = O.constants(alpha=0.4, point_type=pt, **kw)
+        for x in rng.standard_normal((50, 3)) * 4:
+            assert np.array_equal(O.green_local(c, x), O.ref_green_local(c, x, pt, **kw))
+        L = 11.0
+        box = O.make_box((-3, 0, 2), (L - 3, L, L + 2), (1, 0, 1))
+        xyz = np.array([-3, 0, 2]) + rng.uniform(0, L, (120, 3))
+        f = rng.standard_normal((120, 3))
+        nb = O.neighbors_cutoff(box, xyz, 5.5)
+        ul, us = O.ref_local_bead(c, box, xyz, f, nb, pt, **kw)
+        if pt == O.LAGRANGIAN_POINT:
+            assert np.array_equal(O.local_matvec(c, box, xyz, nb, f, O.SELF_LAGRANGIAN), ul)
+        else:
+            assert np.array_equal(O.local_matvec(c, box, xyz, nb, f, O.SELF_BEAD), ul - us + f)
