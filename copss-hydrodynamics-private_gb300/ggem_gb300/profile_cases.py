@@ -9,7 +9,9 @@ finishes in a minute or two while the inputs stay larger than L2.
 
 cases:
   pair_cheb   k_pair_first / k_pair_cheb: two Brownian steps of a 200k-bead
-              suspension (phi = 0.1, rc = 7), 10-ish fused Chebyshev terms each
+              suspension (phi = 0.1, rc = 7), 10-ish fused Chebyshev terms each,
+              tensors evaluated per pair
+  pair_tv     k_pair_first / k_pair_cheb_tv: the same with stored pair tensors
   pair_r1     k_pair_r1: 6 plain FP32 matvecs of the same suspension
   list        k_pair_list_warp: 3 list builds of the same suspension
   pair_f64    k_pair_list_f64: 3 FP64 matvecs over the exact pair list
@@ -47,6 +49,24 @@ def pair_cheb() -> None:
     torch = _torch()
     xyz, L = _bench_suspension()
     ctx = G.Context(box_hi=(L,) * 3, rc=7.0, precision=G.FP32)
+    ctx.set_pair_tensors(False)  # tensors per pair, the form the bench's autotuner keeps
+    ctx.set_particles(xyz)
+    ctx.build_cells()
+    lo, hi = ctx.lanczos_bounds(k=24, seed=7)
+    xi = torch.randn(3 * len(xyz), dtype=torch.float64, device="cuda")
+    dw = torch.empty_like(xi)
+    for _ in range(2):
+        rc, rep = ctx.brownian_displacement_dev(xi.data_ptr(), dw.data_ptr(), 1, 50, lo / 1.05,
+                                                hi * 1.05, 1e-3, check_every=0)
+    ctx.synchronize()
+    print("rc", rc, rep)
+
+
+def pair_tv() -> None:
+    torch = _torch()
+    xyz, L = _bench_suspension()
+    ctx = G.Context(box_hi=(L,) * 3, rc=7.0, precision=G.FP32)
+    ctx.set_pair_tensors(True)
     ctx.set_particles(xyz)
     ctx.build_cells()
     lo, hi = ctx.lanczos_bounds(k=24, seed=7)
@@ -152,7 +172,7 @@ def ens() -> None:
     print("beads", beads, "pairs", pairs, "rc", rc)
 
 
-CASES = {"pair_cheb": pair_cheb, "pair_r1": pair_r1, "list": list_build,
+CASES = {"pair_cheb": pair_cheb, "pair_tv": pair_tv, "pair_r1": pair_r1, "list": list_build,
          "pair_f64": pair_f64, "spread": spread, "mlp": mlp, "ens": ens}
 
 
