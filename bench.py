@@ -52,8 +52,9 @@ CHEB_TOL = 1e-3
 SEED = 20261203
 # DRAM bytes (read + write) per launch of the dominant pair kernel from one
 # ncu capture of this bench's workload (ncu flushes the caches before the
-# launch, so this is the cold-cache figure)
-PAIR_TRAFFIC = {"k_pair_cheb": 73.01e6}
+# launch, so this is the cold-cache figure): k_pair_cheb<1, 0, 0>, 70.60 MB
+# read + 2.18 MB written (profile_cases.py pair_cheb)
+PAIR_TRAFFIC = {"k_pair_cheb": 72.78e6}
 
 
 def measured_peaks():
@@ -308,7 +309,10 @@ def run_gb300(args, rank, world):
         device_step(s)
     torch.cuda.synchronize()
     clk = ClockSampler(dev).__enter__()
-    ctx.set_kernel_timing(True)
+    # only the roofline's kernel is bracketed by events inside the timed
+    # region (its consecutive launches share one event pair per step): an
+    # event pair around every launch of every kind cost ~50 us per step
+    ctx.set_kernel_timing(True, kinds=[G.KERNEL_PAIR_CHEB])
     lc0 = ctx.launch_count()
     t_wall0 = time.perf_counter()
     # an NVTX range around the timed device steps lets a profiler select
@@ -319,15 +323,25 @@ def run_gb300(args, rank, world):
     t_wall = time.perf_counter() - t_wall0
     clk.mark(t_wall0, t_wall0 + t_wall)
     lc1 = ctx.launch_count()
-    kt = {name: ctx.kernel_timing(kind) for kind, name in
-          ((G.KERNEL_PAIR_FP32, "pair_fp32"), (G.KERNEL_PAIR_CHEB, "pair_cheb"),
-           (G.KERNEL_CHEB_TERM, "cheb_term"), (G.KERNEL_LIST_BUILD, "list_build"))}
+    kt = {"pair_cheb": ctx.kernel_timing(G.KERNEL_PAIR_CHEB)}
     ctx.set_kernel_timing(False)
     ms_step, steps_per_s = replica_throughput(float(np.mean(ts)), world)
     # the bound sources of the timed steps (the legs below call Lanczos too)
     calls = {"surrogate_calls": state["surrogate_calls"], "lanczos_calls": state["lanczos_calls"]}
     n_pairs = ctx.pair_count()
     reps = [G.ChebReport.from_buffer_copy(b).as_dict() for b in state["reports"][-args.steps:]]
+
+    # the other kernels of a step, each launch bracketed by its own events,
+    # over a few further steps (outside the headline's timed region)
+    kt_steps = min(5, args.steps)
+    ctx.set_kernel_timing(True)
+    timed(device_step, kt_steps, 0)
+    kt_all = {name: ctx.kernel_timing(kind) for kind, name in
+              ((G.KERNEL_PAIR_FP32, "pair_fp32"), (G.KERNEL_PAIR_CHEB, "pair_cheb"),
+               (G.KERNEL_CHEB_TERM, "cheb_term"), (G.KERNEL_LIST_BUILD, "list_build"))}
+    ctx.set_kernel_timing(False)
+    kt_per_step = {k: {"ms_per_step": v[0] / kt_steps, "launches_per_step": v[1] / kt_steps}
+                   for k, v in kt_all.items()}
 
     # ---- the reference's schedule: the err1 check after every term --------
     # (brownian_system.C:1089-1155: two matvecs per term), the same work per
@@ -529,7 +543,7 @@ def run_gb300(args, rank, world):
     else:
         names = {"pair_cheb": "k_pair_cheb (pair list, tensors per pair + fused Chebyshev term)",
                  "pair_fp32": "k_pair_r1 (pair list, tensors per pair, one RHS)"}
-    dom = max(names, key=lambda k: kt[k][0])
+    dom = "pair_cheb"  # the fused terms: 9 of the 11 pair launches of a step
     pair_ms, pair_n = kt[dom]
     avg_pair_ms = pair_ms / max(pair_n, 1)
     flops_per_launch = n_pairs * (28 + 19 * 1)
@@ -546,9 +560,10 @@ def run_gb300(args, rank, world):
         per_bead = {"pair_fp32": 32 + 4 + 48, "pair_cheb": 32 + 4 + 120 + 32}
         bytes_per_launch = n_pairs * 4 + N_BEADS * per_bead[dom]
     achieved = flops_per_launch / (avg_pair_ms * 1e-3) / 1e12
-    others = {k: {"avg_launch_ms": kt[k][0] / max(kt[k][1], 1), "launches": kt[k][1],
-                  "tflops": (flops_per_launch / (kt[k][0] / kt[k][1] * 1e-3) / 1e12)
-                  if kt[k][1] else None} for k in names}
+    others = {k: {"avg_launch_ms": kt_all[k][0] / max(kt_all[k][1], 1),
+                  "launches": kt_all[k][1],
+                  "tflops": (flops_per_launch / (kt_all[k][0] / kt_all[k][1] * 1e-3) / 1e12)
+                  if kt_all[k][1] else None} for k in names}
     ctx.close()
     if stored:
         gbs = bytes_per_launch / (avg_pair_ms * 1e-3) / 1e9
@@ -597,6 +612,7 @@ def run_gb300(args, rank, world):
         "check_every_term": faithful,
         "roofline": roof,
         "kernel_ms_in_timed_region": {k: v[0] for k, v in kt.items()},
+        "kernel_ms_per_step_separate_run": kt_per_step,
         "gpu_launches": int(lc1 - lc0),
         "clocks": clk.summary(), "wall_s_timed": t_wall,
         "polymer_64rhs": poly,

@@ -388,9 +388,9 @@ constexpr int kRestartCheb = 1;
 // spec_dw (optional, caller order): every error check also queues M dw into
 // it before the host waits for the check's readback; when the series ends at
 // a check, *spec_done says that spec_dw already holds M y.
-int cheb_slots(ggem_ctx *c, int nrhs, int N, double eig_min, double eig_max, double tol,
-               int check_every, const double *xi, ggem_cheb_report *rep, bool *dm_is_my,
-               double *spec_dw = nullptr, bool *spec_done = nullptr) {
+int cheb_slots_impl(ggem_ctx *c, int nrhs, int N, double eig_min, double eig_max, double tol,
+                    int check_every, const double *xi, ggem_cheb_report *rep, bool *dm_is_my,
+                    double *spec_dw, bool *spec_done) {
   if (spec_done) *spec_done = false;
   const int64_t D = 3 * c->n;
   const int sm = brownian_self_mode(c);
@@ -534,6 +534,9 @@ int cheb_slots(ggem_ctx *c, int nrhs, int N, double eig_min, double eig_max, dou
     else if (check_every > 1) check = (i % check_every == 0) || (i == N - 1);
     else check = (i + 1 >= k_first) || (i == N - 1);
     if (can_fuse && (!check || fused)) {
+      // consecutive fused terms share one timing span (closed before the
+      // check's matvec, the next launch of another kernel)
+      if (fused && c->span_kind < 0) kt_span_begin(c, kKPairCheb);
       // a checked fused term leaves its two norms and the records of dw
       if (int rc = pair_cheb_term(c, records_fresh, x0, x1, xm, dw, two_da, two_db, X[i + 1], sm,
                                   check ? p_term : nullptr))
@@ -575,6 +578,7 @@ int cheb_slots(ggem_ctx *c, int nrhs, int N, double eig_min, double eig_max, dou
     *dm_is_my = false;
     if (spec_done) *spec_done = false;
     if (check) {
+      kt_span_end(c);
       if (int rc = check_now(std::fabs(X[i + 1]), true)) return rc;  // incl. kRestartCheb
       *dm_is_my = true;
       if (spec_done) *spec_done = spec_dw != nullptr;
@@ -607,6 +611,15 @@ int cheb_slots(ggem_ctx *c, int nrhs, int N, double eig_min, double eig_max, dou
     if (all) c->cheb_pred_terms = lower ? std::max(2, worst - 1) : worst;
   }
   return GGEM_OK;
+}
+
+int cheb_slots(ggem_ctx *c, int nrhs, int N, double eig_min, double eig_max, double tol,
+               int check_every, const double *xi, ggem_cheb_report *rep, bool *dm_is_my,
+               double *spec_dw = nullptr, bool *spec_done = nullptr) {
+  const int rc = cheb_slots_impl(c, nrhs, N, eig_min, eig_max, tol, check_every, xi, rep,
+                                 dm_is_my, spec_dw, spec_done);
+  kt_span_end(c);  // a span left open by an early return or a series ending unchecked
+  return rc;
 }
 
 }  // namespace

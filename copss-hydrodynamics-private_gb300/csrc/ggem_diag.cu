@@ -21,8 +21,12 @@ static cudaEvent_t take_event(ggem_ctx *c) {
   return e;
 }
 
+static bool kt_on(const ggem_ctx *c, int kind) {
+  return c->timing && (c->timing_mask >> kind & 1u);
+}
+
 void kt_start(ggem_ctx *c, int kind) {
-  if (!c->timing) return;
+  if (!kt_on(c, kind) || c->span_kind == kind) return;
   auto &t = c->ktimer[kind];
   if (t.ev.size() % 2 == 1) {  // a start left open by an error return: restart it
     cudaEventRecord(t.ev.back(), c->stream);
@@ -34,11 +38,10 @@ void kt_start(ggem_ctx *c, int kind) {
   c->ktimer[kind].ev.push_back(e);
 }
 
-void kt_stop(ggem_ctx *c, int kind) {
-  if (!c->timing) return;
+static void kt_stop_n(ggem_ctx *c, int kind, int launches) {
   auto &t = c->ktimer[kind];
   if (t.ev.size() % 2 == 0) return;  // unmatched start
-  cudaEvent_t e = take_event(c);
+  cudaEvent_t e = launches > 0 ? take_event(c) : nullptr;
   if (!e) {
     c->ev_pool.push_back(t.ev.back());
     t.ev.pop_back();
@@ -46,6 +49,31 @@ void kt_stop(ggem_ctx *c, int kind) {
   }
   cudaEventRecord(e, c->stream);
   t.ev.push_back(e);
+  t.n.push_back(launches);
+}
+
+void kt_stop(ggem_ctx *c, int kind) {
+  if (!kt_on(c, kind)) return;
+  if (c->span_kind == kind) {
+    ++c->span_n;
+    return;
+  }
+  kt_stop_n(c, kind, 1);
+}
+
+void kt_span_begin(ggem_ctx *c, int kind) {
+  kt_span_end(c);
+  if (!kt_on(c, kind)) return;
+  kt_start(c, kind);
+  c->span_kind = kind;
+  c->span_n = 0;
+}
+
+void kt_span_end(ggem_ctx *c) {
+  if (c->span_kind < 0) return;
+  const int kind = c->span_kind;
+  c->span_kind = -1;
+  kt_stop_n(c, kind, c->span_n);
 }
 
 void trace_mark(ggem_ctx *c, const char *what) {
@@ -64,14 +92,19 @@ static int drain(ggem_ctx *c) {
       float ms = 0.f;
       if (cudaEventElapsedTime(&ms, t.ev[k], t.ev[k + 1]) == cudaSuccess) {
         t.total_ms += ms;
-        t.count += 1;
+        t.count += k / 2 < t.n.size() ? t.n[k / 2] : 1;
       } else {
         cudaGetLastError();
       }
       c->ev_pool.push_back(t.ev[k]);
       c->ev_pool.push_back(t.ev[k + 1]);
     }
+    // an open start (a span in progress) stays
+    const bool open = t.ev.size() % 2 == 1;
+    cudaEvent_t last = open ? t.ev.back() : nullptr;
     t.ev.clear();
+    t.n.clear();
+    if (open) t.ev.push_back(last);
   }
   return GGEM_OK;
 }
@@ -144,15 +177,24 @@ extern "C" int ggem_set_pair_tensors(ggem_ctx *ctx, int enable) {
   return GGEM_OK;
 }
 
-extern "C" int ggem_set_kernel_timing(ggem_ctx *ctx, int enable) {
+extern "C" int ggem_set_kernel_timing_kinds(ggem_ctx *ctx, int enable, unsigned mask) {
   if (!ctx) return GGEM_ERR_BAD_ARG;
+  kt_span_end(ctx);
   if (int rc = drain(ctx)) return rc;
   for (auto &t : ctx->ktimer) {
     t.total_ms = 0.0;
     t.count = 0;
+    for (cudaEvent_t e : t.ev) ctx->ev_pool.push_back(e);  // an unmatched start
+    t.ev.clear();
+    t.n.clear();
   }
   ctx->timing = enable != 0;
+  ctx->timing_mask = mask & 0x1fu;
   return GGEM_OK;
+}
+
+extern "C" int ggem_set_kernel_timing(ggem_ctx *ctx, int enable) {
+  return ggem_set_kernel_timing_kinds(ctx, enable, 0x1fu);
 }
 
 extern "C" int ggem_get_kernel_timing(ggem_ctx *ctx, int kernel, double *total_ms,

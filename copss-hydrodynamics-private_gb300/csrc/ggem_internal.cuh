@@ -214,9 +214,15 @@ struct ggem_ctx {
   bool timing = false;
   struct KTimer {
     std::vector<cudaEvent_t> ev;  // start/stop pairs
+    std::vector<int> n;           // launches inside each closed pair
     double total_ms = 0.0;
     int64_t count = 0;
   } ktimer[5];
+  unsigned timing_mask = 0x1fu;  // kernel kinds timed while timing is on
+  // an open span (kt_span_begin): one event pair around consecutive
+  // launches of one kind, which then record no events of their own
+  int span_kind = -1;
+  int span_n = 0;
   std::vector<cudaEvent_t> ev_pool;
   // launch trace (ggem_set_launch_trace): one event after every launch
   bool trace = false;
@@ -255,6 +261,11 @@ enum : int { kKPairF32 = 0, kKPairF64 = 1, kKChebTerm = 2, kKListBuild = 3, kKPa
 
 void kt_start(ggem_ctx *c, int kind);
 void kt_stop(ggem_ctx *c, int kind);
+// one event pair around a run of consecutive launches of one kind (kt_start
+// / kt_stop of that kind inside the run only count launches); the run must
+// contain no launch of another kernel
+void kt_span_begin(ggem_ctx *c, int kind);
+void kt_span_end(ggem_ctx *c);
 void trace_mark(ggem_ctx *c, const char *what);
 
 int fail(ggem_ctx *c, int code, const std::string &msg);

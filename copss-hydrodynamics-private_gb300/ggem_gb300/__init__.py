@@ -129,6 +129,7 @@ def lib():
         "ggem_set_pair_variant": (i, [vp, i, i]),
         "ggem_probe_fp32_peak": (i, [vp, P(d)]),
         "ggem_set_kernel_timing": (i, [vp, i]),
+        "ggem_set_kernel_timing_kinds": (i, [vp, i, C.c_uint]),
         "ggem_set_launch_trace": (i, [vp, i]),
         "ggem_diag_convert_f32": (i, [vp, i64, vp, vp, vp]),
         "ggem_get_launch_trace": (i, [vp, i64, vp, vp, P(i64)]),
@@ -582,8 +583,16 @@ class Context:
         self._check(lib().ggem_get_launch_count(self.h, C.byref(v)))
         return v.value
 
-    def set_kernel_timing(self, enable: bool):
-        self._check(lib().ggem_set_kernel_timing(self.h, int(bool(enable))))
+    def set_kernel_timing(self, enable: bool, kinds=None):
+        """CUDA-event timing of the library's kernels (totals reset); kinds,
+        an iterable of KERNEL_* values, restricts it to those kernels"""
+        if kinds is None:
+            self._check(lib().ggem_set_kernel_timing(self.h, int(bool(enable))))
+        else:
+            mask = 0
+            for k in kinds:
+                mask |= 1 << int(k)
+            self._check(lib().ggem_set_kernel_timing_kinds(self.h, int(bool(enable)), mask))
 
     def set_launch_trace(self, enable: bool):
         self._check(lib().ggem_set_launch_trace(self.h, int(bool(enable))))

@@ -82,6 +82,11 @@ int ggem_probe_fp32_peak(ggem_ctx *ctx, double *tflops);
 #define GGEM_KERNEL_LIST_BUILD 3 /* pair-list count + fill                     */
 #define GGEM_KERNEL_PAIR_CHEB 4  /* FP32 pair sum with the Chebyshev term fused */
 int ggem_set_kernel_timing(ggem_ctx *ctx, int enable);
+/* the same for a subset of the kinds above (bit k of mask = kind k), so
+ * that a measurement brackets only the kernel it reports.  Consecutive
+ * fused Chebyshev terms (GGEM_KERNEL_PAIR_CHEB) share one event pair, and
+ * their launches count one each; the span includes the gaps between them */
+int ggem_set_kernel_timing_kinds(ggem_ctx *ctx, int enable, unsigned mask);
 int ggem_get_kernel_timing(ggem_ctx *ctx, int kernel, double *total_ms, int64_t *launches);
 
 #ifdef __cplusplus
