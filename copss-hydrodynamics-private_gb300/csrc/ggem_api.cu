@@ -17,6 +17,8 @@ ggem_ctx::~ggem_ctx() {
   for (cudaEvent_t e : ev_pool) cudaEventDestroy(e);
   for (auto &t : trace_ev) cudaEventDestroy(t.second);
   if (ev_readback) cudaEventDestroy(ev_readback);
+  for (cudaGraphExec_t g : sg_exec)
+    if (g) cudaGraphExecDestroy(g);
   if (ev_copy) cudaEventDestroy(ev_copy);
   if (copy_stream) cudaStreamDestroy(copy_stream);
   for (auto *b : scan_scratch) delete b;

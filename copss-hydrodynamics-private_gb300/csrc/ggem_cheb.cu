@@ -312,9 +312,8 @@ int grid1(int64_t tot) {
 // list_stats, host[nq .. nq+2] receive a deferred build's statistics too.
 // before_wait (optional) queues more work behind the readback before the
 // host waits for it.
-template <typename F>
-int finalize_to_host_then(ggem_ctx *c, int nq, int G, double *host, bool list_stats,
-                          F &&before_wait) {
+// the finalized sums copied to the pinned host mirror (no wait)
+int finalize_issue(ggem_ctx *c, int nq, int G, double *host, bool list_stats) {
   double *out = c->w_red.p + (size_t)nq * G;
   k_finalize<<<nq, kVecThreads, 0, c->stream>>>(G, c->w_red.p, out, nq,
                                                 list_stats ? c->nb_stat.p : nullptr,
@@ -323,13 +322,104 @@ int finalize_to_host_then(ggem_ctx *c, int nq, int G, double *host, bool list_st
   const int nv = nq + (list_stats ? 3 : 0);
   cudaError_t e = cudaMemcpyAsync(host, out, sizeof(double) * nv, cudaMemcpyDeviceToHost, c->stream);
   if (e) return cuda_fail(c, e, "reduction readback");
+  return GGEM_OK;
+}
+
+// the event the host waits on for a readback, recorded after the work so far
+int record_readback(ggem_ctx *c) {
+  cudaError_t e;
   if (!c->ev_readback &&
       (e = cudaEventCreateWithFlags(&c->ev_readback, cudaEventDisableTiming)))
     return cuda_fail(c, e, "readback event");
-  // the host waits for the readback only: work queued by before_wait runs on
   if ((e = cudaEventRecord(c->ev_readback, c->stream))) return cuda_fail(c, e, "readback event");
+  return GGEM_OK;
+}
+
+int wait_readback(ggem_ctx *c) {
+  cudaError_t e = cudaEventSynchronize(c->ev_readback);
+  if (e) return cuda_fail(c, e, "reduction readback");
+  return GGEM_OK;
+}
+
+template <typename F>
+int finalize_to_host_then(ggem_ctx *c, int nq, int G, double *host, bool list_stats,
+                          F &&before_wait) {
+  if (int rc = finalize_issue(c, nq, G, host, list_stats)) return rc;
+  // the host waits for the readback only: work queued by before_wait runs on
+  if (int rc = record_readback(c)) return rc;
   if (int rc = before_wait()) return rc;
-  if ((e = cudaEventSynchronize(c->ev_readback))) return cuda_fail(c, e, "reduction readback");
+  return wait_readback(c);
+}
+
+// ---- the series prefix as CUDA graphs ---------------------------------
+// 0: run live (a new key; it is kept), 1: capture now (the key came back),
+// 2: replay the graphs of this key
+int series_graph_state(ggem_ctx *c, const std::vector<uint64_t> &key) {
+  if (key == c->sg_key) return c->sg_exec[0] ? 2 : 1;
+  for (cudaGraphExec_t &g : c->sg_exec)
+    if (g) {
+      cudaGraphExecDestroy(g);
+      g = nullptr;
+    }
+  c->sg_key = key;
+  return 0;
+}
+
+// capture issue(seg) for seg = 0, 1, 2 into the prefix's three graphs and
+// instantiate them.  The kernel timer records no events inside a capture.
+// On a failed capture the graphs stay off for this context and *fallback
+// is set, with the host state the capture touched put back, so that the
+// caller runs the prefix live.
+template <typename F>
+int series_graph_capture(ggem_ctx *c, F &&issue, bool *fallback) {
+  *fallback = false;
+  const int64_t l0 = c->launches;
+  const int rec0 = c->rec_cur;
+  const bool timing = c->timing;
+  cudaGraphExec_t exec[3] = {nullptr, nullptr, nullptr};
+  bool ok = true;
+  c->timing = false;
+  for (int seg = 0; seg < 3 && ok; ++seg) {
+    if (cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal)) {
+      ok = false;
+      break;
+    }
+    const int rc = issue(seg);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+    if (!rc && !e) e = cudaGraphInstantiate(&exec[seg], g, 0);
+    if (g) cudaGraphDestroy(g);
+    ok = !rc && !e && exec[seg];
+  }
+  c->timing = timing;
+  if (!ok) {
+    cudaGetLastError();
+    for (cudaGraphExec_t g : exec)
+      if (g) cudaGraphExecDestroy(g);
+    c->launches = l0;
+    c->rec_cur = rec0;
+    c->series_graphs = false;
+    c->sg_key.clear();
+    *fallback = true;
+    return GGEM_OK;
+  }
+  for (int seg = 0; seg < 3; ++seg) c->sg_exec[seg] = exec[seg];
+  c->sg_launches = c->launches - l0;
+  ++c->sg_captures;
+  return GGEM_OK;
+}
+
+// one replay: the first step, the fused terms inside the kernel timer's
+// span (i_terms launches), the check
+int series_graph_launch(ggem_ctx *c, int i_terms) {
+  cudaError_t e;
+  if ((e = cudaGraphLaunch(c->sg_exec[0], c->stream))) return cuda_fail(c, e, "series graph");
+  kt_span_begin(c, kKPairCheb);
+  if ((e = cudaGraphLaunch(c->sg_exec[1], c->stream))) return cuda_fail(c, e, "series graph");
+  if (c->span_kind == kKPairCheb) c->span_n = i_terms;
+  kt_span_end(c);
+  if ((e = cudaGraphLaunch(c->sg_exec[2], c->stream))) return cuda_fail(c, e, "series graph");
+  ++c->sg_replays;
   return GGEM_OK;
 }
 
@@ -440,40 +530,54 @@ int cheb_slots_impl(ggem_ctx *c, int nrhs, int N, double eig_min, double eig_max
   // x0 = xi; x1 = M x0; aux2 = x1.x0; x1 = db x0 + da x1   (:1036-1041)
   // dw = c0 x0, dw += c1 x1 (with both norms unless fused)  (:1050-1056)
   bool records_fresh = false;
-  if (fused) {
-    // dm holds m = M x0 until the first check
-    if (int rc = cheb_start_fused(c, xi, x0, dm, x1, dw, da, db, X[0], X[1], sm, p_aux2))
-      return rc;
-    records_fresh = true;
-  } else {
-    int prc = GGEM_OK;
-    if (batch_fused && to_slots_staged(c, nrhs, xi, x0, &prc)) {
-      if (prc) return prc;
-      if (int rc = matvec_slots_prestaged(c, nrhs, x0, x1, sm)) return rc;
+  const double two_da = 2. * da, two_db = 2. * db;
+  int first_check = -1;
+  // The fused adaptive series' prefix: the first step, the unchecked terms,
+  // the first checked term (i_chk) and the device half of its check.  It is
+  // issued by issue_prefix, live or as one CUDA graph (series_graph).
+  const int i_chk = std::min(k_first - 1, N - 1);
+  const bool prefix = fused && check_every == 0 && N >= 2;
+  if (!prefix) {
+    if (fused) {
+      // dm holds m = M x0 until the first check
+      if (int rc = cheb_start_fused(c, xi, x0, dm, x1, dw, da, db, X[0], X[1], sm, p_aux2))
+        return rc;
+      records_fresh = true;
     } else {
-      if (int rc = permute_to_slots(c, nrhs, xi, x0)) return rc;
-      if (int rc = matvec_slots(c, nrhs, x0, x1, sm)) return rc;
+      int prc = GGEM_OK;
+      if (batch_fused && to_slots_staged(c, nrhs, xi, x0, &prc)) {
+        if (prc) return prc;
+        if (int rc = matvec_slots_prestaged(c, nrhs, x0, x1, sm)) return rc;
+      } else {
+        if (int rc = permute_to_slots(c, nrhs, xi, x0)) return rc;
+        if (int rc = matvec_slots(c, nrhs, x0, x1, sm)) return rc;
+      }
+      if (ff_sums) k_dot_ff<<<dim3(G, nrhs), kVecThreads, 0, st>>>(D, x1, x0, p_aux2);
+      else k_dot_partials<<<dim3(G, nrhs), kVecThreads, 0, st>>>(D, x1, x0, p_aux2);
+      if (int rc = check_launch(c, "aux2")) return rc;
+      // the start's norms feed only a check before the first term
+      if (batch_fused) {  // (not faithful) x1's staging for the first fused term
+        if (int rc = cheb_start_staged(c, nrhs, da, db, X[0], X[1], x0, x1, dw)) return rc;
+        staged_fresh = true;
+      } else if (faithful)
+        k_cheb_start<true><<<dim3(G, nrhs), kVecThreads, 0, st>>>(D, da, db, X[0], X[1], x0, x1,
+                                                                  dw, p_term);
+      else
+        k_cheb_start<false><<<dim3(G, nrhs), kVecThreads, 0, st>>>(D, da, db, X[0], X[1], x0,
+                                                                   x1, dw, p_term);
+      if (!batch_fused)
+        if (int rc = check_launch(c, "cheb start")) return rc;
     }
-    if (ff_sums) k_dot_ff<<<dim3(G, nrhs), kVecThreads, 0, st>>>(D, x1, x0, p_aux2);
-    else k_dot_partials<<<dim3(G, nrhs), kVecThreads, 0, st>>>(D, x1, x0, p_aux2);
-    if (int rc = check_launch(c, "aux2")) return rc;
-    // the start's norms feed only a check before the first term
-    if (batch_fused) {  // (not faithful) x1's staging for the first fused term
-      if (int rc = cheb_start_staged(c, nrhs, da, db, X[0], X[1], x0, x1, dw)) return rc;
-      staged_fresh = true;
-    } else if (faithful)
-      k_cheb_start<true><<<dim3(G, nrhs), kVecThreads, 0, st>>>(D, da, db, X[0], X[1], x0, x1,
-                                                                dw, p_term);
-    else
-      k_cheb_start<false><<<dim3(G, nrhs), kVecThreads, 0, st>>>(D, da, db, X[0], X[1], x0, x1,
-                                                                 dw, p_term);
-    if (!batch_fused)
-      if (int rc = check_launch(c, "cheb start")) return rc;
   }
   for (int r = 0; r < nrhs; ++r) rep[r].n_matvecs = 1;
 
-  // evaluate err1 / err2 of the current dw for the active right-hand sides
-  auto check_now = [&](double coef_abs, bool apply_rules) -> int {
+  // the device half of an error check: M dw with |M dw|^2, the finalized
+  // estimator sums (and a deferred list build's statistics) copied to the
+  // host mirror, then the caller's speculative M y.  The host half
+  // (check_eval) waits for the copy; with event_first the wait does not
+  // cover the speculative permute.
+  bool pending = false;
+  auto check_issue = [&](bool event_first) -> int {
     if (fused) {  // dw's records come from the checked term
       if (int rc = matvec_dw_records(c, dw, dm, sm, p_dm)) return rc;
     } else {
@@ -484,11 +588,15 @@ int cheb_slots_impl(ggem_ctx *c, int nrhs, int N, double eig_min, double eig_max
     }
     // a deferred list build is checked in the same readback; the caller's
     // M y is queued behind it in case this check ends the series
-    const bool pending = c->list_unchecked;
-    if (int rc = finalize_to_host_then(c, 4 * nrhs, G, h, pending, [&]() -> int {
-          return spec_dw ? permute_from_slots(c, nrhs, dm, spec_dw) : GGEM_OK;
-        }))
-      return rc;
+    pending = c->list_unchecked;
+    if (int rc = finalize_issue(c, 4 * nrhs, G, h, pending)) return rc;
+    if (event_first)
+      if (int rc = record_readback(c)) return rc;
+    return spec_dw ? permute_from_slots(c, nrhs, dm, spec_dw) : GGEM_OK;
+  };
+  // evaluate err1 / err2 of the current dw for the active right-hand sides
+  auto check_eval = [&](double coef_abs, bool apply_rules) -> int {
+    if (int rc = wait_readback(c)) return rc;
     if (pending) {
       const double *v = h + 4 * nrhs;
       bool rebuilt = false;
@@ -517,15 +625,122 @@ int cheb_slots_impl(ggem_ctx *c, int nrhs, int N, double eig_min, double eig_max
     }
     return GGEM_OK;
   };
+  auto check_now = [&](double coef_abs, bool apply_rules) -> int {
+    if (int rc = check_issue(true)) return rc;
+    return check_eval(coef_abs, apply_rules);
+  };
+
+  int i_begin = 1;
+  if (prefix) {
+    // the prefix's kernels, in the order of the loop below; span_begin /
+    // span_end bracket the fused terms for the kernel timer
+    auto issue_prefix = [&](int seg) -> int {  // seg -1: all of it, live
+      if (seg <= 0)
+        if (int rc = cheb_start_fused(c, xi, x0, dm, x1, dw, da, db, X[0], X[1], sm, p_aux2))
+          return rc;
+      if (seg == -1 || seg == 1) {
+        double *a = x0, *b = x1, *m = xm;
+        if (seg == -1) kt_span_begin(c, kKPairCheb);
+        for (int i = 1; i <= i_chk; ++i) {
+          const bool chk = i == i_chk;
+          if (int rc = pair_cheb_term(c, true, a, b, m, dw, two_da, two_db, X[i + 1], sm,
+                                      chk ? p_term : nullptr))
+            return rc;
+          double *t = a;
+          a = b;
+          b = m;
+          m = t;
+        }
+        if (seg == -1) kt_span_end(c);
+      }
+      if (seg == -1 || seg == 2) return check_issue(seg == -1);
+      return GGEM_OK;
+    };
+    // the records' ping-pong starts from buffer 0 (both are scratch here),
+    // so that the graph's baked pointers hold from one call to the next
+    c->rec_cur = 0;
+    const int rc_cur0 = 0;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(c->stream, &cap) != cudaSuccess) {
+      cudaGetLastError();
+      cap = cudaStreamCaptureStatusActive;
+    }
+    // the kernel timer can bracket the graphs' fused terms only: timing of
+    // any other kind runs the prefix live
+    const bool timed_other = c->timing && (c->timing_mask & ~(1u << kKPairCheb));
+    std::vector<uint64_t> key;
+    if (c->series_graphs && !c->trace && !timed_other && cap == cudaStreamCaptureStatusNone) {
+      auto u = [&](uint64_t v) { key.push_back(v); };
+      auto pbits = [&](const void *q) { u((uint64_t)(uintptr_t)q); };
+      auto dbits = [&](double v) {
+        uint64_t b;
+        std::memcpy(&b, &v, 8);
+        u(b);
+      };
+      u((uint64_t)c->n);
+      u((uint64_t)c->nb_w);
+      u((uint64_t)G);
+      u((uint64_t)i_chk);
+      u((uint64_t)sm);
+      u((uint64_t)c->use_poly);
+      u((uint64_t)c->computed_variant);
+      u((uint64_t)c->list_unchecked);
+      u((uint64_t)rc_cur0);
+      dbits(eig_min);
+      dbits(eig_max);
+      for (const void *q : {(const void *)xi, (const void *)spec_dw, (const void *)c->stream,
+                            (const void *)x0, (const void *)x1, (const void *)xm,
+                            (const void *)dw, (const void *)dm, (const void *)c->w_red.p,
+                            (const void *)c->w_rec[0].p, (const void *)c->w_rec[1].p,
+                            (const void *)c->w_src.p, (const void *)h, (const void *)c->order.p,
+                            (const void *)c->rank.p, (const void *)c->pos32.p,
+                            (const void *)c->nb_cnt.p, (const void *)c->nb_list.p,
+                            (const void *)c->d_shift.p, (const void *)c->tab.p,
+                            (const void *)c->nb_stat.p, (const void *)c->err.p})
+        pbits(q);
+    }
+    pending = c->list_unchecked;
+    int gs = key.empty() ? 0 : series_graph_state(c, key);
+    if (gs == 1) {  // the key came back: capture the prefix once
+      bool fallback = false;
+      if (int rc = series_graph_capture(c, [&](int seg) { return issue_prefix(seg); },
+                                        &fallback))
+        return rc;
+      if (fallback) gs = 0;
+    } else if (gs == 2) {
+      c->launches += c->sg_launches;
+      c->rec_cur = rc_cur0 ^ ((1 + i_chk) & 1);
+    }
+    if (gs == 0) {  // live (a new key, graphs off, or a failed capture)
+      if (int rc = issue_prefix(-1)) return rc;
+    } else {
+      if (int rc = series_graph_launch(c, i_chk)) return rc;
+      if (int rc = record_readback(c)) return rc;
+    }
+    records_fresh = true;
+    for (int i = 1; i <= i_chk; ++i) {  // the loop's bookkeeping for the prefix's terms
+      for (int r = 0; r < nrhs; ++r) {
+        rep[r].n_matvecs += 1;
+        rep[r].n_terms = i + 1;
+      }
+      double *t = x0;
+      x0 = x1;
+      x1 = xm;
+      xm = t;
+    }
+    if (int rc = check_eval(std::fabs(X[i_chk + 1]), true)) return rc;  // incl. kRestartCheb
+    *dm_is_my = true;
+    if (spec_done) *spec_done = spec_dw != nullptr;
+    first_check = i_chk + 1;
+    i_begin = i_chk + 1;
+  }
 
   if (faithful) {  // the estimators before the loop (:1064-1072)
     if (int rc = check_now(std::fabs(X[1]), false)) return rc;
     *dm_is_my = true;
     if (spec_done) *spec_done = spec_dw != nullptr;
   }
-  const double two_da = 2. * da, two_db = 2. * db;
-  int first_check = -1;
-  for (int i = 1; i < N; ++i) {
+  for (int i = i_begin; i < N; ++i) {
     int n_active = 0;
     for (int r = 0; r < nrhs; ++r) n_active += active[r];
     if (n_active == 0) break;

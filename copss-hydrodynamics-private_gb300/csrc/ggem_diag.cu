@@ -25,6 +25,8 @@ static bool kt_on(const ggem_ctx *c, int kind) {
   return c->timing && (c->timing_mask >> kind & 1u);
 }
 
+bool kt_enabled(const ggem_ctx *c, int kind) { return kt_on(c, kind); }
+
 void kt_start(ggem_ctx *c, int kind) {
   if (!kt_on(c, kind) || c->span_kind == kind) return;
   auto &t = c->ktimer[kind];
@@ -190,6 +192,29 @@ extern "C" int ggem_set_kernel_timing_kinds(ggem_ctx *ctx, int enable, unsigned 
   }
   ctx->timing = enable != 0;
   ctx->timing_mask = mask & 0x1fu;
+  return GGEM_OK;
+}
+
+extern "C" int ggem_set_series_graphs(ggem_ctx *ctx, int enable) {
+  if (!ctx) return GGEM_ERR_BAD_ARG;
+  ctx->series_graphs = enable != 0;
+  if (!ctx->series_graphs) {
+    cudaStreamSynchronize(ctx->stream);  // a replay in flight keeps using them
+    for (cudaGraphExec_t &g : ctx->sg_exec)
+      if (g) {
+        cudaGraphExecDestroy(g);
+        g = nullptr;
+      }
+    ctx->sg_key.clear();
+  }
+  return GGEM_OK;
+}
+
+extern "C" int ggem_get_series_graph_stats(const ggem_ctx *ctx, int64_t *captures,
+                                           int64_t *replays) {
+  if (!ctx || !captures || !replays) return GGEM_ERR_BAD_ARG;
+  *captures = ctx->sg_captures;
+  *replays = ctx->sg_replays;
   return GGEM_OK;
 }
 

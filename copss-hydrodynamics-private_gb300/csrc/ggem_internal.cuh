@@ -219,6 +219,16 @@ struct ggem_ctx {
     int64_t count = 0;
   } ktimer[5];
   unsigned timing_mask = 0x1fu;  // kernel kinds timed while timing is on
+  // The fused single-RHS series' prefix (first step, unchecked terms, the
+  // first checked term and its check's device half) as one CUDA graph:
+  // built when the same key comes back, replayed while it holds.
+  // Three graphs: the first step, the fused terms, the check; the kernel
+  // timer's span around the fused terms is recorded between them.
+  bool series_graphs = true;
+  cudaGraphExec_t sg_exec[3] = {nullptr, nullptr, nullptr};
+  std::vector<uint64_t> sg_key;
+  int64_t sg_launches = 0;  // kernel launches inside the three
+  int64_t sg_captures = 0, sg_replays = 0;
   // an open span (kt_span_begin): one event pair around consecutive
   // launches of one kind, which then record no events of their own
   int span_kind = -1;
@@ -266,6 +276,7 @@ void kt_stop(ggem_ctx *c, int kind);
 // contain no launch of another kernel
 void kt_span_begin(ggem_ctx *c, int kind);
 void kt_span_end(ggem_ctx *c);
+bool kt_enabled(const ggem_ctx *c, int kind);
 void trace_mark(ggem_ctx *c, const char *what);
 
 int fail(ggem_ctx *c, int code, const std::string &msg);

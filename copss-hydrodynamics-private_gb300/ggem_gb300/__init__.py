@@ -130,6 +130,8 @@ def lib():
         "ggem_probe_fp32_peak": (i, [vp, P(d)]),
         "ggem_set_kernel_timing": (i, [vp, i]),
         "ggem_set_kernel_timing_kinds": (i, [vp, i, C.c_uint]),
+        "ggem_set_series_graphs": (i, [vp, i]),
+        "ggem_get_series_graph_stats": (i, [vp, P(i64), P(i64)]),
         "ggem_set_launch_trace": (i, [vp, i]),
         "ggem_diag_convert_f32": (i, [vp, i64, vp, vp, vp]),
         "ggem_get_launch_trace": (i, [vp, i64, vp, vp, P(i64)]),
@@ -593,6 +595,15 @@ class Context:
             for k in kinds:
                 mask |= 1 << int(k)
             self._check(lib().ggem_set_kernel_timing_kinds(self.h, int(bool(enable)), mask))
+
+    def set_series_graphs(self, enable: bool):
+        self._check(lib().ggem_set_series_graphs(self.h, int(bool(enable))))
+
+    def series_graph_stats(self):
+        """(graphs captured, replays launched) of the series prefix graph"""
+        a, b = C.c_int64(), C.c_int64()
+        self._check(lib().ggem_get_series_graph_stats(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
 
     def set_launch_trace(self, enable: bool):
         self._check(lib().ggem_set_launch_trace(self.h, int(bool(enable))))

@@ -87,6 +87,16 @@ int ggem_set_kernel_timing(ggem_ctx *ctx, int enable);
  * fused Chebyshev terms (GGEM_KERNEL_PAIR_CHEB) share one event pair, and
  * their launches count one each; the span includes the gaps between them */
 int ggem_set_kernel_timing_kinds(ggem_ctx *ctx, int enable, unsigned mask);
+/* CUDA graph of the fused single-RHS Brownian series (FP32 cut-off context,
+ * tensors per pair, adaptive single check): the first step, the terms up to
+ * the first error check and that check's matvec, sums and readback are
+ * captured as one graph when a call repeats the previous call's
+ * configuration (sizes, buffers, eigen interval, predicted degree), and
+ * replayed while it holds.  Results are those of the launches it replaces.
+ * On by default; a failed capture turns it off for the context. */
+int ggem_set_series_graphs(ggem_ctx *ctx, int enable);
+/* graphs captured and replays launched so far */
+int ggem_get_series_graph_stats(const ggem_ctx *ctx, int64_t *captures, int64_t *replays);
 int ggem_get_kernel_timing(ggem_ctx *ctx, int kernel, double *total_ms, int64_t *launches);
 
 #ifdef __cplusplus
