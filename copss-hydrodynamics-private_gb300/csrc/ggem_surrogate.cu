@@ -156,7 +156,8 @@ constexpr size_t kMlpW0 = kMlpActBytes;
 constexpr size_t kMlpW1 = kMlpW0 + (size_t)kHid * kInPad * 2;
 constexpr size_t kMlpW2 = kMlpW1 + (size_t)kHid * kHid * 2;
 constexpr size_t kMlpW3 = kMlpW2 + (size_t)kHid * kHid * 2;
-constexpr size_t kMlpSmem = kMlpW3 + (size_t)kOutN * kHid * 2;
+constexpr size_t kMlpBias = kMlpW3 + (size_t)kOutN * kHid * 2;  // hidden layers' biases
+constexpr size_t kMlpSmem = kMlpBias + (size_t)(kLayers - 1) * kHid * 4;
 
 // offset of layer l's bias in the flat parameter vector (W1^T [128 x 48],
 // b1, then [128 x 128] weights and 128 biases per layer)
@@ -187,15 +188,42 @@ __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
 }
 
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;" ::: "memory");
+}
+
+// this thread's copies complete but for the N most recent groups
+template <int N>
+__device__ __forceinline__ void cp_async_wait_upto() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// 4 * n floats (16-byte pieces) with asynchronous copies
+__device__ __forceinline__ void stage_f32(float *dst, const float *__restrict__ src, int n4) {
+  for (int c = threadIdx.x; c < n4; c += blockDim.x)
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(tc::smem_u32(dst + 4 * c)),
+                 "l"(src + 4 * c)
+                 : "memory");
+}
+
 // the logistic function on the special-function unit (ex2 and a correctly
 // rounded reciprocal): a few ulp from 1 / (1 + e^-z), far below the BF16
 // rounding of the activations; every kernel of the network uses this one
 __device__ __forceinline__ float sigmoid_sfu(float z) { return __frcp_rn(1.f + __expf(-z)); }
 __device__ __forceinline__ float silu_f(float z) { return z * sigmoid_sfu(z); }
 
-constexpr int kMlpThreads = 256;  // 8 warps: warp w reads TMEM lanes 32 (w % 4) .. + 31,
-                                  // columns 64 (w / 4) .. + 63
+constexpr int kMlpThreads = 1024;  // 32 warps: warp w reads TMEM lanes 32 (w % 4) .. + 31,
+                                   // columns 16 (w / 4) .. + 15
+constexpr int kMlpCols = kHid / (kMlpThreads / 128);  // hidden columns per thread
 
+// The whole forward pass of one 128-row tile in one CTA.  The weights of the
+// four layers (and the hidden biases) arrive by asynchronous copies in one
+// group per layer, so that the first product starts once its own weights
+// are in.  Each product is one tcgen05.mma chain by one thread into TMEM;
+// the epilogue (bias, SiLU, BF16 into the next product's A tile) is spread
+// over 32 warps, 16 columns per thread, and warps whose 32 rows are all
+// past the last row of the batch skip it: rows of a product never mix, so
+// those rows' stale activations reach no output.
 __global__ void __launch_bounds__(kMlpThreads) k_mlp_forward(
     const float *__restrict__ x, int n, const float *__restrict__ mean,
     const float *__restrict__ inv_std, const bf16 *__restrict__ w0, const bf16 *__restrict__ w1,
@@ -205,22 +233,32 @@ __global__ void __launch_bounds__(kMlpThreads) k_mlp_forward(
   __shared__ __align__(8) uint64_t bar;
   __shared__ uint32_t tslot;
   uint8_t *sA = mlp_smem;
+  float *s_bias = reinterpret_cast<float *>(mlp_smem + kMlpBias);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int quarter = warp & 3, half = warp >> 2;
+  const int quarter = warp & 3, cb = warp >> 2;
   const int row = quarter * 32 + lane;  // this thread's row = its TMEM lane
   const int64_t row_g = (int64_t)blockIdx.x * kRowBlock + row;
+  // a warp whose 32 rows all lie past the batch has no epilogue to run
+  const bool live = (int64_t)blockIdx.x * kRowBlock + quarter * 32 < n;
   if (warp == 0) tc::tmem_alloc(&tslot, (uint32_t)kHid);
   if (tid == 0) {
     tc::mbar_init(&bar, 1);
     tc::mbar_fence_init();
   }
-  // weights (asynchronous copies), and meanwhile the standardised input
-  // rows (48 BF16, zero padded; the first half of the block)
+  // weights and hidden biases, one copy group per layer
   stage_wt(mlp_smem + kMlpW0, w0, kHid, kInPad);
+  stage_f32(s_bias, params + bias_off_d(0), kHid / 4);
+  cp_async_commit();
   stage_wt(mlp_smem + kMlpW1, w1, kHid, kHid);
+  stage_f32(s_bias + kHid, params + bias_off_d(1), kHid / 4);
+  cp_async_commit();
   stage_wt(mlp_smem + kMlpW2, w2, kHid, kHid);
+  stage_f32(s_bias + 2 * kHid, params + bias_off_d(2), kHid / 4);
+  cp_async_commit();
   stage_wt(mlp_smem + kMlpW3, w3, kOutN, kHid);
-  if (half == 0) {
+  cp_async_commit();
+  // meanwhile the standardised input rows (48 BF16, zero padded)
+  if (warp < 4) {
 #pragma unroll
     for (int kb = 0; kb < kInPad / 8; ++kb) {
       __align__(16) bf16 h[8];
@@ -235,7 +273,7 @@ __global__ void __launch_bounds__(kMlpThreads) k_mlp_forward(
           *reinterpret_cast<const uint4 *>(h);
     }
   }
-  cp_async_wait();
+  cp_async_wait_upto<3>();  // layer 0's weights and bias
   tc::fence_proxy_async_smem();
   tc::fence_before_sync();
   __syncthreads();
@@ -262,27 +300,37 @@ __global__ void __launch_bounds__(kMlpThreads) k_mlp_forward(
     ok = __syncthreads_and(done) != 0;
     if (!ok) break;
     tc::fence_after_sync();
-    const float *bias = params + bias_off_d(l);
     if (l < kLayers - 1) {
       // H = silu(Z + b) into the activation tile (the product that read it
       // has completed)
-      for (int c0 = half * (kHid / 2); c0 < (half + 1) * (kHid / 2); c0 += 8) {
-        float v[8];
-        tc::tmem_ld8(lane_base + (uint32_t)c0, v);
-        __align__(16) bf16 h[8];
+      if (live) {
+        const int c0 = cb * kMlpCols;
+        const float *bias = s_bias + l * kHid + c0;
+        float v[16];
+        tc::tmem_ld16(lane_base + (uint32_t)c0, v);
 #pragma unroll
-        for (int i = 0; i < 8; ++i) h[i] = __float2bfloat16_rn(silu_f(v[i] + bias[c0 + i]));
-        *reinterpret_cast<uint4 *>(sA + tile_off(row, c0 >> 3, kHid / 8)) =
-            *reinterpret_cast<const uint4 *>(h);
+        for (int h8 = 0; h8 < kMlpCols / 8; ++h8) {
+          __align__(16) bf16 h[8];
+#pragma unroll
+          for (int i = 0; i < 8; ++i)
+            h[i] = __float2bfloat16_rn(silu_f(v[8 * h8 + i] + bias[8 * h8 + i]));
+          *reinterpret_cast<uint4 *>(sA + tile_off(row, (c0 >> 3) + h8, kHid / 8)) =
+              *reinterpret_cast<const uint4 *>(h);
+        }
       }
+      // the next layer's weights are in (at most the later groups pending)
+      if (l == 0) cp_async_wait_upto<2>();
+      else if (l == 1) cp_async_wait_upto<1>();
+      else cp_async_wait_upto<0>();
       tc::fence_proxy_async_smem();
       tc::fence_before_sync();
       __syncthreads();
       tc::fence_after_sync();
-    } else if (half == 0) {
+    } else if (warp < 4 && live) {
       float v[8];
       tc::tmem_ld8(lane_base, v);
       if (row_g < n) {
+        const float *bias = params + bias_off_d(l);
         Y[row_g * kOut] = v[0] + bias[0];
         Y[row_g * kOut + 1] = v[1] + bias[1];
       }
@@ -293,6 +341,7 @@ __global__ void __launch_bounds__(kMlpThreads) k_mlp_forward(
     // the product still in flight completes before TMEM is freed
     tc::mbar_wait_bounded(&bar, phase ^ 1u, kMaxPolls);
   }
+  cp_async_wait_upto<0>();  // no copy outlives the block (the timeout path)
   tc::fence_before_sync();
   __syncthreads();
   if (warp == 0) {
