@@ -852,6 +852,12 @@ def ensemble_leg(G, torch, dev, flush, sur, margins, reps=3):
         t_sur = time.perf_counter() - t0
     xi = torch.randn(beads * ENS_NRHS * 3, dtype=torch.float64, device="cuda")
     dw = torch.empty_like(xi)
+    # the persistent launch's shape and tile size, tuned on a 14-term series
+    # (about the degree these intervals need)
+    t0 = time.perf_counter()
+    s_shape, s_slots, s_ms = ens.autotune_series(ENS_NRHS, 14, lo, hi, xi.data_ptr(),
+                                                 dw.data_ptr())
+    t_tune = time.perf_counter() - t0
     torch.cuda.synchronize()
     fallbacks = 0
 
@@ -924,7 +930,9 @@ def ensemble_leg(G, torch, dev, flush, sur, margins, reps=3):
     return {"workload": f"{ENS_K} periodic suspensions, N log-uniform in [500, 20000] "
                         f"(sum {beads}), phi uniform in [0.02, 0.2], {ENS_NRHS} noise vectors each",
             "beads": beads, "pairs": pairs, "build_s": t_build,
-            "autotune": {"block_threads": block, "ms_per_term": ms_term},
+            "autotune": {"block_threads": block, "ms_per_term": ms_term,
+                         "series_shape": s_shape, "series_slots_per_tile": s_slots,
+                         "series_ms_14_terms": s_ms, "series_tune_s": t_tune},
             "intervals_s": {"network_one_batch": t_sur, "lanczos24_per_suspension": t_lz},
             "lanczos_fallbacks": fallbacks,
             "brownian_step_ms": step_s * 1e3,
