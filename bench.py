@@ -852,8 +852,9 @@ def ensemble_leg(G, torch, dev, flush, sur, margins, reps=3):
         t_sur = time.perf_counter() - t0
     xi = torch.randn(beads * ENS_NRHS * 3, dtype=torch.float64, device="cuda")
     dw = torch.empty_like(xi)
-    # the persistent launch's shape and tile size, tuned on a 14-term series
-    # (about the degree these intervals need)
+    # the step's form (a persistent launch of some shape and tile size, or one
+    # launch per term: shape 3), tuned on a 14-term series (about the degree
+    # these intervals need); the timed steps below run the chosen form
     t0 = time.perf_counter()
     s_shape, s_slots, s_ms = ens.autotune_series(ENS_NRHS, 14, lo, hi, xi.data_ptr(),
                                                  dw.data_ptr())
@@ -905,7 +906,6 @@ def ensemble_leg(G, torch, dev, flush, sur, margins, reps=3):
             torch.cuda.synchronize()
             mts.append((time.perf_counter() - t0) * 1e3)
         modes[name] = {"brownian_step_ms": float(np.mean(mts)), "converged": rc_m == 0}
-    ens.set_series_mode(persistent=True)
     f = torch.randn(beads * ENS_NRHS * 3, dtype=torch.float64, device="cuda")
     u = torch.empty_like(f)
     ens.matvec_dev(ENS_NRHS, f.data_ptr(), u.data_ptr())
@@ -931,6 +931,7 @@ def ensemble_leg(G, torch, dev, flush, sur, margins, reps=3):
                         f"(sum {beads}), phi uniform in [0.02, 0.2], {ENS_NRHS} noise vectors each",
             "beads": beads, "pairs": pairs, "build_s": t_build,
             "autotune": {"block_threads": block, "ms_per_term": ms_term,
+                         "series_form": "persistent launch" if s_shape < 3 else "launch per term",
                          "series_shape": s_shape, "series_slots_per_tile": s_slots,
                          "series_ms_14_terms": s_ms, "series_tune_s": t_tune},
             "intervals_s": {"network_one_batch": t_sur, "lanczos24_per_suspension": t_lz},

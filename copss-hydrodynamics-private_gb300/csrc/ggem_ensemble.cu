@@ -1149,7 +1149,7 @@ extern "C" int ggem_ensemble_autotune_series(ggem_ensemble *e, int nrhs, int N,
       double ms = 0.0;
       bool hit = false;
       while (std::fscanf(fp, "%511s %d %d %lf", k, &sh, &S, &ms) == 4)
-        if (key == k && sh >= 0 && sh < kSeriesShapes && S >= 8 && S <= 1024) {
+        if (key == k && sh >= 0 && sh <= kSeriesShapes && S >= 8 && S <= 1024) {
           e->series_shape = sh;
           e->S = S;
           *shape = sh;
@@ -1159,7 +1159,8 @@ extern "C" int ggem_ensemble_autotune_series(ggem_ensemble *e, int nrhs, int N,
         }
       std::fclose(fp);
       if (hit) {
-        e->persistent = true;
+        e->persistent = e->series_shape < kSeriesShapes;
+        if (!e->persistent) e->series_shape = 1;
         return GGEM_OK;
       }
     }
@@ -1169,6 +1170,7 @@ extern "C" int ggem_ensemble_autotune_series(ggem_ensemble *e, int nrhs, int N,
   const int tiles[3] = {64, 128, 256};
   const bool keep_pers = e->persistent;
   const int keep_pred = e->pred_terms;
+  const int keep_shape = e->series_shape;
   e->persistent = true;
   double best = 1e30;
   int best_sh = e->series_shape, best_S = e->S;
@@ -1198,12 +1200,34 @@ extern "C" int ggem_ensemble_autotune_series(ggem_ensemble *e, int nrhs, int N,
         best_S = S;
       }
     }
+  // and the step as one launch per term (host-side checks; the unchecked
+  // stretch as a graph), candidate kSeriesShapes
+  if (rc == GGEM_OK || rc == GGEM_ERR_CHEB_NOT_CONVERGED) {
+    e->persistent = false;
+    for (int k = 0; k < 2; ++k) {
+      e->pred_terms = N;
+      if (k == 1) cudaEventRecord(t0, e->stream);
+      rc = ggem_ensemble_brownian_dev(e, nrhs, N, eig_min, eig_max, 0.0, d_xi, d_dw, rep.data());
+      if (rc != GGEM_OK && rc != GGEM_ERR_CHEB_NOT_CONVERGED) break;
+    }
+    if (rc == GGEM_OK || rc == GGEM_ERR_CHEB_NOT_CONVERGED) {
+      cudaEventRecord(t1, e->stream);
+      cudaEventSynchronize(t1);
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, t0, t1);
+      if (ms < best) {
+        best = ms;
+        best_sh = kSeriesShapes;
+      }
+    }
+  }
   cudaEventDestroy(t0);
   cudaEventDestroy(t1);
   e->persistent = keep_pers;
   e->pred_terms = keep_pred;
   if (rc != GGEM_OK && rc != GGEM_ERR_CHEB_NOT_CONVERGED) return rc;
-  e->series_shape = best_sh;
+  e->persistent = best_sh < kSeriesShapes;
+  e->series_shape = e->persistent ? best_sh : keep_shape;
   e->S = best_S;
   *shape = best_sh;
   *slots_per_tile = best_S;

@@ -840,8 +840,10 @@ class Ensemble:
                                                         1 if never_ready else 0))
 
     def autotune_series(self, nrhs, N, eig_min, eig_max, d_xi, d_dw, cache_path=None):
-        """(shape, slots per tile, ms per step) of the fastest persistent
-        launch; cache_path keeps the choice across runs"""
+        """(shape, slots per tile, ms per step) of the fastest form of the
+        step: a persistent launch of shape 0, 1 or 2, or one launch per term
+        (shape 3); the series mode follows the choice, and cache_path keeps
+        it across runs"""
         lo = np.ascontiguousarray(eig_min, dtype=np.float64)
         hi = np.ascontiguousarray(eig_max, dtype=np.float64)
         sh, S, ms = C.c_int(), C.c_int(), C.c_double()

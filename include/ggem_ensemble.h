@@ -85,11 +85,13 @@ int ggem_ensemble_autotune(ggem_ensemble *e, int nrhs, int *block_threads, doubl
  * never_ready = 1 is a test hook that makes every wait run out. */
 int ggem_ensemble_set_series_mode(ggem_ensemble *e, int persistent, int slots_per_tile,
                                   uint32_t wait_polls, int never_ready);
-/* Autotune the persistent launch: times one Brownian step of every series
- * (N - 1 terms, no early stop; xi, dw as for ggem_ensemble_brownian_dev) for
- * each launch shape (threads per block and the register cap for 4, 6 or 12
- * resident blocks per SM) and tile size (64, 128, 256 slots), keeps the
- * fastest and returns it (shape index, slots per tile, ms per step).  With
+/* Autotune the step's form: times one Brownian step of every series (N - 1
+ * terms, no early stop; xi, dw as for ggem_ensemble_brownian_dev) as one
+ * persistent launch for each launch shape (threads per block and the
+ * register cap for 4, 6 or 12 resident blocks per SM: shapes 0, 1, 2) and
+ * tile size (64, 128, 256 slots), and as one launch per term (shape 3),
+ * keeps the fastest (the series mode follows it) and returns it (shape
+ * index, slots per tile, ms per step).  With
  * cache_path (may be NULL) a line "key shape slots ms" per tuned ensemble is
  * appended to that text file; a later call with the same device, suspension
  * count, bead and pair counts, row width and right-hand sides reads it back

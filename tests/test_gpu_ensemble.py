@@ -287,7 +287,7 @@ def test_series_autotuner_and_its_cache(tmp_path):
             sh, S, ms = ens.autotune_series(R, 14, lo, hi, xi.data_ptr(), dw.data_ptr(),
                                             str(cache))
             dt = __import__("time").perf_counter() - t0
-            assert 0 <= sh < 3 and S in (64, 128, 256) and ms > 0
+            assert 0 <= sh <= 3 and S in (64, 128, 256) and ms > 0  # 3: a launch per term
             lines = cache.read_text().splitlines()
             assert len(lines) == 1  # the second run reads the line, it does not add one
             out.append((sh, S, ms, dt))
