@@ -83,3 +83,43 @@ def test_series_graph_matches_live_steps():
                   f"graph {graph[3][0] / graph[3][1] * 1e3:.1f} us per launch")
         terms = sorted({r["n_terms"] for r in graph[1]})
         print(f"timing={timing}: {captures} captures, {replays} replays, terms {terms}")
+
+
+def test_replayed_prefix_then_live_terms():
+    """a replayed prefix whose check fails (a tighter tolerance: the key does
+    not hold the tolerance) continues live; the steps equal the live run's"""
+    xyz, L = G.make_suspension(78, 12000, 0.1)
+    probe = G.Context(box_hi=(L,) * 3, rc=7.0, precision=G.FP32)
+    probe.set_particles(xyz)
+    probe.build_cells()
+    lo, hi = probe.lanczos_bounds(k=24, seed=7)
+    probe.close()
+    a, b = lo / 1.05, hi * 1.05
+    n = len(xyz)
+    res = {}
+    for graphs in (False, True):
+        ctx = G.Context(box_hi=(L,) * 3, rc=7.0, precision=G.FP32)
+        ctx.set_pair_tensors(False)
+        ctx.set_series_graphs(graphs)
+        d_xyz = torch.from_numpy(xyz.reshape(-1).copy()).cuda()
+        xi = torch.empty(3 * n, dtype=torch.float64, device="cuda")
+        dw = torch.empty_like(xi)
+        outs, reps = [], []
+        for seed, tol in ((0, 1e-3), (1, 1e-3), (2, 1e-3), (3, 1e-5), (4, 1e-3)):
+            ctx.set_particles_dev(d_xyz.data_ptr(), n)
+            ctx.build_cells()
+            ctx.philox_normals_dev(5, seed, 3 * n, xi.data_ptr())
+            rc, rep = ctx.brownian_displacement_dev(xi.data_ptr(), dw.data_ptr(), 1, 50, a, b,
+                                                    tol, check_every=0)
+            assert rc == 0, rep
+            outs.append(dw.cpu().numpy().copy())
+            reps.append(rep[0])
+        res[graphs] = (outs, reps, ctx.series_graph_stats())
+        ctx.close()
+    for u, v in zip(res[False][0], res[True][0]):
+        assert np.array_equal(u, v)
+    assert res[False][1] == res[True][1]
+    # the tight step ran past the prefix's check
+    assert res[True][1][3]["n_terms"] > res[True][1][2]["n_terms"], res[True][1]
+    assert res[True][2][1] >= 2, res[True][2]
+    print("terms", [r["n_terms"] for r in res[True][1]], "graph stats", res[True][2])
