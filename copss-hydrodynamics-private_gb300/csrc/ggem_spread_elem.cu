@@ -130,7 +130,9 @@ __device__ __forceinline__ int axis_offset(const SpreadGeo &sg, int d, int us, i
   return o;
 }
 
-template <bool F32>
+// ANYFULL: some brick frame spans a whole periodic axis (small meshes);
+// without it the wrapped-offset and minimum-image code is compiled out
+template <bool F32, bool ANYFULL>
 __global__ void __launch_bounds__(kSpThreads) k_spread_brick(
     SpreadGeo sg, DevConsts K, const int32_t *__restrict__ start,
     const float4 *__restrict__ pos32, const double4_32a *__restrict__ pos64,
@@ -166,7 +168,10 @@ __global__ void __launch_bounds__(kSpThreads) k_spread_brick(
                      min(e0[2] + B, sg.g.nc[2])};
   Frame fr[3];
 #pragma unroll
-  for (int d = 0; d < 3; ++d) fr[d] = brick_frame(sg, d, e0[d], e1[d]);
+  for (int d = 0; d < 3; ++d) {
+    fr[d] = brick_frame(sg, d, e0[d], e1[d]);
+    if (!ANYFULL) fr[d].full = 0;  // the host found no frame that spans an axis
+  }
   // x segments per row: a periodic frame that is not the whole axis may
   // wrap once; others are one range
   const int xa = fr[0].F, xz = fr[0].F + fr[0].E - 1;
@@ -281,9 +286,10 @@ __global__ void __launch_bounds__(kSpThreads) k_spread_brick(
         if (k < cn) {
           const uint32_t u = F32 ? __float_as_uint(rec32[2 * k].w)
                                  : (uint32_t)__double_as_longlong(rec64[2 * k].w);
-          const int ix = axis_offset(sg, 0, (int)(u & 31u), uex, fr[0].full) - sg.lo[0];
-          const int iy = axis_offset(sg, 1, (int)((u >> 5) & 31u), uey, fr[1].full) - sg.lo[1];
-          const int iz = axis_offset(sg, 2, (int)(u >> 10), uez, fr[2].full) - sg.lo[2];
+          const int ix = axis_offset(sg, 0, (int)(u & 31u), uex, ANYFULL && fr[0].full) - sg.lo[0];
+          const int iy =
+              axis_offset(sg, 1, (int)((u >> 5) & 31u), uey, ANYFULL && fr[1].full) - sg.lo[1];
+          const int iz = axis_offset(sg, 2, (int)(u >> 10), uez, ANYFULL && fr[2].full) - sg.lo[2];
           if ((unsigned)ix < (unsigned)sg.dim[0] && (unsigned)iy < (unsigned)sg.dim[1] &&
               (unsigned)iz < (unsigned)sg.dim[2]) {
             const int idx = (iz * sg.dim[1] + iy) * sg.dim[0] + ix;
@@ -314,15 +320,15 @@ __global__ void __launch_bounds__(kSpThreads) k_spread_brick(
           float dz = (a.z + s_shift[2][en >> 20]) - qr.z;
           // minimum image (pm_periodic_boundary.C:350-374); only an axis
           // whose frame is the whole box can produce |d| > L/2
-          if (fr[0].full) {
+          if (ANYFULL && fr[0].full) {
             if (dx <= -0.5f * sg.L32[0]) dx += sg.L32[0];
             if (dx > 0.5f * sg.L32[0]) dx -= sg.L32[0];
           }
-          if (fr[1].full) {
+          if (ANYFULL && fr[1].full) {
             if (dy <= -0.5f * sg.L32[1]) dy += sg.L32[1];
             if (dy > 0.5f * sg.L32[1]) dy -= sg.L32[1];
           }
-          if (fr[2].full) {
+          if (ANYFULL && fr[2].full) {
             if (dz <= -0.5f * sg.L32[2]) dz += sg.L32[2];
             if (dz > 0.5f * sg.L32[2]) dz -= sg.L32[2];
           }
@@ -335,7 +341,7 @@ __global__ void __launch_bounds__(kSpThreads) k_spread_brick(
           bx_ = fmaf(gv, fb.x, bx_);
           by_ = fmaf(gv, fb.y, by_);
           bz_ = fmaf(gv, fb.z, bz_);
-          if (++blk == 4) {
+          if (++blk == 8) {  // every 8 pairs into the compensated sums
             kahan_acc(sx, cx, bx_);
             kahan_acc(sy, cy, by_);
             kahan_acc(sz, cz, bz_);
@@ -511,22 +517,27 @@ int spread_elements(ggem_ctx *c, int precision, const double *d_f_slot, double *
   if (int rc = spread_geometry(c, &sg)) return rc;
   const unsigned nblk = (unsigned)((int64_t)sg.nb[0] * sg.nb[1] * sg.nb[2]);
   cudaError_t e;
-  // (the attribute is per device; setting it costs microseconds)
-  if (precision == GGEM_FP32) {
-    if ((e = cudaFuncSetAttribute(k_spread_brick<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  // does any brick frame span a whole periodic axis? (brick_frame: the
+  // frame of a brick of at most B elements spans B + hi - lo)
+  bool any_full = false;
+  for (int d = 0; d < 3; ++d)
+    any_full = any_full || (sg.g.periodic[d] && sg.B + sg.hi[d] - sg.lo[d] >= sg.g.nc[d]);
+  auto launch = [&](auto kernel) -> int {
+    // (the attribute is per device; setting it costs microseconds)
+    if ((e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)kSpShared)))
       return cuda_fail(c, e, "spread attributes");
-    k_spread_brick<true><<<nblk, kSpThreads, kSpShared, c->stream>>>(
+    kernel<<<nblk, kSpThreads, kSpShared, c->stream>>>(
         sg, c->dc, c->cell_start.p, c->pos32.p, c->pos64.p, d_f_slot, c->q_rel.p, c->q_xyz.p,
         c->sp_bits.p, d_rho, d_pairs);
-  } else {
-    if ((e = cudaFuncSetAttribute(k_spread_brick<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)kSpShared)))
-      return cuda_fail(c, e, "spread attributes");
-    k_spread_brick<false><<<nblk, kSpThreads, kSpShared, c->stream>>>(
-        sg, c->dc, c->cell_start.p, c->pos32.p, c->pos64.p, d_f_slot, c->q_rel.p, c->q_xyz.p,
-        c->sp_bits.p, d_rho, d_pairs);
-  }
+    return GGEM_OK;
+  };
+  int rc;
+  if (precision == GGEM_FP32)
+    rc = any_full ? launch(k_spread_brick<true, true>) : launch(k_spread_brick<true, false>);
+  else
+    rc = any_full ? launch(k_spread_brick<false, true>) : launch(k_spread_brick<false, false>);
+  if (rc) return rc;
   return check_launch(c, "spread bricks");
 }
 

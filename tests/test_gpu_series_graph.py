@@ -105,7 +105,7 @@ def test_replayed_prefix_then_live_terms():
         xi = torch.empty(3 * n, dtype=torch.float64, device="cuda")
         dw = torch.empty_like(xi)
         outs, reps = [], []
-        for seed, tol in ((0, 1e-3), (1, 1e-3), (2, 1e-3), (3, 1e-5), (4, 1e-3)):
+        for seed, tol in ((0, 1e-3), (1, 1e-3), (2, 1e-3), (3, 2e-4), (4, 1e-3)):
             ctx.set_particles_dev(d_xyz.data_ptr(), n)
             ctx.build_cells()
             ctx.philox_normals_dev(5, seed, 3 * n, xi.data_ptr())
