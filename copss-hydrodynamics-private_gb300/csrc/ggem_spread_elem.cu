@@ -141,7 +141,10 @@ __global__ void __launch_bounds__(kSpThreads) k_spread_brick(
     double *__restrict__ rho, unsigned long long *__restrict__ pairs) {
   extern __shared__ __align__(16) unsigned char sp_smem[];
   constexpr int CAP = F32 ? kSpCap32 : kSpCap64;
-  float4 *rec32 = reinterpret_cast<float4 *>(sp_smem);        // [CAP][2]
+  // FP32 records as two arrays, positions [CAP] then forces [CAP]: the 16-byte
+  // stride spreads the four members a warp reads at once over more banks
+  // than 32-byte records would
+  float4 *rec32 = reinterpret_cast<float4 *>(sp_smem);        // [2][CAP]
   double4_32a *rec64 = reinterpret_cast<double4_32a *>(sp_smem);  // [CAP][2]
   uint32_t *members = reinterpret_cast<uint32_t *>(sp_smem + kSpRecBytes);
   int32_t *seg_begin = reinterpret_cast<int32_t *>(members + kSpWarps * kSpCap32);
@@ -261,8 +264,8 @@ __global__ void __launch_bounds__(kSpThreads) k_spread_brick(
       const uint32_t u = (uint32_t)ux | ((uint32_t)uy << 5) | ((uint32_t)uz << 10);
       const double *fp = f_slot + 3 * (int64_t)slot;
       if (F32) {
-        rec32[2 * k] = make_float4(p.x, p.y, p.z, __uint_as_float(u));
-        rec32[2 * k + 1] = make_float4(d2f_bits(fp[0]), d2f_bits(fp[1]), d2f_bits(fp[2]), 0.f);
+        rec32[k] = make_float4(p.x, p.y, p.z, __uint_as_float(u));
+        rec32[kSpCap32 + k] = make_float4(d2f_bits(fp[0]), d2f_bits(fp[1]), d2f_bits(fp[2]), 0.f);
       } else {
         const double4_32a q = pos64[slot];
         rec64[2 * k] = make_double4_32a(q.x, q.y, q.z, __longlong_as_double((long long)u));
@@ -284,7 +287,7 @@ __global__ void __launch_bounds__(kSpThreads) k_spread_brick(
         bool in = false;
         uint32_t entry = 0;
         if (k < cn) {
-          const uint32_t u = F32 ? __float_as_uint(rec32[2 * k].w)
+          const uint32_t u = F32 ? __float_as_uint(rec32[k].w)
                                  : (uint32_t)__double_as_longlong(rec64[2 * k].w);
           const int ix = axis_offset(sg, 0, (int)(u & 31u), uex, ANYFULL && fr[0].full) - sg.lo[0];
           const int iy =
@@ -314,7 +317,7 @@ __global__ void __launch_bounds__(kSpThreads) k_spread_brick(
         for (int m = sub; m < M && qok; m += lq) {
           const uint32_t en = mlist[m];
           const int k = (int)(en & 1023u);
-          const float4 a = rec32[2 * k], fb = rec32[2 * k + 1];
+          const float4 a = rec32[k], fb = rec32[kSpCap32 + k];
           float dx = (a.x + s_shift[0][(en >> 10) & 31u]) - qr.x;
           float dy = (a.y + s_shift[1][(en >> 15) & 31u]) - qr.y;
           float dz = (a.z + s_shift[2][en >> 20]) - qr.z;
