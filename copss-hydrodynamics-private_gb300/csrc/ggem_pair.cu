@@ -21,7 +21,6 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
-#include <type_traits>
 
 #include "ggem_ff.cuh"
 #include "ggem_internal.cuh"
@@ -444,7 +443,7 @@ __device__ __forceinline__ PairSum pair_sum_r1(int64_t s, bool act, int sub, con
 
 // The fused series' estimator sums (x0 . M x0, |dw|^2, |x_{k+1}|^2, |M dw|^2)
 // without FP64 arithmetic (ggem_ff.cuh): float-float products and sums, one
-// partial per block written by thread 0.
+// partial per block (256 threads) written by thread 0.
 __device__ __forceinline__ void block_partial_ff(float hi, float lo, double *__restrict__ part) {
   __shared__ float2 sh[32];
   const double v = block_ff_sum(hi, lo, sh);
@@ -572,29 +571,16 @@ __global__ void k_sym_finish(int64_t n, const double *__restrict__ part, float4 
     u[3 * s + c] = fma(self_c, f[3 * s + c], part[3 * s + c] + f2d_bits(v[c]));
 }
 
-// the per-matvec-tensor kernel shapes the autotuner chooses from: threads per
-// block and the blocks per SM that the register cap allows (256 x 6 at 40
-// registers, with a few spilled epilogue values in some kernels; 256 x 5 at
-// 48 without; 128 x 12 at 40: smaller blocks, a shorter tail at the end of
-// the grid)
-constexpr int kComputedThreads[] = {256, 256, 128};
-constexpr int kComputedMinBlocks[] = {6, 5, 12};
-constexpr int kNumComputedVariants = 3;
-
-// calls f(std::integral_constant<int, V>) for the context's computed variant
-template <typename F>
-void with_computed_variant(int v, F &&f) {
-  switch (v) {
-    case 1: f(std::integral_constant<int, 1>{}); break;
-    case 2: f(std::integral_constant<int, 2>{}); break;
-    default: f(std::integral_constant<int, 0>{}); break;
-  }
-}
+// the per-matvec-tensor kernel shapes the autotuner chooses from: blocks of
+// 256 threads per SM that the register cap allows (6 at 40 registers, with a
+// few spilled epilogue values in some kernels; 5 at 48 without)
+constexpr int kComputedMinBlocks[] = {6, 5};
+constexpr int kNumComputedVariants = 2;
 
 // u = M f, single right-hand side; with ORIG, u is written in the caller's
 // particle order (u[order[s]]) instead of slot order
 template <bool POLY, int V, bool ORIG>
-__global__ void __launch_bounds__(kComputedThreads[V], kComputedMinBlocks[V]) k_pair_r1(
+__global__ void __launch_bounds__(256, kComputedMinBlocks[V]) k_pair_r1(
     int64_t n, const Rec32 *__restrict__ src, const int32_t *__restrict__ cnt, int W,
     const uint32_t *__restrict__ list, PolyAB P, const Rec32 *__restrict__ tab, float inv_ds,
     const float4 *__restrict__ shift, double self_c, const double *__restrict__ f,
@@ -627,7 +613,7 @@ __global__ void __launch_bounds__(kComputedThreads[V], kComputedMinBlocks[V]) k_
 // vector kernels: a block-wide FP64 reduction here costs more than the
 // launch it saves, FP64 being 1/64 of the FP32 rate.)
 template <bool POLY, int V>
-__global__ void __launch_bounds__(kComputedThreads[V], kComputedMinBlocks[V]) k_pair_first(
+__global__ void __launch_bounds__(256, kComputedMinBlocks[V]) k_pair_first(
     int64_t n, const Rec32 *__restrict__ src, const int32_t *__restrict__ cnt, int W,
     const uint32_t *__restrict__ list, PolyAB P, const Rec32 *__restrict__ tab, float inv_ds,
     const float4 *__restrict__ shift, double self_c, double da, double db, double c0, double c1,
@@ -671,7 +657,7 @@ __global__ void __launch_bounds__(kComputedThreads[V], kComputedMinBlocks[V]) k_
 // With c1 = 2db + 2da self_c this is xm = 2da (pair sum) + (c1 x1 - x0).
 // src holds the records of x1; next must be a different buffer.
 template <bool POLY, int V, bool NORMS>
-__global__ void __launch_bounds__(kComputedThreads[V], kComputedMinBlocks[V]) k_pair_cheb(
+__global__ void __launch_bounds__(256, kComputedMinBlocks[V]) k_pair_cheb(
     int64_t n, const Rec32 *__restrict__ src, const int32_t *__restrict__ cnt, int W,
     const uint32_t *__restrict__ list, PolyAB P, const Rec32 *__restrict__ tab, float inv_ds,
     const float4 *__restrict__ shift, double two_da, double c1, double coef,
@@ -1374,7 +1360,7 @@ PolyAB poly_of(const ggem_ctx *c) {
 template <bool POLY, int V, bool ORIG>
 void launch_r1(ggem_ctx *c, const Rec32 *src, const double *f, double *u, double self_c,
                double *part) {
-  k_pair_r1<POLY, V, ORIG><<<(unsigned)pair_grid_blocks(c), kComputedThreads[V], 0, c->stream>>>(
+  k_pair_r1<POLY, V, ORIG><<<(unsigned)pair_grid_blocks(c), 256, 0, c->stream>>>(
       c->n, src, c->nb_cnt.p, c->nb_w, c->nb_list.p, poly_of(c),
       reinterpret_cast<const Rec32 *>(c->tab.p), c->tab_inv_ds, c->d_shift.p, self_c, f, u,
       c->order.p, part);
@@ -1383,9 +1369,8 @@ void launch_r1(ggem_ctx *c, const Rec32 *src, const double *f, double *u, double
 template <bool POLY, bool ORIG = false>
 void dispatch_r1(ggem_ctx *c, const Rec32 *src, const double *f, double *u, double self_c,
                  double *part = nullptr) {
-  with_computed_variant(c->computed_variant, [&](auto v) {
-    launch_r1<POLY, decltype(v)::value, ORIG>(c, src, f, u, self_c, part);
-  });
+  if (c->computed_variant == 1) launch_r1<POLY, 1, ORIG>(c, src, f, u, self_c, part);
+  else launch_r1<POLY, 0, ORIG>(c, src, f, u, self_c, part);
 }
 
 // single right-hand side: records from FP64 slot-order f, then the pair sum
@@ -1448,8 +1433,7 @@ template <bool POLY, int V, bool NORMS>
 void launch_cheb(ggem_ctx *c, const Rec32 *src, Rec32 *next, double two_da, double c1,
                  double coef, const double *x0, const double *x1, double *xm, double *dw,
                  double *part, Rec32 *dw_next) {
-  k_pair_cheb<POLY, V, NORMS><<<(unsigned)pair_grid_blocks(c), kComputedThreads[V], 0,
-                                 c->stream>>>(
+  k_pair_cheb<POLY, V, NORMS><<<(unsigned)pair_grid_blocks(c), 256, 0, c->stream>>>(
       c->n, src, c->nb_cnt.p, c->nb_w, c->nb_list.p, poly_of(c),
       reinterpret_cast<const Rec32 *>(c->tab.p), c->tab_inv_ds, c->d_shift.p, two_da, c1, coef,
       x0, x1, xm, dw, next, part, pair_partials(c), dw_next);
@@ -1461,18 +1445,21 @@ template <bool POLY>
 void dispatch_cheb(ggem_ctx *c, const Rec32 *src, Rec32 *next, double two_da, double c1,
                    double coef, const double *x0, const double *x1, double *xm, double *dw,
                    double *part, Rec32 *dw_next) {
-  with_computed_variant(c->computed_variant, [&](auto v) {
-    constexpr int V = decltype(v)::value;
-    if (part) launch_cheb<POLY, V, true>(c, src, next, two_da, c1, coef, x0, x1, xm, dw, part, dw_next);
-    else launch_cheb<POLY, V, false>(c, src, next, two_da, c1, coef, x0, x1, xm, dw, part, dw_next);
-  });
+  const bool v1 = c->computed_variant == 1;
+  if (part) {
+    if (v1) launch_cheb<POLY, 1, true>(c, src, next, two_da, c1, coef, x0, x1, xm, dw, part, dw_next);
+    else launch_cheb<POLY, 0, true>(c, src, next, two_da, c1, coef, x0, x1, xm, dw, part, dw_next);
+  } else {
+    if (v1) launch_cheb<POLY, 1, false>(c, src, next, two_da, c1, coef, x0, x1, xm, dw, part, dw_next);
+    else launch_cheb<POLY, 0, false>(c, src, next, two_da, c1, coef, x0, x1, xm, dw, part, dw_next);
+  }
 }
 
 template <bool POLY, int V>
 void launch_first(ggem_ctx *c, const Rec32 *src, Rec32 *next, double self_c, double da,
                   double db, double c0, double c1, const double *x0, double *m, double *x1,
                   double *dw, double *part) {
-  k_pair_first<POLY, V><<<(unsigned)pair_grid_blocks(c), kComputedThreads[V], 0, c->stream>>>(
+  k_pair_first<POLY, V><<<(unsigned)pair_grid_blocks(c), 256, 0, c->stream>>>(
       c->n, src, c->nb_cnt.p, c->nb_w, c->nb_list.p, poly_of(c),
       reinterpret_cast<const Rec32 *>(c->tab.p), c->tab_inv_ds, c->d_shift.p, self_c, da, db, c0,
       c1, x0, m, x1, dw, next, part);
@@ -1663,9 +1650,7 @@ int batch_cheb_term(ggem_ctx *c, int nrhs, bool staged_fresh, const double *x0, 
 }
 
 int pair_grid_blocks(const ggem_ctx *c) {
-  const int64_t t = kComputedThreads[std::min(std::max(c->computed_variant, 0),
-                                              kNumComputedVariants - 1)];
-  return (int)std::max<int64_t>(1, (c->n * kGroup + t - 1) / t);
+  return (int)std::max<int64_t>(1, (c->n * kGroup + 255) / 256);
 }
 
 int64_t pair_partials(const ggem_ctx *c) { return pair_grid_blocks(c); }
@@ -1689,11 +1674,14 @@ int cheb_start_fused(ggem_ctx *c, const double *xi, double *x0, double *m, doubl
   if (int rc = check_launch(c, "to slots + records")) return rc;
   const double self_c = self_coefficient(c, self_mode);
   kt_start(c, kKPairF32);
-  with_computed_variant(c->computed_variant, [&](auto v) {
-    constexpr int V = decltype(v)::value;
-    if (c->use_poly) launch_first<true, V>(c, cur, nxt, self_c, da, db, c0, c1, x0, m, x1, dw, aux2);
-    else launch_first<false, V>(c, cur, nxt, self_c, da, db, c0, c1, x0, m, x1, dw, aux2);
-  });
+  const bool v1 = c->computed_variant == 1;
+  if (c->use_poly) {
+    if (v1) launch_first<true, 1>(c, cur, nxt, self_c, da, db, c0, c1, x0, m, x1, dw, aux2);
+    else launch_first<true, 0>(c, cur, nxt, self_c, da, db, c0, c1, x0, m, x1, dw, aux2);
+  } else {
+    if (v1) launch_first<false, 1>(c, cur, nxt, self_c, da, db, c0, c1, x0, m, x1, dw, aux2);
+    else launch_first<false, 0>(c, cur, nxt, self_c, da, db, c0, c1, x0, m, x1, dw, aux2);
+  }
   kt_stop(c, kKPairF32);
   c->rec_cur ^= 1;
   return check_launch(c, "pair first step");

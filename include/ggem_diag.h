@@ -59,7 +59,7 @@ int ggem_set_symmetric_pairs(ggem_ctx *ctx, int enable);
  * pair and with stored tensors (plus the one tensor pass per build,
  * amortised over matvecs_per_build matvecs) by CUDA events on the context's
  * stream; each form is timed for each of its kernel shapes (per-matvec
- * tensors: 6 or 5 blocks of 256 or 12 blocks of 128 per SM; stored
+ * tensors: registers capped for 6 or for 5 blocks of 256 per SM; stored
  * tensors: lanes per target, entries in flight, pipelined stream).  The
  * fastest stays selected for this context; both costs are reported in ms
  * per matvec (the stored one with its amortised pass) and variants[0],
@@ -67,7 +67,7 @@ int ggem_set_symmetric_pairs(ggem_ctx *ctx, int enable);
 int ggem_autotune_pair_storage(ggem_ctx *ctx, int reps, double matvecs_per_build,
                                int *use_stored, double *ms_computed, double *ms_stored,
                                int *variants);
-/* select the kernel shapes directly: computed 0 .. 2, stored 0 .. 3 */
+/* select the kernel shapes directly: computed 0 .. 1, stored 0 .. 3 */
 int ggem_set_pair_variant(ggem_ctx *ctx, int computed, int stored);
 /* dense FP32 FMA throughput of this device in TFLOP/s (FMA = 2 flops),
  * measured with CUDA events over a register-resident FMA chain kernel on the
