@@ -155,15 +155,22 @@ __global__ void __launch_bounds__(kVecThreads) k_cheb_start(int64_t D, double da
 // The norms feed only the error estimators: a term that no check follows
 // skips them (NORMS = false), a third of the term's FP64 work.
 // With FF the norms are float-float sums (no FP64 arithmetic; the FP32
-// series) instead of FP64 ones.
-template <bool NORMS, bool FF = false>
+// series) instead of FP64 ones.  With REC (one right-hand side) the term
+// also writes the 32-byte pair-kernel records of the new x and of the new
+// dw (cell-relative position from pos32, then the FP32 values, rounded as
+// the records the pair kernels stage themselves), so that the next matvec
+// and the check's matvec need no staging pass.
+template <bool NORMS, bool FF = false, bool REC = false>
 __global__ void __launch_bounds__(kVecThreads) k_cheb_term(int64_t D, double two_da,
                                                            double two_db, RhsCoef cf,
                                                            const double *__restrict__ x0,
                                                            const double *__restrict__ x1,
                                                            double *__restrict__ xm,
                                                            double *__restrict__ dw,
-                                                           double *__restrict__ partial) {
+                                                           double *__restrict__ partial,
+                                                           const float4 *__restrict__ pos32 = nullptr,
+                                                           float4 *__restrict__ rec_x = nullptr,
+                                                           float4 *__restrict__ rec_dw = nullptr) {
   __shared__ double sh[32];
   __shared__ float2 shf[32];
   const int r = blockIdx.y, nrhs = gridDim.y;
@@ -177,7 +184,23 @@ __global__ void __launch_bounds__(kVecThreads) k_cheb_term(int64_t D, double two
     double v = two_db * x1[off + k] + two_da * xm[off + k];
     v -= x0[off + k];
     xm[off + k] = v;
-    dw[off + k] = y + c * v;
+    const double yn = y + c * v;
+    dw[off + k] = yn;
+    if (REC) {
+      const int64_t s = k / 3;
+      const int comp = (int)(k - 3 * s);
+      float *rx = reinterpret_cast<float *>(rec_x + 2 * s);
+      float *rd = reinterpret_cast<float *>(rec_dw + 2 * s);
+      rx[4 + comp] = d2f_bits(v);
+      rd[4 + comp] = d2f_bits(yn);
+      if (comp == 0) {
+        const float4 p = pos32[s];
+        rec_x[2 * s] = p;
+        rec_dw[2 * s] = p;
+        rx[7] = 0.f;
+        rd[7] = 0.f;
+      }
+    }
     if (NORMS && FF) {
       float ph, pl;
       sq_ff(y, ph, pl);
@@ -499,6 +522,17 @@ int cheb_slots_impl(ggem_ctx *c, int nrhs, int N, double eig_min, double eig_max
   const bool fused = can_fuse && !faithful && !c->pretensor_ok && c->n > 0;
   // 16 .. 64 right-hand sides: an unchecked term is one batched kernel
   const bool batch_fused = !faithful && c->n > 0 && batch_term_fusable(c, nrhs);
+  // one right-hand side on the unfused path with per-pair tensors (the
+  // reference-faithful checks): each term also writes the pair records of
+  // its new x (w_rec[0]) and dw (w_src), so the next matvec and the check's
+  // matvec skip their staging passes
+  const bool rec_terms = can_fuse && !fused && !c->pretensor_ok && c->n > 0;
+  bool xrec_fresh = false, dwrec_fresh = false;
+  if (rec_terms) {
+    cudaError_t e;
+    if ((e = c->w_rec[0].ensure(2 * (size_t)c->n)) || (e = c->w_src.ensure(2 * (size_t)c->n)))
+      return cuda_fail(c, e, "chebyshev records");
+  }
   bool staged_fresh = false;
   // partial sums per reduction: vector-kernel blocks, or in a fused series
   // the pair kernels' blocks (the first step, the checked terms and the
@@ -581,7 +615,9 @@ int cheb_slots_impl(ggem_ctx *c, int nrhs, int N, double eig_min, double eig_max
     if (fused) {  // dw's records come from the checked term
       if (int rc = matvec_dw_records(c, dw, dm, sm, p_dm)) return rc;
     } else {
-      if (int rc = matvec_slots(c, nrhs, dw, dm, sm)) return rc;
+      if (int rc = rec_terms && dwrec_fresh ? matvec_dw_records(c, dw, dm, sm, nullptr)
+                                            : matvec_slots(c, nrhs, dw, dm, sm))
+        return rc;
       if (ff_sums) k_dot_ff<<<dim3(G, nrhs), kVecThreads, 0, st>>>(D, dm, dm, p_dm);
       else k_dot_partials<<<dim3(G, nrhs), kVecThreads, 0, st>>>(D, dm, dm, p_dm);
       if (int rc = check_launch(c, "dm norm")) return rc;
@@ -764,16 +800,23 @@ int cheb_slots_impl(ggem_ctx *c, int nrhs, int N, double eig_min, double eig_max
         return rc;
       staged_fresh = true;
     } else {
-      // (a fused batched term before this one left x1's staging)
-      if (int rc = batch_fused && staged_fresh ? matvec_slots_prestaged(c, nrhs, x1, xm, sm)
-                                               : matvec_slots(c, nrhs, x1, xm, sm))
-        return rc;
+      // (a fused batched term before this one left x1's staging; a recorded
+      // term before this one left x1's pair records)
+      int mrc;
+      if (batch_fused && staged_fresh) mrc = matvec_slots_prestaged(c, nrhs, x1, xm, sm);
+      else if (rec_terms && xrec_fresh) mrc = matvec_records(c, c->w_rec[0].p, x1, xm, sm, nullptr);
+      else mrc = matvec_slots(c, nrhs, x1, xm, sm);
+      if (mrc) return mrc;
       RhsCoef cf;
       for (int r = 0; r < nrhs; ++r) cf.c[r] = active[r] ? X[i + 1] : 0.0;
       kt_start(c, kKChebTerm);
       if (check && ff_sums)
         k_cheb_term<true, true><<<dim3(G, nrhs), kVecThreads, 0, st>>>(D, two_da, two_db, cf,
                                                                         x0, x1, xm, dw, p_term);
+      else if (check && rec_terms)
+        k_cheb_term<true, false, true><<<dim3(G, nrhs), kVecThreads, 0, st>>>(
+            D, two_da, two_db, cf, x0, x1, xm, dw, p_term, c->pos32.p, c->w_rec[0].p,
+            c->w_src.p);
       else if (check)
         k_cheb_term<true><<<dim3(G, nrhs), kVecThreads, 0, st>>>(D, two_da, two_db, cf, x0, x1,
                                                                   xm, dw, p_term);
@@ -784,6 +827,7 @@ int cheb_slots_impl(ggem_ctx *c, int nrhs, int N, double eig_min, double eig_max
       if (int rc = check_launch(c, "cheb term")) return rc;
       records_fresh = false;
       staged_fresh = false;
+      xrec_fresh = dwrec_fresh = check && rec_terms;
     }
     for (int r = 0; r < nrhs; ++r)
       if (active[r]) {

@@ -349,6 +349,8 @@ int64_t pair_partials(const ggem_ctx *c);
 // u = M dw from the dw records a checked fused term left (norms given to
 // pair_cheb_term); |u|^2 as per-block partials into norm
 int matvec_dw_records(ggem_ctx *c, const double *dw, double *u, int self_mode, double *norm);
+int matvec_records(ggem_ctx *c, const float4 *rec, const double *f, double *u, int self_mode,
+                   double *norm);
 // u = M f, one right-hand side, caller order in and out (FP32 list with
 // per-matvec tensors only); f_slot receives f in slot order
 int matvec_orig_fused(ggem_ctx *c, const double *f, double *u, double *f_slot, int self_mode);

@@ -1691,12 +1691,19 @@ int cheb_start_fused(ggem_ctx *c, const double *xi, double *x0, double *m, doubl
 // w_src, so the check matvec is one launch, and |u|^2 leaves as per-block
 // partials (norm)
 int matvec_dw_records(ggem_ctx *c, const double *dw, double *u, int self_mode, double *norm) {
+  return matvec_records(c, c->w_src.p, dw, u, self_mode, norm);
+}
+
+// u = M f from the 32-byte records of f already staged in rec (2 float4 per
+// slot: the cell-relative position, then the FP32 force), f in slot order
+int matvec_records(ggem_ctx *c, const float4 *rec, const double *f, double *u, int self_mode,
+                   double *norm) {
   if (c->n == 0) return GGEM_OK;
-  const Rec32 *src = reinterpret_cast<const Rec32 *>(c->w_src.p);
+  const Rec32 *src = reinterpret_cast<const Rec32 *>(rec);
   const double self_c = self_coefficient(c, self_mode);
   kt_start(c, kKPairF32);
-  if (c->use_poly) dispatch_r1<true>(c, src, dw, u, self_c, norm);
-  else dispatch_r1<false>(c, src, dw, u, self_c, norm);
+  if (c->use_poly) dispatch_r1<true>(c, src, f, u, self_c, norm);
+  else dispatch_r1<false>(c, src, f, u, self_c, norm);
   kt_stop(c, kKPairF32);
   return check_launch(c, "pair f32 r1");
 }

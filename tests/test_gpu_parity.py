@@ -373,6 +373,42 @@ def test_chebyshev_faithful_matches_oracle_fp64():
         assert rel(y, y_o) <= 1e-11
 
 
+def test_chebyshev_faithful_fp32_matches_oracle():
+    """The FP32 context's reference-faithful series (check after every term,
+    FP64 estimator sums; each term writes the pair records of its new x and
+    dw for the next matvecs) against the FP64 oracle's series: the same
+    terms, matvecs and stopping decision, err1 / err2 within the FP32 pair
+    sums' effect, y and dw = M y within 1e-5; a second call repeats the first
+    bit for bit."""
+    xyz, L = suspension(3000, 0.1, 43)
+    box = O.make_box([0] * 3, [L] * 3, [1, 1, 1])
+    c = O.constants(alpha=0.5)
+    nb = O.neighbors_cutoff(box, xyz, 7.0)
+    xi = O.std_normal_vector(987654321, 3 * len(xyz))
+    op = O.Operator(matvec=(c, box, xyz, nb, O.SELF_BEAD, 8))
+    with G.Context(box_hi=(L,) * 3, rc=7.0, precision=G.FP32) as ctx:
+        ctx.set_particles(xyz)
+        ctx.build_cells()
+        lo, hi = ctx.lanczos_bounds(k=24, seed=5)
+        lo, hi = lo / 1.05, hi * 1.05
+        y_o, rep_o = O.cheb_inv_sqrt(op, xi, 50, lo, hi, 1e-3)
+        y, rep = ctx.cheb_inv_sqrt(xi, 50, lo, hi, 1e-3, check_every=1)
+        rc, dw, rep_b = ctx.brownian_displacement(xi, 50, lo, hi, 1e-3, check_every=1)
+        rc2, dw2, _ = ctx.brownian_displacement(xi, 50, lo, hi, 1e-3, check_every=1)
+    r = rep[0]
+    assert r["converged"] == rep_o.converged and r["n_terms"] == rep_o.n_terms
+    assert r["n_matvecs"] == rep_o.n_matvecs
+    assert r["err1"] == pytest.approx(rep_o.err1, rel=5e-2)
+    assert r["err2"] == pytest.approx(rep_o.err2, rel=1e-3)
+    assert rel(y, y_o) <= 1e-5
+    assert rc == 0 and rep_b[0]["n_terms"] == r["n_terms"]
+    My_o = O.local_matvec(c, box, xyz, nb, y_o, O.SELF_BEAD, nthreads=8)
+    assert rel(dw, My_o) <= 1e-5
+    assert rc2 == 0 and np.array_equal(dw, dw2)
+    print(f"FP32 faithful: {r['n_terms']} terms, err1 {r['err1']:.4e} (oracle "
+          f"{rep_o.err1:.4e}), y {rel(y, y_o):.2e}, dw {rel(dw, My_o):.2e}")
+
+
 def test_chebyshev_fp32_batched_rhs_accuracy():
     xyz, L = suspension(1500, 0.1, 43)
     box = O.make_box([0] * 3, [L] * 3, [1, 1, 1])
