@@ -376,10 +376,11 @@ def test_chebyshev_faithful_matches_oracle_fp64():
 def test_chebyshev_faithful_fp32_matches_oracle():
     """The FP32 context's reference-faithful series (check after every term,
     FP64 estimator sums; each term writes the pair records of its new x and
-    dw for the next matvecs) against the FP64 oracle's series: the same
+    dw for the next matvecs, and the next term runs speculatively while the
+    host waits for a check) against the FP64 oracle's series: the same
     terms, matvecs and stopping decision, err1 / err2 within the FP32 pair
-    sums' effect, y and dw = M y within 1e-5; a second call repeats the first
-    bit for bit."""
+    sums' effect, y and dw = M y within 1e-5; dw is the library's own M y of
+    the returned y; a second call repeats the first bit for bit."""
     xyz, L = suspension(3000, 0.1, 43)
     box = O.make_box([0] * 3, [L] * 3, [1, 1, 1])
     c = O.constants(alpha=0.5)
@@ -395,6 +396,9 @@ def test_chebyshev_faithful_fp32_matches_oracle():
         y, rep = ctx.cheb_inv_sqrt(xi, 50, lo, hi, 1e-3, check_every=1)
         rc, dw, rep_b = ctx.brownian_displacement(xi, 50, lo, hi, 1e-3, check_every=1)
         rc2, dw2, _ = ctx.brownian_displacement(xi, 50, lo, hi, 1e-3, check_every=1)
+        # dw is M of the y the series stopped at (not of a speculative next term's)
+        My = ctx.local_matvec(y, G.SELF_BEAD)
+    assert rel(dw, My) <= 1e-12
     r = rep[0]
     assert r["converged"] == rep_o.converged and r["n_terms"] == rep_o.n_terms
     assert r["n_matvecs"] == rep_o.n_matvecs
