@@ -170,8 +170,7 @@ __global__ void __launch_bounds__(kVecThreads) k_cheb_term(int64_t D, double two
                                                            double *__restrict__ partial,
                                                            const float4 *__restrict__ pos32 = nullptr,
                                                            float4 *__restrict__ rec_x = nullptr,
-                                                           float4 *__restrict__ rec_dw = nullptr,
-                                                           const double *__restrict__ dw_in = nullptr) {
+                                                           float4 *__restrict__ rec_dw = nullptr) {
   __shared__ double sh[32];
   __shared__ float2 shf[32];
   const int r = blockIdx.y, nrhs = gridDim.y;
@@ -181,9 +180,7 @@ __global__ void __launch_bounds__(kVecThreads) k_cheb_term(int64_t D, double two
   float h4 = 0.f, l4 = 0.f, h3 = 0.f, l3 = 0.f;
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < D;
        k += (int64_t)gridDim.x * blockDim.x) {
-    // (dw_in: the term reads y from one buffer and writes the new y to
-    // another, so that a speculative term leaves the previous y intact)
-    const double y = REC && dw_in ? dw_in[off + k] : dw[off + k];
+    const double y = dw[off + k];
     double v = two_db * x1[off + k] + two_da * xm[off + k];
     v -= x0[off + k];
     xm[off + k] = v;
@@ -528,19 +525,13 @@ int cheb_slots_impl(ggem_ctx *c, int nrhs, int N, double eig_min, double eig_max
   // one right-hand side on the unfused path with per-pair tensors (the
   // reference-faithful checks): each term also writes the pair records of
   // its new x (w_rec[0]) and dw (w_src), so the next matvec and the check's
-  // matvec skip their staging passes.  Term i + 1 is also issued before the
-  // host waits for check i (it reads y_i and writes y_{i+1} to the other y
-  // buffer); when check i stops the series the speculative term is dropped
-  // and y_i stands, so the host's wait per term overlaps the next term.
+  // matvec skip their staging passes
   const bool rec_terms = can_fuse && !fused && !c->pretensor_ok && c->n > 0;
-  bool xrec_fresh = false, dwrec_fresh = false, spec_issued = false;
-  double *y_other = nullptr;
+  bool xrec_fresh = false, dwrec_fresh = false;
   if (rec_terms) {
     cudaError_t e;
-    if ((e = c->w_rec[0].ensure(2 * (size_t)c->n)) || (e = c->w_src.ensure(2 * (size_t)c->n)) ||
-        (e = c->w_y2.ensure((size_t)D)))
+    if ((e = c->w_rec[0].ensure(2 * (size_t)c->n)) || (e = c->w_src.ensure(2 * (size_t)c->n)))
       return cuda_fail(c, e, "chebyshev records");
-    y_other = c->w_y2.p;
   }
   bool staged_fresh = false;
   // partial sums per reduction: vector-kernel blocks, or in a fused series
@@ -637,7 +628,9 @@ int cheb_slots_impl(ggem_ctx *c, int nrhs, int N, double eig_min, double eig_max
     if (int rc = finalize_issue(c, 4 * nrhs, G, h, pending)) return rc;
     if (event_first)
       if (int rc = record_readback(c)) return rc;
-    return spec_dw ? permute_from_slots(c, nrhs, dm, spec_dw) : GGEM_OK;
+    // (with a check after every term the caller permutes the last check's
+    // M y once, after the series, instead of every check speculatively)
+    return spec_dw && !faithful ? permute_from_slots(c, nrhs, dm, spec_dw) : GGEM_OK;
   };
   // evaluate err1 / err2 of the current dw for the active right-hand sides
   auto check_eval = [&](double coef_abs, bool apply_rules) -> int {
@@ -673,25 +666,6 @@ int cheb_slots_impl(ggem_ctx *c, int nrhs, int N, double eig_min, double eig_max
   auto check_now = [&](double coef_abs, bool apply_rules) -> int {
     if (int rc = check_issue(true)) return rc;
     return check_eval(coef_abs, apply_rules);
-  };
-
-  // one recorded term (rec_terms): M x1 (from x1's records once a term
-  // wrote them), then the FP64 recurrence reading y_in and writing y_out,
-  // with the records of the new x and the new y
-  auto issue_rec_term = [&](int ii, const double *a0, const double *a1, double *am,
-                            const double *y_in, double *y_out) -> int {
-    if (int rc = xrec_fresh ? matvec_records(c, c->w_rec[0].p, a1, am, sm, nullptr)
-                            : matvec_slots(c, 1, a1, am, sm))
-      return rc;
-    RhsCoef cf;
-    cf.c[0] = X[ii + 1];
-    kt_start(c, kKChebTerm);
-    k_cheb_term<true, false, true><<<dim3(G, 1), kVecThreads, 0, st>>>(
-        D, two_da, two_db, cf, a0, a1, am, y_out, p_term, c->pos32.p, c->w_rec[0].p, c->w_src.p,
-        y_in);
-    kt_stop(c, kKChebTerm);
-    xrec_fresh = dwrec_fresh = true;
-    return check_launch(c, "cheb term");
   };
 
   int i_begin = 1;
@@ -794,7 +768,7 @@ int cheb_slots_impl(ggem_ctx *c, int nrhs, int N, double eig_min, double eig_max
     }
     if (int rc = check_eval(std::fabs(X[i_chk + 1]), true)) return rc;  // incl. kRestartCheb
     *dm_is_my = true;
-    if (spec_done) *spec_done = spec_dw != nullptr;
+    if (spec_done) *spec_done = spec_dw != nullptr && !faithful;
     first_check = i_chk + 1;
     i_begin = i_chk + 1;
   }
@@ -802,7 +776,7 @@ int cheb_slots_impl(ggem_ctx *c, int nrhs, int N, double eig_min, double eig_max
   if (faithful) {  // the estimators before the loop (:1064-1072)
     if (int rc = check_now(std::fabs(X[1]), false)) return rc;
     *dm_is_my = true;
-    if (spec_done) *spec_done = spec_dw != nullptr;
+    if (spec_done) *spec_done = spec_dw != nullptr && !faithful;
   }
   for (int i = i_begin; i < N; ++i) {
     int n_active = 0;
@@ -821,14 +795,6 @@ int cheb_slots_impl(ggem_ctx *c, int nrhs, int N, double eig_min, double eig_max
                                   check ? p_term : nullptr))
         return rc;
       records_fresh = true;
-    } else if (rec_terms) {
-      // (term i was already issued while the host waited for check i - 1)
-      if (!spec_issued)
-        if (int rc = issue_rec_term(i, x0, x1, xm, dw, y_other)) return rc;
-      spec_issued = false;
-      std::swap(dw, y_other);  // term i stands: dw holds y_i
-      records_fresh = false;
-      staged_fresh = false;
     } else if (batch_fused && !check) {
       double cf[kMaxRhs];
       for (int r = 0; r < nrhs; ++r) cf[r] = active[r] ? X[i + 1] : 0.0;
@@ -836,16 +802,23 @@ int cheb_slots_impl(ggem_ctx *c, int nrhs, int N, double eig_min, double eig_max
         return rc;
       staged_fresh = true;
     } else {
-      // (a fused batched term before this one left x1's staging)
-      if (int rc = batch_fused && staged_fresh ? matvec_slots_prestaged(c, nrhs, x1, xm, sm)
-                                               : matvec_slots(c, nrhs, x1, xm, sm))
-        return rc;
+      // (a fused batched term before this one left x1's staging; a recorded
+      // term before this one left x1's pair records)
+      int mrc;
+      if (batch_fused && staged_fresh) mrc = matvec_slots_prestaged(c, nrhs, x1, xm, sm);
+      else if (rec_terms && xrec_fresh) mrc = matvec_records(c, c->w_rec[0].p, x1, xm, sm, nullptr);
+      else mrc = matvec_slots(c, nrhs, x1, xm, sm);
+      if (mrc) return mrc;
       RhsCoef cf;
       for (int r = 0; r < nrhs; ++r) cf.c[r] = active[r] ? X[i + 1] : 0.0;
       kt_start(c, kKChebTerm);
       if (check && ff_sums)
         k_cheb_term<true, true><<<dim3(G, nrhs), kVecThreads, 0, st>>>(D, two_da, two_db, cf,
                                                                         x0, x1, xm, dw, p_term);
+      else if (check && rec_terms)
+        k_cheb_term<true, false, true><<<dim3(G, nrhs), kVecThreads, 0, st>>>(
+            D, two_da, two_db, cf, x0, x1, xm, dw, p_term, c->pos32.p, c->w_rec[0].p,
+            c->w_src.p);
       else if (check)
         k_cheb_term<true><<<dim3(G, nrhs), kVecThreads, 0, st>>>(D, two_da, two_db, cf, x0, x1,
                                                                   xm, dw, p_term);
@@ -856,6 +829,7 @@ int cheb_slots_impl(ggem_ctx *c, int nrhs, int N, double eig_min, double eig_max
       if (int rc = check_launch(c, "cheb term")) return rc;
       records_fresh = false;
       staged_fresh = false;
+      xrec_fresh = dwrec_fresh = check && rec_terms;
     }
     for (int r = 0; r < nrhs; ++r)
       if (active[r]) {
@@ -866,14 +840,9 @@ int cheb_slots_impl(ggem_ctx *c, int nrhs, int N, double eig_min, double eig_max
     if (spec_done) *spec_done = false;
     if (check) {
       kt_span_end(c);
-      if (int rc = check_issue(true)) return rc;
-      if (rec_terms && i + 1 < N) {  // term i + 1 while the host waits
-        if (int rc = issue_rec_term(i + 1, x1, xm, x0, dw, y_other)) return rc;
-        spec_issued = true;
-      }
-      if (int rc = check_eval(std::fabs(X[i + 1]), true)) return rc;  // incl. kRestartCheb
+      if (int rc = check_now(std::fabs(X[i + 1]), true)) return rc;  // incl. kRestartCheb
       *dm_is_my = true;
-      if (spec_done) *spec_done = spec_dw != nullptr;
+      if (spec_done) *spec_done = spec_dw != nullptr && !faithful;
       if (first_check < 0) first_check = i + 1;
     }
     // x0 <- x1, x1 <- xm (:1152-1153) by rotating the buffers
@@ -881,10 +850,6 @@ int cheb_slots_impl(ggem_ctx *c, int nrhs, int N, double eig_min, double eig_max
     x0 = x1;
     x1 = xm;
     xm = t;
-  }
-  if (rec_terms && dw != c->w_y.p) {  // callers read y from w_y
-    cudaError_t e = cudaMemcpyAsync(c->w_y.p, dw, sizeof(double) * D, cudaMemcpyDeviceToDevice, st);
-    if (e) return cuda_fail(c, e, "series y");
   }
   if (check_every == 0) {
     int worst = 0;

@@ -194,7 +194,6 @@ struct ggem_ctx {
 
   // vector workspaces (FP64 slot order) and FP32 staging
   ggem::DevBuf<double> w_in, w_out, w_a, w_b, w_c, w_d, w_e, w_y;
-  ggem::DevBuf<double> w_y2;  // the faithful series' second y (speculative terms)
   ggem::DevBuf<float4> w_f32;
   ggem::DevBuf<float> w_fb;     // batched forces [slot][3][64] FP32
   ggem::DevBuf<float> w_fb2;    // the next term's staging in a fused batched series
