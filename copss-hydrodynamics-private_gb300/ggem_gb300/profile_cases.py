@@ -19,6 +19,7 @@ cases:
               onto the 8 Gauss points of each of 72^3 HEX20 elements
   mlp         k_mlp_forward: 3 predictions of 512 rows of the eigen network
   ens         k_ens_series: 3 ensemble steps of 64 suspensions, 8 RHS each
+  ens_term    k_ens_pair: the same steps as one launch per term
 """
 from __future__ import annotations
 
@@ -150,7 +151,7 @@ def mlp() -> None:
     print("ok")
 
 
-def ens() -> None:
+def ens(persistent=True) -> None:
     torch = _torch()
     rng = np.random.default_rng(5)
     K = 64
@@ -160,6 +161,7 @@ def ens() -> None:
     e = G.Ensemble([L for _, L in sus])
     d_xyz = torch.from_numpy(np.concatenate([x for x, _ in sus]).reshape(-1)).cuda()
     e.set_particles_dev(ns, d_xyz.data_ptr())
+    e.set_series_mode(persistent=persistent)
     beads, pairs = e.sizes()
     lz = [e.lanczos(b, 24, 7) for b in range(K)]
     lo = np.array([x[0] for x in lz]) / 1.05
@@ -173,7 +175,8 @@ def ens() -> None:
 
 
 CASES = {"pair_cheb": pair_cheb, "pair_tv": pair_tv, "pair_r1": pair_r1, "list": list_build,
-         "pair_f64": pair_f64, "spread": spread, "mlp": mlp, "ens": ens}
+         "pair_f64": pair_f64, "spread": spread, "mlp": mlp, "ens": ens,
+         "ens_term": lambda: ens(persistent=False)}
 
 
 def main(argv=None) -> int:
