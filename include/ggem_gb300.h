@@ -128,7 +128,12 @@ int ggem_synchronize(ggem_ctx *ctx);
 
 /* ---- particles and neighbour structure -------------------------------- */
 /* replaces PointParticle positions + PointMesh::reinit (point_mesh.C:245-289):
- * cell assignment, sorted cell list and (FP32) the cached pair list */
+ * cell assignment, sorted cell list and (FP32) the cached pair list.
+ * xyz (AoS, 3n doubles) is copied on the context's stream: from pageable
+ * memory the call returns once the copy has read it; from page-locked
+ * memory the copy may still be reading it after the call returns, so keep
+ * xyz unchanged until the next call that synchronises (ggem_build_cells
+ * without deferred checks, ggem_brownian_displacement, ggem_synchronize). */
 int ggem_set_particles(ggem_ctx *ctx, int64_t n, const double *xyz);
 int ggem_set_particles_dev(ggem_ctx *ctx, int64_t n, const double *d_xyz);
 /* (a NaN or infinite coordinate is reported by the cell build, or with
