@@ -210,7 +210,7 @@ def all_kernels() -> None:
                                                                1e-3, check_every=1))
         run("series 64", lambda: c.cheb_inv_sqrt(rng.standard_normal(64 * 3 * n), 50,
                                                  lo / 1.05, hi * 1.05, 1e-3, check_every=0))
-        run("power", lambda: c.power_iteration())
+        run("power", lambda: c.power_iteration(tol=1e-2, maxits=200))
         run("features", lambda: c.surrogate_features())
         d = torch.empty(3 * n, dtype=torch.float64, device="cuda")
         run("philox", lambda: c.philox_normals_dev(1, 2, 3 * n, d.data_ptr()))
@@ -255,16 +255,16 @@ def all_kernels() -> None:
         run("spread fp32", lambda: c.spread_elements(f, G.FP32))
         run("spread fp64", lambda: c.spread_elements(f, G.FP64))
         run("reference matvec", lambda: c.local_matvec(f))
-    # FEM values at the particles (a trivial dof map: 20 own nodes per element)
+    # FEM values at the particles (a trivial dof map: 3 x 20 own dofs per element)
     ne = (8, 8, 8)
     with G.Context(box_hi=(L,) * 3, rc=7.0, precision=G.FP64) as c:
         c.set_particles(xyz)
         ne_tot = int(np.prod(ne))
-        dofs = np.arange(20 * ne_tot, dtype=np.int64).reshape(ne_tot, 20)
-        sol = rng.standard_normal(20 * ne_tot)
+        dofs = np.arange(60 * ne_tot, dtype=np.int64).reshape(ne_tot, 3, 20)
+        sol = rng.standard_normal(60 * ne_tot)
 
         def fem():
-            with G.Fem(c, ne, (0, 0, 0), (L, L, L), 20 * ne_tot, dofs) as fe:
+            with G.Fem(c, ne, (0, 0, 0), (L, L, L), 60 * ne_tot, dofs) as fe:
                 fe.point_values(sol)
         run("fem", fem)
     # the network: a prediction and one short training run
