@@ -345,30 +345,50 @@ __device__ __forceinline__ bool exact_within(const Grid &g, double4_32a a, doubl
 
 // Warp-per-cell pair list, one pass into fixed-width rows.  The candidates
 // of a target cell are the concatenation of its stencil cells (stencil
-// order, slot order inside a cell); lanes take 32 consecutive candidates
-// with coalesced loads, the cell's targets are broadcast one at a time from
-// shared memory, and a ballot prefix places each accepted candidate.  Entries
+// order, slot order inside a cell).  For each chunk of up to 32 targets the
+// lanes first take 32 consecutive candidates at a time with coalesced loads
+// and keep those within reach of the chunk's bounding box; the kept ones
+// queue in shared memory, in candidate order, and every 32 of them are
+// tested against the chunk's targets, which are broadcast one at a time from
+// shared memory; a ballot prefix places each accepted candidate.  Entries
 // therefore come out in exactly the per-target order of a sequential sweep.
 // Row s holds entries [s*W, s*W + cnt[s]); a row longer than W is counted
 // but not stored: the kernel records the longest row and sets
 // kErrListCapacity, and the host rebuilds with a wider W.
-constexpr int kListWarps = 8;     // warps per CTA
+// One warp per block, one block per cell: cells hold different numbers of
+// targets, and a block of several cell-warps held its resources until its
+// longest cell was done (N = 200k, phi = 0.1: 92 us against 101 us with 8
+// warps per block, and against 97 us with 8-warp blocks claiming cells from
+// a counter).
 constexpr int kMaxStencil = 128;  // stencil cells per target cell
+constexpr int kListQueue = 64;    // queued candidates per warp (< 32 left + 32 new)
 
-__global__ void __launch_bounds__(32 * kListWarps, 6) k_pair_list_warp(
+// FP32 distance of a candidate from the targets' box, formed like the pair
+// test's r2 below (the same subtractions, squares and fused adds, each
+// monotone in its operands), so that it never exceeds the r2 of any target
+// inside the box: a candidate whose box distance is above rc2_hi is above it
+// for every target and would be rejected there without the exact test
+__device__ __forceinline__ float box_r2(float qx, float qy, float qz, float3 lo, float3 hi) {
+  const float bx = qx > hi.x ? qx - hi.x : (qx < lo.x ? lo.x - qx : 0.f);
+  const float by = qy > hi.y ? qy - hi.y : (qy < lo.y ? lo.y - qy : 0.f);
+  const float bz = qz > hi.z ? qz - hi.z : (qz < lo.z ? lo.z - qz : 0.f);
+  return fmaf(bz, bz, fmaf(by, by, bx * bx));
+}
+
+__global__ void __launch_bounds__(32, 32) k_pair_list_warp(
     Grid g, const int4 *__restrict__ stencil, int nst, const float4 *__restrict__ shift,
     const int32_t *__restrict__ start, const float4 *__restrict__ pos32,
     const double4_32a *__restrict__ pos64, float rc2_lo, float rc2_hi, double rc2, int W,
     int32_t *__restrict__ count, uint32_t *__restrict__ list,
     unsigned long long *__restrict__ stat, int *__restrict__ err,
     int32_t *__restrict__ count_h, uint32_t *__restrict__ list_h) {
-  __shared__ int32_t s_base[kListWarps][kMaxStencil];
-  __shared__ int32_t s_pre[kListWarps][kMaxStencil + 1];
-  __shared__ int32_t s_code[kListWarps][kMaxStencil];
-  __shared__ float4 s_pi[kListWarps][32];  // the targets of the current chunk
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t C = blockIdx.x * (int64_t)kListWarps + w;
-  if (C >= g.ncell) return;  // whole warp
+  __shared__ int32_t s_base[kMaxStencil];
+  __shared__ int32_t s_pre[kMaxStencil + 1];
+  __shared__ int32_t s_code[kMaxStencil];
+  __shared__ float4 s_pi[32];          // the targets of the current chunk
+  __shared__ float4 s_q[kListQueue];   // kept candidates: frame position, entry
+  const int lane = threadIdx.x;
+  const int64_t C = blockIdx.x;
   const int32_t tb = start[C], te = start[C + 1];
   if (te <= tb) return;
   const int cx = (int)(C % g.nc[0]), cy = (int)((C / g.nc[0]) % g.nc[1]),
@@ -394,13 +414,13 @@ __global__ void __launch_bounds__(32 * kListWarps, 6) k_pair_list_warp(
       if (lane >= o) incl += y;
     }
     if (k < nst) {
-      s_base[w][k] = base;
-      s_code[w][k] = code;
-      s_pre[w][k] = carry + incl - cnt;
+      s_base[k] = base;
+      s_code[k] = code;
+      s_pre[k] = carry + incl - cnt;
     }
     carry += __shfl_sync(0xffffffffu, incl, 31);
   }
-  if (lane == 0) s_pre[w][nst] = carry;
+  if (lane == 0) s_pre[nst] = carry;
   __syncwarp();
   const int32_t V = carry;
   const unsigned lt_mask = (1u << lane) - 1u;
@@ -411,9 +431,25 @@ __global__ void __launch_bounds__(32 * kListWarps, 6) k_pair_list_warp(
     const int32_t own = t0 + lane;
     const bool own_ok = lane < ntc;
     __syncwarp();  // the previous chunk's targets are no longer read
-    s_pi[w][lane] = own_ok ? pos32[own] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 mine = own_ok ? pos32[own] : make_float4(0.f, 0.f, 0.f, 0.f);
+    s_pi[lane] = mine;
+    // the chunk's bounding box (FP32 min / max of the targets' own values)
+    float3 blo = own_ok ? make_float3(mine.x, mine.y, mine.z)
+                        : make_float3(INFINITY, INFINITY, INFINITY);
+    float3 bhi = own_ok ? make_float3(mine.x, mine.y, mine.z)
+                        : make_float3(-INFINITY, -INFINITY, -INFINITY);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      blo.x = fminf(blo.x, __shfl_xor_sync(0xffffffffu, blo.x, o));
+      blo.y = fminf(blo.y, __shfl_xor_sync(0xffffffffu, blo.y, o));
+      blo.z = fminf(blo.z, __shfl_xor_sync(0xffffffffu, blo.z, o));
+      bhi.x = fmaxf(bhi.x, __shfl_xor_sync(0xffffffffu, bhi.x, o));
+      bhi.y = fmaxf(bhi.y, __shfl_xor_sync(0xffffffffu, bhi.y, o));
+      bhi.z = fmaxf(bhi.z, __shfl_xor_sync(0xffffffffu, bhi.z, o));
+    }
     __syncwarp();
     int32_t own_cnt = 0, own_cnt_h = 0;
+    int queued = 0;  // warp-uniform
     for (int32_t v0 = 0; v0 < V; v0 += 32) {
       const int32_t v = v0 + lane;
       const bool valid = v < V;
@@ -421,50 +457,73 @@ __global__ void __launch_bounds__(32 * kListWarps, 6) k_pair_list_warp(
       int lo = 0, hi = nst - 1;
       while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
-        if (s_pre[w][mid] <= v) lo = mid;
+        if (s_pre[mid] <= v) lo = mid;
         else hi = mid - 1;
       }
-      const int32_t t = valid ? s_base[w][lo] + (v - s_pre[w][lo]) : 0;
-      const int code = s_code[w][lo];
+      const int32_t t = valid ? s_base[lo] + (v - s_pre[lo]) : 0;
+      const int code = s_code[lo];
       const float4 sh = shift[code];
       const float4 pj = valid ? pos32[t] : make_float4(0.f, 0.f, 0.f, 0.f);
       // the candidate in the target cell's frame (the shift added once per
       // candidate; the filter's band absorbs the different rounding)
       const float qx = pj.x + sh.x, qy = pj.y + sh.y, qz = pj.z + sh.z;
-      for (int i = 0; i < ntc; ++i) {
-        const float4 pi = s_pi[w][i];  // one broadcast read
-        const int32_t ti = t0 + i;
-        const float dx = qx - pi.x;
-        const float dy = qy - pi.y;
-        const float dz = qz - pi.z;
-        const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-        // accepted below rc2_lo, rejected above rc2_hi; in between (FP32
-        // rounding of |r| = rc) the exact FP64 test decides, behind a
-        // warp-uniform branch so that the common case carries none of it
-        bool in = valid && t != ti && !(r2 > rc2_hi);
-        const bool band = in && !(r2 < rc2_lo);
-        if (__any_sync(0xffffffffu, band)) {
-          if (band) in = exact_within(g, pos64[ti], pos64[t], rc2);
-        }
-        const unsigned bal = __ballot_sync(0xffffffffu, in);
-        const int32_t at = __shfl_sync(0xffffffffu, own_cnt, i);
-        if (in) {
-          const int32_t k = at + __popc(bal & lt_mask);
-          if (k < W) list[(int64_t)ti * W + k] = ((uint32_t)t << kCodeBits) | (uint32_t)code;
-        }
-        if (lane == i) own_cnt += __popc(bal);
-        if (list_h) {
-          // the half list: each unordered pair once, in the row of its
-          // smaller slot (the full list is symmetric, its predicate exact)
-          const bool in_h = in && t > ti;
-          const unsigned bal_h = __ballot_sync(0xffffffffu, in_h);
-          const int32_t at_h = __shfl_sync(0xffffffffu, own_cnt_h, i);
-          if (in_h) {
-            const int32_t k = at_h + __popc(bal_h & lt_mask);
-            if (k < W) list_h[(int64_t)ti * W + k] = ((uint32_t)t << kCodeBits) | (uint32_t)code;
+      const bool keep = valid && !(box_r2(qx, qy, qz, blo, bhi) > rc2_hi);
+      const unsigned kb = __ballot_sync(0xffffffffu, keep);
+      if (keep)
+        s_q[queued + __popc(kb & lt_mask)] =
+            make_float4(qx, qy, qz, __uint_as_float(((uint32_t)t << kCodeBits) | (uint32_t)code));
+      queued += __popc(kb);
+      const bool last = v0 + 32 >= V;
+      // test the queue 32 at a time (a partial batch only after the last
+      // candidates); at most two batches per pass
+      while (queued >= 32 || (last && queued > 0)) {
+        __syncwarp();
+        const int m = min(queued, 32);
+        // lanes past the batch carry a far point: r2 overflows, never accepted
+        const float4 c = lane < m ? s_q[lane] : make_float4(1e30f, 1e30f, 1e30f, 0.f);
+        const uint32_t en = __float_as_uint(c.w);
+        const int32_t tj = (int32_t)(en >> kCodeBits);
+        for (int i = 0; i < ntc; ++i) {
+          const float4 pi = s_pi[i];  // one broadcast read
+          const int32_t ti = t0 + i;
+          const float dx = c.x - pi.x;
+          const float dy = c.y - pi.y;
+          const float dz = c.z - pi.z;
+          const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+          // accepted below rc2_lo, rejected above rc2_hi; in between (FP32
+          // rounding of |r| = rc) the exact FP64 test decides, behind a
+          // warp-uniform branch so that the common case carries none of it
+          bool in = tj != ti && !(r2 > rc2_hi);
+          const bool band = in && !(r2 < rc2_lo);
+          if (__any_sync(0xffffffffu, band)) {
+            if (band) in = exact_within(g, pos64[ti], pos64[tj], rc2);
           }
-          if (lane == i) own_cnt_h += __popc(bal_h);
+          const unsigned bal = __ballot_sync(0xffffffffu, in);
+          const int32_t at = __shfl_sync(0xffffffffu, own_cnt, i);
+          if (in) {
+            const int32_t k = at + __popc(bal & lt_mask);
+            if (k < W) list[(int64_t)ti * W + k] = en;
+          }
+          if (lane == i) own_cnt += __popc(bal);
+          if (list_h) {
+            // the half list: each unordered pair once, in the row of its
+            // smaller slot (the full list is symmetric, its predicate exact)
+            const bool in_h = in && tj > ti;
+            const unsigned bal_h = __ballot_sync(0xffffffffu, in_h);
+            const int32_t at_h = __shfl_sync(0xffffffffu, own_cnt_h, i);
+            if (in_h) {
+              const int32_t k = at_h + __popc(bal_h & lt_mask);
+              if (k < W) list_h[(int64_t)ti * W + k] = en;
+            }
+            if (lane == i) own_cnt_h += __popc(bal_h);
+          }
         }
+        // move the rest of the queue to its front
+        const int rest = queued - m;
+        const float4 r = lane < rest ? s_q[32 + lane] : c;
+        __syncwarp();
+        if (lane < rest) s_q[lane] = r;
+        queued = rest;
       }
     }
     if (own_ok) {
@@ -573,6 +632,13 @@ int cell_flag_error(ggem_ctx *c, int flags) {
   return GGEM_OK;
 }
 
+void launch_pair_list(ggem_ctx *c, int nst, int W, cudaStream_t st) {
+  k_pair_list_warp<<<(unsigned)c->grid.ncell, 32, 0, st>>>(
+      c->grid, c->d_stencil.p, nst, c->d_shift.p, c->cell_start.p, c->pos32.p, c->pos64.p,
+      c->rc2_lo, c->rc2_hi, c->rc2, W, c->nb_cnt.p, c->nb_list.p, c->nb_stat.p, c->err.p,
+      c->sym_pairs ? c->nb_cnt_h.p : nullptr, c->sym_pairs ? c->nb_list_h.p : nullptr);
+}
+
 int build_pair_list(ggem_ctx *c) {
   const int64_t n = c->n;
   cudaError_t e = cudaSuccess;
@@ -595,7 +661,6 @@ int build_pair_list(ggem_ctx *c) {
   }
   const int nst = (int)c->stencil.size();
   if (nst > kMaxStencil) return fail(c, GGEM_ERR_BAD_ARG, "stencil too large for the list builder");
-  const unsigned cb = (unsigned)((c->grid.ncell + kListWarps - 1) / kListWarps);
   if (c->defer_checks && c->list_checked_once) {
     // keep the width of the previous build; a longer row is stored clipped
     // (counts never exceed W) and found when the statistics are read
@@ -609,10 +674,7 @@ int build_pair_list(ggem_ctx *c) {
     if (c->sym_pairs && ((e = c->nb_list_h.ensure((size_t)n * c->nb_w)) ||
                          (e = c->nb_cnt_h.ensure(n))))
       return cuda_fail(c, e, "half pair list");
-    k_pair_list_warp<<<cb, 32 * kListWarps, 0, st>>>(
-        c->grid, c->d_stencil.p, nst, c->d_shift.p, c->cell_start.p, c->pos32.p, c->pos64.p,
-        c->rc2_lo, c->rc2_hi, c->rc2, c->nb_w, c->nb_cnt.p, c->nb_list.p, c->nb_stat.p, c->err.p,
-        c->sym_pairs ? c->nb_cnt_h.p : nullptr, c->sym_pairs ? c->nb_list_h.p : nullptr);
+    launch_pair_list(c, nst, c->nb_w, st);
     kt_stop(c, kKListBuild);
     if (int rc = check_launch(c, "pair list")) return rc;
     c->cells_built = true;
@@ -634,10 +696,7 @@ int build_pair_list(ggem_ctx *c) {
     if (c->sym_pairs && ((e = c->nb_list_h.ensure((size_t)n * W)) || (e = c->nb_cnt_h.ensure(n))))
       return cuda_fail(c, e, "half pair list");
     if (attempt == 0) kt_start(c, kKListBuild);
-    k_pair_list_warp<<<cb, 32 * kListWarps, 0, st>>>(
-        c->grid, c->d_stencil.p, nst, c->d_shift.p, c->cell_start.p, c->pos32.p, c->pos64.p,
-        c->rc2_lo, c->rc2_hi, c->rc2, W, c->nb_cnt.p, c->nb_list.p, c->nb_stat.p, c->err.p,
-        c->sym_pairs ? c->nb_cnt_h.p : nullptr, c->sym_pairs ? c->nb_list_h.p : nullptr);
+    launch_pair_list(c, nst, W, st);
     if (attempt == 0) kt_stop(c, kKListBuild);  // a widened refill is left out
     if (int rc = check_launch(c, "pair list")) return rc;
     h[2] = 0;
