@@ -575,6 +575,7 @@ extern "C" int ggem_local_matvec_dev(ggem_ctx *ctx, int nrhs, const double *d_f,
   if (!ctx || nrhs < 1 || self_mode < 0 || self_mode > 2) return GGEM_ERR_BAD_ARG;
   if (ctx->n > 0 && (!d_f || !d_u)) return GGEM_ERR_BAD_ARG;
   if (int rc = require_built(ctx)) return rc;
+  if (ctx->n == 0) return GGEM_OK;  // no particles: nothing to write
   DeviceGuard dg(ctx->device);
   const size_t len = (size_t)ctx->n * 3 * nrhs;
   cudaError_t e = ctx->w_in.ensure(len);

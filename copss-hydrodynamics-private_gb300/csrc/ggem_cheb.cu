@@ -899,10 +899,19 @@ static int cheb_common(ggem_ctx *ctx, int nrhs, int N, double eig_min, double ei
   return GGEM_OK;
 }
 
+// a context without particles: the series of an empty vector is exact at
+// degree 0 (no operator application), reported converged
+static bool empty_series(const ggem_ctx *ctx, int nrhs, ggem_cheb_report *rep) {
+  if (ctx->n != 0) return false;
+  for (int r = 0; r < nrhs; ++r) rep[r] = ggem_cheb_report{1, 0, 0, 0.0, 0.0};
+  return true;
+}
+
 extern "C" int ggem_cheb_inv_sqrt_dev(ggem_ctx *ctx, int nrhs, int N, double eig_min,
                                       double eig_max, double tol_cheb, int check_every,
                                       double *d_xi, ggem_cheb_report *rep) {
   if (int rc = cheb_common(ctx, nrhs, N, eig_min, eig_max, tol_cheb, check_every, rep)) return rc;
+  if (empty_series(ctx, nrhs, rep)) return GGEM_OK;
   DeviceGuard dg(ctx->device);
   const size_t len = (size_t)ctx->n * 3 * nrhs;
   if (int rc = ensure_cheb_buffers(ctx, len)) return rc;
@@ -981,6 +990,7 @@ extern "C" int ggem_brownian_displacement_dev(ggem_ctx *ctx, int nrhs, int N, do
                                               ggem_cheb_report *rep) {
   if (int rc = cheb_common(ctx, nrhs, N, eig_min, eig_max, tol_cheb, check_every, rep)) return rc;
   if (ctx->n && (!d_xi || !d_dw)) return GGEM_ERR_BAD_ARG;
+  if (empty_series(ctx, nrhs, rep)) return GGEM_OK;
   DeviceGuard dg(ctx->device);
   const size_t len = (size_t)ctx->n * 3 * nrhs;
   if (int rc = ensure_cheb_buffers(ctx, len)) return rc;

@@ -223,7 +223,9 @@ int ggem_cheb_coeffs(int N, double da, double db, int method, double *coef);
 /* BrownianSystem::chebyshev_polynomial_approximation (brownian_system.C:967-1178)
  * on the local mobility: xi_inout (nrhs x 3n) becomes y ~ M^{-1/2} xi.
  * check_every = 1 reproduces the reference exactly (an error-check matvec
- * every term); k > 1 checks err1 every k terms.  rep has nrhs entries. */
+ * every term); k > 1 checks err1 every k terms.  rep has nrhs entries.
+ * A context without particles returns at once with every report converged
+ * at degree 0 and no matvec (the pointers may then be NULL). */
 int ggem_cheb_inv_sqrt(ggem_ctx *ctx, int nrhs, int N, double eig_min, double eig_max,
                        double tol_cheb, int check_every, double *xi_inout,
                        ggem_cheb_report *rep);
