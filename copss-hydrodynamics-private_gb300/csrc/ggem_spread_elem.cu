@@ -54,7 +54,8 @@ constexpr int kSpMaxSeg = 2048;  // contiguous slot ranges of one dilated brick
 constexpr int kSpMaxExt = 32;    // dilated brick extent per axis (5-bit coordinates)
 constexpr size_t kSpRecBytes = 16384;
 constexpr int kSpMaxWords = 1024;  // stencil bitmap words (32768 element offsets)
-constexpr size_t kSpShared = kSpRecBytes + kSpWarps * kSpCap32 * sizeof(uint32_t) +
+constexpr int kSpQueue = 64;      // queued members per warp (< 32 left + 32 new)
+constexpr size_t kSpShared = kSpRecBytes + kSpWarps * kSpQueue * sizeof(float4) +
                              2 * (kSpMaxSeg + 1) * sizeof(int32_t) +
                              kSpMaxWords * sizeof(uint32_t);
 
@@ -146,8 +147,8 @@ __global__ void __launch_bounds__(kSpThreads) k_spread_brick(
   // than 32-byte records would
   float4 *rec32 = reinterpret_cast<float4 *>(sp_smem);        // [2][CAP]
   double4_32a *rec64 = reinterpret_cast<double4_32a *>(sp_smem);  // [CAP][2]
-  uint32_t *members = reinterpret_cast<uint32_t *>(sp_smem + kSpRecBytes);
-  int32_t *seg_begin = reinterpret_cast<int32_t *>(members + kSpWarps * kSpCap32);
+  float4 *queue = reinterpret_cast<float4 *>(sp_smem + kSpRecBytes);
+  int32_t *seg_begin = reinterpret_cast<int32_t *>(queue + kSpWarps * kSpQueue);
   int32_t *seg_pre = seg_begin + kSpMaxSeg + 1;
   uint32_t *s_bits = reinterpret_cast<uint32_t *>(seg_pre + kSpMaxSeg + 1);
   // the element-offset shifts and the stencil bitmap in shared memory: lanes
@@ -236,9 +237,11 @@ __global__ void __launch_bounds__(kSpThreads) k_spread_brick(
   const int nq = sg.nq, lq = sg.lq;
   const int qi = lane / lq, sub = lane - qi * lq;
   unsigned long long my_pairs = 0;
-  // member entry: staged index (10 bits; < kSpCap32) and the element offset minus the
-  // stencil's lower corner (5 bits per axis)
-  uint32_t *mlist = members + warp * kSpCap32;
+  // the warp's member queue: per member its position in the element's frame
+  // (FP32; the staged position plus the element offset's shift, formed once
+  // per member instead of once per point) and its staged index in .w
+  float4 *mq = queue + warp * kSpQueue;
+  const unsigned lt_mask = (1u << lane) - 1u;
   for (int c0 = 0; c0 < total; c0 += CAP) {
     const int cn = min(CAP, total - c0);
     // stage particles [c0, c0 + cn): segment by binary search
@@ -280,12 +283,30 @@ __global__ void __launch_bounds__(kSpThreads) k_spread_brick(
       const int uex = fr[0].full ? ex : ex - fr[0].F;
       const int uey = fr[1].full ? ey : ey - fr[1].F;
       const int uez = fr[2].full ? ez : ez - fr[2].F;
-      // members: staged particles whose element offset is a stencil offset
-      int M = 0;
+      const bool qok = qi < nq;
+      const int64_t qg = e * nq + (qok ? qi : 0);
+      float4 qr = make_float4(0.f, 0.f, 0.f, 0.f);
+      double q0 = 0.0, q1 = 0.0, q2 = 0.0;
+      if (F32) {
+        qr = q_rel[qg];
+      } else {
+        q0 = q_xyz[3 * qg];
+        q1 = q_xyz[3 * qg + 1];
+        q2 = q_xyz[3 * qg + 2];
+      }
+      float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
+      float bx_ = 0.f, by_ = 0.f, bz_ = 0.f;
+      int blk = 0;
+      double ax = 0.0, ay = 0.0, az = 0.0;
+      // members: staged particles whose element offset is a stencil offset,
+      // queued in staging order and summed 32 at a time; lane (qi, sub)
+      // takes members sub, sub + lq, ... of each batch, so every lane sees its
+      // members in the order of one pass over the whole member list
+      int queued = 0;  // warp-uniform
       for (int k0 = 0; k0 < cn; k0 += 32) {
         const int k = k0 + lane;
         bool in = false;
-        uint32_t entry = 0;
+        float4 item = make_float4(0.f, 0.f, 0.f, 0.f);
         if (k < cn) {
           const uint32_t u = F32 ? __float_as_uint(rec32[k].w)
                                  : (uint32_t)__double_as_longlong(rec64[2 * k].w);
@@ -297,61 +318,93 @@ __global__ void __launch_bounds__(kSpThreads) k_spread_brick(
               (unsigned)iz < (unsigned)sg.dim[2]) {
             const int idx = (iz * sg.dim[1] + iy) * sg.dim[0] + ix;
             in = (s_bits[idx >> 5] >> (idx & 31)) & 1u;
-            entry = (uint32_t)k | ((uint32_t)ix << 10) | ((uint32_t)iy << 15) | ((uint32_t)iz << 20);
+            if (F32) {
+              const float4 a = rec32[k];
+              item = make_float4(a.x + s_shift[0][ix], a.y + s_shift[1][iy], a.z + s_shift[2][iz],
+                                 __uint_as_float((uint32_t)k));
+            } else {
+              item.w = __uint_as_float((uint32_t)k);
+            }
           }
         }
         const unsigned bal = __ballot_sync(0xffffffffu, in);
-        if (in) mlist[M + __popc(bal & ((1u << lane) - 1u))] = entry;
-        M += __popc(bal);
+        if (in) mq[queued + __popc(bal & lt_mask)] = item;
+        queued += __popc(bal);
+        my_pairs += (unsigned long long)__popc(bal);
+        const bool last = k0 + 32 >= cn;
+        while (queued >= 32 || (last && queued > 0)) {
+          __syncwarp();
+          const int m = min(queued, 32);
+          for (int j = sub; j < m && qok; j += lq) {
+            const float4 mp = mq[j];
+            const int kk = (int)__float_as_uint(mp.w);
+            if (F32) {
+              const float4 fb = rec32[kSpCap32 + kk];
+              float dx = mp.x - qr.x;
+              float dy = mp.y - qr.y;
+              float dz = mp.z - qr.z;
+              // minimum image (pm_periodic_boundary.C:350-374); only an axis
+              // whose frame is the whole box can produce |d| > L/2
+              if (ANYFULL && fr[0].full) {
+                if (dx <= -0.5f * sg.L32[0]) dx += sg.L32[0];
+                if (dx > 0.5f * sg.L32[0]) dx -= sg.L32[0];
+              }
+              if (ANYFULL && fr[1].full) {
+                if (dy <= -0.5f * sg.L32[1]) dy += sg.L32[1];
+                if (dy > 0.5f * sg.L32[1]) dy -= sg.L32[1];
+              }
+              if (ANYFULL && fr[2].full) {
+                if (dz <= -0.5f * sg.L32[2]) dz += sg.L32[2];
+                if (dz > 0.5f * sg.L32[2]) dz -= sg.L32[2];
+              }
+              const float s2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+              const float p = s2 * sg.e_hi;
+              const float r = fmaf(s2, sg.e_lo, fmaf(s2, sg.e_hi, -p));
+              const float E0 = ex2_approx(p);
+              const float E = fmaf(E0, r * 0.6931471805599453f, E0);
+              const float gv = E * fmaf(-sg.c1, s2, sg.c25);
+              bx_ = fmaf(gv, fb.x, bx_);
+              by_ = fmaf(gv, fb.y, by_);
+              bz_ = fmaf(gv, fb.z, bz_);
+              if (++blk == 8) {  // every 8 pairs into the compensated sums
+                kahan_acc(sx, cx, bx_);
+                kahan_acc(sy, cy, by_);
+                kahan_acc(sz, cz, bz_);
+                bx_ = by_ = bz_ = 0.f;
+                blk = 0;
+              }
+            } else {
+              const double4_32a a = rec64[2 * kk], fb = rec64[2 * kk + 1];
+              // point_vector(q, x_j) with the minimum image (pm_periodic_boundary.C:350-374)
+              double x[3] = {a.x - q0, a.y - q1, a.z - q2};
+#pragma unroll
+              for (int d = 0; d < 3; ++d) {
+                if (sg.g.periodic[d]) {
+                  const double xs = sg.g.L[d];
+                  if (x[d] <= -xs / 2.0) x[d] += xs;
+                  if (x[d] > xs / 2.0) x[d] -= xs;
+                }
+              }
+              // smoothed_force_exp (ggem_stokes.C:117-128)
+              const double r2 = x[0] * x[0] + x[1] * x[1] + x[2] * x[2];
+              const double a2r2 = K.alpha2 * r2;
+              const double gv = K.alpha3_pi_23 * exp(-a2r2) * (2.5 - a2r2);
+              ax += gv * fb.x;
+              ay += gv * fb.y;
+              az += gv * fb.z;
+            }
+          }
+          // the rest of the queue to its front
+          const int rest = queued - m;
+          const float4 rv = lane < rest ? mq[32 + lane] : make_float4(0.f, 0.f, 0.f, 0.f);
+          __syncwarp();
+          if (lane < rest) mq[lane] = rv;
+          queued = rest;
+        }
       }
       __syncwarp();
-      my_pairs += (unsigned long long)M;
-      const bool qok = qi < nq;
-      const int64_t qg = e * nq + (qok ? qi : 0);
       double out[3];
       if (F32) {
-        const float4 qr = q_rel[qg];
-        float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
-        float bx_ = 0.f, by_ = 0.f, bz_ = 0.f;
-        int blk = 0;
-        for (int m = sub; m < M && qok; m += lq) {
-          const uint32_t en = mlist[m];
-          const int k = (int)(en & 1023u);
-          const float4 a = rec32[k], fb = rec32[kSpCap32 + k];
-          float dx = (a.x + s_shift[0][(en >> 10) & 31u]) - qr.x;
-          float dy = (a.y + s_shift[1][(en >> 15) & 31u]) - qr.y;
-          float dz = (a.z + s_shift[2][en >> 20]) - qr.z;
-          // minimum image (pm_periodic_boundary.C:350-374); only an axis
-          // whose frame is the whole box can produce |d| > L/2
-          if (ANYFULL && fr[0].full) {
-            if (dx <= -0.5f * sg.L32[0]) dx += sg.L32[0];
-            if (dx > 0.5f * sg.L32[0]) dx -= sg.L32[0];
-          }
-          if (ANYFULL && fr[1].full) {
-            if (dy <= -0.5f * sg.L32[1]) dy += sg.L32[1];
-            if (dy > 0.5f * sg.L32[1]) dy -= sg.L32[1];
-          }
-          if (ANYFULL && fr[2].full) {
-            if (dz <= -0.5f * sg.L32[2]) dz += sg.L32[2];
-            if (dz > 0.5f * sg.L32[2]) dz -= sg.L32[2];
-          }
-          const float s2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-          const float p = s2 * sg.e_hi;
-          const float r = fmaf(s2, sg.e_lo, fmaf(s2, sg.e_hi, -p));
-          const float E0 = ex2_approx(p);
-          const float E = fmaf(E0, r * 0.6931471805599453f, E0);
-          const float gv = E * fmaf(-sg.c1, s2, sg.c25);
-          bx_ = fmaf(gv, fb.x, bx_);
-          by_ = fmaf(gv, fb.y, by_);
-          bz_ = fmaf(gv, fb.z, bz_);
-          if (++blk == 8) {  // every 8 pairs into the compensated sums
-            kahan_acc(sx, cx, bx_);
-            kahan_acc(sy, cy, by_);
-            kahan_acc(sz, cz, bz_);
-            bx_ = by_ = bz_ = 0.f;
-            blk = 0;
-          }
-        }
         kahan_acc(sx, cx, bx_);
         kahan_acc(sy, cy, by_);
         kahan_acc(sz, cz, bz_);
@@ -367,29 +420,6 @@ __global__ void __launch_bounds__(kSpThreads) k_spread_brick(
 #pragma unroll
         for (int c = 0; c < 3; ++c) out[c] = f2d_bits(h[c]) + f2d_bits(l[c]);
       } else {
-        const double q0 = q_xyz[3 * qg], q1 = q_xyz[3 * qg + 1], q2 = q_xyz[3 * qg + 2];
-        double ax = 0.0, ay = 0.0, az = 0.0;
-        for (int m = sub; m < M && qok; m += lq) {
-          const int k = (int)(mlist[m] & 1023u);
-          const double4_32a a = rec64[2 * k], fb = rec64[2 * k + 1];
-          // point_vector(q, x_j) with the minimum image (pm_periodic_boundary.C:350-374)
-          double x[3] = {a.x - q0, a.y - q1, a.z - q2};
-#pragma unroll
-          for (int d = 0; d < 3; ++d) {
-            if (sg.g.periodic[d]) {
-              const double xs = sg.g.L[d];
-              if (x[d] <= -xs / 2.0) x[d] += xs;
-              if (x[d] > xs / 2.0) x[d] -= xs;
-            }
-          }
-          // smoothed_force_exp (ggem_stokes.C:117-128)
-          const double r2 = x[0] * x[0] + x[1] * x[1] + x[2] * x[2];
-          const double a2r2 = K.alpha2 * r2;
-          const double gv = K.alpha3_pi_23 * exp(-a2r2) * (2.5 - a2r2);
-          ax += gv * fb.x;
-          ay += gv * fb.y;
-          az += gv * fb.z;
-        }
         out[0] = ax;
         out[1] = ay;
         out[2] = az;
