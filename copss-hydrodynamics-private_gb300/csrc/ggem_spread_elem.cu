@@ -63,6 +63,9 @@ struct SpreadGeo {
   Grid g;
   int lo[3], hi[3], dim[3];  // element-offset range of the stencil bitmap
   int nwords;                // 32-bit words of the bitmap
+  int pad;                   // padded bitmap: bit (i + B - 1) + 32 (j + B - 1) + 1024 (k + B - 1)
+                             // for the stencil offset index (i, j, k), read with the packed
+                             // frame coordinates of a particle minus one value per element
   int B;                     // brick edge in elements
   int nb[3];                 // bricks per axis
   int nq;                    // quadrature points per element (<= 32)
@@ -133,7 +136,7 @@ __device__ __forceinline__ int axis_offset(const SpreadGeo &sg, int d, int us, i
 
 // ANYFULL: some brick frame spans a whole periodic axis (small meshes);
 // without it the wrapped-offset and minimum-image code is compiled out
-template <bool F32, bool ANYFULL>
+template <bool F32, bool ANYFULL, bool PAD>
 __global__ void __launch_bounds__(kSpThreads) k_spread_brick(
     SpreadGeo sg, DevConsts K, const int32_t *__restrict__ start,
     const float4 *__restrict__ pos32, const double4_32a *__restrict__ pos64,
@@ -283,6 +286,11 @@ __global__ void __launch_bounds__(kSpThreads) k_spread_brick(
       const int uex = fr[0].full ? ex : ex - fr[0].F;
       const int uey = fr[1].full ? ey : ey - fr[1].F;
       const int uez = fr[2].full ? ez : ez - fr[2].F;
+      // with the padded bitmap, the packed frame coordinates u of a staged
+      // particle minus qe index the bitmap directly (each 5-bit field stays
+      // in [0, 32) for every particle of the brick's frame)
+      const int qe = (uex + sg.lo[0] - B + 1) + 32 * (uey + sg.lo[1] - B + 1) +
+                     1024 * (uez + sg.lo[2] - B + 1);
       const bool qok = qi < nq;
       const int64_t qg = e * nq + (qok ? qi : 0);
       float4 qr = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -310,20 +318,38 @@ __global__ void __launch_bounds__(kSpThreads) k_spread_brick(
         if (k < cn) {
           const uint32_t u = F32 ? __float_as_uint(rec32[k].w)
                                  : (uint32_t)__double_as_longlong(rec64[2 * k].w);
-          const int ix = axis_offset(sg, 0, (int)(u & 31u), uex, ANYFULL && fr[0].full) - sg.lo[0];
-          const int iy =
-              axis_offset(sg, 1, (int)((u >> 5) & 31u), uey, ANYFULL && fr[1].full) - sg.lo[1];
-          const int iz = axis_offset(sg, 2, (int)(u >> 10), uez, ANYFULL && fr[2].full) - sg.lo[2];
-          if ((unsigned)ix < (unsigned)sg.dim[0] && (unsigned)iy < (unsigned)sg.dim[1] &&
-              (unsigned)iz < (unsigned)sg.dim[2]) {
-            const int idx = (iz * sg.dim[1] + iy) * sg.dim[0] + ix;
+          if (PAD) {
+            const int idx = (int)u - qe;
             in = (s_bits[idx >> 5] >> (idx & 31)) & 1u;
-            if (F32) {
-              const float4 a = rec32[k];
-              item = make_float4(a.x + s_shift[0][ix], a.y + s_shift[1][iy], a.z + s_shift[2][iz],
-                                 __uint_as_float((uint32_t)k));
-            } else {
-              item.w = __uint_as_float((uint32_t)k);
+            if (in) {
+              if (F32) {
+                const int ix = (idx & 31) - (B - 1), iy = ((idx >> 5) & 31) - (B - 1),
+                          iz = (idx >> 10) - (B - 1);
+                const float4 a = rec32[k];
+                item = make_float4(a.x + s_shift[0][ix], a.y + s_shift[1][iy],
+                                   a.z + s_shift[2][iz], __uint_as_float((uint32_t)k));
+              } else {
+                item.w = __uint_as_float((uint32_t)k);
+              }
+            }
+          } else {
+            const int ix =
+                axis_offset(sg, 0, (int)(u & 31u), uex, ANYFULL && fr[0].full) - sg.lo[0];
+            const int iy =
+                axis_offset(sg, 1, (int)((u >> 5) & 31u), uey, ANYFULL && fr[1].full) - sg.lo[1];
+            const int iz =
+                axis_offset(sg, 2, (int)(u >> 10), uez, ANYFULL && fr[2].full) - sg.lo[2];
+            if ((unsigned)ix < (unsigned)sg.dim[0] && (unsigned)iy < (unsigned)sg.dim[1] &&
+                (unsigned)iz < (unsigned)sg.dim[2]) {
+              const int idx = (iz * sg.dim[1] + iy) * sg.dim[0] + ix;
+              in = (s_bits[idx >> 5] >> (idx & 31)) & 1u;
+              if (F32) {
+                const float4 a = rec32[k];
+                item = make_float4(a.x + s_shift[0][ix], a.y + s_shift[1][iy],
+                                   a.z + s_shift[2][iz], __uint_as_float((uint32_t)k));
+              } else {
+                item.w = __uint_as_float((uint32_t)k);
+              }
             }
           }
         }
@@ -515,13 +541,27 @@ int spread_geometry(ggem_ctx *c, SpreadGeo *sg) {
     }
     sg->L32[d] = (float)g.L[d];
   }
-  const int nbits = sg->dim[0] * sg->dim[1] * sg->dim[2];
+  // the padded layout needs every frame offset field in [0, 32): offsets
+  // run over [-(B - 1), dim + B - 2] per axis, so dim + 2B - 2 <= 32; a
+  // frame spanning a whole periodic axis wraps its offsets and keeps the
+  // compact layout
+  bool any_full = false;
+  sg->pad = 1;
+  for (int d = 0; d < 3; ++d) {
+    any_full = any_full || (g.periodic[d] && B + sg->hi[d] - sg->lo[d] >= g.nc[d]);
+    if (sg->dim[d] + 2 * B - 2 > 32) sg->pad = 0;
+  }
+  if (any_full) sg->pad = 0;
+  const int nbits = sg->pad ? 1024 * (sg->dim[2] + 2 * B - 2)
+                            : sg->dim[0] * sg->dim[1] * sg->dim[2];
   sg->nwords = (nbits + 31) / 32;
   if (sg->nwords > kSpMaxWords)
     return fail(c, GGEM_ERR_BAD_ARG, "element stencil bitmap too large for the brick spread");
   std::vector<uint32_t> bits(sg->nwords, 0u);
   auto set = [&](int x, int y, int z) {
-    const int idx = ((z - sg->lo[2]) * sg->dim[1] + (y - sg->lo[1])) * sg->dim[0] + (x - sg->lo[0]);
+    const int i = x - sg->lo[0], j = y - sg->lo[1], k = z - sg->lo[2];
+    const int idx = sg->pad ? (i + B - 1) + 32 * (j + B - 1) + 1024 * (k + B - 1)
+                            : (k * sg->dim[1] + j) * sg->dim[0] + i;
     bits[idx >> 5] |= 1u << (idx & 31);
   };
   set(0, 0, 0);  // the element's own particles come first in its list
@@ -567,9 +607,13 @@ int spread_elements(ggem_ctx *c, int precision, const double *d_f_slot, double *
   };
   int rc;
   if (precision == GGEM_FP32)
-    rc = any_full ? launch(k_spread_brick<true, true>) : launch(k_spread_brick<true, false>);
+    rc = any_full   ? launch(k_spread_brick<true, true, false>)
+         : sg.pad   ? launch(k_spread_brick<true, false, true>)
+                    : launch(k_spread_brick<true, false, false>);
   else
-    rc = any_full ? launch(k_spread_brick<false, true>) : launch(k_spread_brick<false, false>);
+    rc = any_full   ? launch(k_spread_brick<false, true, false>)
+         : sg.pad   ? launch(k_spread_brick<false, false, true>)
+                    : launch(k_spread_brick<false, false, false>);
   if (rc) return rc;
   return check_launch(c, "spread bricks");
 }
