@@ -55,7 +55,7 @@ constexpr int kSpMaxExt = 32;    // dilated brick extent per axis (5-bit coordin
 constexpr size_t kSpRecBytes = 16384;
 constexpr int kSpMaxWords = 1024;  // stencil bitmap words (32768 element offsets)
 constexpr int kSpQueue = 64;      // queued members per warp (< 32 left + 32 new)
-constexpr size_t kSpShared = kSpRecBytes + kSpWarps * kSpQueue * sizeof(float4) +
+constexpr size_t kSpShared = kSpRecBytes + kSpWarps * (32 * sizeof(float4) + kSpQueue * sizeof(uint32_t)) +
                              2 * (kSpMaxSeg + 1) * sizeof(int32_t) +
                              kSpMaxWords * sizeof(uint32_t);
 
@@ -137,7 +137,7 @@ __device__ __forceinline__ int axis_offset(const SpreadGeo &sg, int d, int us, i
 // ANYFULL: some brick frame spans a whole periodic axis (small meshes);
 // without it the wrapped-offset and minimum-image code is compiled out
 template <bool F32, bool ANYFULL, bool PAD>
-__global__ void __launch_bounds__(kSpThreads) k_spread_brick(
+__global__ void __launch_bounds__(kSpThreads, F32 ? 4 : 1) k_spread_brick(
     SpreadGeo sg, DevConsts K, const int32_t *__restrict__ start,
     const float4 *__restrict__ pos32, const double4_32a *__restrict__ pos64,
     const double *__restrict__ f_slot, const float4 *__restrict__ q_rel,
@@ -150,7 +150,8 @@ __global__ void __launch_bounds__(kSpThreads) k_spread_brick(
   // than 32-byte records would
   float4 *rec32 = reinterpret_cast<float4 *>(sp_smem);        // [2][CAP]
   double4_32a *rec64 = reinterpret_cast<double4_32a *>(sp_smem);  // [CAP][2]
-  float4 *queue = reinterpret_cast<float4 *>(sp_smem + kSpRecBytes);
+  float4 *batch = reinterpret_cast<float4 *>(sp_smem + kSpRecBytes);       // [warps][32]
+  uint32_t *queue = reinterpret_cast<uint32_t *>(batch + kSpWarps * 32);  // [warps][kSpQueue]
   int32_t *seg_begin = reinterpret_cast<int32_t *>(queue + kSpWarps * kSpQueue);
   int32_t *seg_pre = seg_begin + kSpMaxSeg + 1;
   uint32_t *s_bits = reinterpret_cast<uint32_t *>(seg_pre + kSpMaxSeg + 1);
@@ -240,10 +241,13 @@ __global__ void __launch_bounds__(kSpThreads) k_spread_brick(
   const int nq = sg.nq, lq = sg.lq;
   const int qi = lane / lq, sub = lane - qi * lq;
   unsigned long long my_pairs = 0;
-  // the warp's member queue: per member its position in the element's frame
-  // (FP32; the staged position plus the element offset's shift, formed once
-  // per member instead of once per point) and its staged index in .w
-  float4 *mq = queue + warp * kSpQueue;
+  // the warp's member queue: per member its staged index (10 bits) and its
+  // element offset (the padded bitmap index, or three 5-bit offsets); each
+  // batch of 32 becomes positions in the element's frame (FP32: the staged
+  // position plus the offset's shift, formed once per member instead of
+  // once per point, one member per lane) with the staged index in .w
+  uint32_t *mq = queue + warp * kSpQueue;
+  float4 *mb = batch + warp * 32;
   const unsigned lt_mask = (1u << lane) - 1u;
   for (int c0 = 0; c0 < total; c0 += CAP) {
     const int cn = min(CAP, total - c0);
@@ -314,24 +318,14 @@ __global__ void __launch_bounds__(kSpThreads) k_spread_brick(
       for (int k0 = 0; k0 < cn; k0 += 32) {
         const int k = k0 + lane;
         bool in = false;
-        float4 item = make_float4(0.f, 0.f, 0.f, 0.f);
+        uint32_t item = 0;
         if (k < cn) {
           const uint32_t u = F32 ? __float_as_uint(rec32[k].w)
                                  : (uint32_t)__double_as_longlong(rec64[2 * k].w);
           if (PAD) {
             const int idx = (int)u - qe;
             in = (s_bits[idx >> 5] >> (idx & 31)) & 1u;
-            if (in) {
-              if (F32) {
-                const int ix = (idx & 31) - (B - 1), iy = ((idx >> 5) & 31) - (B - 1),
-                          iz = (idx >> 10) - (B - 1);
-                const float4 a = rec32[k];
-                item = make_float4(a.x + s_shift[0][ix], a.y + s_shift[1][iy],
-                                   a.z + s_shift[2][iz], __uint_as_float((uint32_t)k));
-              } else {
-                item.w = __uint_as_float((uint32_t)k);
-              }
-            }
+            item = (uint32_t)k | ((uint32_t)idx << 10);
           } else {
             const int ix =
                 axis_offset(sg, 0, (int)(u & 31u), uex, ANYFULL && fr[0].full) - sg.lo[0];
@@ -343,13 +337,8 @@ __global__ void __launch_bounds__(kSpThreads) k_spread_brick(
                 (unsigned)iz < (unsigned)sg.dim[2]) {
               const int idx = (iz * sg.dim[1] + iy) * sg.dim[0] + ix;
               in = (s_bits[idx >> 5] >> (idx & 31)) & 1u;
-              if (F32) {
-                const float4 a = rec32[k];
-                item = make_float4(a.x + s_shift[0][ix], a.y + s_shift[1][iy],
-                                   a.z + s_shift[2][iz], __uint_as_float((uint32_t)k));
-              } else {
-                item.w = __uint_as_float((uint32_t)k);
-              }
+              item = (uint32_t)k | ((uint32_t)ix << 10) | ((uint32_t)iy << 15) |
+                     ((uint32_t)iz << 20);
             }
           }
         }
@@ -361,9 +350,33 @@ __global__ void __launch_bounds__(kSpThreads) k_spread_brick(
         while (queued >= 32 || (last && queued > 0)) {
           __syncwarp();
           const int m = min(queued, 32);
+          if (F32 && lane < m) {
+            const uint32_t en = mq[lane];
+            const int kk = (int)(en & 1023u);
+            float4 v = make_float4(0.f, 0.f, 0.f, __uint_as_float((uint32_t)kk));
+            if (F32) {
+              int ix, iy, iz;
+              if (PAD) {
+                const int idx = (int)(en >> 10);
+                ix = (idx & 31) - (B - 1);
+                iy = ((idx >> 5) & 31) - (B - 1);
+                iz = (idx >> 10) - (B - 1);
+              } else {
+                ix = (int)((en >> 10) & 31u);
+                iy = (int)((en >> 15) & 31u);
+                iz = (int)(en >> 20);
+              }
+              const float4 a = rec32[kk];
+              v.x = a.x + s_shift[0][ix];
+              v.y = a.y + s_shift[1][iy];
+              v.z = a.z + s_shift[2][iz];
+            }
+            mb[lane] = v;
+          }
+          __syncwarp();
           for (int j = sub; j < m && qok; j += lq) {
-            const float4 mp = mq[j];
-            const int kk = (int)__float_as_uint(mp.w);
+            const float4 mp = F32 ? mb[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+            const int kk = F32 ? (int)__float_as_uint(mp.w) : (int)(mq[j] & 1023u);
             if (F32) {
               const float4 fb = rec32[kSpCap32 + kk];
               float dx = mp.x - qr.x;
@@ -422,7 +435,7 @@ __global__ void __launch_bounds__(kSpThreads) k_spread_brick(
           }
           // the rest of the queue to its front
           const int rest = queued - m;
-          const float4 rv = lane < rest ? mq[32 + lane] : make_float4(0.f, 0.f, 0.f, 0.f);
+          const uint32_t rv = lane < rest ? mq[32 + lane] : 0u;
           __syncwarp();
           if (lane < rest) mq[lane] = rv;
           queued = rest;
