@@ -374,63 +374,76 @@ __global__ void __launch_bounds__(kSpThreads, F32 ? 4 : 1) k_spread_brick(
             mb[lane] = v;
           }
           __syncwarp();
-          for (int j = sub; j < m && qok; j += lq) {
-            const float4 mp = F32 ? mb[j] : make_float4(0.f, 0.f, 0.f, 0.f);
-            const int kk = F32 ? (int)__float_as_uint(mp.w) : (int)(mq[j] & 1023u);
-            if (F32) {
-              const float4 fb = rec32[kSpCap32 + kk];
-              float dx = mp.x - qr.x;
-              float dy = mp.y - qr.y;
-              float dz = mp.z - qr.z;
-              // minimum image (pm_periodic_boundary.C:350-374); only an axis
-              // whose frame is the whole box can produce |d| > L/2
-              if (ANYFULL && fr[0].full) {
-                if (dx <= -0.5f * sg.L32[0]) dx += sg.L32[0];
-                if (dx > 0.5f * sg.L32[0]) dx -= sg.L32[0];
-              }
-              if (ANYFULL && fr[1].full) {
-                if (dy <= -0.5f * sg.L32[1]) dy += sg.L32[1];
-                if (dy > 0.5f * sg.L32[1]) dy -= sg.L32[1];
-              }
-              if (ANYFULL && fr[2].full) {
-                if (dz <= -0.5f * sg.L32[2]) dz += sg.L32[2];
-                if (dz > 0.5f * sg.L32[2]) dz -= sg.L32[2];
-              }
-              const float s2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-              const float p = s2 * sg.e_hi;
-              const float r = fmaf(s2, sg.e_lo, fmaf(s2, sg.e_hi, -p));
-              const float E0 = ex2_approx(p);
-              const float E = fmaf(E0, r * 0.6931471805599453f, E0);
-              const float gv = E * fmaf(-sg.c1, s2, sg.c25);
-              bx_ = fmaf(gv, fb.x, bx_);
-              by_ = fmaf(gv, fb.y, by_);
-              bz_ = fmaf(gv, fb.z, bz_);
-              if (++blk == 8) {  // every 8 pairs into the compensated sums
-                kahan_acc(sx, cx, bx_);
-                kahan_acc(sy, cy, by_);
-                kahan_acc(sz, cz, bz_);
-                bx_ = by_ = bz_ = 0.f;
-                blk = 0;
-              }
-            } else {
-              const double4_32a a = rec64[2 * kk], fb = rec64[2 * kk + 1];
-              // point_vector(q, x_j) with the minimum image (pm_periodic_boundary.C:350-374)
-              double x[3] = {a.x - q0, a.y - q1, a.z - q2};
+          // one (point, member) term of the FP32 sum into the block sums
+          auto term32 = [&](const float4 &mp) {
+            const float4 fb = rec32[kSpCap32 + (int)__float_as_uint(mp.w)];
+            float dx = mp.x - qr.x;
+            float dy = mp.y - qr.y;
+            float dz = mp.z - qr.z;
+            // minimum image (pm_periodic_boundary.C:350-374); only an axis
+            // whose frame is the whole box can produce |d| > L/2
+            if (ANYFULL && fr[0].full) {
+              if (dx <= -0.5f * sg.L32[0]) dx += sg.L32[0];
+              if (dx > 0.5f * sg.L32[0]) dx -= sg.L32[0];
+            }
+            if (ANYFULL && fr[1].full) {
+              if (dy <= -0.5f * sg.L32[1]) dy += sg.L32[1];
+              if (dy > 0.5f * sg.L32[1]) dy -= sg.L32[1];
+            }
+            if (ANYFULL && fr[2].full) {
+              if (dz <= -0.5f * sg.L32[2]) dz += sg.L32[2];
+              if (dz > 0.5f * sg.L32[2]) dz -= sg.L32[2];
+            }
+            const float s2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+            const float p = s2 * sg.e_hi;
+            const float r = fmaf(s2, sg.e_lo, fmaf(s2, sg.e_hi, -p));
+            const float E0 = ex2_approx(p);
+            const float E = fmaf(E0, r * 0.6931471805599453f, E0);
+            const float gv = E * fmaf(-sg.c1, s2, sg.c25);
+            bx_ = fmaf(gv, fb.x, bx_);
+            by_ = fmaf(gv, fb.y, by_);
+            bz_ = fmaf(gv, fb.z, bz_);
+          };
+          auto flush32 = [&]() {  // the block sums into the compensated sums
+            kahan_acc(sx, cx, bx_);
+            kahan_acc(sy, cy, by_);
+            kahan_acc(sz, cz, bz_);
+            bx_ = by_ = bz_ = 0.f;
+            blk = 0;
+          };
+          if (F32 && lq == 4 && m == 32 && qok) {
+            // a full batch with four lanes per point: eight members per
+            // lane, which is one block of the compensated sums (blk is 0
+            // here: every earlier batch was full)
 #pragma unroll
-              for (int d = 0; d < 3; ++d) {
-                if (sg.g.periodic[d]) {
-                  const double xs = sg.g.L[d];
-                  if (x[d] <= -xs / 2.0) x[d] += xs;
-                  if (x[d] > xs / 2.0) x[d] -= xs;
+            for (int t = 0; t < 8; ++t) term32(mb[sub + 4 * t]);
+            flush32();
+          } else {
+            for (int j = sub; j < m && qok; j += lq) {
+              if (F32) {
+                term32(mb[j]);
+                if (++blk == 8) flush32();  // every 8 pairs into the compensated sums
+              } else {
+                const int kk = (int)(mq[j] & 1023u);
+                const double4_32a a = rec64[2 * kk], fb = rec64[2 * kk + 1];
+                // point_vector(q, x_j) with the minimum image (pm_periodic_boundary.C:350-374)
+                double x[3] = {a.x - q0, a.y - q1, a.z - q2};
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                  if (sg.g.periodic[d]) {
+                    const double xs = sg.g.L[d];
+                    if (x[d] <= -xs / 2.0) x[d] += xs;
+                    if (x[d] > xs / 2.0) x[d] -= xs;
+                  }
                 }
+                // smoothed_force_exp (ggem_stokes.C:117-128)
+                const double r2 = x[0] * x[0] + x[1] * x[1] + x[2] * x[2];
+                const double a2r2 = K.alpha2 * r2;
+                const double gv = K.alpha3_pi_23 * exp(-a2r2) * (2.5 - a2r2);
+                ax += gv * fb.x;
+                ay += gv * fb.y;
+                az += gv * fb.z;
               }
-              // smoothed_force_exp (ggem_stokes.C:117-128)
-              const double r2 = x[0] * x[0] + x[1] * x[1] + x[2] * x[2];
-              const double a2r2 = K.alpha2 * r2;
-              const double gv = K.alpha3_pi_23 * exp(-a2r2) * (2.5 - a2r2);
-              ax += gv * fb.x;
-              ay += gv * fb.y;
-              az += gv * fb.z;
             }
           }
           // the rest of the queue to its front
