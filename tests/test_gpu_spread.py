@@ -107,3 +107,14 @@ def test_spread_dense_staging_in_several_passes():
     L = 40.0
     xyz = rng.uniform(0, L, (6400, 3))
     _check((0, 0, 0), (L,) * 3, (28, 28, 28), (1, 1, 1), xyz, 4)
+
+
+def test_spread_wide_stencil_compact_bitmap():
+    """elements of h = 0.55 under the spread's search radius (0.5 h + 8):
+    offsets up to 15 elements, so the stencil (31 per axis) plus twice the
+    2-element brick exceeds 32 and the kernel reads the compact stencil
+    bitmap instead of the padded one (an open box, whose frames are clipped
+    to the mesh, keeps the case small)"""
+    rng = np.random.default_rng(6)
+    L = 12 * 0.55
+    _check((0, 0, 0), (L,) * 3, (12, 12, 12), (0, 0, 0), rng.uniform(0, L, (60, 3)), 5)
