@@ -387,7 +387,9 @@ __global__ void __launch_bounds__(32, 32) k_pair_list_warp(
   __shared__ int32_t s_code[kMaxStencil];
   __shared__ float4 s_pi[32];          // the targets of the current chunk
   __shared__ float4 s_q[kListQueue];   // kept candidates: frame position, entry
+  __shared__ int s_mark[32];           // stencil cell starting at each lane of a chunk
   const int lane = threadIdx.x;
+  s_mark[lane] = -1;
   const int64_t C = blockIdx.x;
   const int32_t tb = start[C], te = start[C + 1];
   if (te <= tb) return;
@@ -450,16 +452,30 @@ __global__ void __launch_bounds__(32, 32) k_pair_list_warp(
     __syncwarp();
     int32_t own_cnt = 0, own_cnt_h = 0;
     int queued = 0;  // warp-uniform
+    int kcur = -1;   // warp-uniform: the stencil cell of candidate v0 - 1
     for (int32_t v0 = 0; v0 < V; v0 += 32) {
       const int32_t v = v0 + lane;
       const bool valid = v < V;
-      // stencil cell of candidate v: the last k with s_pre[k] <= v
-      int lo = 0, hi = nst - 1;
-      while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (s_pre[mid] <= v) lo = mid;
-        else hi = mid - 1;
+      // stencil cell of candidate v, the last k with s_pre[k] <= v: the
+      // cells after kcur that start inside this chunk mark their first lane
+      // (the largest k wins, skipping empty cells), and a max-scan over the
+      // lanes carries each cell forward
+      for (int kk = kcur + 1;; kk += 32) {
+        const int k = kk + lane;
+        const int p = k < nst ? s_pre[k] - v0 : 32;
+        if (p < 32) atomicMax(&s_mark[p], k);
+        if (__shfl_sync(0xffffffffu, p, 31) >= 32) break;
       }
+      __syncwarp();
+      int lo = max(s_mark[lane], kcur);
+      s_mark[lane] = -1;  // ready for the next chunk
+      __syncwarp();
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, lo, o);
+        if (lane >= o) lo = max(lo, y);
+      }
+      kcur = __shfl_sync(0xffffffffu, lo, 31);
       const int32_t t = valid ? s_base[lo] + (v - s_pre[lo]) : 0;
       const int code = s_code[lo];
       const float4 sh = shift[code];
