@@ -347,6 +347,15 @@ __device__ __forceinline__ void stage_shifts(float4 *sh, const float4 *__restric
   __syncthreads();
 }
 
+// The series kernels may be launched as programmatic dependents of the
+// kernel before them (PTX griddepcontrol): their blocks can start while
+// that kernel's last blocks finish, stage the constant shift table, and
+// wait here until its results are complete and visible.  Without such a
+// launch the wait returns at once.
+__device__ __forceinline__ void wait_prior_grid() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
 // reduce-scatter of the group's float-float sums: afterwards lane sub
 // (0, 1, 2) holds component sub of the target's total, summed in the same
 // tree as the all-reduce ((lane 0 + lane 2) + (lane 1 + lane 3))
@@ -587,6 +596,7 @@ __global__ void __launch_bounds__(256, kComputedMinBlocks[V]) k_pair_r1(
     double *__restrict__ u, const int32_t *__restrict__ order, double *__restrict__ part) {
   __shared__ float4 sh[kMaxCode];
   stage_shifts(sh, shift);
+  wait_prior_grid();
   const int64_t gid = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / kGroup;
   const int sub = (int)(threadIdx.x % kGroup);
   const bool act = gid < n;
@@ -621,6 +631,7 @@ __global__ void __launch_bounds__(256, kComputedMinBlocks[V]) k_pair_first(
     double *__restrict__ dw, Rec32 *__restrict__ next, double *__restrict__ part) {
   __shared__ float4 sh[kMaxCode];
   stage_shifts(sh, shift);
+  wait_prior_grid();
   const int64_t gid = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / kGroup;
   const int sub = (int)(threadIdx.x % kGroup);
   const bool act = gid < n;
@@ -666,6 +677,7 @@ __global__ void __launch_bounds__(256, kComputedMinBlocks[V]) k_pair_cheb(
     int64_t nw, Rec32 *__restrict__ dw_next) {
   __shared__ float4 sh[kMaxCode];
   stage_shifts(sh, shift);
+  wait_prior_grid();
   const int64_t gid = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / kGroup;
   const int sub = (int)(threadIdx.x % kGroup);
   const bool act = gid < n;
@@ -1357,13 +1369,34 @@ PolyAB poly_of(const ggem_ctx *c) {
   return P;
 }
 
+// a series kernel launched as a programmatic dependent of the kernel
+// before it on the stream (its first global reads wait in wait_prior_grid);
+// measured at N = 200k: the reference-faithful series (a vector kernel
+// between pair kernels) 777-781 -> 795-797 steps/s, the host-buffer leg
+// 1492-1496 -> 1512-1519, the device-resident fused series unchanged
+template <typename... KArgs, typename... Args>
+void launch_dependent(void (*kern)(KArgs...), unsigned grid, unsigned block, cudaStream_t st,
+                      Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, kern, args...);
+}
+
 template <bool POLY, int V, bool ORIG>
 void launch_r1(ggem_ctx *c, const Rec32 *src, const double *f, double *u, double self_c,
                double *part) {
-  k_pair_r1<POLY, V, ORIG><<<(unsigned)pair_grid_blocks(c), 256, 0, c->stream>>>(
-      c->n, src, c->nb_cnt.p, c->nb_w, c->nb_list.p, poly_of(c),
-      reinterpret_cast<const Rec32 *>(c->tab.p), c->tab_inv_ds, c->d_shift.p, self_c, f, u,
-      c->order.p, part);
+  launch_dependent(k_pair_r1<POLY, V, ORIG>, (unsigned)pair_grid_blocks(c), 256u, c->stream,
+                   c->n, src, (const int32_t *)c->nb_cnt.p, c->nb_w, (const uint32_t *)c->nb_list.p,
+                   poly_of(c), reinterpret_cast<const Rec32 *>(c->tab.p), c->tab_inv_ds,
+                   (const float4 *)c->d_shift.p, self_c, f, u, (const int32_t *)c->order.p, part);
 }
 
 template <bool POLY, bool ORIG = false>
@@ -1433,10 +1466,11 @@ template <bool POLY, int V, bool NORMS>
 void launch_cheb(ggem_ctx *c, const Rec32 *src, Rec32 *next, double two_da, double c1,
                  double coef, const double *x0, const double *x1, double *xm, double *dw,
                  double *part, Rec32 *dw_next) {
-  k_pair_cheb<POLY, V, NORMS><<<(unsigned)pair_grid_blocks(c), 256, 0, c->stream>>>(
-      c->n, src, c->nb_cnt.p, c->nb_w, c->nb_list.p, poly_of(c),
-      reinterpret_cast<const Rec32 *>(c->tab.p), c->tab_inv_ds, c->d_shift.p, two_da, c1, coef,
-      x0, x1, xm, dw, next, part, pair_partials(c), dw_next);
+  launch_dependent(k_pair_cheb<POLY, V, NORMS>, (unsigned)pair_grid_blocks(c), 256u, c->stream,
+                   c->n, src, (const int32_t *)c->nb_cnt.p, c->nb_w, (const uint32_t *)c->nb_list.p,
+                   poly_of(c), reinterpret_cast<const Rec32 *>(c->tab.p), c->tab_inv_ds,
+                   (const float4 *)c->d_shift.p, two_da, c1, coef, x0, x1, xm, dw, next, part,
+                   pair_partials(c), dw_next);
 }
 
 // with part (and dw_next) the term also leaves the estimators' two norms as
@@ -1459,10 +1493,11 @@ template <bool POLY, int V>
 void launch_first(ggem_ctx *c, const Rec32 *src, Rec32 *next, double self_c, double da,
                   double db, double c0, double c1, const double *x0, double *m, double *x1,
                   double *dw, double *part) {
-  k_pair_first<POLY, V><<<(unsigned)pair_grid_blocks(c), 256, 0, c->stream>>>(
-      c->n, src, c->nb_cnt.p, c->nb_w, c->nb_list.p, poly_of(c),
-      reinterpret_cast<const Rec32 *>(c->tab.p), c->tab_inv_ds, c->d_shift.p, self_c, da, db, c0,
-      c1, x0, m, x1, dw, next, part);
+  launch_dependent(k_pair_first<POLY, V>, (unsigned)pair_grid_blocks(c), 256u, c->stream, c->n,
+                   src, (const int32_t *)c->nb_cnt.p, c->nb_w, (const uint32_t *)c->nb_list.p,
+                   poly_of(c), reinterpret_cast<const Rec32 *>(c->tab.p), c->tab_inv_ds,
+                   (const float4 *)c->d_shift.p, self_c, da, db, c0, c1, x0, m, x1, dw, next,
+                   part);
 }
 
 template <int CD, bool POLY>
