@@ -206,6 +206,14 @@ def _f64(a) -> np.ndarray:
     return np.ascontiguousarray(a, dtype=np.float64)
 
 
+def _nrhs(x: np.ndarray, n: int) -> int:
+    """right-hand sides in x ([nrhs][n][3] or [n][3]); for a context without
+    particles the leading dimension of a 3-D array, else one"""
+    if n:
+        return x.size // (3 * n)
+    return x.shape[0] if x.ndim == 3 else 1
+
+
 def cheb_coeffs(N, da, db, method=CHEB_GAUSS) -> np.ndarray:
     c = np.zeros(N + 1)
     rc = lib().ggem_cheb_coeffs(int(N), float(da), float(db), int(method), _p(c))
@@ -549,7 +557,7 @@ class Context:
 
     def cheb_inv_sqrt(self, xi, N, eig_min, eig_max, tol, check_every=1):
         xi = _f64(xi).copy()
-        nrhs = xi.size // (3 * self.n)
+        nrhs = _nrhs(xi, self.n)
         reps = (ChebReport * nrhs)()
         self._check(lib().ggem_cheb_inv_sqrt(self.h, nrhs, int(N), float(eig_min), float(eig_max),
                                              float(tol), int(check_every), _p(xi), reps))
@@ -572,7 +580,7 @@ class Context:
 
     def brownian_displacement(self, xi, N, eig_min, eig_max, tol, check_every=1):
         xi = _f64(xi)
-        nrhs = xi.size // (3 * self.n)
+        nrhs = _nrhs(xi, self.n)
         dw = np.zeros_like(xi)
         reps = (ChebReport * nrhs)()
         rc = lib().ggem_brownian_displacement(self.h, nrhs, int(N), float(eig_min),

@@ -53,6 +53,11 @@ def test_empty_context_then_particles(prec):
         reps = (G.ChebReport * 1)()
         rc = lib.ggem_cheb_inv_sqrt(ctx.h, 1, 30, 0.5, 2.0, 1e-3, 1, None, reps)
         assert rc == 0 and reps[0].converged == 1 and reps[0].n_matvecs == 0
+        # the Python binding over the same calls
+        rc, dw, r = ctx.brownian_displacement(np.zeros((3, 0, 3)), 30, 0.5, 2.0, 1e-3)
+        assert rc == 0 and dw.shape == (3, 0, 3) and len(r) == 3 and r[0]["converged"] == 1
+        y, r = ctx.cheb_inv_sqrt(np.zeros((0, 3)), 30, 0.5, 2.0, 1e-3)
+        assert y.shape == (0, 3) and len(r) == 1 and r[0]["n_matvecs"] == 0
         targets = np.random.default_rng(1).uniform(0, L, (5, 3))
         assert np.array_equal(ctx.local_field(targets, np.zeros((0, 3))), np.zeros((5, 3)))
         with pytest.raises(G.GGEMError):
